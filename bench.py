@@ -1,0 +1,319 @@
+"""Benchmark: STEM probe-slices/s on the SrTiO3 512^2, 4096-probe HAADF/ABF scan.
+
+Workload (one step): SrTiO3 [001], 8x8x50 cells, 512x512 grid over 31.24 A,
+100 slices of 1.9525 A, 200 kV, 25 mrad aberration-free probe, 64x64 raster
+over the central 2x2 cells (4096 probes), HAADF 80-200 mrad and ABF 11-22 mrad
+detector sums after the last slice.  Synthetic specimen on ideal sites.
+
+  value : msl_stem_scan over all 4096 probes with the transmission functions
+          already resident in HBM (device buffers in and out).
+  e2e   : the whole user call chain from host memory, copies included:
+          msl_potential_build (host atoms) -> msl_transmission_build ->
+          msl_stem_scan -> detector sums back in host memory.
+
+--impl reference times the reference's CPU path (the oracle port of Kirkland's
+mulslice loop with the C# probe and detector, scipy FFTs on all host threads)
+on a bounded sample of the same workload.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "STEM probe-slices/s at 512^2 (SrTiO3, 4096-probe HAADF/ABF scan)"
+UNIT = "probe-slices/s"
+NSLICE = 100
+PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def workload():
+    from multislice_gb300 import specimen as S
+    cfg = S.config_srtio3_stem()
+    return cfg
+
+
+def peaks():
+    try:
+        with open(PEAKS) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ------------------------------------------------------------------ our arm
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+    from multislice_gb300 import Context
+
+    world, rank, local = dist_env()
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    cfg = workload()
+    spec = cfg["spec"]
+    nx = ny = 512
+    # weak scaling: every rank scans its own 4096-probe raster (shifted by one
+    # probe step per rank so ranks never repeat work)
+    xy = cfg["probe_xy"].copy()
+    xy[:, 0] += rank * (2 * 3.905 / 64) / max(world, 1)
+    nprobe = len(xy)
+    dz = spec.cz / NSLICE
+    seq = np.arange(NSLICE, dtype=np.int32)
+    det_k = cfg["det_k"]
+
+    ctx = Context(local)
+    # device-resident inputs for `value`
+    v_dev = torch.empty((NSLICE, nx, ny), dtype=torch.float32, device=dev)
+    ctx.potential(spec, nx, ny, NSLICE, cfg["radius"], out=v_dev)
+    t_dev = torch.empty((NSLICE, nx, ny, 2), dtype=torch.float32, device=dev)
+    ctx.transmission(v_dev, spec.ax, spec.by, 200.0, out=t_dev)
+    out_dev = torch.empty((nprobe, 1, len(det_k)), dtype=torch.float64, device=dev)
+
+    def step():
+        ctx.stem_scan(t_dev, dz, seq, spec.ax, spec.by, 200.0, cfg["k_ap"], xy, det_k, out=out_dev)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        step()
+    barrier()
+    l0 = ctx.launches
+    ctx.profile(True)
+    with ClockSampler(local) as clk:
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            step()
+        barrier()
+        t1 = time.perf_counter()
+    prof = ctx.profile_read()
+    ctx.profile(False)
+    launches = ctx.launches - l0
+    elapsed = t1 - t0
+    if world > 1:
+        tt = torch.tensor([elapsed], dtype=torch.float64, device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        elapsed = float(tt.item())
+    units = nprobe * NSLICE * world * args.steps
+    value = units / elapsed
+
+    # e2e: host atoms in, host detector sums out, through the public API
+    res_host = np.empty((nprobe, 1, len(det_k)), np.float64)
+
+    def e2e_step():
+        ctx.potential(spec, nx, ny, NSLICE, cfg["radius"], out=v_dev)
+        ctx.transmission(v_dev, spec.ax, spec.by, 200.0, out=t_dev)
+        ctx.stem_scan(t_dev, dz, seq, spec.ax, spec.by, 200.0, cfg["k_ap"], xy, det_k, out=res_host)
+
+    e2e_step()
+    barrier()
+    e0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    barrier()
+    e_el = time.perf_counter() - e0
+    if world > 1:
+        tt = torch.tensor([e_el], dtype=torch.float64, device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e_el = float(tt.item())
+    e2e_value = units / e_el
+    h2d = spec.natom * (3 * 8 + 4) + 104 * 12 * 8 + nprobe * 2 * 8
+    d2h = res_host.nbytes
+
+    # roofline of the dominant kernel (the column pass; row pass reported beside it)
+    hbm, peak_kind = peaks()
+    rows = {}
+    for kind in ("row", "col"):
+        n, ms = prof[kind]
+        per_launch = ms / max(n, 1)
+        # algorithmic bytes per launch: every launch streams the batch's waves
+        # once in and once out: 16 * nx * ny bytes per probe
+        bytes_per_launch = 16.0 * nx * ny * nprobe
+        rows[kind] = dict(launches=n, ms_per_launch=per_launch,
+                          achieved_gbs=bytes_per_launch / (per_launch * 1e-3) / 1e9 if n else None)
+    dom = "col" if prof["col"][1] >= prof["row"][1] else "row"
+    ach = rows[dom]["achieved_gbs"]
+    traffic = None
+    tr_file = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tr_file):
+        try:
+            traffic = json.load(open(tr_file)).get(f"{dom}_pass_bytes_per_launch_4096")
+        except Exception:
+            traffic = None
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64/f32",
+        "data": "synthetic (SrTiO3 on ideal sites, seeded raster)",
+        "config": {"workload": "SrTiO3 [001] 8x8x50 cells, 512x512, 100 slices, 200 kV, "
+                               "25 mrad probe, 64x64 raster (4096 probes), HAADF 80-200 + ABF 11-22 mrad",
+                   "probes_per_gpu": nprobe, "slices": NSLICE, "grid": [nx, ny],
+                   "l2": "inputs larger than L2 (waves 8.6 GB, transmission 210 MB)",
+                   "parallelism": f"replicas x{world} (probe rasters per GPU)"},
+        "gpu_launches": launches,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h,
+                "chain": "potential_build(host atoms) + transmission_build + stem_scan(host out)"},
+        "roofline": {"bound": "hbm", "kernel": f"{dom}_pass", "achieved": ach, "peak": hbm,
+                     "unit": "GB/s", "frac": (ach / hbm) if ach else None, "traffic": traffic,
+                     "peak_source": peak_kind, "passes": rows},
+    }
+    if rank == 0:
+        if world == 1 and not args.no_cpu:
+            line["cpu_baseline"] = cpu_baseline(cfg, args.cpu_probes)
+        line["clocks"] = clk.summary()
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+# ------------------------------------------------------------- CPU baseline
+def cpu_baseline(cfg, nprobe, spawn_pool=False):
+    """Oracle port of the reference CPU loop on a bounded probe sample."""
+    from oracle import msl_oracle as O
+    spec = cfg["spec"]
+    nx = ny = 512
+    workers = os.cpu_count() or 1
+    fp = np.load(os.path.join(ROOT, "multislice_gb300", "data", "fparams.npy"))
+    # inputs (not timed): transmission functions from the oracle's potential
+    V = O.potential(spec.x, spec.y, spec.z, spec.Z, fp, spec.ax, spec.by, spec.cz, nx, ny,
+                    NSLICE, cfg["radius"])
+    T = O.transmission(V, 200.0, spec.ax, spec.by, np.complex64)
+    props = [O.propagator_tables(nx, ny, spec.ax, spec.by, 200.0, spec.cz / NSLICE, "f32")] * NSLICE
+    mask = O.band_mask(nx, ny, spec.ax, spec.by)
+    dm = O.detector_masks(nx, ny, spec.ax, spec.by, cfg["det_k"])
+    xy = cfg["probe_xy"][:nprobe]
+    t0 = time.perf_counter()
+    P = O.probe(nx, ny, spec.ax, spec.by, 200.0, 0.0, cfg["k_ap"], 0.0, 0.0, xy, np.complex64)
+    O.stem(T, props, np.arange(NSLICE), mask, P, dm, [NSLICE - 1], workers=workers)
+    el = time.perf_counter() - t0
+    return {"value": nprobe * NSLICE / el, "unit": UNIT, "cores": workers, "kind": "port",
+            "sample": f"{nprobe} probes x {NSLICE} slices of the 512^2 SrTiO3 scan "
+                      f"(numpy/scipy oracle, FFT workers={workers}), {el:.1f} s"}
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    cfg = workload()
+    res = None
+    times = []
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        res = cpu_baseline(cfg, args.cpu_probes)
+        if i >= args.warmup:
+            times.append(res["value"])
+    value = float(np.median(times))
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "c64/f32", "data": "synthetic (SrTiO3 on ideal sites, seeded raster)",
+        "impl": "reference",
+        "config": {"workload": "SrTiO3 [001] 8x8x50 cells, 512x512, 100 slices, 200 kV, "
+                               "25 mrad probe, 64x64 raster (4096 probes), HAADF 80-200 + ABF 11-22 mrad",
+                   "sample_probes_per_step": args.cpu_probes},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": res["cores"], "kind": "port",
+                         "sample": res["sample"]},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-probes", type=int, default=32)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,190 @@
+/*
+ * msl.h — C ABI of the GB300 multislice library (libmsl.so).
+ *
+ * The library replaces the reference's hot path on one GPU:
+ *   projected potential  ->  per-slice transmit / 2D FFT / Fresnel propagate /
+ *   inverse FFT          ->  STEM annular detection.
+ * Every entry point is a plain C function over plain pointers and sizes; no
+ * CUDA or framework type appears in a signature.  Buffers are owned by the
+ * caller and may live in host memory or in device memory of the context's GPU:
+ * the library inspects each pointer (cudaPointerGetAttributes) and copies host
+ * buffers in and out itself.  Calls are synchronous: when one returns, its
+ * outputs are complete.  All calls return MSL_OK (0) or a negative MSL_E_*
+ * status; msl_last_error() gives the message of the context's last failure.
+ * One context per host thread; a context drives one GPU.
+ *
+ * Conventions (those of Kirkland's mulslice, ImageSimulation/multislice):
+ *   - a wave or image of nx*ny complex64 values is x-major: element (ix, iy)
+ *     sits at index iy + ix*ny (cfpix.hpp:99-125), stored as (re, im) floats;
+ *   - "fft" is exp(+2 pi i ...) and unscaled, "ifft" is exp(-2 pi i ...) and
+ *     scaled by 1/(nx*ny) (cfpix.cpp:115-230, FFTW_BACKWARD / FFTW_FORWARD);
+ *   - spatial frequency of index i is i/a for i <= (n/2 rounded), else (i-n)/a
+ *     (slicelib.cpp:433-463);
+ *   - lengths in Angstrom, energies in keV, angles in radians, potentials in
+ *     volt-Angstrom.
+ * Supported grid sides: 64, 128, 256, 384, 512, 768, 1024, 2048 (nx and ny
+ * chosen independently).
+ */
+#ifndef MSL_H
+#define MSL_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MSL_OK 0
+#define MSL_E_ARG (-1)        /* invalid argument (size, range, NaN, null)   */
+#define MSL_E_CUDA (-2)       /* a CUDA runtime call failed                  */
+#define MSL_E_NOMEM (-3)      /* device or host allocation failed            */
+#define MSL_E_UNSUPPORTED (-4) /* grid side or option not built              */
+
+#define MSL_MAX_DETECTORS 8
+
+typedef struct msl_ctx msl_ctx;
+
+/* Cell and sampling: nx x ny pixels over ax x by Angstrom. */
+typedef struct {
+    int nx, ny;
+    double ax, by;
+} msl_grid;
+
+/* Atom list (the .coo content after conversion to Cartesian Angstrom,
+ * amodel/include/ModelCoo.cpp:20-90).  z runs along the beam; cz is the
+ * specimen thickness that is cut into slices. */
+typedef struct {
+    int natom;
+    const double *x, *y, *z; /* Angstrom */
+    const int *Z;            /* atomic numbers 1..103 */
+    double cz;               /* thickness, Angstrom */
+} msl_atoms;
+
+/* Electron optics of the slice loop. */
+typedef struct {
+    double kev;          /* beam energy */
+    double bandlimit;    /* fraction of the Nyquist radius kept; 2/3 in mulslice.cpp:24 */
+    double tilt_x, tilt_y; /* crystal tilt (rad), mulslice.cpp:497-513 */
+    int f32_prop_args;   /* 0: propagator arguments in FP64 (default);
+                            1: built in float exactly as mulslice.cpp:499-513 */
+} msl_optics;
+
+/* Converged STEM probe (MSProject.cs:458-514), reciprocal lengths in 1/A. */
+typedef struct {
+    double k_in, k_out;  /* aperture: k_in^2 <= |k|^2 <= k_out^2 */
+    double df;           /* defocus, Angstrom */
+    double cs;           /* spherical aberration, Angstrom */
+} msl_probe;
+
+/* Annular detectors (MSProject.cs:792-842): detector d sums |Psi(k)|^2 over
+ * k_in[d]^2 <= |k|^2 <= k_out[d]^2 (1/A), bounds inclusive. */
+typedef struct {
+    int ndet;
+    const double *k_in, *k_out;
+} msl_detectors;
+
+/* ---------------------------------------------------------------- context */
+
+/* Create a context on CUDA device `device`.  Allocates the context's stream
+ * and lazily its work buffers.  Replaces the device set-up of
+ * LMultiSlice/Dispatcher.cu:191-207. */
+int msl_ctx_create(int device, msl_ctx **out);
+int msl_ctx_destroy(msl_ctx *ctx);
+/* Message of the last failed call on ctx (static string owned by ctx). */
+const char *msl_last_error(const msl_ctx *ctx);
+/* Library version string. */
+const char *msl_version(void);
+/* Number of kernels this context has launched since creation. */
+int64_t msl_kernel_launches(const msl_ctx *ctx);
+
+/* ------------------------------------------------------------ parameters */
+
+/* Parse FPARAMS.DAT text (ImageSimulation/parserFPARAMS/FPARAMS.DAT; reader
+ * parserFPARAMS/main.cpp:18-98) into tab[104*12]: row Z holds
+ * a1 b1 a2 b2 a3 b3 c1 d1 c2 d2 c3 d3, row 0 is zero. */
+int msl_fparams_parse(const char *text, size_t len, double *tab);
+
+/* Electron wavelength (A) and interaction constant sigma (rad/(kV*A)):
+ * slicelib.cpp:2795-2806 and :2387-2412. */
+double msl_wavelength(double kev);
+double msl_sigma(double kev);
+
+/* ------------------------------------------------------------- potential */
+
+/* Projected potential V_z of every slice: the PotentialBuilder step.
+ * Replaces ModelPotential::calculatePotentialGrid (LMultiSlice/ModelPotential.cu:27-99,
+ * kernel :125-230, atom form :232-292) with Kirkland's vzatom form
+ * (slicelib.cpp:2666-2716) and FPARAMS coefficients `fparams[104*12]`.
+ * Atoms are binned by floor(z / (cz/nslice)); those outside [0, cz) are
+ * dropped.  Each pixel sums, over the atoms of its slice, vzatom(Z, r) for the
+ * single minimum image with r < radius (r clamped below at 1e-10 A);
+ * radius must be below half of ax and of by.
+ * v_out: float [nslice][nx][ny] (host or device). */
+int msl_potential_build(msl_ctx *ctx, const msl_atoms *atoms, const double *fparams,
+                        const msl_grid *grid, int nslice, double radius, float *v_out);
+
+/* Band-limited transmission functions t = exp(i sigma V_z) of nlayer slices:
+ * mulslice.cpp:414-421 (phase), :515-522 (fft -> zero |k| beyond the band
+ * limit -> ifft).  The phase sigma*V is formed in FP64 before exponentiation.
+ * v: float [nlayer][nx][ny]; t_out: complex64 [nlayer][nx][ny]. */
+int msl_transmission_build(msl_ctx *ctx, const msl_grid *grid, const msl_optics *optics,
+                           const float *v, int nlayer, float *t_out);
+
+/* -------------------------------------------------------------- the FFT */
+
+/* In-place 2D transform of `batch` complex64 images, Kirkland's cfpix::fft
+ * (dir = +1: exp(+i), unscaled) or cfpix::ifft (dir = -1: exp(-i), x 1/(nx*ny))
+ * (cfpix.cpp:115-167). */
+int msl_fft2d(msl_ctx *ctx, const msl_grid *grid, float *psi, int batch, int dir);
+
+/* ------------------------------------------------------------ multislice */
+
+/* Coherent multislice of a batch of waves: for islice in 0..nslice-1 with
+ * l = layer_seq[islice]: psi *= trans[l]; fft; propagate with the separable
+ * Fresnel propagator of thickness dz[l] and the band limit; ifft
+ * (mulslice.cpp:706-739, propagate slicelib.cpp:744-790).  Replaces
+ * ModelSimulated::imageCalculation's slice loop (ModelSimulated.cu:52-119).
+ * trans: complex64 [ntrans][nx][ny]; dz: double [ntrans];
+ * psi: complex64 [batch][nx][ny], in: entrance waves, out: exit waves;
+ * psi == NULL is not allowed; to start from a plane wave of amplitude 1 pass
+ * plane_wave = 1 (psi is then output only). */
+int msl_multislice(msl_ctx *ctx, const msl_grid *grid, const msl_optics *optics,
+                   const float *trans, int ntrans, const double *dz,
+                   const int *layer_seq, int nslice, float *psi, int batch, int plane_wave);
+
+/* STEM scan and detect: for each probe position (x, y) in probe_xy[nprobe*2]
+ * build the converged probe (MSProject.cs:458-514), run the slice loop, and
+ * after the propagator of every slice listed in checkpoints[ncheck]
+ * (ascending, 0-based; MSReuseCalculator.cs:36-92) sum |Psi(k)|^2 over each
+ * annulus (MSProject.cs:792-842).  Sums are FP64 and in the reference's scale
+ * (unscaled forward transform of a wave whose reciprocal-space probe has unit
+ * amplitude inside the aperture).  det_out: double [nprobe][ncheck][ndet]. */
+int msl_stem_scan(msl_ctx *ctx, const msl_grid *grid, const msl_optics *optics,
+                  const float *trans, int ntrans, const double *dz, const int *layer_seq,
+                  int nslice, const msl_probe *probe, const double *probe_xy, int nprobe,
+                  const msl_detectors *det, const int *checkpoints, int ncheck,
+                  double *det_out);
+
+/* Per-kernel timing.  When enabled, every launch of the context is bracketed
+ * by CUDA events on the context's stream and its duration is added to the
+ * totals of its kind (row pass, column pass, potential, other).  Enabling
+ * resets the totals.  The reference times its phases the same way
+ * (ModelPotential.cu:46-50,92-96; ModelSimulated.cu:43-47,178-182). */
+#define MSL_PROF_ROW 0
+#define MSL_PROF_COL 1
+#define MSL_PROF_POTENTIAL 2
+#define MSL_PROF_OTHER 3
+#define MSL_PROF_KINDS 4
+int msl_profile_enable(msl_ctx *ctx, int on);
+int msl_profile_read(const msl_ctx *ctx, int kind, int64_t *launches, double *ms);
+
+/* Probe batch size used by msl_stem_scan (0 = automatic).  Work buffers are
+ * sized batch * nx * ny * 8 bytes. */
+int msl_set_probe_batch(msl_ctx *ctx, int batch);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MSL_H */

@@ -1,0 +1,94 @@
+"""ctypes binding of libmsl.so (include/msl.h).
+
+The library is built in-tree by multislice_gb300/build.py.  Loading fails loudly
+when it is missing: there is no CPU fallback anywhere in this package.
+"""
+import ctypes
+import os
+from ctypes import POINTER, c_char_p, c_double, c_int, c_int64, c_size_t, c_void_p
+
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libmsl.so")
+
+MSL_OK = 0
+MSL_E_ARG = -1
+MSL_E_CUDA = -2
+MSL_E_NOMEM = -3
+MSL_E_UNSUPPORTED = -4
+MAX_DETECTORS = 8
+
+# every symbol include/msl.h declares
+EXPORTS = (
+    "msl_ctx_create", "msl_ctx_destroy", "msl_last_error", "msl_version", "msl_kernel_launches",
+    "msl_fparams_parse", "msl_wavelength", "msl_sigma", "msl_potential_build",
+    "msl_transmission_build", "msl_fft2d", "msl_multislice", "msl_stem_scan",
+    "msl_set_probe_batch", "msl_profile_enable", "msl_profile_read",
+)
+PROF_ROW, PROF_COL, PROF_POTENTIAL, PROF_OTHER = 0, 1, 2, 3
+
+
+class Grid(ctypes.Structure):
+    _fields_ = [("nx", c_int), ("ny", c_int), ("ax", c_double), ("by", c_double)]
+
+
+class Atoms(ctypes.Structure):
+    _fields_ = [("natom", c_int), ("x", c_void_p), ("y", c_void_p), ("z", c_void_p),
+                ("Z", c_void_p), ("cz", c_double)]
+
+
+class Optics(ctypes.Structure):
+    _fields_ = [("kev", c_double), ("bandlimit", c_double), ("tilt_x", c_double),
+                ("tilt_y", c_double), ("f32_prop_args", c_int)]
+
+
+class Probe(ctypes.Structure):
+    _fields_ = [("k_in", c_double), ("k_out", c_double), ("df", c_double), ("cs", c_double)]
+
+
+class Detectors(ctypes.Structure):
+    _fields_ = [("ndet", c_int), ("k_in", c_void_p), ("k_out", c_void_p)]
+
+
+class MslError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"msl error {code}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def load(path=LIB_PATH):
+    """Load libmsl.so and declare every entry point's signature."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"libmsl.so not built ({path}); run multislice_gb300/build.py")
+    lib = ctypes.CDLL(path)
+    P = c_void_p
+    sig = {
+        "msl_ctx_create": (c_int, [c_int, POINTER(c_void_p)]),
+        "msl_ctx_destroy": (c_int, [P]),
+        "msl_last_error": (c_char_p, [P]),
+        "msl_version": (c_char_p, []),
+        "msl_kernel_launches": (c_int64, [P]),
+        "msl_fparams_parse": (c_int, [c_char_p, c_size_t, P]),
+        "msl_wavelength": (c_double, [c_double]),
+        "msl_sigma": (c_double, [c_double]),
+        "msl_potential_build": (c_int, [P, POINTER(Atoms), P, POINTER(Grid), c_int, c_double, P]),
+        "msl_transmission_build": (c_int, [P, POINTER(Grid), POINTER(Optics), P, c_int, P]),
+        "msl_fft2d": (c_int, [P, POINTER(Grid), P, c_int, c_int]),
+        "msl_multislice": (c_int, [P, POINTER(Grid), POINTER(Optics), P, c_int, P, P, c_int, P,
+                                   c_int, c_int]),
+        "msl_stem_scan": (c_int, [P, POINTER(Grid), POINTER(Optics), P, c_int, P, P, c_int,
+                                  POINTER(Probe), P, c_int, POINTER(Detectors), P, c_int, P]),
+        "msl_set_probe_batch": (c_int, [P, c_int]),
+        "msl_profile_enable": (c_int, [P, c_int]),
+        "msl_profile_read": (c_int, [P, c_int, POINTER(c_int64), POINTER(c_double)]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib

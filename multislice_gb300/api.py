@@ -1,0 +1,223 @@
+"""Python host mirror of the reference's multislice entry points over libmsl.so.
+
+Each method is a thin wrapper over one C-ABI call of include/msl.h.  Arrays are
+numpy arrays (host memory; the library copies them in and out) or CUDA tensors
+of the context's device (anything with ``data_ptr()``; used in place).
+
+Reference entry points mirrored here:
+  * ModelPotential::calculatePotentialGrid   -> Context.potential
+    (ImageSimulation/LMultiSlice/ModelPotential.cu:27-99)
+  * mulslice transmission set-up             -> Context.transmission
+    (ImageSimulation/multislice/mulslice.cpp:414-421, :515-522)
+  * cfpix::fft / cfpix::ifft                  -> Context.fft2d (cfpix.cpp:115-167)
+  * mulslice coherent loop / ModelSimulated   -> Context.multislice
+    (mulslice.cpp:706-739; LMultiSlice/ModelSimulated.cu:52-119)
+  * MSProjectReuse.StartCalculations STEM loop -> Context.stem_scan
+    (Musli console 1.3 (STEM) 2/MSProjectReuse.cs:170-362)
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import _abi
+from ._abi import Atoms, Detectors, Grid, MslError, Optics, Probe
+
+_DATA = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data")
+
+
+def fparams_table():
+    """Kirkland's FPARAMS coefficients (104 x 12, row Z), as shipped in the reference."""
+    return np.load(os.path.join(_DATA, "fparams.npy"))
+
+
+def _is_device(a):
+    return hasattr(a, "data_ptr") and getattr(getattr(a, "device", None), "type", "cpu") == "cuda"
+
+
+def _ptr(a, dtype):
+    """c_void_p for a C-contiguous numpy array of `dtype` or a contiguous CUDA tensor."""
+    if _is_device(a):
+        if not a.is_contiguous():
+            raise ValueError("device tensors must be contiguous")
+        return ctypes.c_void_p(a.data_ptr())
+    if not isinstance(a, np.ndarray) or a.dtype != dtype or not a.flags.c_contiguous:
+        raise ValueError(f"expected a C-contiguous numpy array of {np.dtype(dtype)}")
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def _cshape(a):
+    """Shape of a complex array; a float CUDA tensor with a trailing dim of 2 counts as complex."""
+    if _is_device(a) and not a.is_complex() and a.shape[-1] == 2:
+        return tuple(a.shape[:-1])
+    return tuple(a.shape)
+
+
+def _as(a, dtype):
+    if _is_device(a):
+        return a
+    return np.ascontiguousarray(a, dtype=dtype)
+
+
+class Context:
+    """One GPU, one stream: wraps msl_ctx."""
+
+    def __init__(self, device=0):
+        self._lib = _abi.load()
+        h = ctypes.c_void_p()
+        rc = self._lib.msl_ctx_create(int(device), ctypes.byref(h))
+        if rc != _abi.MSL_OK:
+            raise MslError(rc, f"msl_ctx_create(device={device}) failed")
+        self._h = h
+        self.device = device
+
+    # -------------------------------------------------------------- plumbing
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.msl_ctx_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != _abi.MSL_OK:
+            raise MslError(rc, self._lib.msl_last_error(self._h).decode())
+
+    @property
+    def launches(self):
+        """Kernels launched by this context so far."""
+        return int(self._lib.msl_kernel_launches(self._h))
+
+    def profile(self, on=True):
+        """Enable (and reset) per-kernel-kind event timing on the context's stream."""
+        self._check(self._lib.msl_profile_enable(self._h, 1 if on else 0))
+
+    def profile_read(self):
+        """{kind: (launches, total ms)} for row, col, potential, other."""
+        out = {}
+        for k, name in enumerate(("row", "col", "potential", "other")):
+            n = ctypes.c_int64()
+            ms = ctypes.c_double()
+            self._check(self._lib.msl_profile_read(self._h, k, ctypes.byref(n), ctypes.byref(ms)))
+            out[name] = (int(n.value), float(ms.value))
+        return out
+
+    def set_probe_batch(self, batch):
+        self._check(self._lib.msl_set_probe_batch(self._h, int(batch)))
+
+    @staticmethod
+    def _optics(kev, bandlimit=2.0 / 3.0, tilt=(0.0, 0.0), f32_prop_args=False):
+        return Optics(float(kev), float(bandlimit), float(tilt[0]), float(tilt[1]),
+                      1 if f32_prop_args else 0)
+
+    # ------------------------------------------------------------- potential
+    def potential(self, spec, nx, ny, nslice, radius, fparams=None, out=None):
+        """Projected potential V_z (V*A) per slice, float32 [nslice, nx, ny]."""
+        fp = np.ascontiguousarray(fparams_table() if fparams is None else fparams, np.float64)
+        x = np.ascontiguousarray(spec.x, np.float64)
+        y = np.ascontiguousarray(spec.y, np.float64)
+        z = np.ascontiguousarray(spec.z, np.float64)
+        Z = np.ascontiguousarray(spec.Z, np.int32)
+        at = Atoms(len(x), x.ctypes.data, y.ctypes.data, z.ctypes.data, Z.ctypes.data, float(spec.cz))
+        g = Grid(int(nx), int(ny), float(spec.ax), float(spec.by))
+        if out is None:
+            out = np.empty((nslice, nx, ny), np.float32)
+        self._check(self._lib.msl_potential_build(self._h, ctypes.byref(at), _ptr(fp, np.float64),
+                                                  ctypes.byref(g), int(nslice), float(radius),
+                                                  _ptr(out, np.float32)))
+        return out
+
+    # ---------------------------------------------------------- transmission
+    def transmission(self, v, ax, by, kev, bandlimit=2.0 / 3.0, out=None):
+        """Band-limited exp(i sigma V) per layer, complex64 [nlayer, nx, ny]."""
+        v = _as(v, np.float32)
+        nl, nx, ny = v.shape
+        g = Grid(nx, ny, float(ax), float(by))
+        o = self._optics(kev, bandlimit)
+        if out is None:
+            out = np.empty((nl, nx, ny), np.complex64)
+        self._check(self._lib.msl_transmission_build(self._h, ctypes.byref(g), ctypes.byref(o),
+                                                     _ptr(v, np.float32), nl, _ptr(out, np.complex64)))
+        return out
+
+    # ------------------------------------------------------------------- fft
+    def fft2d(self, psi, ax, by, direction):
+        """In-place Kirkland fft (+1, exp(+i), unscaled) or ifft (-1, exp(-i), 1/(nx ny))."""
+        shp = _cshape(psi)
+        nx, ny = shp[-2], shp[-1]
+        batch = int(np.prod(shp[:-2])) if len(shp) > 2 else 1
+        g = Grid(nx, ny, float(ax), float(by))
+        self._check(self._lib.msl_fft2d(self._h, ctypes.byref(g), _ptr(psi, np.complex64), batch,
+                                        int(direction)))
+        return psi
+
+    # ------------------------------------------------------------ multislice
+    def multislice(self, trans, dz, layer_seq, ax, by, kev, psi=None, batch=1,
+                   bandlimit=2.0 / 3.0, tilt=(0.0, 0.0), f32_prop_args=False):
+        """Exit waves of the coherent slice loop; psi=None starts from a plane wave."""
+        trans = _as(trans, np.complex64)
+        nt, nx, ny = _cshape(trans)
+        dz = np.ascontiguousarray(np.broadcast_to(np.asarray(dz, np.float64), (nt,)))
+        seq = np.ascontiguousarray(layer_seq, np.int32)
+        g = Grid(nx, ny, float(ax), float(by))
+        o = self._optics(kev, bandlimit, tilt, f32_prop_args)
+        plane = psi is None
+        if plane:
+            psi = np.empty((batch, nx, ny), np.complex64)
+        else:
+            shp = _cshape(psi)
+            batch = int(np.prod(shp[:-2])) if len(shp) > 2 else 1
+        self._check(self._lib.msl_multislice(self._h, ctypes.byref(g), ctypes.byref(o),
+                                             _ptr(trans, np.complex64), nt, _ptr(dz, np.float64),
+                                             _ptr(seq, np.int32), len(seq), _ptr(psi, np.complex64),
+                                             batch, 1 if plane else 0))
+        return psi
+
+    # ------------------------------------------------------------------ STEM
+    def stem_scan(self, trans, dz, layer_seq, ax, by, kev, k_ap, probe_xy, det_k,
+                  checkpoints=None, df=0.0, cs=0.0, k_ap_in=0.0, bandlimit=2.0 / 3.0,
+                  f32_prop_args=False, out=None):
+        """Annular detector sums, float64 [nprobe, ncheck, ndet] (reference scale)."""
+        trans = _as(trans, np.complex64)
+        nt, nx, ny = _cshape(trans)
+        dz = np.ascontiguousarray(np.broadcast_to(np.asarray(dz, np.float64), (nt,)))
+        seq = np.ascontiguousarray(layer_seq, np.int32)
+        if checkpoints is None:
+            checkpoints = [len(seq) - 1]
+        cps = np.ascontiguousarray(checkpoints, np.int32)
+        xy = np.ascontiguousarray(probe_xy, np.float64).reshape(-1, 2)
+        det = np.asarray(det_k, np.float64).reshape(-1, 2)
+        kin = np.ascontiguousarray(det[:, 0])
+        kout = np.ascontiguousarray(det[:, 1])
+        dets = Detectors(len(det), kin.ctypes.data, kout.ctypes.data)
+        pr = Probe(float(k_ap_in), float(k_ap), float(df), float(cs))
+        g = Grid(nx, ny, float(ax), float(by))
+        o = self._optics(kev, bandlimit, (0.0, 0.0), f32_prop_args)
+        if out is None:
+            out = np.empty((len(xy), len(cps), len(det)), np.float64)
+        self._check(self._lib.msl_stem_scan(self._h, ctypes.byref(g), ctypes.byref(o),
+                                            _ptr(trans, np.complex64), nt, _ptr(dz, np.float64),
+                                            _ptr(seq, np.int32), len(seq), ctypes.byref(pr),
+                                            _ptr(xy, np.float64), len(xy), ctypes.byref(dets),
+                                            _ptr(cps, np.int32), len(cps), _ptr(out, np.float64)))
+        return out
+
+
+def wavelength(kev):
+    return _abi.load().msl_wavelength(float(kev))
+
+
+def sigma(kev):
+    return _abi.load().msl_sigma(float(kev))

@@ -1,0 +1,795 @@
+// C ABI of libmsl.so: validation, buffer staging and pass sequencing on the host.
+// Kernels live in msl_passes.cu and msl_potential.cu; the ABI is declared in
+// include/msl.h.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/msl.h"
+#include "msl_internal.h"
+
+using msl::ColArgs;
+using msl::RowArgs;
+
+namespace {
+
+const char kVersion[] = "msl 0.1 (sm_103a)";
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t bytes) {
+        if (bytes <= cap) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        cudaError_t e = cudaMalloc(&p, bytes ? bytes : 1);
+        if (e == cudaSuccess) cap = bytes;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
+}  // namespace
+
+struct msl_ctx {
+    int device = 0;
+    int nsm = 1;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    int64_t launches = 0;
+    int probe_batch = 0;
+    std::map<int, float2 *> tw;
+    // optional per-kernel-kind timing with events on the context's stream
+    bool prof = false;
+    std::vector<cudaEvent_t> ev_free;
+    struct Pending { int kind; cudaEvent_t a, b; };
+    std::vector<Pending> pending;
+    int64_t prof_count[MSL_PROF_KINDS] = {0};
+    double prof_ms[MSL_PROF_KINDS] = {0};
+    DevBuf wave, in_stage, trans_stage, tabs, apchi, exy, fxy, detmask, partial, detout, pot,
+        atoms;
+};
+
+namespace {
+
+int fail(msl_ctx *c, int code, const std::string &msg) {
+    if (c) c->err = msg;
+    return code;
+}
+
+cudaEvent_t take_event(msl_ctx *c) {
+    if (!c->ev_free.empty()) {
+        cudaEvent_t e = c->ev_free.back();
+        c->ev_free.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+// Bracket one launch with events when profiling is on.
+template <class F> cudaError_t timed(msl_ctx *c, int kind, F &&launch) {
+    if (!c->prof) return launch();
+    cudaEvent_t a = take_event(c), b = take_event(c);
+    cudaEventRecord(a, c->stream);
+    cudaError_t e = launch();
+    cudaEventRecord(b, c->stream);
+    c->pending.push_back({kind, a, b});
+    return e;
+}
+
+// Fold finished launch timings into the per-kind totals (stream is synchronized).
+void collect_profile(msl_ctx *c) {
+    for (auto &p : c->pending) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+            c->prof_count[p.kind] += 1;
+            c->prof_ms[p.kind] += ms;
+        }
+        c->ev_free.push_back(p.a);
+        c->ev_free.push_back(p.b);
+    }
+    c->pending.clear();
+}
+
+#define CUDA_TRY(ctx, call)                                                                  \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess)                                                               \
+            return fail(ctx, e_ == cudaErrorMemoryAllocation ? MSL_E_NOMEM : MSL_E_CUDA,      \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                \
+    } while (0)
+
+bool on_device(const void *p) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+bool is_fin(double x) { return std::isfinite(x); }
+
+int check_grid(msl_ctx *c, const msl_grid *g) {
+    if (!g) return fail(c, MSL_E_ARG, "grid is null");
+    if (!msl::plan_supported(g->nx) || !msl::plan_supported(g->ny))
+        return fail(c, MSL_E_UNSUPPORTED,
+                    "grid side not supported (64,128,256,384,512,768,1024,2048): " +
+                        std::to_string(g->nx) + "x" + std::to_string(g->ny));
+    if (!(g->ax > 0) || !(g->by > 0) || !is_fin(g->ax) || !is_fin(g->by))
+        return fail(c, MSL_E_ARG, "cell size must be positive and finite");
+    return MSL_OK;
+}
+
+int check_optics(msl_ctx *c, const msl_optics *o) {
+    if (!o) return fail(c, MSL_E_ARG, "optics is null");
+    if (!(o->kev > 0) || !is_fin(o->kev)) return fail(c, MSL_E_ARG, "beam energy must be positive");
+    if (!(o->bandlimit > 0) || o->bandlimit > 1.0)
+        return fail(c, MSL_E_ARG, "bandlimit must lie in (0, 1]");
+    if (!is_fin(o->tilt_x) || !is_fin(o->tilt_y)) return fail(c, MSL_E_ARG, "tilt must be finite");
+    return MSL_OK;
+}
+
+// Spatial frequencies in float exactly as freqn() (slicelib.cpp:433-463).
+void freqn_f32(int n, double a, std::vector<float> &k, std::vector<float> &k2) {
+    k.resize(n);
+    k2.resize(n);
+    const int imid = (int)(n / 2.0 + 0.5);
+    for (int i = 0; i < n; ++i) {
+        const float num = (float)(i > imid ? i - n : i);
+        k[i] = num / (float)a;
+        k2[i] = k[i] * k[i];
+    }
+}
+
+// Squared band limit in float as mulslice.cpp:481-489.
+float k2max_f32(int nx, int ny, double ax, double by, double bw) {
+    float k = (float)nx / (2.0F * (float)ax);
+    float t = (float)ny / (2.0F * (float)by);
+    if (t < k) k = t;
+    k = (float)bw * k;
+    return k * k;
+}
+
+// Propagator tables of one slice thickness (mulslice.cpp:494-513): px, py with
+// py already carrying the ifft scale 1/(nx ny).
+void prop_tables(int nx, int ny, double ax, double by, const msl_optics *o, double dz,
+                 const std::vector<float> &kx, const std::vector<float> &kx2,
+                 const std::vector<float> &ky, const std::vector<float> &ky2, float2 *px,
+                 float2 *py) {
+    const float scale = 1.0f / ((float)nx * (float)ny);
+    const double lam = msl_wavelength(o->kev);
+    if (o->f32_prop_args) {
+        const float wl = (float)lam;
+        const float sc = (float)(4.0 * atan(1.0)) * (float)dz;
+        const float tctx = (float)(2.0 * tan(o->tilt_x)), tcty = (float)(2.0 * tan(o->tilt_y));
+        for (int i = 0; i < nx; ++i) {
+            const double t = sc * (kx2[i] * wl - kx[i] * tctx);
+            px[i] = make_float2((float)cos(t), (float)-sin(t));
+        }
+        for (int i = 0; i < ny; ++i) {
+            const double t = sc * (ky2[i] * wl - ky[i] * tcty);
+            py[i] = make_float2((float)cos(t) * scale, (float)-sin(t) * scale);
+        }
+        return;
+    }
+    const double pi = 3.14159265358979323846;
+    const double ttx = 2.0 * tan(o->tilt_x), tty = 2.0 * tan(o->tilt_y);
+    for (int i = 0; i < nx; ++i) {
+        const double k = kx[i];
+        const double t = pi * dz * (k * k * lam - k * ttx);
+        px[i] = make_float2((float)cos(t), (float)-sin(t));
+    }
+    for (int i = 0; i < ny; ++i) {
+        const double k = ky[i];
+        const double t = pi * dz * (k * k * lam - k * tty);
+        py[i] = make_float2((float)cos(t) * scale, (float)-sin(t) * scale);
+    }
+}
+
+float2 *twiddles(msl_ctx *c, int n) {
+    auto it = c->tw.find(n);
+    if (it != c->tw.end()) return it->second;
+    std::vector<float2> h;
+    msl::plan_twiddles(n, h);
+    float2 *d = nullptr;
+    if (cudaMalloc(&d, h.size() * sizeof(float2)) != cudaSuccess) return nullptr;
+    if (cudaMemcpy(d, h.data(), h.size() * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaFree(d);
+        return nullptr;
+    }
+    c->tw[n] = d;
+    return d;
+}
+
+// Device view of a caller buffer: the pointer itself if it is device memory,
+// else a staging buffer (copied in when `copy_in`).
+template <class T>
+int stage_in(msl_ctx *c, const T *p, size_t bytes, DevBuf &st, const T **out, bool copy_in = true) {
+    if (on_device(p)) {
+        *out = p;
+        return MSL_OK;
+    }
+    CUDA_TRY(c, st.ensure(bytes));
+    if (copy_in) CUDA_TRY(c, cudaMemcpyAsync(st.p, p, bytes, cudaMemcpyHostToDevice, c->stream));
+    *out = (const T *)st.p;
+    return MSL_OK;
+}
+
+int upload(msl_ctx *c, DevBuf &b, const void *h, size_t bytes) {
+    CUDA_TRY(c, b.ensure(bytes));
+    CUDA_TRY(c, cudaMemcpyAsync(b.p, h, bytes, cudaMemcpyHostToDevice, c->stream));
+    return MSL_OK;
+}
+
+struct SliceTables {
+    std::vector<float> kx, kx2, ky, ky2;
+    float k2max;
+    // device layout: kx2[nx] ky2[ny] | px py per layer
+    float *d_kx2, *d_ky2;
+    float2 *d_prop;  // [ntrans][nx + ny]
+};
+
+int build_slice_tables(msl_ctx *c, const msl_grid *g, const msl_optics *o, int ntrans,
+                       const double *dz, SliceTables &st) {
+    const int nx = g->nx, ny = g->ny;
+    freqn_f32(nx, g->ax, st.kx, st.kx2);
+    freqn_f32(ny, g->by, st.ky, st.ky2);
+    st.k2max = k2max_f32(nx, ny, g->ax, g->by, o->bandlimit);
+    const size_t fbytes = sizeof(float) * (nx + ny);
+    const size_t pbytes = sizeof(float2) * (size_t)ntrans * (nx + ny);
+    std::vector<unsigned char> h(fbytes + pbytes);
+    memcpy(h.data(), st.kx2.data(), sizeof(float) * nx);
+    memcpy(h.data() + sizeof(float) * nx, st.ky2.data(), sizeof(float) * ny);
+    float2 *hp = (float2 *)(h.data() + fbytes);
+    for (int l = 0; l < ntrans; ++l) {
+        if (dz) {
+            prop_tables(nx, ny, g->ax, g->by, o, dz[l], st.kx, st.kx2, st.ky, st.ky2,
+                        hp + (size_t)l * (nx + ny), hp + (size_t)l * (nx + ny) + nx);
+        } else {  // identity propagator: band limit and ifft scale only
+            const float scale = 1.0f / ((float)nx * (float)ny);
+            for (int i = 0; i < nx; ++i) hp[(size_t)l * (nx + ny) + i] = make_float2(1.f, 0.f);
+            for (int i = 0; i < ny; ++i) hp[(size_t)l * (nx + ny) + nx + i] = make_float2(scale, 0.f);
+        }
+    }
+    int rc = upload(c, c->tabs, h.data(), h.size());
+    if (rc) return rc;
+    st.d_kx2 = (float *)c->tabs.p;
+    st.d_ky2 = st.d_kx2 + nx;
+    st.d_prop = (float2 *)((unsigned char *)c->tabs.p + fbytes);
+    return MSL_OK;
+}
+
+ColArgs col_args(const msl_grid *g, const SliceTables &st, float2 *tw, int layer, float2 *wave,
+                 int batch, int flags) {
+    ColArgs a;
+    memset(&a, 0, sizeof(a));
+    a.in = wave;
+    a.out = wave;
+    a.batch = batch;
+    a.ny = g->ny;
+    a.tw = tw;
+    a.flags = flags;
+    a.px = st.d_prop + (size_t)layer * (g->nx + g->ny);
+    a.py = a.px + g->nx;
+    a.kx2 = st.d_kx2;
+    a.ky2 = st.d_ky2;
+    a.k2max = st.k2max;
+    return a;
+}
+
+RowArgs row_args(const msl_grid *g, float2 *tw, const float2 *trans, float2 *wave, int batch,
+                 int flags) {
+    RowArgs a;
+    memset(&a, 0, sizeof(a));
+    a.in = wave;
+    a.out = wave;
+    a.nlines = batch * g->nx;
+    a.nx = g->nx;
+    a.trans = trans;
+    a.tw = tw;
+    a.flags = flags;
+    a.scale = 1.0f;
+    return a;
+}
+
+#define LAUNCH_TRY(ctx, call)                                                                \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess)                                                               \
+            return fail(ctx, MSL_E_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e_)); \
+    } while (0)
+
+int check_layers(msl_ctx *c, int ntrans, const double *dz, const int *layer_seq, int nslice) {
+    if (ntrans < 1) return fail(c, MSL_E_ARG, "ntrans must be >= 1");
+    if (nslice < 1) return fail(c, MSL_E_ARG, "nslice must be >= 1");
+    if (!dz || !layer_seq) return fail(c, MSL_E_ARG, "dz and layer_seq are required");
+    for (int l = 0; l < ntrans; ++l)
+        if (!(dz[l] > 0) || !is_fin(dz[l])) return fail(c, MSL_E_ARG, "slice thickness must be positive");
+    for (int s = 0; s < nslice; ++s)
+        if (layer_seq[s] < 0 || layer_seq[s] >= ntrans)
+            return fail(c, MSL_E_ARG, "layer_seq entry out of range at slice " + std::to_string(s));
+    return MSL_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *msl_version(void) { return kVersion; }
+
+double msl_wavelength(double kev) {
+    const double emass = 510.99906, hc = 12.3984244;
+    return hc / sqrt(kev * (2.0 * emass + kev));
+}
+
+double msl_sigma(double kev) {
+    const double emass = 510.99906;
+    const double x = (emass + kev) / (2.0 * emass + kev);
+    return 2.0 * (4.0 * atan(1.0)) * x / (msl_wavelength(kev) * kev);
+}
+
+int msl_ctx_create(int device, msl_ctx **out) {
+    if (!out) return MSL_E_ARG;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+        cudaGetLastError();
+        return MSL_E_CUDA;
+    }
+    if (device < 0 || device >= ndev) return MSL_E_ARG;
+    msl_ctx *c = new msl_ctx();
+    c->device = device;
+    if (cudaSetDevice(device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete c;
+        return MSL_E_CUDA;
+    }
+    *out = c;
+    return MSL_OK;
+}
+
+int msl_ctx_destroy(msl_ctx *c) {
+    if (!c) return MSL_E_ARG;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    for (auto &kv : c->tw) cudaFree(kv.second);
+    DevBuf *bufs[] = {&c->wave, &c->in_stage, &c->trans_stage, &c->tabs, &c->apchi, &c->exy,
+                      &c->fxy, &c->detmask, &c->partial, &c->detout, &c->pot, &c->atoms};
+    for (DevBuf *b : bufs) b->release();
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return MSL_OK;
+}
+
+const char *msl_last_error(const msl_ctx *c) { return c ? c->err.c_str() : "null context"; }
+
+int64_t msl_kernel_launches(const msl_ctx *c) { return c ? c->launches : 0; }
+
+int msl_profile_enable(msl_ctx *c, int on) {
+    if (!c) return MSL_E_ARG;
+    c->prof = on != 0;
+    for (int k = 0; k < MSL_PROF_KINDS; ++k) {
+        c->prof_count[k] = 0;
+        c->prof_ms[k] = 0.0;
+    }
+    return MSL_OK;
+}
+
+int msl_profile_read(const msl_ctx *c, int kind, int64_t *launches, double *ms) {
+    if (!c || kind < 0 || kind >= MSL_PROF_KINDS || !launches || !ms) return MSL_E_ARG;
+    *launches = c->prof_count[kind];
+    *ms = c->prof_ms[kind];
+    return MSL_OK;
+}
+
+int msl_set_probe_batch(msl_ctx *c, int batch) {
+    if (!c || batch < 0) return fail(c, MSL_E_ARG, "probe batch must be >= 0");
+    c->probe_batch = batch;
+    return MSL_OK;
+}
+
+int msl_fparams_parse(const char *text, size_t len, double *tab) {
+    if (!text || !tab) return MSL_E_ARG;
+    std::string s(text, len);
+    memset(tab, 0, sizeof(double) * 104 * 12);
+    size_t pos = 0;
+    int seen = 0;
+    while ((pos = s.find("Z=", pos)) != std::string::npos) {
+        int z = atoi(s.c_str() + pos + 2);
+        size_t eol = s.find('\n', pos);
+        if (eol == std::string::npos) return MSL_E_ARG;
+        const char *p = s.c_str() + eol + 1;
+        double v[12];
+        for (int i = 0; i < 12; ++i) {
+            char *end = nullptr;
+            v[i] = strtod(p, &end);
+            if (end == p) return MSL_E_ARG;
+            p = end;
+        }
+        if (z < 1 || z > 103) return MSL_E_ARG;
+        for (int i = 0; i < 12; ++i) tab[z * 12 + i] = v[i];
+        ++seen;
+        pos = (size_t)(p - s.c_str());
+    }
+    return seen == 103 ? MSL_OK : MSL_E_ARG;
+}
+
+int msl_potential_build(msl_ctx *c, const msl_atoms *at, const double *fparams, const msl_grid *g,
+                        int nslice, double radius, float *v_out) {
+    if (!c) return MSL_E_ARG;
+    int rc = check_grid(c, g);
+    if (rc) return rc;
+    if (!at || !fparams || !v_out) return fail(c, MSL_E_ARG, "null argument");
+    if (nslice < 1) return fail(c, MSL_E_ARG, "nslice must be >= 1");
+    if (!(at->cz > 0) || !is_fin(at->cz)) return fail(c, MSL_E_ARG, "thickness cz must be positive");
+    if (!(radius > 0) || !(2.0 * radius < g->ax) || !(2.0 * radius < g->by))
+        return fail(c, MSL_E_ARG, "cutoff radius must be positive and below half the cell");
+    if (at->natom < 0 || (at->natom > 0 && (!at->x || !at->y || !at->z || !at->Z)))
+        return fail(c, MSL_E_ARG, "atom arrays are required");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    const int nx = g->nx, ny = g->ny;
+    const double dz = at->cz / nslice;
+    // bin by slice (stable, so the sum order inside a slice is the input order)
+    std::vector<int> kz(at->natom), count(nslice + 1, 0);
+    for (int i = 0; i < at->natom; ++i) {
+        if (!is_fin(at->x[i]) || !is_fin(at->y[i]) || !is_fin(at->z[i]))
+            return fail(c, MSL_E_ARG, "atom coordinates must be finite (atom " + std::to_string(i) + ")");
+        int k = (int)std::floor(at->z[i] / dz);
+        if (at->z[i] < 0.0 || k < 0 || k >= nslice) k = -1;
+        if (k >= 0 && (at->Z[i] < 1 || at->Z[i] > 103))
+            return fail(c, MSL_E_ARG, "atomic number out of range 1..103 (atom " + std::to_string(i) + ")");
+        kz[i] = k;
+        if (k >= 0) count[k + 1]++;
+    }
+    for (int k = 0; k < nslice; ++k) count[k + 1] += count[k];
+    const int nkeep = count[nslice];
+    std::vector<double> xs(nkeep > 0 ? nkeep : 1), ys(nkeep > 0 ? nkeep : 1);
+    std::vector<int> zs(nkeep > 0 ? nkeep : 1), fill(count.begin(), count.end() - 1);
+    bool used[104] = {false};
+    for (int i = 0; i < at->natom; ++i) {
+        if (kz[i] < 0) continue;
+        const int p = fill[kz[i]]++;
+        xs[p] = at->x[i] - g->ax * std::floor(at->x[i] / g->ax);
+        ys[p] = at->y[i] - g->by * std::floor(at->y[i] / g->by);
+        zs[p] = at->Z[i];
+        used[at->Z[i]] = true;
+    }
+    // per-species float parameters: A = AL a, B = 2 pi sqrt(b), C = AG c / d, D = pi^2 / d
+    // (constants of slicelib.cpp:2673-2674)
+    const double AL = 300.8242834, AG = 150.4121417, PIK = 3.141592654;
+    std::vector<float> sp(104 * 12, 0.f);
+    for (int z = 1; z <= 103; ++z) {
+        if (!used[z]) continue;
+        const double *f = fparams + z * 12;
+        for (int i = 0; i < 3; ++i) {
+            const double a = f[2 * i], b = f[2 * i + 1], cc = f[6 + 2 * i], d = f[7 + 2 * i];
+            if (!(b > 0) || !(d > 0) || !is_fin(a) || !is_fin(cc))
+                return fail(c, MSL_E_ARG, "invalid FPARAMS row for Z=" + std::to_string(z));
+            sp[z * 12 + 2 * i] = (float)(AL * a);
+            sp[z * 12 + 2 * i + 1] = (float)(2.0 * PIK * sqrt(b));
+            sp[z * 12 + 6 + 2 * i] = (float)(AG * cc / d);
+            sp[z * 12 + 7 + 2 * i] = (float)(PIK * PIK / d);
+        }
+    }
+    // one upload: off | x | y | Z | sp
+    const size_t o_off = 0, o_x = ((sizeof(int) * (nslice + 1) + 15) / 16) * 16;
+    const size_t o_y = o_x + sizeof(double) * xs.size(), o_z = o_y + sizeof(double) * ys.size();
+    const size_t o_sp = ((o_z + sizeof(int) * zs.size() + 15) / 16) * 16;
+    const size_t total = o_sp + sizeof(float) * sp.size();
+    std::vector<unsigned char> h(total, 0);
+    memcpy(h.data() + o_off, count.data(), sizeof(int) * (nslice + 1));
+    memcpy(h.data() + o_x, xs.data(), sizeof(double) * xs.size());
+    memcpy(h.data() + o_y, ys.data(), sizeof(double) * ys.size());
+    memcpy(h.data() + o_z, zs.data(), sizeof(int) * zs.size());
+    memcpy(h.data() + o_sp, sp.data(), sizeof(float) * sp.size());
+    rc = upload(c, c->atoms, h.data(), total);
+    if (rc) return rc;
+    unsigned char *d = (unsigned char *)c->atoms.p;
+    const size_t vbytes = sizeof(float) * (size_t)nslice * nx * ny;
+    float *vd;
+    const bool vdev = on_device(v_out);
+    if (vdev) {
+        vd = v_out;
+    } else {
+        CUDA_TRY(c, c->pot.ensure(vbytes));
+        vd = (float *)c->pot.p;
+    }
+    msl::PotArgs a;
+    a.x = (const double *)(d + o_x);
+    a.y = (const double *)(d + o_y);
+    a.Z = (const int *)(d + o_z);
+    a.off = (const int *)(d + o_off);
+    a.nslice = nslice;
+    a.nx = nx;
+    a.ny = ny;
+    a.ax = g->ax;
+    a.by = g->by;
+    a.dxp = g->ax / nx;
+    a.dyp = g->by / ny;
+    a.rad2 = (float)(radius * radius);
+    a.sp = (const float *)(d + o_sp);
+    a.v = vd;
+    LAUNCH_TRY(c, timed(c, MSL_PROF_POTENTIAL, [&] { return msl::launch_potential(a, c->stream, &c->launches); }));
+    if (!vdev) CUDA_TRY(c, cudaMemcpyAsync(v_out, vd, vbytes, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    collect_profile(c);
+    return MSL_OK;
+}
+
+int msl_transmission_build(msl_ctx *c, const msl_grid *g, const msl_optics *o, const float *v,
+                           int nlayer, float *t_out) {
+    if (!c) return MSL_E_ARG;
+    int rc = check_grid(c, g);
+    if (rc) return rc;
+    if ((rc = check_optics(c, o))) return rc;
+    if (!v || !t_out || nlayer < 1) return fail(c, MSL_E_ARG, "null argument or nlayer < 1");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    const int nx = g->nx, ny = g->ny;
+    const size_t n2 = (size_t)nx * ny;
+    const float *vd;
+    if ((rc = stage_in(c, v, sizeof(float) * n2 * nlayer, c->in_stage, &vd))) return rc;
+    float2 *td;
+    const bool tdev = on_device(t_out);
+    if (tdev) {
+        td = (float2 *)t_out;
+    } else {
+        CUDA_TRY(c, c->wave.ensure(sizeof(float2) * n2 * nlayer));
+        td = (float2 *)c->wave.p;
+    }
+    SliceTables st;
+    if ((rc = build_slice_tables(c, g, o, 1, nullptr, st))) return rc;
+    float2 *twr = twiddles(c, ny), *twc = twiddles(c, nx);
+    if (!twr || !twc) return fail(c, MSL_E_NOMEM, "twiddle table allocation failed");
+    RowArgs r = row_args(g, twr, nullptr, td, nlayer, msl::ROW_GENT | msl::ROW_FWD);
+    r.vpot = vd;
+    r.phase_scale = msl_sigma(o->kev) / 1000.0;  // rad per V*A
+    LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_row_pass(ny, r, c->stream, c->nsm, &c->launches); }));
+    ColArgs ca = col_args(g, st, twc, 0, td, nlayer,
+                          msl::COL_LOAD | msl::COL_FWD | msl::COL_PROP | msl::COL_INV | msl::COL_STORE);
+    LAUNCH_TRY(c, timed(c, MSL_PROF_COL, [&] { return msl::launch_col_pass(nx, ca, c->stream, c->nsm, &c->launches); }));
+    r = row_args(g, twr, nullptr, td, nlayer, msl::ROW_LOAD | msl::ROW_INV);
+    LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_row_pass(ny, r, c->stream, c->nsm, &c->launches); }));
+    if (!tdev)
+        CUDA_TRY(c, cudaMemcpyAsync(t_out, td, sizeof(float2) * n2 * nlayer, cudaMemcpyDeviceToHost,
+                                    c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    collect_profile(c);
+    return MSL_OK;
+}
+
+int msl_fft2d(msl_ctx *c, const msl_grid *g, float *psi, int batch, int dir) {
+    if (!c) return MSL_E_ARG;
+    int rc = check_grid(c, g);
+    if (rc) return rc;
+    if (!psi || batch < 1 || (dir != 1 && dir != -1))
+        return fail(c, MSL_E_ARG, "psi must be non-null, batch >= 1, dir = +1 or -1");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    const int nx = g->nx, ny = g->ny;
+    const size_t bytes = sizeof(float2) * (size_t)nx * ny * batch;
+    const bool dev = on_device(psi);
+    float2 *w;
+    if (dev) {
+        w = (float2 *)psi;
+    } else {
+        CUDA_TRY(c, c->wave.ensure(bytes));
+        w = (float2 *)c->wave.p;
+        CUDA_TRY(c, cudaMemcpyAsync(w, psi, bytes, cudaMemcpyHostToDevice, c->stream));
+    }
+    float2 *twr = twiddles(c, ny), *twc = twiddles(c, nx);
+    if (!twr || !twc) return fail(c, MSL_E_NOMEM, "twiddle table allocation failed");
+    SliceTables st;
+    memset(&st.k2max, 0, sizeof(st.k2max));
+    st.d_kx2 = nullptr;
+    st.d_ky2 = nullptr;
+    st.d_prop = nullptr;
+    if (dir > 0) {
+        RowArgs r = row_args(g, twr, nullptr, w, batch, msl::ROW_LOAD | msl::ROW_FWD);
+        LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_row_pass(ny, r, c->stream, c->nsm, &c->launches); }));
+        ColArgs ca = col_args(g, st, twc, 0, w, batch, msl::COL_LOAD | msl::COL_FWD | msl::COL_STORE);
+        LAUNCH_TRY(c, timed(c, MSL_PROF_COL, [&] { return msl::launch_col_pass(nx, ca, c->stream, c->nsm, &c->launches); }));
+    } else {
+        ColArgs ca = col_args(g, st, twc, 0, w, batch, msl::COL_LOAD | msl::COL_INV | msl::COL_STORE);
+        LAUNCH_TRY(c, timed(c, MSL_PROF_COL, [&] { return msl::launch_col_pass(nx, ca, c->stream, c->nsm, &c->launches); }));
+        RowArgs r = row_args(g, twr, nullptr, w, batch, msl::ROW_LOAD | msl::ROW_INV);
+        r.scale = 1.0f / ((float)nx * (float)ny);
+        LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_row_pass(ny, r, c->stream, c->nsm, &c->launches); }));
+    }
+    if (!dev) CUDA_TRY(c, cudaMemcpyAsync(psi, w, bytes, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    collect_profile(c);
+    return MSL_OK;
+}
+
+int msl_multislice(msl_ctx *c, const msl_grid *g, const msl_optics *o, const float *trans,
+                   int ntrans, const double *dz, const int *layer_seq, int nslice, float *psi,
+                   int batch, int plane_wave) {
+    if (!c) return MSL_E_ARG;
+    int rc = check_grid(c, g);
+    if (rc) return rc;
+    if ((rc = check_optics(c, o))) return rc;
+    if ((rc = check_layers(c, ntrans, dz, layer_seq, nslice))) return rc;
+    if (!trans || !psi || batch < 1) return fail(c, MSL_E_ARG, "trans/psi null or batch < 1");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    const int nx = g->nx, ny = g->ny;
+    const size_t n2 = (size_t)nx * ny;
+    const float2 *td;
+    if ((rc = stage_in(c, (const float2 *)trans, sizeof(float2) * n2 * ntrans, c->trans_stage, &td)))
+        return rc;
+    const bool dev = on_device(psi);
+    const size_t wbytes = sizeof(float2) * n2 * batch;
+    float2 *w;
+    if (dev) {
+        w = (float2 *)psi;
+    } else {
+        CUDA_TRY(c, c->wave.ensure(wbytes));
+        w = (float2 *)c->wave.p;
+        if (!plane_wave) CUDA_TRY(c, cudaMemcpyAsync(w, psi, wbytes, cudaMemcpyHostToDevice, c->stream));
+    }
+    SliceTables st;
+    if ((rc = build_slice_tables(c, g, o, ntrans, dz, st))) return rc;
+    float2 *twr = twiddles(c, ny), *twc = twiddles(c, nx);
+    if (!twr || !twc) return fail(c, MSL_E_NOMEM, "twiddle table allocation failed");
+    const int colf = msl::COL_LOAD | msl::COL_FWD | msl::COL_PROP | msl::COL_INV | msl::COL_STORE;
+    for (int s = 0; s < nslice; ++s) {
+        const int l = layer_seq[s];
+        int rf = msl::ROW_TRANS | msl::ROW_FWD;
+        if (s > 0) rf |= msl::ROW_LOAD | msl::ROW_INV;
+        else if (!plane_wave) rf |= msl::ROW_LOAD;
+        RowArgs r = row_args(g, twr, td + (size_t)l * n2, w, batch, rf);
+        LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_row_pass(ny, r, c->stream, c->nsm, &c->launches); }));
+        ColArgs ca = col_args(g, st, twc, l, w, batch, colf);
+        LAUNCH_TRY(c, timed(c, MSL_PROF_COL, [&] { return msl::launch_col_pass(nx, ca, c->stream, c->nsm, &c->launches); }));
+    }
+    RowArgs r = row_args(g, twr, nullptr, w, batch, msl::ROW_LOAD | msl::ROW_INV);
+    LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_row_pass(ny, r, c->stream, c->nsm, &c->launches); }));
+    if (!dev) CUDA_TRY(c, cudaMemcpyAsync(psi, w, wbytes, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    collect_profile(c);
+    return MSL_OK;
+}
+
+int msl_stem_scan(msl_ctx *c, const msl_grid *g, const msl_optics *o, const float *trans,
+                  int ntrans, const double *dz, const int *layer_seq, int nslice,
+                  const msl_probe *pr, const double *probe_xy, int nprobe,
+                  const msl_detectors *det, const int *checkpoints, int ncheck, double *det_out) {
+    if (!c) return MSL_E_ARG;
+    int rc = check_grid(c, g);
+    if (rc) return rc;
+    if ((rc = check_optics(c, o))) return rc;
+    if ((rc = check_layers(c, ntrans, dz, layer_seq, nslice))) return rc;
+    if (!trans || !pr || !probe_xy || !det || !checkpoints || !det_out)
+        return fail(c, MSL_E_ARG, "null argument");
+    if (nprobe < 1) return fail(c, MSL_E_ARG, "nprobe must be >= 1");
+    if (det->ndet < 1 || det->ndet > MSL_MAX_DETECTORS || !det->k_in || !det->k_out)
+        return fail(c, MSL_E_ARG, "1..8 detectors with k_in/k_out arrays are required");
+    for (int d = 0; d < det->ndet; ++d)
+        if (!(det->k_in[d] >= 0) || !(det->k_out[d] >= det->k_in[d]) || !is_fin(det->k_out[d]))
+            return fail(c, MSL_E_ARG, "detector bounds must satisfy 0 <= k_in <= k_out");
+    if (!(pr->k_in >= 0) || !(pr->k_out > pr->k_in) || !is_fin(pr->k_out) || !is_fin(pr->df) ||
+        !is_fin(pr->cs))
+        return fail(c, MSL_E_ARG, "probe aperture must satisfy 0 <= k_in < k_out; df, cs finite");
+    if (ncheck < 1) return fail(c, MSL_E_ARG, "ncheck must be >= 1");
+    for (int i = 0; i < ncheck; ++i)
+        if (checkpoints[i] < 0 || checkpoints[i] >= nslice || (i > 0 && checkpoints[i] <= checkpoints[i - 1]))
+            return fail(c, MSL_E_ARG, "checkpoints must be ascending slice indices in [0, nslice)");
+    for (int p = 0; p < 2 * nprobe; ++p)
+        if (!is_fin(probe_xy[p])) return fail(c, MSL_E_ARG, "probe positions must be finite");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    const int nx = g->nx, ny = g->ny, ndet = det->ndet;
+    const size_t n2 = (size_t)nx * ny;
+    const int C = msl::plan_col_c(nx);
+    const int ntile = ny / C;
+    const float2 *td;
+    if ((rc = stage_in(c, (const float2 *)trans, sizeof(float2) * n2 * ntrans, c->trans_stage, &td)))
+        return rc;
+    SliceTables st;
+    if ((rc = build_slice_tables(c, g, o, ntrans, dz, st))) return rc;
+    float2 *twr = twiddles(c, ny), *twc = twiddles(c, nx);
+    if (!twr || !twc) return fail(c, MSL_E_NOMEM, "twiddle table allocation failed");
+
+    // reciprocal coordinates (double) of MSProject.cs:470-484 and detector bounds
+    std::vector<double> hk(nx + ny + 2 * ndet);
+    for (int i = 0; i < nx; ++i) hk[i] = (double)(i < nx / 2 ? i : i - nx) / g->ax;
+    for (int i = 0; i < ny; ++i) hk[nx + i] = (double)(i < ny / 2 ? i : i - ny) / g->by;
+    for (int d = 0; d < ndet; ++d) {
+        hk[nx + ny + d] = det->k_in[d] * det->k_in[d];
+        hk[nx + ny + ndet + d] = det->k_out[d] * det->k_out[d];
+    }
+    if ((rc = upload(c, c->fxy, hk.data(), sizeof(double) * hk.size()))) return rc;
+    const double *kxd = (const double *)c->fxy.p, *kyd = kxd + nx;
+    CUDA_TRY(c, c->apchi.ensure(sizeof(float2) * n2 + n2));
+    float2 *apchi = (float2 *)c->apchi.p;
+    uint8_t *mask = (uint8_t *)(apchi + n2);
+    const double lam = msl_wavelength(o->kev);
+    LAUNCH_TRY(c, timed(c, MSL_PROF_OTHER, [&] { return msl::launch_probe_table(nx, ny, kxd, kyd, pr->k_in * pr->k_in, pr->k_out * pr->k_out,
+                                          lam, pr->df, pr->cs, 1.0 / ((double)nx * ny), apchi,
+                                          c->stream, &c->launches); }));
+    LAUNCH_TRY(c, timed(c, MSL_PROF_OTHER, [&] { return msl::launch_detector_mask(nx, ny, kxd, kyd, ndet, kyd + ny, kyd + ny + ndet, mask,
+                                            c->stream, &c->launches); }));
+    int B = c->probe_batch;
+    if (B <= 0) {
+        const size_t budget = (size_t)8 << 30;  // wave buffer budget, bytes
+        B = (int)std::max<size_t>(1, std::min<size_t>(budget / (sizeof(float2) * n2), 65536));
+    }
+    if (B > nprobe) B = nprobe;
+    CUDA_TRY(c, c->wave.ensure(sizeof(float2) * n2 * B));
+    CUDA_TRY(c, c->exy.ensure(sizeof(float2) * (size_t)B * (nx + ny) + sizeof(double) * 2 * B));
+    CUDA_TRY(c, c->partial.ensure(sizeof(double) * (size_t)ncheck * B * ntile * ndet));
+    const size_t obytes = sizeof(double) * (size_t)nprobe * ncheck * ndet;
+    const bool odev = on_device(det_out);
+    double *od;
+    if (odev) {
+        od = det_out;
+    } else {
+        CUDA_TRY(c, c->detout.ensure(obytes));
+        od = (double *)c->detout.p;
+    }
+    float2 *w = (float2 *)c->wave.p;
+    float2 *ex = (float2 *)c->exy.p, *ey = ex + (size_t)B * nx;
+    double *fxy = (double *)(ey + (size_t)B * ny);
+    double *partial = (double *)c->partial.p;
+    const int last = checkpoints[ncheck - 1];
+    std::vector<double> hf(2 * (size_t)B);
+    const double dscale = (double)n2 * (double)n2;
+    for (int p0 = 0; p0 < nprobe; p0 += B) {
+        const int nb = std::min(B, nprobe - p0);
+        for (int b = 0; b < nb; ++b) {
+            hf[2 * b] = probe_xy[2 * (p0 + b)] / g->ax;
+            hf[2 * b + 1] = probe_xy[2 * (p0 + b) + 1] / g->by;
+        }
+        CUDA_TRY(c, cudaMemcpyAsync(fxy, hf.data(), sizeof(double) * 2 * nb, cudaMemcpyHostToDevice,
+                                    c->stream));
+        LAUNCH_TRY(c, timed(c, MSL_PROF_OTHER, [&] { return msl::launch_probe_shifts(nx, ny, nb, fxy, ex, ey, c->stream, &c->launches); }));
+        ColArgs pa = col_args(g, st, twc, 0, w, nb, msl::COL_PROBE | msl::COL_INV | msl::COL_STORE);
+        pa.apchi = apchi;
+        pa.ex = ex;
+        pa.ey = ey;
+        LAUNCH_TRY(c, timed(c, MSL_PROF_COL, [&] { return msl::launch_col_pass(nx, pa, c->stream, c->nsm, &c->launches); }));
+        int ic = 0;
+        for (int s = 0; s <= last; ++s) {
+            const int l = layer_seq[s];
+            RowArgs r = row_args(g, twr, td + (size_t)l * n2, w, nb,
+                                 msl::ROW_LOAD | msl::ROW_INV | msl::ROW_TRANS | msl::ROW_FWD);
+            LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_row_pass(ny, r, c->stream, c->nsm, &c->launches); }));
+            const bool detect = checkpoints[ic] == s;
+            int cf = msl::COL_LOAD | msl::COL_FWD | msl::COL_PROP;
+            if (detect) cf |= msl::COL_DETECT;
+            if (s < last) cf |= msl::COL_INV | msl::COL_STORE;
+            ColArgs ca = col_args(g, st, twc, l, w, nb, cf);
+            ca.detmask = mask;
+            ca.ndet = ndet;
+            ca.partial = partial + (size_t)ic * B * ntile * ndet;
+            LAUNCH_TRY(c, timed(c, MSL_PROF_COL, [&] { return msl::launch_col_pass(nx, ca, c->stream, c->nsm, &c->launches); }));
+            if (detect) {
+                LAUNCH_TRY(c, timed(c, MSL_PROF_OTHER, [&] { return msl::launch_detector_finalize(
+                                  nb, ntile, ndet, ca.partial, dscale,
+                                  od + ((size_t)p0 * ncheck + ic) * ndet, ncheck * ndet, c->stream,
+                                  &c->launches); }));
+                ++ic;
+            }
+        }
+    }
+    if (!odev) CUDA_TRY(c, cudaMemcpyAsync(det_out, od, obytes, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    collect_profile(c);
+    return MSL_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,251 @@
+// Register-resident Stockham line FFTs for sm_103a.
+//
+// One line of N complex64 values is spread over T threads; thread t holds
+// x[t + T*e] for e in [0, E), E = N/T, in registers.  A plan is a sequence of
+// radices R_s (each dividing E).  Stage s (span NS = R_0*...*R_{s-1}) runs
+// E/R_s radix-R_s butterflies per thread on butterfly indices j = t + T*q:
+// inputs x[j + r*N/R] (= register slot q + r*E/R), twiddled by
+// w^(r*(j mod NS)/(NS*R)), outputs to position (j/NS)*NS*R + j mod NS + r*NS.
+// Between stages the outputs go through shared memory; after the last stage
+// every output lands in the register slot its input came from, so a line
+// leaves the transform in natural order with the same thread ownership it
+// entered with.  That is what lets the slice loop fuse pointwise work
+// (transmission, propagator, band limit, detectors) between an inverse and a
+// forward transform without any extra data movement.
+//
+// Sign: DIR = +1 computes sum_n x[n] exp(+2 pi i n k / N) (Kirkland's "fft",
+// FFTW_BACKWARD), DIR = -1 the exp(-...) transform.  Neither scales.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace msl {
+
+// ------------------------------------------------------------------ plans
+// T: threads per line; radices; row_swz: shared-memory address scheme for
+// contiguous lines (0: pad i + (i >> s), 1: xor i ^ ((i >> s) & 15));
+// col_c: columns per column-pass tile; col_ps: row-permutation shift there.
+template <int N> struct Plan;
+#define MSL_PLAN(N_, T_, NST_, R0, R1, R2, R3, R4, RSWZ, RSH, CC, CPS)          \
+    template <> struct Plan<N_> {                                               \
+        static constexpr int N = N_, T = T_, E = N_ / T_, NSTAGE = NST_;         \
+        static constexpr int row_swz = RSWZ, row_sh = RSH;                      \
+        static constexpr int col_c = CC, col_ps = CPS;                          \
+        static constexpr int radix(int s) {                                     \
+            return s == 0 ? R0 : s == 1 ? R1 : s == 2 ? R2 : s == 3 ? R3 : R4;  \
+        }                                                                       \
+    };
+//       N     T   S  radices          row  sh  C   ps
+MSL_PLAN(64,    8, 2,  8,  8, 1, 1, 1,  0,  3, 16, 0)
+MSL_PLAN(128,  16, 3,  8,  8, 2, 1, 1,  1,  3, 16, 0)
+MSL_PLAN(256,  32, 3,  8,  8, 4, 1, 1,  1,  3, 16, 0)
+MSL_PLAN(512,  64, 3,  8,  8, 8, 1, 1,  1,  3,  8, 3)
+MSL_PLAN(1024, 64, 3, 16,  8, 8, 1, 1,  1,  4,  8, 4)
+MSL_PLAN(2048,128, 3, 16, 16, 8, 1, 1,  0,  4,  4, 4)
+MSL_PLAN(384,  32, 5,  3,  4, 4, 4, 2,  0,  5, 16, 0)
+MSL_PLAN(768,  64, 5,  3,  4, 4, 4, 4,  0,  5,  8, 3)
+#undef MSL_PLAN
+
+template <class P> __host__ __device__ constexpr int plan_span(int s) {
+    int ns = 1;
+    for (int i = 0; i < s; ++i) ns *= P::radix(i);
+    return ns;
+}
+// Offset of stage s's twiddle table ([r][k], R_s * NS_s entries; stage 0 has none).
+template <class P> __host__ __device__ constexpr int plan_tw_offset(int s) {
+    int off = 0;
+    for (int i = 1; i < s; ++i) off += P::radix(i) * plan_span<P>(i);
+    return off;
+}
+template <class P> __host__ __device__ constexpr int plan_tw_size() {
+    return plan_tw_offset<P>(P::NSTAGE);
+}
+// Shared-memory float2 slots one contiguous line needs.
+template <class P> __host__ __device__ constexpr int row_line_slots() {
+    return P::row_swz == 0 ? P::N + (P::N >> P::row_sh) : P::N;
+}
+
+// --------------------------------------------------------- complex helpers
+__device__ __forceinline__ float2 c_add(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 c_sub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 c_mul(float2 a, float2 b) {
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 c_scale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+// multiply by DIR * i
+template <int DIR> __device__ __forceinline__ float2 c_muli(float2 a) {
+    return DIR > 0 ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
+}
+
+// ---------------------------------------------------------- radix kernels
+template <int DIR> __device__ __forceinline__ void dft2(float2 &a, float2 &b) {
+    float2 t = a;
+    a = c_add(t, b);
+    b = c_sub(t, b);
+}
+
+template <int DIR> __device__ __forceinline__ void dft3(float2 &x0, float2 &x1, float2 &x2) {
+    const float s3 = 0.86602540378443864676f;
+    float2 t = c_add(x1, x2), u = c_sub(x1, x2);
+    float2 m = make_float2(x0.x - 0.5f * t.x, x0.y - 0.5f * t.y);
+    x0 = c_add(x0, t);
+    float2 v = c_muli<DIR>(c_scale(u, s3));
+    x1 = c_add(m, v);
+    x2 = c_sub(m, v);
+}
+
+template <int DIR>
+__device__ __forceinline__ void dft4(float2 &x0, float2 &x1, float2 &x2, float2 &x3) {
+    float2 t0 = c_add(x0, x2), t1 = c_sub(x0, x2);
+    float2 t2 = c_add(x1, x3), t3 = c_muli<DIR>(c_sub(x1, x3));
+    x0 = c_add(t0, t2);
+    x2 = c_sub(t0, t2);
+    x1 = c_add(t1, t3);
+    x3 = c_sub(t1, t3);
+}
+
+template <int DIR> __device__ __forceinline__ void dft8(float2 *a) {
+    float2 e0 = a[0], e1 = a[2], e2 = a[4], e3 = a[6];
+    float2 o0 = a[1], o1 = a[3], o2 = a[5], o3 = a[7];
+    dft4<DIR>(e0, e1, e2, e3);
+    dft4<DIR>(o0, o1, o2, o3);
+    const float h = 0.70710678118654752440f;
+    // w8^1 = (1 + DIR i) h, w8^2 = DIR i, w8^3 = (-1 + DIR i) h
+    float2 t1 = make_float2(h * (o1.x - DIR * o1.y), h * (o1.y + DIR * o1.x));
+    float2 t2 = c_muli<DIR>(o2);
+    float2 t3 = make_float2(h * (-o3.x - DIR * o3.y), h * (-o3.y + DIR * o3.x));
+    a[0] = c_add(e0, o0);
+    a[4] = c_sub(e0, o0);
+    a[1] = c_add(e1, t1);
+    a[5] = c_sub(e1, t1);
+    a[2] = c_add(e2, t2);
+    a[6] = c_sub(e2, t2);
+    a[3] = c_add(e3, t3);
+    a[7] = c_sub(e3, t3);
+}
+
+// exp(DIR * i * 2 pi m / 16) for m in 0..9
+template <int DIR> __device__ __forceinline__ float2 w16(int m) {
+    const float c1 = 0.92387953251128675613f, s1 = 0.38268343236508977173f;
+    const float h = 0.70710678118654752440f;
+    float re, im;
+    switch (m) {
+        case 0: re = 1.f; im = 0.f; break;
+        case 1: re = c1; im = s1; break;
+        case 2: re = h; im = h; break;
+        case 3: re = s1; im = c1; break;
+        case 4: re = 0.f; im = 1.f; break;
+        case 5: re = -s1; im = c1; break;
+        case 6: re = -h; im = h; break;
+        case 7: re = -c1; im = s1; break;
+        case 8: re = -1.f; im = 0.f; break;
+        default: re = -c1; im = -s1; break;  // m = 9
+    }
+    return make_float2(re, DIR * im);
+}
+
+template <int DIR> __device__ __forceinline__ void dft16(float2 *a) {
+    // n = 4 n1 + n2, k = k1 + 4 k2
+#pragma unroll
+    for (int n2 = 0; n2 < 4; ++n2) dft4<DIR>(a[n2], a[4 + n2], a[8 + n2], a[12 + n2]);
+    // a[4 k1 + n2] = Y[n2][k1]; twiddle by w16^(n2 k1)
+#pragma unroll
+    for (int k1 = 1; k1 < 4; ++k1)
+#pragma unroll
+        for (int n2 = 1; n2 < 4; ++n2) a[4 * k1 + n2] = c_mul(a[4 * k1 + n2], w16<DIR>(n2 * k1));
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1) dft4<DIR>(a[4 * k1], a[4 * k1 + 1], a[4 * k1 + 2], a[4 * k1 + 3]);
+    // X[k1 + 4 k2] sits at a[4 k1 + k2]: transpose the 4x4 block
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = i + 1; j < 4; ++j) {
+            float2 t = a[4 * i + j];
+            a[4 * i + j] = a[4 * j + i];
+            a[4 * j + i] = t;
+        }
+}
+
+template <int R, int DIR> __device__ __forceinline__ void dft(float2 *a) {
+    if constexpr (R == 2) dft2<DIR>(a[0], a[1]);
+    else if constexpr (R == 3) dft3<DIR>(a[0], a[1], a[2]);
+    else if constexpr (R == 4) dft4<DIR>(a[0], a[1], a[2], a[3]);
+    else if constexpr (R == 8) dft8<DIR>(a);
+    else if constexpr (R == 16) dft16<DIR>(a);
+    else static_assert(R == 2, "unsupported radix");
+}
+
+// ------------------------------------------------------ shared addressing
+// Contiguous lines: each line owns row_line_slots<P>() float2 slots.
+template <class P> struct RowAddr {
+    float2 *base;
+    __device__ __forceinline__ int operator()(int i) const {
+        if constexpr (P::row_swz == 0) return i + (i >> P::row_sh);
+        else return i ^ ((i >> P::row_sh) & 15);
+    }
+};
+// Column tiles: C interleaved columns, slot = perm(i) * C + c.
+template <class P> struct ColAddr {
+    float2 *base;
+    int c;
+    __device__ __forceinline__ int operator()(int i) const {
+        constexpr int C = P::col_c;
+        if constexpr (C >= 16) return i * C + c;
+        else return (i ^ ((i >> P::col_ps) & (16 / C - 1))) * C + c;
+    }
+};
+
+// ------------------------------------------------------------ the transform
+// tw: this plan's stage tables (exp(+2 pi i r k / (NS R)) at [r][k]).
+template <class P, int S, int DIR>
+__device__ __forceinline__ void fft_stage(float2 (&v)[P::E], int t, const float2 *__restrict__ tw) {
+    constexpr int R = P::radix(S), NS = plan_span<P>(S), E = P::E, Q = E / R, T = P::T;
+    const float2 *tws = tw + plan_tw_offset<P>(S);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        float2 a[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) a[r] = v[q + r * Q];
+        if constexpr (NS > 1) {
+            const int k = (t + T * q) % NS;
+#pragma unroll
+            for (int r = 1; r < R; ++r) {
+                float2 w = tws[r * NS + k];
+                if constexpr (DIR < 0) w.y = -w.y;
+                a[r] = c_mul(a[r], w);
+            }
+        }
+        dft<R, DIR>(a);
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[q + r * Q] = a[r];
+    }
+}
+
+template <class P, int S, class Addr>
+__device__ __forceinline__ void fft_exchange(float2 (&v)[P::E], int t, const Addr &ad) {
+    constexpr int R = P::radix(S), NS = plan_span<P>(S), E = P::E, Q = E / R, T = P::T;
+    __syncthreads();  // previous readers of the buffer are done
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const int j = t + T * q;
+        const int d = (j / NS) * NS * R + (j % NS);
+#pragma unroll
+        for (int r = 0; r < R; ++r) ad.base[ad(d + r * NS)] = v[q + r * Q];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int e = 0; e < E; ++e) v[e] = ad.base[ad(t + T * e)];
+}
+
+template <class P, int DIR, int S = 0, class Addr>
+__device__ __forceinline__ void fft_line(float2 (&v)[P::E], int t, const Addr &ad,
+                                         const float2 *__restrict__ tw) {
+    fft_stage<P, S, DIR>(v, t, tw);
+    if constexpr (S + 1 < P::NSTAGE) {
+        fft_exchange<P, S>(v, t, ad);
+        fft_line<P, DIR, S + 1>(v, t, ad, tw);
+    }
+}
+
+}  // namespace msl

@@ -1,0 +1,97 @@
+// Internal host-side interface between the C ABI (msl_api.cu) and the kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <vector>
+
+namespace msl {
+
+// Row pass: contiguous lines of length ny (one line = one ix of one image).
+enum RowFlags {
+    ROW_LOAD = 1,    // load the line from `in` (else start from constant 1 + 0i)
+    ROW_GENT = 2,    // start from exp(i * phase_scale * vpot) (FP64 phase)
+    ROW_INV = 4,     // exp(-i) line transform
+    ROW_TRANS = 8,   // multiply by trans[ix][iy]
+    ROW_FWD = 16,    // exp(+i) line transform
+};
+
+struct RowArgs {
+    const float2 *in;
+    float2 *out;        // may equal in
+    int nlines;         // images * nx
+    int nx;             // lines per image
+    const float2 *trans;   // [nx][ny] of the current layer (ROW_TRANS)
+    const float *vpot;     // [nx][ny] per image (ROW_GENT)
+    double phase_scale;    // rad per unit of vpot (ROW_GENT)
+    const float2 *tw;      // twiddle tables of the ny plan
+    int flags;
+    float scale;           // multiplies the output when != 1
+};
+
+// Column pass: strided lines of length nx (one line = one iy of one image).
+enum ColFlags {
+    COL_LOAD = 1,     // load from `in`
+    COL_PROBE = 2,    // start from apchi[ix][iy] * ex[b][ix] * ey[b][iy]
+    COL_FWD = 4,      // exp(+i) line transform
+    COL_PROP = 8,     // * py[iy] * px[ix] inside the band limit, 0 outside
+    COL_DETECT = 16,  // annular detector partial sums of |psi|^2
+    COL_INV = 32,     // exp(-i) line transform
+    COL_STORE = 64,   // store to `out`
+};
+
+struct ColArgs {
+    const float2 *in;
+    float2 *out;
+    int batch;        // images
+    int ny;           // columns per image
+    const float2 *tw; // twiddle tables of the nx plan
+    int flags;
+    const float2 *px, *py;    // propagator tables (py carries the 1/(nx ny) scale)
+    const float *kx2, *ky2;   // float k^2 tables (freqn semantics)
+    float k2max;
+    const float2 *apchi;      // [nx][ny]
+    const float2 *ex, *ey;    // [batch][nx], [batch][ny]
+    const uint8_t *detmask;   // [nx][ny], bit d = detector d
+    int ndet;
+    double *partial;          // [batch][ny / C][ndet]
+};
+
+struct PotArgs {
+    const double *x, *y;      // wrapped into [0, ax), [0, by)
+    const int *Z;
+    const int *off;           // [nslice + 1] atom ranges per slice
+    int nslice, nx, ny;
+    double ax, by, dxp, dyp;
+    float rad2;               // radius^2 (float compare, r < radius)
+    const float *sp;          // [104][12] A1 B1 A2 B2 A3 B3 C1 D1 C2 D2 C3 D3
+    float *v;                 // [nslice][nx][ny]
+};
+
+bool plan_supported(int n);
+int plan_col_c(int n);
+// Per-stage twiddle tables for side n (exp(+2 pi i r k / (NS R)) at [r][k]).
+void plan_twiddles(int n, std::vector<float2> &out);
+
+// Each launcher returns cudaSuccess or the launch error; *launches is bumped.
+cudaError_t launch_row_pass(int ny, const RowArgs &a, cudaStream_t s, int nsm, int64_t *launches);
+cudaError_t launch_col_pass(int nx, const ColArgs &a, cudaStream_t s, int nsm, int64_t *launches);
+cudaError_t launch_potential(const PotArgs &a, cudaStream_t s, int64_t *launches);
+// apchi[ix][iy] = A(s) exp(-i chi(s)) * scale, s = kx^2 + ky^2 from kxd/kyd (FP64)
+cudaError_t launch_probe_table(int nx, int ny, const double *kxd, const double *kyd, double s_in,
+                               double s_out, double lam, double df, double cs, double scale,
+                               float2 *apchi, cudaStream_t s, int64_t *launches);
+// ex[b][ix] = exp(2 pi i * sidx(ix) * fx[b]), same for ey
+cudaError_t launch_probe_shifts(int nx, int ny, int nb, const double *fxy, float2 *ex, float2 *ey,
+                                cudaStream_t s, int64_t *launches);
+// bit d of mask[ix][iy] set when kin2[d] <= s <= kout2[d]
+cudaError_t launch_detector_mask(int nx, int ny, const double *kxd, const double *kyd, int ndet,
+                                 const double *kin2, const double *kout2, uint8_t *mask,
+                                 cudaStream_t s, int64_t *launches);
+// out[b * out_stride + d] = scale * sum_t partial[b][t][d]
+cudaError_t launch_detector_finalize(int nb, int ntile, int ndet, const double *partial,
+                                     double scale, double *out, int out_stride, cudaStream_t s,
+                                     int64_t *launches);
+
+}  // namespace msl

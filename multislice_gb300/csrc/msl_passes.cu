@@ -1,0 +1,385 @@
+// The two slice-loop passes and the small set-up kernels of the multislice path.
+//
+// Wave layout: [image][ix][iy], iy contiguous (Kirkland's x-major cfpix,
+// multislice/cfpix.hpp:99-125).  One slice of mulslice.cpp:706-739
+//     psi *= t;  fft2;  propagate (slicelib.cpp:744-790);  ifft2
+// becomes, with the 2D transforms split into their y (row) and x (column) halves,
+//     row pass    : ifft_y (finishing the previous slice) -> * t -> fft_y
+//     column pass : fft_x -> * py * px, band limit -> ifft_x
+// so each slice reads and writes the wave exactly twice (32 * nx * ny bytes per
+// probe-slice), and every pointwise step of the reference runs in registers
+// between two line transforms.  Kirkland's 1/(nx ny) ifft scale rides in py.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include <vector>
+
+#include "msl_fft.cuh"
+#include "msl_internal.h"
+
+namespace msl {
+
+constexpr int kMaxDet = 8;
+
+template <int N> struct RowCfg {
+    using P = Plan<N>;
+    static constexpr int LPB = (256 / P::T) > 0 ? 256 / P::T : 1;
+    static constexpr int THREADS = P::T * LPB;
+    static constexpr size_t SMEM =
+        sizeof(float2) * (plan_tw_size<P>() + (size_t)LPB * row_line_slots<P>());
+};
+template <int N> struct ColCfg {
+    using P = Plan<N>;
+    static constexpr int C = P::col_c;
+    static constexpr int THREADS = P::T * C;
+    static constexpr int NWARP = THREADS / 32;
+    static constexpr size_t SMEM = sizeof(float2) * (plan_tw_size<P>() + (size_t)N * C) +
+                                   sizeof(double) * NWARP * kMaxDet;
+};
+
+// ---------------------------------------------------------------- row pass
+template <int N>
+__global__ void __launch_bounds__(RowCfg<N>::THREADS) row_pass_kernel(RowArgs a) {
+    using P = Plan<N>;
+    constexpr int T = P::T, E = P::E, LPB = RowCfg<N>::LPB, TW = plan_tw_size<P>();
+    extern __shared__ float2 sm[];
+    float2 *tw = sm;
+    float2 *lines = sm + TW;
+    const int tid = threadIdx.x + T * threadIdx.y;
+    for (int i = tid; i < TW; i += RowCfg<N>::THREADS) tw[i] = a.tw[i];
+    const int t = threadIdx.x;
+    RowAddr<P> ad{lines + threadIdx.y * row_line_slots<P>()};
+    const int ngroups = (a.nlines + LPB - 1) / LPB;
+    for (int g = blockIdx.x; g < ngroups; g += gridDim.x) {
+        const int line = g * LPB + threadIdx.y;
+        const bool valid = line < a.nlines;
+        const size_t base = (size_t)line * N;
+        float2 v[E];
+        if (valid && (a.flags & ROW_LOAD)) {
+#pragma unroll
+            for (int e = 0; e < E; ++e) v[e] = a.in[base + t + T * e];
+        } else if (valid && (a.flags & ROW_GENT)) {
+            // t = exp(i sigma V): phase in FP64, reduced to [-pi, pi] before the
+            // single-precision sincos (mulslice.cpp:414-421 forms it in float).
+#pragma unroll
+            for (int e = 0; e < E; ++e) {
+                const double ph = a.phase_scale * (double)a.vpot[base + t + T * e];
+                const double k = rint(ph * 0.15915494309189533577);
+                const double r = fma(-k, 6.283185307179586477, ph);
+                float s, c;
+                sincosf((float)r, &s, &c);
+                v[e] = make_float2(c, s);
+            }
+        } else {
+#pragma unroll
+            for (int e = 0; e < E; ++e) v[e] = make_float2(valid ? 1.f : 0.f, 0.f);
+        }
+        if (a.flags & ROW_INV) fft_line<P, -1>(v, t, ad, tw);
+        if (valid && (a.flags & ROW_TRANS)) {
+            const float2 *tr = a.trans + (size_t)(line % a.nx) * N;
+#pragma unroll
+            for (int e = 0; e < E; ++e) v[e] = c_mul(v[e], tr[t + T * e]);
+        }
+        if (a.flags & ROW_FWD) fft_line<P, +1>(v, t, ad, tw);
+        if (valid) {
+            if (a.scale != 1.0f) {
+#pragma unroll
+                for (int e = 0; e < E; ++e) v[e] = c_scale(v[e], a.scale);
+            }
+#pragma unroll
+            for (int e = 0; e < E; ++e) a.out[base + t + T * e] = v[e];
+        }
+    }
+}
+
+// ------------------------------------------------------------- column pass
+template <int N>
+__global__ void __launch_bounds__(ColCfg<N>::THREADS) col_pass_kernel(ColArgs a) {
+    using P = Plan<N>;
+    constexpr int T = P::T, E = P::E, C = P::col_c, TW = plan_tw_size<P>();
+    constexpr int NWARP = ColCfg<N>::NWARP;
+    extern __shared__ float2 sm[];
+    float2 *tw = sm;
+    float2 *buf = sm + TW;
+    double *red = reinterpret_cast<double *>(buf + (size_t)N * C);
+    for (int i = threadIdx.x; i < TW; i += ColCfg<N>::THREADS) tw[i] = a.tw[i];
+    const int c = threadIdx.x % C, t = threadIdx.x / C;
+    ColAddr<P> ad{buf, c};
+    const int tiles_per_img = a.ny / C;
+    const int ntiles = a.batch * tiles_per_img;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int b = tile / tiles_per_img, ty = tile % tiles_per_img;
+        const int iy = ty * C + c;
+        const size_t base = (size_t)b * N * a.ny + iy;
+        float2 v[E];
+        if (a.flags & COL_PROBE) {
+            const float2 eyv = a.ey[(size_t)b * a.ny + iy];
+            const float2 *exb = a.ex + (size_t)b * N;
+#pragma unroll
+            for (int e = 0; e < E; ++e) {
+                const int ix = t + T * e;
+                v[e] = c_mul(c_mul(a.apchi[(size_t)ix * a.ny + iy], exb[ix]), eyv);
+            }
+        } else {
+#pragma unroll
+            for (int e = 0; e < E; ++e) v[e] = a.in[base + (size_t)(t + T * e) * a.ny];
+        }
+        if (a.flags & COL_FWD) fft_line<P, +1>(v, t, ad, tw);
+        if (a.flags & COL_PROP) {
+            const float ky2 = a.ky2[iy];
+            const float2 pyv = a.py[iy];
+#pragma unroll
+            for (int e = 0; e < E; ++e) {
+                const int ix = t + T * e;
+                const float k2 = __fadd_rn(a.kx2[ix], ky2);
+                if (k2 < a.k2max) v[e] = c_mul(c_mul(v[e], pyv), a.px[ix]);
+                else v[e] = make_float2(0.f, 0.f);
+            }
+        }
+        if (a.flags & COL_DETECT) {
+            float acc[kMaxDet];
+#pragma unroll
+            for (int d = 0; d < kMaxDet; ++d) acc[d] = 0.f;
+#pragma unroll
+            for (int e = 0; e < E; ++e) {
+                const int ix = t + T * e;
+                const unsigned bits = a.detmask[(size_t)ix * a.ny + iy];
+                const float p = v[e].x * v[e].x + v[e].y * v[e].y;
+#pragma unroll
+                for (int d = 0; d < kMaxDet; ++d)
+                    if (bits & (1u << d)) acc[d] += p;
+            }
+            const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+            __syncthreads();  // red[] of the previous tile has been consumed
+#pragma unroll
+            for (int d = 0; d < kMaxDet; ++d) {
+                if (d < a.ndet) {
+                    double x = (double)acc[d];
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+                    if (lane == 0) red[warp * kMaxDet + d] = x;
+                }
+            }
+            __syncthreads();
+            if (threadIdx.x < a.ndet) {
+                double s = 0.0;
+                for (int w = 0; w < NWARP; ++w) s += red[w * kMaxDet + threadIdx.x];
+                a.partial[((size_t)b * tiles_per_img + ty) * a.ndet + threadIdx.x] = s;
+            }
+        }
+        if (a.flags & COL_INV) fft_line<P, -1>(v, t, ad, tw);
+        if (a.flags & COL_STORE) {
+#pragma unroll
+            for (int e = 0; e < E; ++e) a.out[base + (size_t)(t + T * e) * a.ny] = v[e];
+        }
+    }
+}
+
+// ------------------------------------------------------------ set-up kernels
+__global__ void probe_table_kernel(int nx, int ny, const double *kxd, const double *kyd,
+                                   double s_in, double s_out, double lam, double df, double cs,
+                                   double scale, float2 *apchi) {
+    const int iy = blockIdx.x * blockDim.x + threadIdx.x;
+    const int ix = blockIdx.y;
+    if (iy >= ny || ix >= nx) return;
+    const double s = __dadd_rn(__dmul_rn(kxd[ix], kxd[ix]), __dmul_rn(kyd[iy], kyd[iy]));
+    float2 out = make_float2(0.f, 0.f);
+    if (s >= s_in && s <= s_out) {
+        // chi = pi (lambda df s + Cs lambda^3 s^2 / 2)   (MSProject.cs:511-514)
+        const double chi = 3.14159265358979323846 * (lam * df * s + 0.5 * cs * lam * lam * lam * s * s);
+        double sn, cn;
+        sincos(chi, &sn, &cn);
+        out = make_float2((float)(cn * scale), (float)(-sn * scale));
+    }
+    apchi[(size_t)ix * ny + iy] = out;
+}
+
+__global__ void probe_shift_kernel(int nx, int ny, int nb, const double *fxy, float2 *ex,
+                                   float2 *ey) {
+    const int b = blockIdx.y;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nb) return;
+    if (i < nx) {
+        const int si = i < nx / 2 ? i : i - nx;
+        double p = (double)si * fxy[2 * b];
+        p -= rint(p);
+        double sn, cn;
+        sincospi(2.0 * p, &sn, &cn);
+        ex[(size_t)b * nx + i] = make_float2((float)cn, (float)sn);
+    }
+    if (i < ny) {
+        const int sj = i < ny / 2 ? i : i - ny;
+        double p = (double)sj * fxy[2 * b + 1];
+        p -= rint(p);
+        double sn, cn;
+        sincospi(2.0 * p, &sn, &cn);
+        ey[(size_t)b * ny + i] = make_float2((float)cn, (float)sn);
+    }
+}
+
+__global__ void detector_mask_kernel(int nx, int ny, const double *kxd, const double *kyd, int ndet,
+                                     const double *kin2, const double *kout2, uint8_t *mask) {
+    const int iy = blockIdx.x * blockDim.x + threadIdx.x;
+    const int ix = blockIdx.y;
+    if (iy >= ny || ix >= nx) return;
+    const double s = __dadd_rn(__dmul_rn(kxd[ix], kxd[ix]), __dmul_rn(kyd[iy], kyd[iy]));
+    unsigned bits = 0;
+    for (int d = 0; d < ndet; ++d)
+        if (s <= kout2[d] && s >= kin2[d]) bits |= 1u << d;
+    mask[(size_t)ix * ny + iy] = (uint8_t)bits;
+}
+
+__global__ void detector_finalize_kernel(int nb, int ntile, int ndet, const double *partial,
+                                         double scale, double *out, int out_stride) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nb * ndet) return;
+    const int b = i / ndet, d = i % ndet;
+    double s = 0.0;
+    for (int t = 0; t < ntile; ++t) s += partial[((size_t)b * ntile + t) * ndet + d];
+    out[(size_t)b * out_stride + d] = s * scale;
+}
+
+// ----------------------------------------------------------------- dispatch
+template <int N> static cudaError_t row_launch(const RowArgs &a, cudaStream_t s, int nsm) {
+    static int blocks_per_sm = -1;
+    if (blocks_per_sm < 0) {
+        cudaError_t e = cudaFuncSetAttribute(row_pass_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)RowCfg<N>::SMEM);
+        if (e != cudaSuccess) return e;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, row_pass_kernel<N>,
+                                                          RowCfg<N>::THREADS, RowCfg<N>::SMEM);
+        if (e != cudaSuccess) return e;
+        if (blocks_per_sm < 1) blocks_per_sm = 1;
+    }
+    const int ngroups = (a.nlines + RowCfg<N>::LPB - 1) / RowCfg<N>::LPB;
+    int grid = nsm * blocks_per_sm;
+    if (grid > ngroups) grid = ngroups;
+    if (grid < 1) grid = 1;
+    dim3 block(Plan<N>::T, RowCfg<N>::LPB);
+    row_pass_kernel<N><<<grid, block, RowCfg<N>::SMEM, s>>>(a);
+    return cudaGetLastError();
+}
+
+template <int N> static cudaError_t col_launch(const ColArgs &a, cudaStream_t s, int nsm) {
+    static int blocks_per_sm = -1;
+    if (blocks_per_sm < 0) {
+        cudaError_t e = cudaFuncSetAttribute(col_pass_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)ColCfg<N>::SMEM);
+        if (e != cudaSuccess) return e;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, col_pass_kernel<N>,
+                                                          ColCfg<N>::THREADS, ColCfg<N>::SMEM);
+        if (e != cudaSuccess) return e;
+        if (blocks_per_sm < 1) blocks_per_sm = 1;
+    }
+    const int ntiles = a.batch * (a.ny / ColCfg<N>::C);
+    int grid = nsm * blocks_per_sm;
+    if (grid > ntiles) grid = ntiles;
+    if (grid < 1) grid = 1;
+    col_pass_kernel<N><<<grid, ColCfg<N>::THREADS, ColCfg<N>::SMEM, s>>>(a);
+    return cudaGetLastError();
+}
+
+#define MSL_FOR_EACH_SIDE(X) X(64) X(128) X(256) X(384) X(512) X(768) X(1024) X(2048)
+
+bool plan_supported(int n) {
+    switch (n) {
+#define X(N) case N:
+        MSL_FOR_EACH_SIDE(X)
+#undef X
+        return true;
+        default: return false;
+    }
+}
+
+int plan_col_c(int n) {
+    switch (n) {
+#define X(N) case N: return Plan<N>::col_c;
+        MSL_FOR_EACH_SIDE(X)
+#undef X
+        default: return 0;
+    }
+}
+
+template <int N> static void twiddles_for(std::vector<float2> &out) {
+    using P = Plan<N>;
+    out.assign(plan_tw_size<P>() > 0 ? plan_tw_size<P>() : 1, make_float2(0.f, 0.f));
+    for (int s = 1; s < P::NSTAGE; ++s) {
+        const int R = P::radix(s), NS = plan_span<P>(s), off = plan_tw_offset<P>(s);
+        for (int r = 0; r < R; ++r)
+            for (int k = 0; k < NS; ++k) {
+                // exp(+2 pi i r k / (NS R)), argument reduced exactly in integers
+                const long m = ((long)r * k) % ((long)NS * R);
+                const double ang = 2.0 * 3.14159265358979323846 * (double)m / (double)(NS * R);
+                out[off + r * NS + k] = make_float2((float)cos(ang), (float)sin(ang));
+            }
+    }
+}
+
+void plan_twiddles(int n, std::vector<float2> &out) {
+    switch (n) {
+#define X(N) case N: twiddles_for<N>(out); break;
+        MSL_FOR_EACH_SIDE(X)
+#undef X
+        default: out.clear();
+    }
+}
+
+cudaError_t launch_row_pass(int ny, const RowArgs &a, cudaStream_t s, int nsm, int64_t *launches) {
+    ++*launches;
+    switch (ny) {
+#define X(N) case N: return row_launch<N>(a, s, nsm);
+        MSL_FOR_EACH_SIDE(X)
+#undef X
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_col_pass(int nx, const ColArgs &a, cudaStream_t s, int nsm, int64_t *launches) {
+    ++*launches;
+    switch (nx) {
+#define X(N) case N: return col_launch<N>(a, s, nsm);
+        MSL_FOR_EACH_SIDE(X)
+#undef X
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_probe_table(int nx, int ny, const double *kxd, const double *kyd, double s_in,
+                               double s_out, double lam, double df, double cs, double scale,
+                               float2 *apchi, cudaStream_t s, int64_t *launches) {
+    ++*launches;
+    dim3 grid((ny + 255) / 256, nx);
+    probe_table_kernel<<<grid, 256, 0, s>>>(nx, ny, kxd, kyd, s_in, s_out, lam, df, cs, scale, apchi);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_probe_shifts(int nx, int ny, int nb, const double *fxy, float2 *ex, float2 *ey,
+                                cudaStream_t s, int64_t *launches) {
+    ++*launches;
+    const int n = nx > ny ? nx : ny;
+    dim3 grid((n + 255) / 256, nb);
+    probe_shift_kernel<<<grid, 256, 0, s>>>(nx, ny, nb, fxy, ex, ey);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_detector_mask(int nx, int ny, const double *kxd, const double *kyd, int ndet,
+                                 const double *kin2, const double *kout2, uint8_t *mask,
+                                 cudaStream_t s, int64_t *launches) {
+    ++*launches;
+    dim3 grid((ny + 255) / 256, nx);
+    detector_mask_kernel<<<grid, 256, 0, s>>>(nx, ny, kxd, kyd, ndet, kin2, kout2, mask);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_detector_finalize(int nb, int ntile, int ndet, const double *partial,
+                                     double scale, double *out, int out_stride, cudaStream_t s,
+                                     int64_t *launches) {
+    ++*launches;
+    const int n = nb * ndet;
+    detector_finalize_kernel<<<(n + 255) / 256, 256, 0, s>>>(nb, ntile, ndet, partial, scale, out,
+                                                            out_stride);
+    return cudaGetLastError();
+}
+
+}  // namespace msl

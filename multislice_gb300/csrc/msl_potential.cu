@@ -1,0 +1,147 @@
+// Projected-potential gather kernel: the PotentialBuilder step.
+//
+// Reference: LMultiSlice ModelPotential::calculatePotentialGrid
+// (ImageSimulation/LMultiSlice/ModelPotential.cu:27-99) bins atoms by z and, for
+// every pixel, sums calculateProjectedPotential over all atoms of the slice in
+// 4608-atom constant-memory batches (:125-230), evaluating K0 in FP64 for every
+// pixel-atom pair before the cutoff test.  The atom form used here is Kirkland's
+// vzatom (multislice/slicelib.cpp:2666-2716):
+//     V(r) = AL sum_i a_i K0(2 pi r sqrt(b_i)) + AG sum_i (c_i/d_i) exp(-pi^2 r^2 / d_i)
+// with FPARAMS coefficients, K0/I0 by the Abramowitz & Stegun 9.8.1/9.8.5/9.8.6
+// polynomials the reference uses (slicelib.cpp:168-235).
+//
+// GB300 design: one CTA per 8 x 32 pixel tile of one slice.  The slice's atoms
+// stream through in chunks of 256; each chunk is culled against the tile's
+// periodic bounding box and compacted in atom order (so the float sum order is
+// fixed), then the per-atom x and y offsets of the tile's 8 columns and 32 rows
+// are formed once in FP64 (so an atom sitting exactly on a pixel gives r = 0,
+// clamped to 1e-10 A as the reference does, never a float rounding residue)
+// and the pair loop runs in FP32 on those offsets.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "msl_internal.h"
+
+namespace msl {
+
+namespace {
+constexpr int TX = 8, TY = 32, THREADS = TX * TY, CHUNK = 256;
+
+__device__ __forceinline__ float poly(const float *c, int n, float t) {
+    float s = c[n - 1];
+    for (int i = n - 2; i >= 0; --i) s = fmaf(s, t, c[i]);
+    return s;
+}
+
+__constant__ float kI0A[7] = {1.0f, 3.5156229f, 3.0899424f, 1.2067492f, 0.2659732f, 0.0360768f, 0.0045813f};
+__constant__ float kK0A[7] = {-0.57721566f, 0.42278420f, 0.23069756f, 0.03488590f, 0.00262698f,
+                              0.00010750f, 0.00000740f};
+__constant__ float kK0B[7] = {1.25331414f, -0.07832358f, 0.02189568f, -0.01062446f, 0.00587872f,
+                              -0.00251540f, 0.00053208f};
+
+// K0(x), x > 0 (A&S 9.8.5 for x <= 2 with I0 from 9.8.1, 9.8.6 above).
+__device__ __forceinline__ float bessk0f(float x) {
+    if (x <= 2.0f) {
+        const float t = (x / 3.75f) * (x / 3.75f);
+        const float i0 = poly(kI0A, 7, t);
+        const float x2 = 0.25f * x * x;
+        return -logf(0.5f * x) * i0 + poly(kK0A, 7, x2);
+    }
+    return expf(-x) * poly(kK0B, 7, 2.0f / x) * rsqrtf(x);
+}
+}  // namespace
+
+__global__ void __launch_bounds__(THREADS) potential_kernel(PotArgs a) {
+    __shared__ int sZ[CHUNK];
+    __shared__ double sxa[CHUNK], sya[CHUNK];
+    __shared__ float sdx[CHUNK][TX];
+    __shared__ float sdy[CHUNK][TY];
+    __shared__ int wcount[THREADS / 32];
+    const int tid = threadIdx.x;
+    const int ty = tid % TY, tx = tid / TY;
+    const int lane = tid & 31, warp = tid >> 5;
+    const int iy0 = blockIdx.x * TY, ix0 = blockIdx.y * TX, s = blockIdx.z;
+
+    // tile bounding box (pixel positions) for culling
+    const double xc = (ix0 + 0.5 * (TX - 1)) * a.dxp, hx = 0.5 * (TX - 1) * a.dxp;
+    const double yc = (iy0 + 0.5 * (TY - 1)) * a.dyp, hy = 0.5 * (TY - 1) * a.dyp;
+    const double rad = sqrt((double)a.rad2) * (1.0 + 1e-6) + 1e-6;
+    const int a0 = a.off[s], a1 = a.off[s + 1];
+    float acc = 0.f;
+
+    for (int c0 = a0; c0 < a1; c0 += CHUNK) {
+        const int ai = c0 + tid;
+        bool keep = false;
+        double xa = 0.0, ya = 0.0;
+        int z = 0;
+        if (ai < a1) {
+            xa = a.x[ai];
+            ya = a.y[ai];
+            z = a.Z[ai];
+            double dx = fabs(xa - xc);
+            dx = fmin(dx, a.ax - dx);
+            double dy = fabs(ya - yc);
+            dy = fmin(dy, a.by - dy);
+            keep = (dx - hx < rad) && (dy - hy < rad);
+        }
+        // order-preserving compaction of the kept atoms
+        const unsigned ball = __ballot_sync(0xffffffffu, keep);
+        __syncthreads();  // the previous chunk's pair loop is done with the lists
+        if (lane == 0) wcount[warp] = __popc(ball);
+        __syncthreads();
+        int pos = __popc(ball & ((1u << lane) - 1u));
+        int total = 0;
+        for (int w = 0; w < THREADS / 32; ++w) {
+            if (w < warp) pos += wcount[w];
+            total += wcount[w];
+        }
+        if (keep) {
+            sZ[pos] = z;
+            sxa[pos] = xa;
+            sya[pos] = ya;
+        }
+        __syncthreads();
+        // per-atom offsets of this tile's columns and rows, formed in FP64 with
+        // the minimum image of ModelPotential.cu:154-203 (|d|, folded past half a cell)
+        for (int idx = tid; idx < total * (TX + TY); idx += THREADS) {
+            const int k = idx / (TX + TY), i = idx % (TX + TY);
+            if (i < TX) {
+                double d = fabs(sxa[k] - (double)(ix0 + i) * a.dxp);
+                if (d >= 0.5 * a.ax) d = a.ax - d;
+                sdx[k][i] = (float)d;
+            } else {
+                double d = fabs(sya[k] - (double)(iy0 + i - TX) * a.dyp);
+                if (d >= 0.5 * a.by) d = a.by - d;
+                sdy[k][i - TX] = (float)d;
+            }
+        }
+        __syncthreads();
+        for (int k = 0; k < total; ++k) {
+            const float dx = sdx[k][tx], dy = sdy[k][ty];
+            const float r2 = dx * dx + dy * dy;
+            if (r2 < a.rad2) {
+                const float r = fmaxf(sqrtf(r2), 1.0e-10f);
+                const float *p = a.sp + sZ[k] * 12;
+                float v = __ldg(p + 0) * bessk0f(__ldg(p + 1) * r) +
+                          __ldg(p + 2) * bessk0f(__ldg(p + 3) * r) +
+                          __ldg(p + 4) * bessk0f(__ldg(p + 5) * r);
+                const float rr = r * r;
+                v += __ldg(p + 6) * expf(-__ldg(p + 7) * rr) + __ldg(p + 8) * expf(-__ldg(p + 9) * rr) +
+                     __ldg(p + 10) * expf(-__ldg(p + 11) * rr);
+                acc += v;
+            }
+        }
+    }
+    const int ix = ix0 + tx, iy = iy0 + ty;
+    if (ix < a.nx && iy < a.ny) a.v[((size_t)s * a.nx + ix) * a.ny + iy] = acc;
+}
+
+cudaError_t launch_potential(const PotArgs &a, cudaStream_t s, int64_t *launches) {
+    ++*launches;
+    dim3 grid(a.ny / TY, a.nx / TX, a.nslice);
+    potential_kernel<<<grid, THREADS, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace msl

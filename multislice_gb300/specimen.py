@@ -1,0 +1,157 @@
+"""Seeded specimen generators and scan geometry for the benchmark workloads.
+
+Host logic only (numpy).  Atom lists use Cartesian Angstrom coordinates with z
+along the beam, the content a reference .coo file carries once its fractional
+coordinates are scaled by the cell (amodel/include/ModelCoo.cpp:20-90).
+
+Every generator takes ``z_offset``: a rigid shift of the whole crystal along z.
+Crystals on ideal sites put whole atomic layers exactly on slice boundaries
+when the slice thickness divides the period (Si with a/4 slices, SrTiO3 with
+a/2, Au with a/2); binning by floor(z/dz) then depends on the last bit of z.
+Shifting by half a slice centres every layer in its slice and removes that
+ambiguity without changing the specimen.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+SI_DIAMOND_BASIS = np.array([
+    [0.0, 0.0, 0.0], [0.0, 0.5, 0.5], [0.5, 0.0, 0.5], [0.5, 0.5, 0.0],
+    [0.25, 0.25, 0.25], [0.25, 0.75, 0.75], [0.75, 0.25, 0.75], [0.75, 0.75, 0.25],
+])
+FCC_BASIS = np.array([[0.0, 0.0, 0.0], [0.0, 0.5, 0.5], [0.5, 0.0, 0.5], [0.5, 0.5, 0.0]])
+# SrTiO3 perovskite: Sr (0,0,0), Ti (1/2,1/2,1/2), O at the face centres
+SRTIO3_BASIS = np.array([[0.0, 0.0, 0.0], [0.5, 0.5, 0.5], [0.5, 0.5, 0.0], [0.5, 0.0, 0.5],
+                         [0.0, 0.5, 0.5]])
+SRTIO3_Z = np.array([38, 22, 8, 8, 8])
+
+
+@dataclass
+class Specimen:
+    x: np.ndarray
+    y: np.ndarray
+    z: np.ndarray
+    Z: np.ndarray
+    ax: float
+    by: float
+    cz: float
+
+    @property
+    def natom(self):
+        return len(self.x)
+
+
+def crystal(a, basis, Zs, ncx, ncy, ncz, z_offset=0.0):
+    """Tile a cubic cell of side a, basis in fractional coordinates."""
+    basis = np.asarray(basis, dtype=np.float64)
+    Zs = np.broadcast_to(np.asarray(Zs), (len(basis),))
+    i, j, k = np.meshgrid(np.arange(ncx), np.arange(ncy), np.arange(ncz), indexing="ij")
+    cells = np.stack([i.ravel(), j.ravel(), k.ravel()], axis=1).astype(np.float64)
+    pos = (cells[:, None, :] + basis[None, :, :]).reshape(-1, 3) * a
+    Z = np.tile(Zs, len(cells)).astype(np.int32)
+    return Specimen(pos[:, 0].copy(), pos[:, 1].copy(), pos[:, 2] + z_offset, Z,
+                    ncx * a, ncy * a, ncz * a)
+
+
+def si_diamond(ncx=5, ncy=5, ncz=20, a=5.431, z_offset=None):
+    """Diamond-cubic Si on ideal sites (8 atoms per cell)."""
+    if z_offset is None:
+        z_offset = a / 8.0  # half of an a/4 slice
+    return crystal(a, SI_DIAMOND_BASIS, 14, ncx, ncy, ncz, z_offset)
+
+
+def srtio3(ncx=8, ncy=8, ncz=50, a=3.905, z_offset=None):
+    """SrTiO3 perovskite on ideal sites (5 atoms per cell)."""
+    if z_offset is None:
+        z_offset = a / 4.0  # half of an a/2 slice
+    return crystal(a, SRTIO3_BASIS, SRTIO3_Z, ncx, ncy, ncz, z_offset)
+
+
+def fcc_au(ncx=16, ncy=16, ncz=40, a=4.078, z_offset=None):
+    """fcc Au on ideal sites (4 atoms per cell)."""
+    if z_offset is None:
+        z_offset = a / 4.0
+    return crystal(a, FCC_BASIS, 79, ncx, ncy, ncz, z_offset)
+
+
+def jitter(spec: Specimen, sigma, rng):
+    """Frozen-phonon configuration: iid Gaussian displacement per axis."""
+    d = rng.normal(0.0, sigma, size=(spec.natom, 3))
+    return Specimen(spec.x + d[:, 0], spec.y + d[:, 1], spec.z + d[:, 2], spec.Z.copy(),
+                    spec.ax, spec.by, spec.cz)
+
+
+def amorphous(box, thickness, density, dmin, Zs, weights, rng, max_tries=60):
+    """Atoms uniform in a box with a minimum separation (dart throwing on a cell grid)."""
+    vol = box[0] * box[1] * thickness
+    n_target = int(round(density * vol))
+    cell = dmin
+    nc = np.maximum((np.array([box[0], box[1], thickness]) / cell).astype(int), 1)
+    grid = {}
+    pts = []
+    tries = 0
+    while len(pts) < n_target and tries < max_tries * n_target:
+        tries += 1
+        p = rng.random(3) * np.array([box[0], box[1], thickness])
+        c = tuple((p / cell).astype(int) % nc)
+        ok = True
+        for dx in (-1, 0, 1):
+            for dy in (-1, 0, 1):
+                for dz in (-1, 0, 1):
+                    q = ((c[0] + dx) % nc[0], (c[1] + dy) % nc[1], (c[2] + dz) % nc[2])
+                    for o in grid.get(q, ()):
+                        d = p - pts[o]
+                        d[:2] -= np.round(d[:2] / np.array(box)) * np.array(box)
+                        if d @ d < dmin * dmin:
+                            ok = False
+                            break
+                    if not ok:
+                        break
+                if not ok:
+                    break
+            if not ok:
+                break
+        if ok:
+            grid.setdefault(c, []).append(len(pts))
+            pts.append(p)
+    pts = np.array(pts).reshape(-1, 3)
+    Z = rng.choice(np.asarray(Zs), size=len(pts), p=np.asarray(weights) / np.sum(weights))
+    return Specimen(pts[:, 0].copy(), pts[:, 1].copy(), pts[:, 2].copy(), Z.astype(np.int32),
+                    float(box[0]), float(box[1]), float(thickness))
+
+
+def raster(x0, x1, y0, y1, nx, ny):
+    """Probe positions of an nx x ny raster over [x0, x1) x [y0, y1), x-major."""
+    xs = x0 + (x1 - x0) * np.arange(nx) / nx
+    ys = y0 + (y1 - y0) * np.arange(ny) / ny
+    X, Y = np.meshgrid(xs, ys, indexing="ij")
+    return np.stack([X.ravel(), Y.ravel()], axis=1)
+
+
+def mrad_to_k(mrad, kev):
+    """Scattering angle (mrad) to spatial frequency theta/lambda (1/A)."""
+    emass, hc = 510.99906, 12.3984244
+    lam = hc / np.sqrt(kev * (2.0 * emass + kev))
+    return np.asarray(mrad, dtype=np.float64) * 1e-3 / lam
+
+
+# --------------------------------------------------------------- workloads
+def config_si_ctem():
+    """Si [001], 5x5x20 cells, 256^2, dz = a/4 (80 slices), 200 kV plane wave."""
+    spec = si_diamond()
+    return dict(spec=spec, nx=256, ny=256, nslice=80, kev=200.0, radius=5.0)
+
+
+def config_srtio3_stem(nprobe_side=64):
+    """SrTiO3 [001], 8x8x50 cells, 512^2, 100 slices, 200 kV, 25 mrad probe,
+    64x64 raster over the central 2x2 cells, HAADF 80-200 mrad, ABF 11-22 mrad."""
+    a = 3.905
+    spec = srtio3()
+    kev = 200.0
+    xy = raster(3 * a, 5 * a, 3 * a, 5 * a, nprobe_side, nprobe_side)
+    return dict(spec=spec, nx=512, ny=512, nslice=100, kev=kev, radius=5.0,
+                k_ap=float(mrad_to_k(25.0, kev)), probe_xy=xy,
+                det_k=[(float(mrad_to_k(80.0, kev)), float(mrad_to_k(200.0, kev))),
+                       (float(mrad_to_k(11.0, kev)), float(mrad_to_k(22.0, kev)))])

@@ -1,0 +1,334 @@
+"""CPU oracle for the multislice hot path — TEST INFRASTRUCTURE ONLY.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may import
+this module, and only as the checker (or the timed CPU baseline), never as the
+product path.  The product is libmsl.so (include/msl.h).
+
+A numpy restatement of the reference's algorithm, in Kirkland's conventions:
+
+* FFT: Kirkland's "fft" is FFTW_BACKWARD (exp(+i..)) unscaled and his "ifft" is
+  FFTW_FORWARD (exp(-i..)) scaled by 1/(nx*ny)   (multislice/cfpix.cpp:115-230).
+* Layout: x-major, element (ix, iy) at iy + ix*ny   (cfpix.hpp:99-125).
+* Potential: Kirkland's vzatom() functional form (multislice/slicelib.cpp:2666-2716,
+  Bessel K0/I0 of Abramowitz & Stegun 9.8.1-9.8.6 at :168-235) with the
+  reference's FPARAMS.DAT coefficients, summed in real space per slice with the
+  z-binning, single minimum image and strict cutoff of LMultiSlice
+  (ImageSimulation/LMultiSlice/ModelPotential.cu:27-99, :125-230).
+* Transmission: t = exp(i*sigma*V_z) band-limited to k < (2/3) k_Nyquist by
+  fft -> mask -> ifft   (multislice/mulslice.cpp:414-421, :481-489, :515-522).
+* Propagator: separable px(kx)*py(ky) with py applied first, zero outside the
+  same band limit   (mulslice.cpp:494-513, slicelib.cpp:744-790).
+* Slice loop: wave *= t; fft; propagate; ifft   (mulslice.cpp:706-739).
+* STEM: probe of MSProject.cs:458-514, detection after the propagator of each
+  checkpoint slice (MSReuseCalculator.cs:36-92), annular sums with inclusive
+  bounds (MSProject.cs:792-842).  The C# code works in the complex-conjugate
+  convention of Kirkland's; every intensity is identical, so the probe here is
+  the conjugate of the C# probe and the loop is Kirkland's.
+
+Two precisions: ``complex64`` mirrors Kirkland's single-precision arithmetic
+(float tables built as mulslice.cpp builds them); ``complex128`` is the FP64
+oracle (all phase arguments and tables in double).
+
+Pinning: tests/test_oracle_golden.py checks this module against golden vectors
+produced by the reference's own compiled code (oracle/ref, see
+tests/golden/make_golden.py).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+try:  # scipy.fft gives multi-threaded transforms for the CPU baseline
+    import scipy.fft as _sfft
+except Exception:  # pragma: no cover
+    _sfft = None
+
+EMASS_KEV = 510.99906      # slicelib.cpp:2800
+HC_KEV_A = 12.3984244      # slicelib.cpp:2801
+AL = 300.8242834           # slicelib.cpp:2673 (Lorentzian prefactor)
+AG = 150.4121417           # slicelib.cpp:2673 (Gaussian prefactor)
+PI_K = 3.141592654         # slicelib.cpp:2674
+
+_I0A = (1.0, 3.5156229, 3.0899424, 1.2067492, 0.2659732, 0.0360768, 0.0045813)
+_I0B = (0.39894228, 0.01328592, 0.00225319, -0.00157565, 0.00916281, -0.02057706,
+        0.02635537, -0.01647633, 0.00392377)
+_K0A = (-0.57721566, 0.42278420, 0.23069756, 0.03488590, 0.00262698, 0.00010750, 0.00000740)
+_K0B = (1.25331414, -0.07832358, 0.02189568, -0.01062446, 0.00587872, -0.00251540, 0.00053208)
+
+
+# ----------------------------------------------------------------- constants
+def wavelength(kev):
+    """Electron wavelength in Angstrom (slicelib.cpp:2795-2806)."""
+    return HC_KEV_A / np.sqrt(kev * (2.0 * EMASS_KEV + kev))
+
+
+def sigma(kev):
+    """Interaction constant in rad/(kV*Angstrom) (slicelib.cpp:2387-2412)."""
+    x = (EMASS_KEV + kev) / (2.0 * EMASS_KEV + kev)
+    return 2.0 * (4.0 * np.arctan(1.0)) * x / (wavelength(kev) * kev)
+
+
+# ----------------------------------------------------------------- potential
+def _horner(coefs, t):
+    s = np.full_like(t, coefs[-1])
+    for c in coefs[-2::-1]:
+        s = s * t + c
+    return s
+
+
+def bessi0(x):
+    """Modified Bessel I0, A&S 9.8.1-9.8.2 (slicelib.cpp:168-196)."""
+    x = np.asarray(x, dtype=np.float64)
+    ax = np.abs(x)
+    small = ax <= 3.75
+    t_s = (x / 3.75) ** 2
+    t_l = 3.75 / np.where(small, 1.0, ax)
+    s_s = _horner(_I0A, t_s)
+    s_l = _horner(_I0B, t_l) * np.exp(np.where(small, 0.0, ax)) / np.sqrt(np.where(small, 1.0, ax))
+    return np.where(small, s_s, s_l)
+
+
+def bessk0(x):
+    """Modified Bessel K0, A&S 9.8.5-9.8.6 (slicelib.cpp:210-235)."""
+    x = np.asarray(x, dtype=np.float64)
+    ax = np.abs(x)
+    small = ax <= 2.0
+    axs = np.where(small & (ax > 0), ax, 1.0)
+    x2 = (axs / 2.0) ** 2
+    s_s = -np.log(axs / 2.0) * bessi0(axs) + _horner(_K0A, x2)
+    axl = np.where(small, 3.0, ax)
+    s_l = np.exp(-axl) * _horner(_K0B, 2.0 / axl) / np.sqrt(axl)
+    out = np.where(small, s_s, s_l)
+    return np.where(ax > 0, out, 1.0e20)
+
+
+def vzatom(Z, r, fparams):
+    """Projected atomic potential in V*Angstrom (slicelib.cpp:2666-2716)."""
+    r = np.maximum(np.abs(np.asarray(r, dtype=np.float64)), 1.0e-10)
+    p = fparams[Z]
+    x = 2.0 * PI_K * r
+    suml = (p[0] * bessk0(x * np.sqrt(p[1])) + p[2] * bessk0(x * np.sqrt(p[3]))
+            + p[4] * bessk0(x * np.sqrt(p[5])))
+    x = (PI_K * r) ** 2
+    sumg = (p[6] * np.exp(-x / p[7]) / p[7] + p[8] * np.exp(-x / p[9]) / p[9]
+            + p[10] * np.exp(-x / p[11]) / p[11])
+    return AL * suml + AG * sumg
+
+
+def slice_index(z, cz_total, nslice):
+    """Slice bin of each atom: floor(z/dz), -1 if outside [0, cz) (ModelPotential.cu:63-71)."""
+    dz = cz_total / nslice
+    kz = np.floor(np.asarray(z, dtype=np.float64) / dz).astype(np.int64)
+    bad = (np.asarray(z) < 0.0) | (kz < 0) | (kz >= nslice)
+    return np.where(bad, -1, kz)
+
+
+def potential(x, y, z, Znum, fparams, ax, by, cz_total, nx, ny, nslice, radius):
+    """V_z per slice, float64 [nslice, nx, ny] (ModelPotential.cu:27-99, :154-203)."""
+    if 2.0 * radius >= ax or 2.0 * radius >= by:
+        raise ValueError("cutoff radius must be below half the cell")
+    out = np.zeros((nslice, nx, ny), dtype=np.float64)
+    kz = slice_index(z, cz_total, nslice)
+    dxp, dyp = ax / nx, by / ny
+    ixs = np.arange(nx)
+    iys = np.arange(ny)
+    for a in range(len(x)):
+        if kz[a] < 0:
+            continue
+        xa = x[a] - ax * np.floor(x[a] / ax)
+        ya = y[a] - by * np.floor(y[a] / by)
+        ddx = np.abs(xa - ixs * dxp)
+        ddx = np.where(ddx >= ax / 2.0, ax - ddx, ddx)
+        ddy = np.abs(ya - iys * dyp)
+        ddy = np.where(ddy >= by / 2.0, by - ddy, ddy)
+        sx = np.nonzero(ddx < radius)[0]
+        sy = np.nonzero(ddy < radius)[0]
+        r = np.sqrt(ddx[sx, None] ** 2 + ddy[None, sy] ** 2)
+        m = r < radius
+        v = np.where(m, vzatom(int(Znum[a]), np.maximum(r, 1.0e-10), fparams), 0.0)
+        out[kz[a]][np.ix_(sx, sy)] += v
+    return out
+
+
+# ------------------------------------------------------------ FFT conventions
+def _fft_mod():
+    return _sfft if _sfft is not None else np.fft
+
+
+def kfft(w, workers=1):
+    """Kirkland fft: exp(+i..), unscaled, over the last two axes."""
+    m = _fft_mod()
+    if m is np.fft:
+        return np.fft.ifft2(w, axes=(-2, -1), norm="forward")
+    return m.ifft2(w, axes=(-2, -1), norm="forward", workers=workers)
+
+
+def kifft(w, workers=1):
+    """Kirkland ifft: exp(-i..), scaled by 1/(nx*ny), over the last two axes."""
+    m = _fft_mod()
+    if m is np.fft:
+        return np.fft.fft2(w, axes=(-2, -1), norm="forward")
+    return m.fft2(w, axes=(-2, -1), norm="forward", workers=workers)
+
+
+# --------------------------------------------------------------- k-space grid
+def freqn(n, a):
+    """Spatial frequencies k and k^2 as float32 (slicelib.cpp:433-463)."""
+    f32 = np.float32
+    imid = int(n / 2.0 + 0.5)
+    i = np.arange(n)
+    num = np.where(i > imid, i - n, i).astype(f32)
+    k = num / f32(a)
+    return k.astype(f32), (k * k).astype(f32)
+
+
+def k2max_f32(nx, ny, ax, by, bw=2.0 / 3.0):
+    """Squared band limit in float32 (mulslice.cpp:481-489)."""
+    f32 = np.float32
+    k = f32(nx) / (f32(2.0) * f32(ax))
+    t = f32(ny) / (f32(2.0) * f32(by))
+    if t < k:
+        k = t
+    k = f32(bw) * k
+    return f32(k * k)
+
+
+def band_mask(nx, ny, ax, by, bw=2.0 / 3.0):
+    kx, kx2 = freqn(nx, ax)
+    ky, ky2 = freqn(ny, by)
+    return (kx2[:, None] + ky2[None, :]) < k2max_f32(nx, ny, ax, by, bw)
+
+
+# ------------------------------------------------------------ transmission
+def transmission(vz, v0, ax, by, dtype=np.complex64, bw=2.0 / 3.0):
+    """Band-limited exp(i sigma V_z) per layer (mulslice.cpp:414-421, :515-522)."""
+    nl, nx, ny = vz.shape
+    sig = sigma(v0) / 1000.0
+    if dtype == np.complex64:
+        f32 = np.float32
+        wl = f32(wavelength(v0))
+        mm0 = f32(1.0) + f32(v0) / f32(511.0)
+        vfile = (sig * vz / (float(wl) * float(mm0))).astype(f32)
+        ph = (wl * mm0) * vfile
+        t = (np.cos(ph.astype(np.float64)).astype(f32)
+             + 1j * np.sin(ph.astype(np.float64)).astype(f32)).astype(np.complex64)
+    else:
+        ph = sig * vz
+        t = np.exp(1j * ph).astype(np.complex128)
+    m = band_mask(nx, ny, ax, by, bw)
+    T = kfft(t)
+    T = np.where(m[None], T, 0)
+    return kifft(T).astype(dtype)
+
+
+def propagator_tables(nx, ny, ax, by, v0, dz, ctilt=(0.0, 0.0), precision="f32"):
+    """px, py complex tables for one slice thickness (mulslice.cpp:494-513).
+
+    precision "f32" builds the argument in float as mulslice.cpp does;
+    "f64" builds it in double (the FP64 oracle and the product's tables)."""
+    f32 = np.float32
+    kx, kx2 = freqn(nx, ax)
+    ky, ky2 = freqn(ny, by)
+    if precision == "f32":
+        wl = f32(wavelength(v0))
+        sc = f32(f32(4.0 * np.arctan(1.0)) * f32(dz))
+        tctx = f32(2.0 * np.tan(ctilt[0]))
+        tcty = f32(2.0 * np.tan(ctilt[1]))
+        tx = (sc * (kx2 * wl - kx * tctx)).astype(np.float64)
+        ty = (sc * (ky2 * wl - ky * tcty)).astype(np.float64)
+        px = np.cos(tx).astype(f32) + 1j * (-np.sin(tx)).astype(f32)
+        py = np.cos(ty).astype(f32) + 1j * (-np.sin(ty)).astype(f32)
+        return px.astype(np.complex64), py.astype(np.complex64)
+    wl = wavelength(v0)
+    kxd, kyd = kx.astype(np.float64), ky.astype(np.float64)
+    tx = np.pi * dz * (kxd * kxd * wl - kxd * 2.0 * np.tan(ctilt[0]))
+    ty = np.pi * dz * (kyd * kyd * wl - kyd * 2.0 * np.tan(ctilt[1]))
+    return np.exp(-1j * tx), np.exp(-1j * ty)
+
+
+# --------------------------------------------------------------- slice loop
+def propagate(W, px, py, mask):
+    """Multiply by py(ky) then px(kx), zero outside the band (slicelib.cpp:744-790)."""
+    W = W * py[None, :]
+    W = W * px[:, None]
+    return np.where(mask, W, 0).astype(W.dtype)
+
+
+def multislice(wave, trans, props, layer_seq, mask, workers=1, detect=None):
+    """Run the coherent slice loop on wave [..., nx, ny] (mulslice.cpp:706-739).
+
+    trans [nlayer, nx, ny]; props: list of (px, py) per layer; detect: optional
+    (checkpoints, fn) where fn(W) -> array is called after the propagator of each
+    checkpoint slice.  Returns the exit wave (and the detector results)."""
+    w = np.array(wave, copy=True)
+    out = []
+    cps = list(detect[0]) if detect else []
+    last = cps[-1] if cps else None
+    for s, l in enumerate(layer_seq):
+        w = w * trans[l]
+        W = kfft(w, workers)
+        px, py = props[l]
+        W = propagate(W, px, py, mask)
+        if detect and s in cps:
+            out.append(detect[1](W))
+            if s == last:
+                return w, out
+        w = kifft(W, workers).astype(wave.dtype)
+    return w, out
+
+
+# --------------------------------------------------------------------- STEM
+def signed_index(n):
+    i = np.arange(n)
+    return np.where(i < n // 2, i, i - n)
+
+
+def k_tables_f64(nx, ny, ax, by):
+    """C#-style reciprocal coordinates (double) of MSProject.cs:470-484."""
+    return signed_index(nx) / ax, signed_index(ny) / by
+
+
+def probe(nx, ny, ax, by, v0, kap_in, kap_out, df, cs, xy, dtype=np.complex64):
+    """Converged probe(s) in real space, [nprobe, nx, ny] (MSProject.cs:458-514)."""
+    lam = wavelength(v0)
+    kxd, kyd = k_tables_f64(nx, ny, ax, by)
+    s = kxd[:, None] ** 2 + kyd[None, :] ** 2
+    ap = (s >= kap_in ** 2) & (s <= kap_out ** 2)
+    chi = np.pi * (lam * df * s + 0.5 * cs * lam ** 3 * s * s)
+    i = signed_index(nx)[:, None]
+    j = signed_index(ny)[None, :]
+    xy = np.atleast_2d(np.asarray(xy, dtype=np.float64))
+    out = np.empty((len(xy), nx, ny), dtype=dtype)
+    for p, (xp, yp) in enumerate(xy):
+        ph = 2.0 * np.pi * (i * (xp / ax) + j * (yp / by)) - chi
+        if dtype == np.complex64:
+            P = np.where(ap, np.cos(ph).astype(np.float32) + 1j * np.sin(ph).astype(np.float32), 0)
+        else:
+            P = np.where(ap, np.exp(1j * ph), 0)
+        out[p] = kifft(P.astype(dtype))
+    return out
+
+
+def detector_masks(nx, ny, ax, by, det_k):
+    """Boolean annulus masks [ndet, nx, ny]: kin^2 <= s <= kout^2 (MSProject.cs:806-829)."""
+    kxd, kyd = k_tables_f64(nx, ny, ax, by)
+    s = kxd[:, None] ** 2 + kyd[None, :] ** 2
+    return np.stack([(s <= ko * ko) & (s >= ki * ki) for ki, ko in det_k])
+
+
+def stem(trans, props, layer_seq, mask, probes, det_masks, checkpoints, workers=1):
+    """Detector sums [nprobe, ncheck, ndet] in the C# scale (unscaled |Psi(k)|^2)."""
+    dm = det_masks.astype(np.float64)
+
+    def fn(W):
+        I = (W.real.astype(np.float64) ** 2 + W.imag.astype(np.float64) ** 2)
+        return np.einsum("...xy,dxy->...d", I, dm)
+
+    _, res = multislice(probes, trans, props, layer_seq, mask, workers,
+                        detect=(list(checkpoints), fn))
+    return np.stack(res, axis=-2)
+
+
+def rel_l2(a, b):
+    a = np.asarray(a)
+    b = np.asarray(b)
+    return float(np.linalg.norm((a - b).ravel()) / np.linalg.norm(b.ravel()))
