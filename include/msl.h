@@ -183,6 +183,37 @@ int msl_profile_read(const msl_ctx *ctx, int kind, int64_t *launches, double *ms
  * sized batch * nx * ny * 8 bytes. */
 int msl_set_probe_batch(msl_ctx *ctx, int batch);
 
+/* ------------------------------------------------- no-allocation variant */
+
+/* msl_multislice for callers that may not allocate device memory -- for
+ * instance code living inside an application whose own pool allocator owns
+ * the GPU's memory, or a latency-critical loop in which a cudaMalloc/cudaFree
+ * would stall the whole device.  No counterpart exists in the reference: it is
+ * an addition of this library.
+ *
+ * Same arithmetic, kernels and launch sequence as msl_multislice, but no
+ * context and no allocation of any kind: trans and psi must be device buffers
+ * of the current device, owned by the caller; dz and layer_seq are host
+ * arrays.  The twiddle, band-limit and propagator tables go into one
+ * file-scope device array of MSL_NOALLOC_SCRATCH_BYTES that every GPU loading
+ * the library keeps until exit.  Limits: sides up to MSL_NOALLOC_MAX_SIDE and
+ * at most MSL_NOALLOC_MAX_LAYERS layers (ntrans); larger requests return
+ * MSL_E_ARG / MSL_E_UNSUPPORTED without touching the device.
+ *
+ * Work runs on `stream` (a cudaStream_t, NULL for the default stream) and the
+ * call waits for that stream before returning.  The first call on each device
+ * looks up the array's device address (cudaGetSymbolAddress) with that device
+ * current; make that first call before any stream capture.  All calls share
+ * the array: calls that overlap on the GPU (several host threads, several
+ * streams of one device) race on it.  Errors are reported by the return code
+ * only (there is no context to hold a message). */
+#define MSL_NOALLOC_MAX_SIDE 2048
+#define MSL_NOALLOC_MAX_LAYERS 64
+#define MSL_NOALLOC_SCRATCH_BYTES 2150400
+int msl_multislice_noalloc(const msl_grid *grid, const msl_optics *optics, const float *trans,
+                           int ntrans, const double *dz, const int *layer_seq, int nslice,
+                           float *psi, int batch, int plane_wave, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

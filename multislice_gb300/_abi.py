@@ -21,7 +21,7 @@ EXPORTS = (
     "msl_ctx_create", "msl_ctx_destroy", "msl_last_error", "msl_version", "msl_kernel_launches",
     "msl_fparams_parse", "msl_wavelength", "msl_sigma", "msl_potential_build",
     "msl_transmission_build", "msl_fft2d", "msl_multislice", "msl_stem_scan",
-    "msl_set_probe_batch", "msl_profile_enable", "msl_profile_read",
+    "msl_set_probe_batch", "msl_profile_enable", "msl_profile_read", "msl_multislice_noalloc",
 )
 PROF_ROW, PROF_COL, PROF_POTENTIAL, PROF_OTHER = 0, 1, 2, 3
 
@@ -85,6 +85,8 @@ def load(path=LIB_PATH):
         "msl_set_probe_batch": (c_int, [P, c_int]),
         "msl_profile_enable": (c_int, [P, c_int]),
         "msl_profile_read": (c_int, [P, c_int, POINTER(c_int64), POINTER(c_double)]),
+        "msl_multislice_noalloc": (c_int, [POINTER(Grid), POINTER(Optics), P, c_int, P, P, c_int,
+                                           P, c_int, c_int, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
