@@ -61,6 +61,7 @@ struct msl_ctx {
     double prof_ms[MSL_PROF_KINDS] = {0};
     DevBuf wave, in_stage, trans_stage, tabs, apchi, exy, fxy, detmask, partial, detout, pot,
         atoms;
+    int *dflag = nullptr;  // device flag raised by a kernel whose bounded wait gave up
 };
 
 namespace {
@@ -276,9 +277,10 @@ int build_slice_tables(msl_ctx *c, const msl_grid *g, const msl_optics *o, int n
 }
 
 ColArgs col_args(const msl_grid *g, const SliceTables &st, float2 *tw, int layer, float2 *wave,
-                 int batch, int flags) {
+                 int batch, int flags, int *err) {
     ColArgs a;
     memset(&a, 0, sizeof(a));
+    a.err = err;
     a.in = wave;
     a.out = wave;
     a.batch = batch;
@@ -314,6 +316,23 @@ RowArgs row_args(const msl_grid *g, float2 *tw, const float2 *trans, float2 *wav
         if (e_ != cudaSuccess)                                                               \
             return fail(ctx, MSL_E_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e_)); \
     } while (0)
+
+// Zero the kernel error flag before a call's launches.
+int err_reset(msl_ctx *c) {
+    if (!c->dflag) {
+        CUDA_TRY(c, cudaMalloc(&c->dflag, sizeof(int)));
+    }
+    CUDA_TRY(c, cudaMemsetAsync(c->dflag, 0, sizeof(int), c->stream));
+    return MSL_OK;
+}
+
+// After the stream is synchronized: fail if a kernel raised the flag.
+int err_check(msl_ctx *c) {
+    int h = 0;
+    CUDA_TRY(c, cudaMemcpy(&h, c->dflag, sizeof(int), cudaMemcpyDeviceToHost));
+    if (h) return fail(c, MSL_E_CUDA, "a column-pass wait for its TMA tile timed out");
+    return MSL_OK;
+}
 
 int check_layers(msl_ctx *c, int ntrans, const double *dz, const int *layer_seq, int nslice) {
     if (ntrans < 1) return fail(c, MSL_E_ARG, "ntrans must be >= 1");
@@ -373,6 +392,7 @@ int msl_ctx_destroy(msl_ctx *c) {
     DevBuf *bufs[] = {&c->wave, &c->in_stage, &c->trans_stage, &c->tabs, &c->apchi, &c->exy,
                       &c->fxy, &c->detmask, &c->partial, &c->detout, &c->pot, &c->atoms};
     for (DevBuf *b : bufs) b->release();
+    if (c->dflag) cudaFree(c->dflag);
     cudaStreamDestroy(c->stream);
     delete c;
     return MSL_OK;
@@ -541,6 +561,7 @@ int msl_transmission_build(msl_ctx *c, const msl_grid *g, const msl_optics *o, c
     if ((rc = check_optics(c, o))) return rc;
     if (!v || !t_out || nlayer < 1) return fail(c, MSL_E_ARG, "null argument or nlayer < 1");
     CUDA_TRY(c, cudaSetDevice(c->device));
+    if ((rc = err_reset(c))) return rc;
     const int nx = g->nx, ny = g->ny;
     const size_t n2 = (size_t)nx * ny;
     const float *vd;
@@ -561,8 +582,7 @@ int msl_transmission_build(msl_ctx *c, const msl_grid *g, const msl_optics *o, c
     r.vpot = vd;
     r.phase_scale = msl_sigma(o->kev) / 1000.0;  // rad per V*A
     LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_row_pass(ny, r, c->stream, c->nsm, &c->launches); }));
-    ColArgs ca = col_args(g, st, twc, 0, td, nlayer,
-                          msl::COL_LOAD | msl::COL_FWD | msl::COL_PROP | msl::COL_INV | msl::COL_STORE);
+    ColArgs ca = col_args(g, st, twc, 0, td, nlayer, msl::COL_LOAD | msl::COL_FWD | msl::COL_PROP | msl::COL_INV | msl::COL_STORE, c->dflag);
     LAUNCH_TRY(c, timed(c, MSL_PROF_COL, [&] { return msl::launch_col_pass(nx, ca, c->stream, c->nsm, &c->launches); }));
     r = row_args(g, twr, nullptr, td, nlayer, msl::ROW_LOAD | msl::ROW_INV);
     LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_row_pass(ny, r, c->stream, c->nsm, &c->launches); }));
@@ -571,6 +591,7 @@ int msl_transmission_build(msl_ctx *c, const msl_grid *g, const msl_optics *o, c
                                     c->stream));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     collect_profile(c);
+    if (c->dflag && (rc = err_check(c))) return rc;
     return MSL_OK;
 }
 
@@ -581,6 +602,7 @@ int msl_fft2d(msl_ctx *c, const msl_grid *g, float *psi, int batch, int dir) {
     if (!psi || batch < 1 || (dir != 1 && dir != -1))
         return fail(c, MSL_E_ARG, "psi must be non-null, batch >= 1, dir = +1 or -1");
     CUDA_TRY(c, cudaSetDevice(c->device));
+    if ((rc = err_reset(c))) return rc;
     const int nx = g->nx, ny = g->ny;
     const size_t bytes = sizeof(float2) * (size_t)nx * ny * batch;
     const bool dev = on_device(psi);
@@ -602,10 +624,10 @@ int msl_fft2d(msl_ctx *c, const msl_grid *g, float *psi, int batch, int dir) {
     if (dir > 0) {
         RowArgs r = row_args(g, twr, nullptr, w, batch, msl::ROW_LOAD | msl::ROW_FWD);
         LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_row_pass(ny, r, c->stream, c->nsm, &c->launches); }));
-        ColArgs ca = col_args(g, st, twc, 0, w, batch, msl::COL_LOAD | msl::COL_FWD | msl::COL_STORE);
+        ColArgs ca = col_args(g, st, twc, 0, w, batch, msl::COL_LOAD | msl::COL_FWD | msl::COL_STORE, c->dflag);
         LAUNCH_TRY(c, timed(c, MSL_PROF_COL, [&] { return msl::launch_col_pass(nx, ca, c->stream, c->nsm, &c->launches); }));
     } else {
-        ColArgs ca = col_args(g, st, twc, 0, w, batch, msl::COL_LOAD | msl::COL_INV | msl::COL_STORE);
+        ColArgs ca = col_args(g, st, twc, 0, w, batch, msl::COL_LOAD | msl::COL_INV | msl::COL_STORE, c->dflag);
         LAUNCH_TRY(c, timed(c, MSL_PROF_COL, [&] { return msl::launch_col_pass(nx, ca, c->stream, c->nsm, &c->launches); }));
         RowArgs r = row_args(g, twr, nullptr, w, batch, msl::ROW_LOAD | msl::ROW_INV);
         r.scale = 1.0f / ((float)nx * (float)ny);
@@ -614,6 +636,7 @@ int msl_fft2d(msl_ctx *c, const msl_grid *g, float *psi, int batch, int dir) {
     if (!dev) CUDA_TRY(c, cudaMemcpyAsync(psi, w, bytes, cudaMemcpyDeviceToHost, c->stream));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     collect_profile(c);
+    if (c->dflag && (rc = err_check(c))) return rc;
     return MSL_OK;
 }
 
@@ -627,6 +650,7 @@ int msl_multislice(msl_ctx *c, const msl_grid *g, const msl_optics *o, const flo
     if ((rc = check_layers(c, ntrans, dz, layer_seq, nslice))) return rc;
     if (!trans || !psi || batch < 1) return fail(c, MSL_E_ARG, "trans/psi null or batch < 1");
     CUDA_TRY(c, cudaSetDevice(c->device));
+    if ((rc = err_reset(c))) return rc;
     const int nx = g->nx, ny = g->ny;
     const size_t n2 = (size_t)nx * ny;
     const float2 *td;
@@ -654,7 +678,7 @@ int msl_multislice(msl_ctx *c, const msl_grid *g, const msl_optics *o, const flo
         else if (!plane_wave) rf |= msl::ROW_LOAD;
         RowArgs r = row_args(g, twr, td + (size_t)l * n2, w, batch, rf);
         LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_row_pass(ny, r, c->stream, c->nsm, &c->launches); }));
-        ColArgs ca = col_args(g, st, twc, l, w, batch, colf);
+        ColArgs ca = col_args(g, st, twc, l, w, batch, colf, c->dflag);
         LAUNCH_TRY(c, timed(c, MSL_PROF_COL, [&] { return msl::launch_col_pass(nx, ca, c->stream, c->nsm, &c->launches); }));
     }
     RowArgs r = row_args(g, twr, nullptr, w, batch, msl::ROW_LOAD | msl::ROW_INV);
@@ -662,6 +686,7 @@ int msl_multislice(msl_ctx *c, const msl_grid *g, const msl_optics *o, const flo
     if (!dev) CUDA_TRY(c, cudaMemcpyAsync(psi, w, wbytes, cudaMemcpyDeviceToHost, c->stream));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     collect_profile(c);
+    if (c->dflag && (rc = err_check(c))) return rc;
     return MSL_OK;
 }
 
@@ -692,10 +717,10 @@ int msl_stem_scan(msl_ctx *c, const msl_grid *g, const msl_optics *o, const floa
     for (int p = 0; p < 2 * nprobe; ++p)
         if (!is_fin(probe_xy[p])) return fail(c, MSL_E_ARG, "probe positions must be finite");
     CUDA_TRY(c, cudaSetDevice(c->device));
+    if ((rc = err_reset(c))) return rc;
     const int nx = g->nx, ny = g->ny, ndet = det->ndet;
     const size_t n2 = (size_t)nx * ny;
-    const int C = msl::plan_col_c(nx);
-    const int ntile = ny / C;
+    int ntile = 0;  // column tiles per image of the column pass that will run (set below)
     const float2 *td;
     if ((rc = stage_in(c, (const float2 *)trans, sizeof(float2) * n2 * ntrans, c->trans_stage, &td)))
         return rc;
@@ -731,7 +756,6 @@ int msl_stem_scan(msl_ctx *c, const msl_grid *g, const msl_optics *o, const floa
     if (B > nprobe) B = nprobe;
     CUDA_TRY(c, c->wave.ensure(sizeof(float2) * n2 * B));
     CUDA_TRY(c, c->exy.ensure(sizeof(float2) * (size_t)B * (nx + ny) + sizeof(double) * 2 * B));
-    CUDA_TRY(c, c->partial.ensure(sizeof(double) * (size_t)ncheck * B * ntile * ndet));
     const size_t obytes = sizeof(double) * (size_t)nprobe * ncheck * ndet;
     const bool odev = on_device(det_out);
     double *od;
@@ -742,6 +766,11 @@ int msl_stem_scan(msl_ctx *c, const msl_grid *g, const msl_optics *o, const floa
         od = (double *)c->detout.p;
     }
     float2 *w = (float2 *)c->wave.p;
+    {
+        ColArgs probe_cfg = col_args(g, st, twc, 0, w, 1, msl::COL_LOAD | msl::COL_STORE, c->dflag);
+        ntile = ny / msl::plan_col_c_launch(nx, probe_cfg);
+    }
+    CUDA_TRY(c, c->partial.ensure(sizeof(double) * (size_t)ncheck * B * ntile * ndet));
     float2 *ex = (float2 *)c->exy.p, *ey = ex + (size_t)B * nx;
     double *fxy = (double *)(ey + (size_t)B * ny);
     double *partial = (double *)c->partial.p;
@@ -757,7 +786,7 @@ int msl_stem_scan(msl_ctx *c, const msl_grid *g, const msl_optics *o, const floa
         CUDA_TRY(c, cudaMemcpyAsync(fxy, hf.data(), sizeof(double) * 2 * nb, cudaMemcpyHostToDevice,
                                     c->stream));
         LAUNCH_TRY(c, timed(c, MSL_PROF_OTHER, [&] { return msl::launch_probe_shifts(nx, ny, nb, fxy, ex, ey, c->stream, &c->launches); }));
-        ColArgs pa = col_args(g, st, twc, 0, w, nb, msl::COL_PROBE | msl::COL_INV | msl::COL_STORE);
+        ColArgs pa = col_args(g, st, twc, 0, w, nb, msl::COL_PROBE | msl::COL_INV | msl::COL_STORE, c->dflag);
         pa.apchi = apchi;
         pa.ex = ex;
         pa.ey = ey;
@@ -772,7 +801,7 @@ int msl_stem_scan(msl_ctx *c, const msl_grid *g, const msl_optics *o, const floa
             int cf = msl::COL_LOAD | msl::COL_FWD | msl::COL_PROP;
             if (detect) cf |= msl::COL_DETECT;
             if (s < last) cf |= msl::COL_INV | msl::COL_STORE;
-            ColArgs ca = col_args(g, st, twc, l, w, nb, cf);
+            ColArgs ca = col_args(g, st, twc, l, w, nb, cf, c->dflag);
             ca.detmask = mask;
             ca.ndet = ndet;
             ca.partial = partial + (size_t)ic * B * ntile * ndet;
@@ -789,6 +818,7 @@ int msl_stem_scan(msl_ctx *c, const msl_grid *g, const msl_optics *o, const floa
     if (!odev) CUDA_TRY(c, cudaMemcpyAsync(det_out, od, obytes, cudaMemcpyDeviceToHost, c->stream));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     collect_profile(c);
+    if (c->dflag && (rc = err_check(c))) return rc;
     return MSL_OK;
 }
 

@@ -56,6 +56,7 @@ struct ColArgs {
     const uint8_t *detmask;   // [nx][ny], bit d = detector d
     int ndet;
     double *partial;          // [batch][ny / C][ndet]
+    int *err;                 // set to 1 when a bounded wait gives up (may be null)
 };
 
 struct PotArgs {
@@ -70,7 +71,10 @@ struct PotArgs {
 };
 
 bool plan_supported(int n);
+// Columns per tile of the column pass that will run for this call (TMA-fed
+// kernel when the wave buffer allows it, else the register-only kernel).
 int plan_col_c(int n);
+int plan_col_c_launch(int n, const ColArgs &a);
 // Per-stage twiddle tables for side n (exp(+2 pi i r k / (NS R)) at [r][k]).
 void plan_twiddles(int n, std::vector<float2> &out);
 

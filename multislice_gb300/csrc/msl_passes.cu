@@ -17,6 +17,7 @@
 
 #include "msl_fft.cuh"
 #include "msl_internal.h"
+#include "msl_tma.cuh"
 
 namespace msl {
 
@@ -93,6 +94,71 @@ __global__ void __launch_bounds__(RowCfg<N>::THREADS) row_pass_kernel(RowArgs a)
     }
 }
 
+
+// --------------------------------------------------- column-pass pointwise
+// Reciprocal-space probe of MSProject.cs:458-514: A(k) exp(-i chi) / (nx ny)
+// times the two separable position phases.
+template <class P>
+__device__ __forceinline__ void col_probe(float2 (&v)[P::E], const ColArgs &a, int b, int iy, int t) {
+    const float2 eyv = a.ey[(size_t)b * a.ny + iy];
+    const float2 *exb = a.ex + (size_t)b * P::N;
+#pragma unroll
+    for (int e = 0; e < P::E; ++e) {
+        const int ix = t + P::T * e;
+        v[e] = c_mul(c_mul(a.apchi[(size_t)ix * a.ny + iy], exb[ix]), eyv);
+    }
+}
+
+// propagate() of slicelib.cpp:744-790: py then px inside the band limit, 0 outside.
+template <class P>
+__device__ __forceinline__ void col_propagate(float2 (&v)[P::E], const ColArgs &a, int iy, int t) {
+    const float ky2 = a.ky2[iy];
+    const float2 pyv = a.py[iy];
+#pragma unroll
+    for (int e = 0; e < P::E; ++e) {
+        const int ix = t + P::T * e;
+        const float k2 = __fadd_rn(a.kx2[ix], ky2);
+        if (k2 < a.k2max) v[e] = c_mul(c_mul(v[e], pyv), a.px[ix]);
+        else v[e] = make_float2(0.f, 0.f);
+    }
+}
+
+// Annular detector partial sums of one tile (MSProject.cs:806-829): float per
+// thread over its E pixels, then double across the CTA in a fixed order.
+template <class P, int NWARP>
+__device__ __forceinline__ void col_detect(const float2 (&v)[P::E], const ColArgs &a, int b, int iy,
+                                           int t, int ty, int tiles_per_img, double *red) {
+    float acc[kMaxDet];
+#pragma unroll
+    for (int d = 0; d < kMaxDet; ++d) acc[d] = 0.f;
+#pragma unroll
+    for (int e = 0; e < P::E; ++e) {
+        const int ix = t + P::T * e;
+        const unsigned bits = a.detmask[(size_t)ix * a.ny + iy];
+        const float p = v[e].x * v[e].x + v[e].y * v[e].y;
+#pragma unroll
+        for (int d = 0; d < kMaxDet; ++d)
+            if (bits & (1u << d)) acc[d] += p;
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __syncthreads();  // red[] of the previous tile has been consumed
+#pragma unroll
+    for (int d = 0; d < kMaxDet; ++d) {
+        if (d < a.ndet) {
+            double x = (double)acc[d];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+            if (lane == 0) red[warp * kMaxDet + d] = x;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < a.ndet) {
+        double sum = 0.0;
+        for (int w = 0; w < NWARP; ++w) sum += red[w * kMaxDet + threadIdx.x];
+        a.partial[((size_t)b * tiles_per_img + ty) * a.ndet + threadIdx.x] = sum;
+    }
+}
+
 // ------------------------------------------------------------- column pass
 template <int N>
 __global__ void __launch_bounds__(ColCfg<N>::THREADS) col_pass_kernel(ColArgs a) {
@@ -114,64 +180,135 @@ __global__ void __launch_bounds__(ColCfg<N>::THREADS) col_pass_kernel(ColArgs a)
         const size_t base = (size_t)b * N * a.ny + iy;
         float2 v[E];
         if (a.flags & COL_PROBE) {
-            const float2 eyv = a.ey[(size_t)b * a.ny + iy];
-            const float2 *exb = a.ex + (size_t)b * N;
-#pragma unroll
-            for (int e = 0; e < E; ++e) {
-                const int ix = t + T * e;
-                v[e] = c_mul(c_mul(a.apchi[(size_t)ix * a.ny + iy], exb[ix]), eyv);
-            }
+            col_probe<P>(v, a, b, iy, t);
         } else {
 #pragma unroll
             for (int e = 0; e < E; ++e) v[e] = a.in[base + (size_t)(t + T * e) * a.ny];
         }
         if (a.flags & COL_FWD) fft_line<P, +1>(v, t, ad, tw);
-        if (a.flags & COL_PROP) {
-            const float ky2 = a.ky2[iy];
-            const float2 pyv = a.py[iy];
-#pragma unroll
-            for (int e = 0; e < E; ++e) {
-                const int ix = t + T * e;
-                const float k2 = __fadd_rn(a.kx2[ix], ky2);
-                if (k2 < a.k2max) v[e] = c_mul(c_mul(v[e], pyv), a.px[ix]);
-                else v[e] = make_float2(0.f, 0.f);
-            }
-        }
-        if (a.flags & COL_DETECT) {
-            float acc[kMaxDet];
-#pragma unroll
-            for (int d = 0; d < kMaxDet; ++d) acc[d] = 0.f;
-#pragma unroll
-            for (int e = 0; e < E; ++e) {
-                const int ix = t + T * e;
-                const unsigned bits = a.detmask[(size_t)ix * a.ny + iy];
-                const float p = v[e].x * v[e].x + v[e].y * v[e].y;
-#pragma unroll
-                for (int d = 0; d < kMaxDet; ++d)
-                    if (bits & (1u << d)) acc[d] += p;
-            }
-            const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-            __syncthreads();  // red[] of the previous tile has been consumed
-#pragma unroll
-            for (int d = 0; d < kMaxDet; ++d) {
-                if (d < a.ndet) {
-                    double x = (double)acc[d];
-#pragma unroll
-                    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-                    if (lane == 0) red[warp * kMaxDet + d] = x;
-                }
-            }
-            __syncthreads();
-            if (threadIdx.x < a.ndet) {
-                double s = 0.0;
-                for (int w = 0; w < NWARP; ++w) s += red[w * kMaxDet + threadIdx.x];
-                a.partial[((size_t)b * tiles_per_img + ty) * a.ndet + threadIdx.x] = s;
-            }
-        }
+        if (a.flags & COL_PROP) col_propagate<P>(v, a, iy, t);
+        if (a.flags & COL_DETECT) col_detect<P, NWARP>(v, a, b, iy, t, ty, tiles_per_img, red);
         if (a.flags & COL_INV) fft_line<P, -1>(v, t, ad, tw);
         if (a.flags & COL_STORE) {
 #pragma unroll
             for (int e = 0; e < E; ++e) a.out[base + (size_t)(t + T * e) * a.ny] = v[e];
+        }
+    }
+}
+
+
+// ------------------------------------------------- TMA-fed column pass
+// Persistent kernel, one CTA per SM.  Column tiles of C columns x N rows
+// (C * 8 bytes wide: 128 B for N <= 512) arrive by cp.async.bulk.tensor into a
+// ring of three shared-memory buffers: while tile k is transformed in buffer
+// k % 3, tile k+1 is already resident and tile k+2 is in flight.  The same
+// buffer then serves as the transform's exchange space and as the source of
+// the TMA store of the result, so a tile never touches registers-to-global
+// stores.  Every mbarrier wait is bounded; on a timeout the CTA raises *err,
+// waits (bounded) for its loads still in flight and leaves.
+constexpr uint32_t kWaitLimit = 1u << 22;
+
+template <int N> struct ColTmaCfg {
+    using P = ColPlan<N>;
+    static constexpr int C = P::col_c, T = P::T, THREADS = T * C, NWARP = THREADS / 32;
+    static constexpr int NBUF = 3;
+    // rows per TMA box: the largest divisor of N not above 256 (the box limit)
+    static constexpr int BOXR = N <= 256 ? N : (N % 256 == 0 ? 256 : N / 2), NBOX = N / BOXR;
+    static_assert(BOXR <= 256 && BOXR * NBOX == N, "TMA boxes must tile the column");
+    static constexpr size_t TILE_BYTES = sizeof(float2) * (size_t)N * C;
+    static constexpr size_t OFF_TW = NBUF * TILE_BYTES;
+    static constexpr size_t OFF_RED = OFF_TW + ((sizeof(float2) * plan_tw_size<P>() + 15) / 16) * 16;
+    static constexpr size_t OFF_BAR = OFF_RED + sizeof(double) * NWARP * kMaxDet;
+    static constexpr size_t SMEM = OFF_BAR + sizeof(uint64_t) * NBUF + 1024;  // + base alignment
+};
+
+template <int N>
+__global__ void __launch_bounds__(ColTmaCfg<N>::THREADS, 1)
+    col_tma_kernel(const __grid_constant__ CUtensorMap map, ColArgs a) {
+    using Cfg = ColTmaCfg<N>;
+    using P = ColPlan<N>;
+    constexpr int C = Cfg::C, T = P::T, E = P::E, TW = plan_tw_size<P>(), NBUF = Cfg::NBUF;
+    extern __shared__ unsigned char smraw[];
+    unsigned char *base = smraw + ((1024u - (smem_u32(smraw) & 1023u)) & 1023u);
+    float2 *buf0 = reinterpret_cast<float2 *>(base);
+    float2 *tw = reinterpret_cast<float2 *>(base + Cfg::OFF_TW);
+    double *red = reinterpret_cast<double *>(base + Cfg::OFF_RED);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(base + Cfg::OFF_BAR);
+    const int tid = threadIdx.x, c = tid % C, t = tid / C;
+    const bool load = (a.flags & COL_LOAD) != 0, store = (a.flags & COL_STORE) != 0;
+    const int tpi = a.ny / C, ntiles = a.batch * tpi;
+    const int nmine = (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
+    for (int i = tid; i < TW; i += Cfg::THREADS) tw[i] = a.tw[i];
+    if (tid == 0) {
+        for (int s = 0; s < NBUF; ++s) mbar_init(&bar[s], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    int issued = 0;  // loads issued (thread 0's count)
+    auto issue_load = [&](int k) {
+        const int tile = blockIdx.x + k * gridDim.x, b = tile / tpi, ty = tile % tpi, s = k % NBUF;
+        float2 *dst = buf0 + (size_t)s * N * C;
+        fence_proxy_async();
+        mbar_arrive_expect_tx(&bar[s], (uint32_t)Cfg::TILE_BYTES);
+#pragma unroll
+        for (int q = 0; q < Cfg::NBOX; ++q)
+            tma_load_2d(dst + (size_t)q * Cfg::BOXR * C, &map, ty * C, b * N + q * Cfg::BOXR, &bar[s]);
+        issued = k + 1;
+    };
+    if (load && tid == 0)
+        for (int k = 0; k < NBUF - 1 && k < nmine; ++k) issue_load(k);
+    int k = 0;
+    bool ok = true;
+    for (; k < nmine; ++k) {
+        const int tile = blockIdx.x + k * gridDim.x, b = tile / tpi, ty = tile % tpi;
+        const int iy = ty * C + c, s = k % NBUF;
+        float2 *bs = buf0 + (size_t)s * N * C;
+        ColAddr<P> ad{bs, c};
+        float2 v[E];
+        if (!load && store && tid == 0) tma_wait_read<NBUF - 1>();  // store of tile k-3 left bs
+        if (load) {
+            const bool got = mbar_wait_bounded(&bar[s], (uint32_t)((k / NBUF) & 1), kWaitLimit);
+            if (__syncthreads_or(!got)) {
+                ok = false;
+                break;
+            }
+#pragma unroll
+            for (int e = 0; e < E; ++e) v[e] = bs[(t + T * e) * C + c];
+        } else if (a.flags & COL_PROBE) {
+            col_probe<P>(v, a, b, iy, t);
+        } else {
+#pragma unroll
+            for (int e = 0; e < E; ++e) v[e] = make_float2(0.f, 0.f);
+        }
+        if (a.flags & COL_FWD) fft_line<P, +1>(v, t, ad, tw);
+        if (a.flags & COL_PROP) col_propagate<P>(v, a, iy, t);
+        if (a.flags & COL_DETECT) col_detect<P, Cfg::NWARP>(v, a, b, iy, t, ty, tpi, red);
+        if (a.flags & COL_INV) fft_line<P, -1>(v, t, ad, tw);
+        if (store) {
+            __syncthreads();  // every thread is done reading bs
+#pragma unroll
+            for (int e = 0; e < E; ++e) bs[(t + T * e) * C + c] = v[e];
+            fence_proxy_async();
+            __syncthreads();
+            if (tid == 0) {
+#pragma unroll
+                for (int q = 0; q < Cfg::NBOX; ++q)
+                    tma_store_2d(&map, ty * C, b * N + q * Cfg::BOXR, bs + (size_t)q * Cfg::BOXR * C);
+                tma_commit();
+            }
+        }
+        if (load && tid == 0 && k + NBUF - 1 < nmine) {
+            if (store) tma_wait_read<1>();  // the store of tile k-1 has left its buffer
+            issue_load(k + NBUF - 1);       // into buffer (k + 2) % 3 == (k - 1) % 3
+        }
+    }
+    if (tid == 0) {
+        if (store) tma_wait_all();
+        if (!ok) {
+            if (a.err) atomicExch(a.err, 1);
+            // loads still in flight land in this CTA's shared memory: let them finish
+            for (int j = k; j < issued; ++j)
+                mbar_wait_bounded(&bar[j % NBUF], (uint32_t)((j / NBUF) & 1), kWaitLimit);
         }
     }
 }
@@ -280,6 +417,63 @@ template <int N> static cudaError_t col_launch(const ColArgs &a, cudaStream_t s,
     return cudaGetLastError();
 }
 
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn() {
+    static EncodeTiledFn fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiledFn)p;
+        else
+            cudaGetLastError();
+    }
+    return fn;
+}
+
+// The TMA kernel needs one buffer for load and store (in place) at a 16-byte
+// aligned address; other calls take the register-only kernel.
+static bool tma_eligible(const ColArgs &a) {
+    if (!a.out || ((uintptr_t)a.out & 15u)) return false;
+    if ((a.flags & COL_LOAD) && a.in != a.out) return false;
+    if (!(a.flags & (COL_LOAD | COL_STORE))) return false;
+    return encode_fn() != nullptr;
+}
+
+template <int N> static cudaError_t col_tma_launch(const ColArgs &a, cudaStream_t s, int nsm) {
+    using Cfg = ColTmaCfg<N>;
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(col_tma_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)Cfg::SMEM);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    CUtensorMap map;
+    const cuuint64_t gdim[2] = {(cuuint64_t)a.ny, (cuuint64_t)a.batch * N};
+    const cuuint64_t gstride[1] = {(cuuint64_t)a.ny * sizeof(float2)};
+    const cuuint32_t box[2] = {(cuuint32_t)Cfg::C, (cuuint32_t)Cfg::BOXR};
+    const cuuint32_t estride[2] = {1, 1};
+    CUresult r = encode_fn()(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, (void *)a.out, gdim, gstride, box,
+                             estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                             CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
+    const int ntiles = a.batch * (a.ny / Cfg::C);
+    int grid = nsm < ntiles ? nsm : ntiles;
+    if (grid < 1) grid = 1;
+    col_tma_kernel<N><<<grid, Cfg::THREADS, Cfg::SMEM, s>>>(map, a);
+    return cudaGetLastError();
+}
+
 #define MSL_FOR_EACH_SIDE(X) X(64) X(128) X(256) X(384) X(512) X(768) X(1024) X(2048)
 
 bool plan_supported(int n) {
@@ -299,6 +493,18 @@ int plan_col_c(int n) {
 #undef X
         default: return 0;
     }
+}
+
+int plan_col_c_launch(int n, const ColArgs &a) {
+    if (tma_eligible(a)) {
+        switch (n) {
+#define X(N) case N: return ColPlan<N>::col_c;
+            MSL_FOR_EACH_SIDE(X)
+#undef X
+            default: return 0;
+        }
+    }
+    return plan_col_c(n);
 }
 
 template <int N> static void twiddles_for(std::vector<float2> &out) {
@@ -337,6 +543,14 @@ cudaError_t launch_row_pass(int ny, const RowArgs &a, cudaStream_t s, int nsm, i
 
 cudaError_t launch_col_pass(int nx, const ColArgs &a, cudaStream_t s, int nsm, int64_t *launches) {
     ++*launches;
+    if (tma_eligible(a)) {
+        switch (nx) {
+#define X(N) case N: return col_tma_launch<N>(a, s, nsm);
+            MSL_FOR_EACH_SIDE(X)
+#undef X
+            default: return cudaErrorInvalidValue;
+        }
+    }
     switch (nx) {
 #define X(N) case N: return col_launch<N>(a, s, nsm);
         MSL_FOR_EACH_SIDE(X)
