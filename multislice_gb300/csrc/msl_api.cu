@@ -296,9 +296,10 @@ ColArgs col_args(const msl_grid *g, const SliceTables &st, float2 *tw, int layer
 }
 
 RowArgs row_args(const msl_grid *g, float2 *tw, const float2 *trans, float2 *wave, int batch,
-                 int flags) {
+                 int flags, int *err) {
     RowArgs a;
     memset(&a, 0, sizeof(a));
+    a.err = err;
     a.in = wave;
     a.out = wave;
     a.nlines = batch * g->nx;
@@ -578,13 +579,13 @@ int msl_transmission_build(msl_ctx *c, const msl_grid *g, const msl_optics *o, c
     if ((rc = build_slice_tables(c, g, o, 1, nullptr, st))) return rc;
     float2 *twr = twiddles(c, ny), *twc = twiddles(c, nx);
     if (!twr || !twc) return fail(c, MSL_E_NOMEM, "twiddle table allocation failed");
-    RowArgs r = row_args(g, twr, nullptr, td, nlayer, msl::ROW_GENT | msl::ROW_FWD);
+    RowArgs r = row_args(g, twr, nullptr, td, nlayer, msl::ROW_GENT | msl::ROW_FWD, c->dflag);
     r.vpot = vd;
     r.phase_scale = msl_sigma(o->kev) / 1000.0;  // rad per V*A
     LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_row_pass(ny, r, c->stream, c->nsm, &c->launches); }));
     ColArgs ca = col_args(g, st, twc, 0, td, nlayer, msl::COL_LOAD | msl::COL_FWD | msl::COL_PROP | msl::COL_INV | msl::COL_STORE, c->dflag);
     LAUNCH_TRY(c, timed(c, MSL_PROF_COL, [&] { return msl::launch_col_pass(nx, ca, c->stream, c->nsm, &c->launches); }));
-    r = row_args(g, twr, nullptr, td, nlayer, msl::ROW_LOAD | msl::ROW_INV);
+    r = row_args(g, twr, nullptr, td, nlayer, msl::ROW_LOAD | msl::ROW_INV, c->dflag);
     LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_row_pass(ny, r, c->stream, c->nsm, &c->launches); }));
     if (!tdev)
         CUDA_TRY(c, cudaMemcpyAsync(t_out, td, sizeof(float2) * n2 * nlayer, cudaMemcpyDeviceToHost,
@@ -622,14 +623,14 @@ int msl_fft2d(msl_ctx *c, const msl_grid *g, float *psi, int batch, int dir) {
     st.d_ky2 = nullptr;
     st.d_prop = nullptr;
     if (dir > 0) {
-        RowArgs r = row_args(g, twr, nullptr, w, batch, msl::ROW_LOAD | msl::ROW_FWD);
+        RowArgs r = row_args(g, twr, nullptr, w, batch, msl::ROW_LOAD | msl::ROW_FWD, c->dflag);
         LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_row_pass(ny, r, c->stream, c->nsm, &c->launches); }));
         ColArgs ca = col_args(g, st, twc, 0, w, batch, msl::COL_LOAD | msl::COL_FWD | msl::COL_STORE, c->dflag);
         LAUNCH_TRY(c, timed(c, MSL_PROF_COL, [&] { return msl::launch_col_pass(nx, ca, c->stream, c->nsm, &c->launches); }));
     } else {
         ColArgs ca = col_args(g, st, twc, 0, w, batch, msl::COL_LOAD | msl::COL_INV | msl::COL_STORE, c->dflag);
         LAUNCH_TRY(c, timed(c, MSL_PROF_COL, [&] { return msl::launch_col_pass(nx, ca, c->stream, c->nsm, &c->launches); }));
-        RowArgs r = row_args(g, twr, nullptr, w, batch, msl::ROW_LOAD | msl::ROW_INV);
+        RowArgs r = row_args(g, twr, nullptr, w, batch, msl::ROW_LOAD | msl::ROW_INV, c->dflag);
         r.scale = 1.0f / ((float)nx * (float)ny);
         LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_row_pass(ny, r, c->stream, c->nsm, &c->launches); }));
     }
@@ -676,12 +677,12 @@ int msl_multislice(msl_ctx *c, const msl_grid *g, const msl_optics *o, const flo
         int rf = msl::ROW_TRANS | msl::ROW_FWD;
         if (s > 0) rf |= msl::ROW_LOAD | msl::ROW_INV;
         else if (!plane_wave) rf |= msl::ROW_LOAD;
-        RowArgs r = row_args(g, twr, td + (size_t)l * n2, w, batch, rf);
+        RowArgs r = row_args(g, twr, td + (size_t)l * n2, w, batch, rf, c->dflag);
         LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_row_pass(ny, r, c->stream, c->nsm, &c->launches); }));
         ColArgs ca = col_args(g, st, twc, l, w, batch, colf, c->dflag);
         LAUNCH_TRY(c, timed(c, MSL_PROF_COL, [&] { return msl::launch_col_pass(nx, ca, c->stream, c->nsm, &c->launches); }));
     }
-    RowArgs r = row_args(g, twr, nullptr, w, batch, msl::ROW_LOAD | msl::ROW_INV);
+    RowArgs r = row_args(g, twr, nullptr, w, batch, msl::ROW_LOAD | msl::ROW_INV, c->dflag);
     LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_row_pass(ny, r, c->stream, c->nsm, &c->launches); }));
     if (!dev) CUDA_TRY(c, cudaMemcpyAsync(psi, w, wbytes, cudaMemcpyDeviceToHost, c->stream));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
@@ -794,8 +795,7 @@ int msl_stem_scan(msl_ctx *c, const msl_grid *g, const msl_optics *o, const floa
         int ic = 0;
         for (int s = 0; s <= last; ++s) {
             const int l = layer_seq[s];
-            RowArgs r = row_args(g, twr, td + (size_t)l * n2, w, nb,
-                                 msl::ROW_LOAD | msl::ROW_INV | msl::ROW_TRANS | msl::ROW_FWD);
+            RowArgs r = row_args(g, twr, td + (size_t)l * n2, w, nb, msl::ROW_LOAD | msl::ROW_INV | msl::ROW_TRANS | msl::ROW_FWD, c->dflag);
             LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_row_pass(ny, r, c->stream, c->nsm, &c->launches); }));
             const bool detect = checkpoints[ic] == s;
             int cf = msl::COL_LOAD | msl::COL_FWD | msl::COL_PROP;

@@ -204,6 +204,12 @@ template <class P> struct RowAddr {
         else return i ^ ((i >> P::row_sh) & 15);
     }
 };
+// Contiguous lines packed back to back (the TMA row tiles): always the xor
+// scheme, which stays inside the line's N slots.
+template <class P> struct RowXorAddr {
+    float2 *base;
+    __device__ __forceinline__ int operator()(int i) const { return i ^ ((i >> P::row_sh) & 15); }
+};
 // Column tiles: C interleaved columns, slot = perm(i) * C + c.
 template <class P> struct ColAddr {
     float2 *base;

@@ -28,6 +28,7 @@ struct RowArgs {
     const float2 *tw;      // twiddle tables of the ny plan
     int flags;
     float scale;           // multiplies the output when != 1
+    int *err;              // set to 1 when a bounded wait gives up (may be null)
 };
 
 // Column pass: strided lines of length nx (one line = one iy of one image).

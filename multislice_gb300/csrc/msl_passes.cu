@@ -313,6 +313,122 @@ __global__ void __launch_bounds__(ColTmaCfg<N>::THREADS, 1)
     }
 }
 
+
+// ---------------------------------------------------- TMA-fed row pass
+// Persistent kernel, one CTA per SM, 512 threads = L lines x T threads.  Tiles
+// of L consecutive lines (L * N * 8 bytes, contiguous) arrive by TMA into a ring
+// of three buffers; the buffer is then the line transforms' exchange space and
+// the source of the TMA store.  The tile is viewed as [L][N/BX][BX] so every box
+// dimension stays within the 256-element TMA limit while the shared-memory
+// image of the tile is plain [line][N].  The transmission row of each line is
+// read straight from global memory (it is shared by the whole probe batch and
+// sits in L2) at the start of the tile, so its latency overlaps the inverse
+// transform.
+template <int N> struct RowTmaCfg {
+    using P = Plan<N>;
+    static constexpr int T = P::T, L = 512 / T, THREADS = T * L;
+    static constexpr int NBUF = 3;
+    static constexpr int BX = N <= 256 ? N : (N % 256 == 0 ? 256 : N / 2), NBX = N / BX;
+    static_assert(BX <= 256 && BX * NBX == N && NBX <= 256 && L <= 256, "TMA box limits");
+    static constexpr size_t TILE_BYTES = sizeof(float2) * (size_t)L * N;
+    static constexpr size_t OFF_TW = NBUF * TILE_BYTES;
+    static constexpr size_t OFF_BAR = OFF_TW + ((sizeof(float2) * plan_tw_size<P>() + 15) / 16) * 16;
+    static constexpr size_t SMEM = OFF_BAR + sizeof(uint64_t) * NBUF + 1024;
+};
+
+template <int N>
+__global__ void __launch_bounds__(RowTmaCfg<N>::THREADS, 1)
+    row_tma_kernel(const __grid_constant__ CUtensorMap map, RowArgs a) {
+    using Cfg = RowTmaCfg<N>;
+    using P = Plan<N>;
+    constexpr int T = P::T, E = P::E, L = Cfg::L, TW = plan_tw_size<P>(), NBUF = Cfg::NBUF;
+    extern __shared__ unsigned char smraw[];
+    unsigned char *base = smraw + ((1024u - (smem_u32(smraw) & 1023u)) & 1023u);
+    float2 *buf0 = reinterpret_cast<float2 *>(base);
+    float2 *tw = reinterpret_cast<float2 *>(base + Cfg::OFF_TW);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(base + Cfg::OFF_BAR);
+    const int tid = threadIdx.x, t = tid % T, l = tid / T;
+    const bool load = (a.flags & ROW_LOAD) != 0;
+    const int ntiles = a.nlines / L;
+    const int nmine = (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
+    for (int i = tid; i < TW; i += Cfg::THREADS) tw[i] = a.tw[i];
+    if (tid == 0) {
+        for (int s = 0; s < NBUF; ++s) mbar_init(&bar[s], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    int issued = 0;
+    auto issue_load = [&](int k) {
+        const int tile = blockIdx.x + k * gridDim.x, s = k % NBUF;
+        fence_proxy_async();
+        mbar_arrive_expect_tx(&bar[s], (uint32_t)Cfg::TILE_BYTES);
+        tma_load_3d(buf0 + (size_t)s * L * N, &map, 0, 0, tile * L, &bar[s]);
+        issued = k + 1;
+    };
+    if (load && tid == 0)
+        for (int k = 0; k < NBUF - 1 && k < nmine; ++k) issue_load(k);
+    int k = 0;
+    bool ok = true;
+    for (; k < nmine; ++k) {
+        const int tile = blockIdx.x + k * gridDim.x, s = k % NBUF;
+        const int line = tile * L + l;
+        float2 *bs = buf0 + (size_t)s * L * N;
+        float2 *mine = bs + (size_t)l * N;
+        RowXorAddr<P> ad{mine};
+        float2 tr[E];
+        if (a.flags & ROW_TRANS) {
+            const float2 *trow = a.trans + (size_t)(line % a.nx) * N;
+#pragma unroll
+            for (int e = 0; e < E; ++e) tr[e] = __ldg(trow + t + T * e);
+        }
+        if (tid == 0) tma_wait_read<NBUF - 1>();  // the store of tile k-3 has left bs
+        float2 v[E];
+        if (load) {
+            const bool got = mbar_wait_bounded(&bar[s], (uint32_t)((k / NBUF) & 1), kWaitLimit);
+            if (__syncthreads_or(!got)) {
+                ok = false;
+                break;
+            }
+#pragma unroll
+            for (int e = 0; e < E; ++e) v[e] = mine[t + T * e];
+        } else {
+#pragma unroll
+            for (int e = 0; e < E; ++e) v[e] = make_float2(1.f, 0.f);
+        }
+        if (a.flags & ROW_INV) fft_line<P, -1>(v, t, ad, tw);
+        if (a.flags & ROW_TRANS) {
+#pragma unroll
+            for (int e = 0; e < E; ++e) v[e] = c_mul(v[e], tr[e]);
+        }
+        if (a.flags & ROW_FWD) fft_line<P, +1>(v, t, ad, tw);
+        if (a.scale != 1.0f) {
+#pragma unroll
+            for (int e = 0; e < E; ++e) v[e] = c_scale(v[e], a.scale);
+        }
+        __syncthreads();  // every thread is done reading bs
+#pragma unroll
+        for (int e = 0; e < E; ++e) mine[t + T * e] = v[e];
+        fence_proxy_async();
+        __syncthreads();
+        if (tid == 0) {
+            tma_store_3d(&map, 0, 0, tile * L, bs);
+            tma_commit();
+            if (load && k + NBUF - 1 < nmine) {
+                tma_wait_read<1>();        // the store of tile k-1 has left its buffer
+                issue_load(k + NBUF - 1);  // into buffer (k + 2) % 3
+            }
+        }
+    }
+    if (tid == 0) {
+        tma_wait_all();
+        if (!ok) {
+            if (a.err) atomicExch(a.err, 1);
+            for (int j = k; j < issued; ++j)
+                mbar_wait_bounded(&bar[j % NBUF], (uint32_t)((j / NBUF) & 1), kWaitLimit);
+        }
+    }
+}
+
 // ------------------------------------------------------------ set-up kernels
 __global__ void probe_table_kernel(int nx, int ny, const double *kxd, const double *kyd,
                                    double s_in, double s_out, double lam, double df, double cs,
@@ -474,6 +590,40 @@ template <int N> static cudaError_t col_tma_launch(const ColArgs &a, cudaStream_
     return cudaGetLastError();
 }
 
+
+static bool row_tma_eligible(const RowArgs &a) {
+    if (!a.out || ((uintptr_t)a.out & 15u)) return false;
+    if ((a.flags & ROW_LOAD) && a.in != a.out) return false;
+    if (a.flags & ROW_GENT) return false;
+    return encode_fn() != nullptr;
+}
+
+template <int N> static cudaError_t row_tma_launch(const RowArgs &a, cudaStream_t s, int nsm) {
+    using Cfg = RowTmaCfg<N>;
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(row_tma_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)Cfg::SMEM);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    if (a.nlines % Cfg::L) return cudaErrorInvalidValue;
+    CUtensorMap map;
+    const cuuint64_t gdim[3] = {(cuuint64_t)Cfg::BX, (cuuint64_t)Cfg::NBX, (cuuint64_t)a.nlines};
+    const cuuint64_t gstride[2] = {(cuuint64_t)Cfg::BX * sizeof(float2), (cuuint64_t)N * sizeof(float2)};
+    const cuuint32_t box[3] = {(cuuint32_t)Cfg::BX, (cuuint32_t)Cfg::NBX, (cuuint32_t)Cfg::L};
+    const cuuint32_t estride[3] = {1, 1, 1};
+    CUresult r = encode_fn()(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, (void *)a.out, gdim, gstride, box,
+                             estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                             CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
+    const int ntiles = a.nlines / Cfg::L;
+    int grid = nsm < ntiles ? nsm : ntiles;
+    if (grid < 1) grid = 1;
+    row_tma_kernel<N><<<grid, Cfg::THREADS, Cfg::SMEM, s>>>(map, a);
+    return cudaGetLastError();
+}
+
 #define MSL_FOR_EACH_SIDE(X) X(64) X(128) X(256) X(384) X(512) X(768) X(1024) X(2048)
 
 bool plan_supported(int n) {
@@ -533,6 +683,14 @@ void plan_twiddles(int n, std::vector<float2> &out) {
 
 cudaError_t launch_row_pass(int ny, const RowArgs &a, cudaStream_t s, int nsm, int64_t *launches) {
     ++*launches;
+    if (row_tma_eligible(a)) {
+        switch (ny) {
+#define X(N) case N: return row_tma_launch<N>(a, s, nsm);
+            MSL_FOR_EACH_SIDE(X)
+#undef X
+            default: return cudaErrorInvalidValue;
+        }
+    }
     switch (ny) {
 #define X(N) case N: return row_launch<N>(a, s, nsm);
         MSL_FOR_EACH_SIDE(X)
