@@ -13,6 +13,8 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <stdlib.h>
+
 #include <vector>
 
 #include "msl_fft.cuh"
@@ -208,8 +210,9 @@ __global__ void __launch_bounds__(ColCfg<N>::THREADS) col_pass_kernel(ColArgs a)
 // waits (bounded) for its loads still in flight and leaves.
 constexpr uint32_t kWaitLimit = 1u << 22;
 
-template <int N> struct ColTmaCfg {
-    using P = ColPlan<N>;
+template <class PL> struct ColTmaCfg {
+    using P = PL;
+    static constexpr int N = P::N;
     static constexpr int C = P::col_c, T = P::T, THREADS = T * C, NWARP = THREADS / 32;
     static constexpr int NBUF = 3;
     // rows per TMA box: the largest divisor of N not above 256 (the box limit)
@@ -222,11 +225,12 @@ template <int N> struct ColTmaCfg {
     static constexpr size_t SMEM = OFF_BAR + sizeof(uint64_t) * NBUF + 1024;  // + base alignment
 };
 
-template <int N>
-__global__ void __launch_bounds__(ColTmaCfg<N>::THREADS, 1)
+template <class PL, int MINB>
+__global__ void __launch_bounds__(ColTmaCfg<PL>::THREADS, MINB)
     col_tma_kernel(const __grid_constant__ CUtensorMap map, ColArgs a) {
-    using Cfg = ColTmaCfg<N>;
-    using P = ColPlan<N>;
+    using Cfg = ColTmaCfg<PL>;
+    using P = PL;
+    constexpr int N = P::N;
     constexpr int C = Cfg::C, T = P::T, E = P::E, TW = plan_tw_size<P>(), NBUF = Cfg::NBUF;
     extern __shared__ unsigned char smraw[];
     unsigned char *base = smraw + ((1024u - (smem_u32(smraw) & 1023u)) & 1023u);
@@ -324,9 +328,9 @@ __global__ void __launch_bounds__(ColTmaCfg<N>::THREADS, 1)
 // read straight from global memory (it is shared by the whole probe batch and
 // sits in L2) at the start of the tile, so its latency overlaps the inverse
 // transform.
-template <int N> struct RowTmaCfg {
+template <int N, int TH> struct RowTmaCfg {
     using P = Plan<N>;
-    static constexpr int T = P::T, L = 512 / T, THREADS = T * L;
+    static constexpr int T = P::T, L = TH / T, THREADS = T * L;
     static constexpr int NBUF = 3;
     static constexpr int BX = N <= 256 ? N : (N % 256 == 0 ? 256 : N / 2), NBX = N / BX;
     static_assert(BX <= 256 && BX * NBX == N && NBX <= 256 && L <= 256, "TMA box limits");
@@ -336,10 +340,10 @@ template <int N> struct RowTmaCfg {
     static constexpr size_t SMEM = OFF_BAR + sizeof(uint64_t) * NBUF + 1024;
 };
 
-template <int N>
-__global__ void __launch_bounds__(RowTmaCfg<N>::THREADS, 1)
+template <int N, int TH, int MINB>
+__global__ void __launch_bounds__(RowTmaCfg<N, TH>::THREADS, MINB)
     row_tma_kernel(const __grid_constant__ CUtensorMap map, RowArgs a) {
-    using Cfg = RowTmaCfg<N>;
+    using Cfg = RowTmaCfg<N, TH>;
     using P = Plan<N>;
     constexpr int T = P::T, E = P::E, L = Cfg::L, TW = plan_tw_size<P>(), NBUF = Cfg::NBUF;
     extern __shared__ unsigned char smraw[];
@@ -558,21 +562,28 @@ static EncodeTiledFn encode_fn() {
 
 // The TMA kernel needs one buffer for load and store (in place) at a 16-byte
 // aligned address; other calls take the register-only kernel.
+static int env_knob(const char *name);
 static bool tma_eligible(const ColArgs &a) {
+    static const int k = env_knob("MSL_COLK");
+    if (k < 0) return false;
     if (!a.out || ((uintptr_t)a.out & 15u)) return false;
     if ((a.flags & COL_LOAD) && a.in != a.out) return false;
     if (!(a.flags & (COL_LOAD | COL_STORE))) return false;
     return encode_fn() != nullptr;
 }
 
-template <int N> static cudaError_t col_tma_launch(const ColArgs &a, cudaStream_t s, int nsm) {
-    using Cfg = ColTmaCfg<N>;
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(col_tma_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+template <class PL, int MINB> static cudaError_t col_tma_launch_v(const ColArgs &a, cudaStream_t s, int nsm) {
+    using Cfg = ColTmaCfg<PL>;
+    constexpr int N = PL::N;
+    static int per_sm = 0;
+    if (!per_sm) {
+        cudaError_t e = cudaFuncSetAttribute(col_tma_kernel<PL, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)Cfg::SMEM);
         if (e != cudaSuccess) return e;
-        attr = true;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, col_tma_kernel<PL, MINB>, Cfg::THREADS,
+                                                          Cfg::SMEM);
+        if (e != cudaSuccess) return e;
+        if (per_sm < 1) per_sm = 1;
     }
     CUtensorMap map;
     const cuuint64_t gdim[2] = {(cuuint64_t)a.ny, (cuuint64_t)a.batch * N};
@@ -584,28 +595,49 @@ template <int N> static cudaError_t col_tma_launch(const ColArgs &a, cudaStream_
                              CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
     const int ntiles = a.batch * (a.ny / Cfg::C);
-    int grid = nsm < ntiles ? nsm : ntiles;
+    int grid = nsm * per_sm < ntiles ? nsm * per_sm : ntiles;
     if (grid < 1) grid = 1;
-    col_tma_kernel<N><<<grid, Cfg::THREADS, Cfg::SMEM, s>>>(map, a);
+    col_tma_kernel<PL, MINB><<<grid, Cfg::THREADS, Cfg::SMEM, s>>>(map, a);
     return cudaGetLastError();
 }
 
+// Variant knob for tuning runs (MSL_COLK): 1 = ColPlan<N>, 2 = 8 columns x 32 threads (N = 512).
+static int env_knob(const char *name) {
+    const char *v = getenv(name);
+    return v ? atoi(v) : 0;
+}
 
+template <int N> static cudaError_t col_tma_launch(const ColArgs &a, cudaStream_t s, int nsm) {
+    if constexpr (N == 512) {
+        static const int k = env_knob("MSL_COLK");
+        if (k == 2) return col_tma_launch_v<ColPlanT<512, 32, 8, 3>, 2>(a, s, nsm);
+    }
+    return col_tma_launch_v<ColPlan<N>, 1>(a, s, nsm);
+}
+
+
+static int env_knob(const char *name);
 static bool row_tma_eligible(const RowArgs &a) {
+    static const int k = env_knob("MSL_ROWK");
+    if (k == 0) return false;
     if (!a.out || ((uintptr_t)a.out & 15u)) return false;
     if ((a.flags & ROW_LOAD) && a.in != a.out) return false;
     if (a.flags & ROW_GENT) return false;
     return encode_fn() != nullptr;
 }
 
-template <int N> static cudaError_t row_tma_launch(const RowArgs &a, cudaStream_t s, int nsm) {
-    using Cfg = RowTmaCfg<N>;
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(row_tma_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)Cfg::SMEM);
+template <int N, int TH, int MINB>
+static cudaError_t row_tma_launch_v(const RowArgs &a, cudaStream_t s, int nsm) {
+    using Cfg = RowTmaCfg<N, TH>;
+    static int per_sm = 0;
+    if (!per_sm) {
+        cudaError_t e = cudaFuncSetAttribute(row_tma_kernel<N, TH, MINB>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::SMEM);
         if (e != cudaSuccess) return e;
-        attr = true;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, row_tma_kernel<N, TH, MINB>, Cfg::THREADS,
+                                                          Cfg::SMEM);
+        if (e != cudaSuccess) return e;
+        if (per_sm < 1) per_sm = 1;
     }
     if (a.nlines % Cfg::L) return cudaErrorInvalidValue;
     CUtensorMap map;
@@ -618,10 +650,19 @@ template <int N> static cudaError_t row_tma_launch(const RowArgs &a, cudaStream_
                              CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
     const int ntiles = a.nlines / Cfg::L;
-    int grid = nsm < ntiles ? nsm : ntiles;
+    int grid = nsm * per_sm < ntiles ? nsm * per_sm : ntiles;
     if (grid < 1) grid = 1;
-    row_tma_kernel<N><<<grid, Cfg::THREADS, Cfg::SMEM, s>>>(map, a);
+    row_tma_kernel<N, TH, MINB><<<grid, Cfg::THREADS, Cfg::SMEM, s>>>(map, a);
     return cudaGetLastError();
+}
+
+template <int N> static cudaError_t row_tma_launch(const RowArgs &a, cudaStream_t s, int nsm) {
+    if constexpr (N == 512) {
+        static const int k = env_knob("MSL_ROWK");
+        if (k == 2) return row_tma_launch_v<512, 256, 3>(a, s, nsm);
+        if (k == 3) return row_tma_launch_v<512, 128, 6>(a, s, nsm);
+    }
+    return row_tma_launch_v<N, 512, 1>(a, s, nsm);
 }
 
 #define MSL_FOR_EACH_SIDE(X) X(64) X(128) X(256) X(384) X(512) X(768) X(1024) X(2048)
@@ -647,6 +688,7 @@ int plan_col_c(int n) {
 
 int plan_col_c_launch(int n, const ColArgs &a) {
     if (tma_eligible(a)) {
+        if (n == 512 && env_knob("MSL_COLK") == 2) return 8;
         switch (n) {
 #define X(N) case N: return ColPlan<N>::col_c;
             MSL_FOR_EACH_SIDE(X)
