@@ -48,23 +48,25 @@ MSL_PLAN(768,  64, 5,  3,  4, 4, 4, 4,  0,  5,  8, 3)
 #undef MSL_PLAN
 
 // Column-pass plan of the TMA-fed kernel: same radices (and so the same twiddle
-// tables) as Plan<N>, its own threads per line T and columns per tile C.
-template <int N_, int T_, int C_, int PS_> struct ColPlanT {
+// tables) as Plan<N>, its own threads per line T, columns per tile C, exchange
+// row permutation shift PS (>= 30: none) and CTAs per SM the registers allow.
+template <int N_, int T_, int C_, int PS_, int MINB_> struct ColPlanT {
     using B = Plan<N_>;
-    static constexpr int N = N_, T = T_, E = N_ / T_, NSTAGE = B::NSTAGE;
+    static constexpr int N = N_, T = T_, E = N_ / T_, NSTAGE = B::NSTAGE, MINB = MINB_;
     static constexpr int row_swz = B::row_swz, row_sh = B::row_sh;
     static constexpr int col_c = C_, col_ps = PS_;
     static constexpr int radix(int s) { return B::radix(s); }
 };
+// Tile shapes chosen by a shared-memory bank model and by timing the 512 case.
 template <int N> struct ColPlan;
-template <> struct ColPlan<64> : ColPlanT<64, 8, 16, 0> {};
-template <> struct ColPlan<128> : ColPlanT<128, 16, 16, 0> {};
-template <> struct ColPlan<256> : ColPlanT<256, 32, 16, 0> {};
-template <> struct ColPlan<384> : ColPlanT<384, 32, 16, 0> {};
-template <> struct ColPlan<512> : ColPlanT<512, 32, 16, 0> {};
-template <> struct ColPlan<768> : ColPlanT<768, 64, 8, 3> {};
-template <> struct ColPlan<1024> : ColPlanT<1024, 64, 8, 4> {};
-template <> struct ColPlan<2048> : ColPlanT<2048, 128, 4, 4> {};
+template <> struct ColPlan<64> : ColPlanT<64, 8, 16, 30, 4> {};
+template <> struct ColPlan<128> : ColPlanT<128, 16, 16, 30, 2> {};
+template <> struct ColPlan<256> : ColPlanT<256, 32, 8, 3, 2> {};
+template <> struct ColPlan<384> : ColPlanT<384, 32, 8, 30, 2> {};
+template <> struct ColPlan<512> : ColPlanT<512, 32, 8, 3, 2> {};
+template <> struct ColPlan<768> : ColPlanT<768, 64, 4, 30, 2> {};
+template <> struct ColPlan<1024> : ColPlanT<1024, 64, 8, 4, 1> {};
+template <> struct ColPlan<2048> : ColPlanT<2048, 128, 4, 4, 1> {};
 
 template <class P> __host__ __device__ constexpr int plan_span(int s) {
     int ns = 1;
@@ -216,7 +218,7 @@ template <class P> struct ColAddr {
     int c;
     __device__ __forceinline__ int operator()(int i) const {
         constexpr int C = P::col_c;
-        if constexpr (C >= 16) return i * C + c;
+        if constexpr (C >= 16 || P::col_ps >= 30) return i * C + c;
         else return (i ^ ((i >> P::col_ps) & (16 / C - 1))) * C + c;
     }
 };

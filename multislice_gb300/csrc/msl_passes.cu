@@ -13,8 +13,6 @@
 #include <math.h>
 #include <stdint.h>
 
-#include <stdlib.h>
-
 #include <vector>
 
 #include "msl_fft.cuh"
@@ -562,10 +560,7 @@ static EncodeTiledFn encode_fn() {
 
 // The TMA kernel needs one buffer for load and store (in place) at a 16-byte
 // aligned address; other calls take the register-only kernel.
-static int env_knob(const char *name);
 static bool tma_eligible(const ColArgs &a) {
-    static const int k = env_knob("MSL_COLK");
-    if (k < 0) return false;
     if (!a.out || ((uintptr_t)a.out & 15u)) return false;
     if ((a.flags & COL_LOAD) && a.in != a.out) return false;
     if (!(a.flags & (COL_LOAD | COL_STORE))) return false;
@@ -601,25 +596,12 @@ template <class PL, int MINB> static cudaError_t col_tma_launch_v(const ColArgs 
     return cudaGetLastError();
 }
 
-// Variant knob for tuning runs (MSL_COLK): 1 = ColPlan<N>, 2 = 8 columns x 32 threads (N = 512).
-static int env_knob(const char *name) {
-    const char *v = getenv(name);
-    return v ? atoi(v) : 0;
-}
-
 template <int N> static cudaError_t col_tma_launch(const ColArgs &a, cudaStream_t s, int nsm) {
-    if constexpr (N == 512) {
-        static const int k = env_knob("MSL_COLK");
-        if (k == 2) return col_tma_launch_v<ColPlanT<512, 32, 8, 3>, 2>(a, s, nsm);
-    }
-    return col_tma_launch_v<ColPlan<N>, 1>(a, s, nsm);
+    return col_tma_launch_v<ColPlan<N>, ColPlan<N>::MINB>(a, s, nsm);
 }
 
 
-static int env_knob(const char *name);
 static bool row_tma_eligible(const RowArgs &a) {
-    static const int k = env_knob("MSL_ROWK");
-    if (k == 0) return false;
     if (!a.out || ((uintptr_t)a.out & 15u)) return false;
     if ((a.flags & ROW_LOAD) && a.in != a.out) return false;
     if (a.flags & ROW_GENT) return false;
@@ -656,13 +638,11 @@ static cudaError_t row_tma_launch_v(const RowArgs &a, cudaStream_t s, int nsm) {
     return cudaGetLastError();
 }
 
+// 128-thread CTAs, as many per SM as registers and shared memory allow (six
+// for 8-element lines): timing the 512 case, more independent CTAs beat wider
+// ones because every exchange of a line transform is a CTA-wide barrier.
 template <int N> static cudaError_t row_tma_launch(const RowArgs &a, cudaStream_t s, int nsm) {
-    if constexpr (N == 512) {
-        static const int k = env_knob("MSL_ROWK");
-        if (k == 2) return row_tma_launch_v<512, 256, 3>(a, s, nsm);
-        if (k == 3) return row_tma_launch_v<512, 128, 6>(a, s, nsm);
-    }
-    return row_tma_launch_v<N, 512, 1>(a, s, nsm);
+    return row_tma_launch_v<N, 128, (Plan<N>::E <= 8 ? 6 : 4)>(a, s, nsm);
 }
 
 #define MSL_FOR_EACH_SIDE(X) X(64) X(128) X(256) X(384) X(512) X(768) X(1024) X(2048)
@@ -688,7 +668,6 @@ int plan_col_c(int n) {
 
 int plan_col_c_launch(int n, const ColArgs &a) {
     if (tma_eligible(a)) {
-        if (n == 512 && env_knob("MSL_COLK") == 2) return 8;
         switch (n) {
 #define X(N) case N: return ColPlan<N>::col_c;
             MSL_FOR_EACH_SIDE(X)
