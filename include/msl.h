@@ -179,6 +179,54 @@ int msl_stem_scan(msl_ctx *ctx, const msl_grid *grid, const msl_optics *optics,
 int msl_profile_enable(msl_ctx *ctx, int on);
 int msl_profile_read(const msl_ctx *ctx, int kind, int64_t *launches, double *ms);
 
+/* ------------------------------------------------------- CTEM imaging */
+
+/* Objective lens of the CTEM image (mulslice.cpp:539-676): the exit wave's
+ * spectrum is multiplied by exp(-i chi(k)) inside the objective aperture
+ * k^2 <= k_obj^2, chi = pi lambda k^2 (Cs lambda^2 k^2 / 2 - df) (slicelib.cpp:
+ * 258-323, rotationally symmetric terms), and |ifft|^2 is summed over defocus
+ * values df + j*df_step, |j| <= 2.5 df_spread / df_step, with Gaussian weights
+ * exp(-(j df_step / df_spread)^2 / 2) normalised to 1 (df_spread = 0: one
+ * coherent image).  chi is evaluated in FP64. */
+typedef struct {
+    double cs;         /* spherical aberration, Angstrom */
+    double df;         /* mean defocus, Angstrom (Kirkland's sign) */
+    double k_obj;      /* objective aperture radius, 1/A */
+    double df_spread;  /* defocus spread (standard deviation), Angstrom; 0 = none */
+    double df_step;    /* defocus integration step, Angstrom (used when df_spread > 0) */
+} msl_lens;
+
+/* CTEM image of a batch of waves: runs the slice loop of msl_multislice on psi
+ * (plane_wave = 1: start from amplitude 1), then images every exit wave through
+ * the lens and adds weight * sum over the batch of the (defocus-averaged) image
+ * intensity into image[nx][ny] (FP64, accumulated, not cleared).  psi receives
+ * the exit waves.  When exit_intensity is not NULL, weight * |exit wave|^2 is
+ * added to it the same way. */
+int msl_ctem_image(msl_ctx *ctx, const msl_grid *grid, const msl_optics *optics,
+                   const float *trans, int ntrans, const double *dz, const int *layer_seq,
+                   int nslice, const msl_lens *lens, float *psi, int batch, int plane_wave,
+                   double weight, double *image, double *exit_intensity);
+
+/* Frozen-phonon displacements (MSUseOnceCalculator.cs:179-199 jitters every atom
+ * by a Gaussian per axis; the reference's System.Random stream cannot be
+ * reproduced, so this library defines its own): for configuration `config`,
+ * atom i and axis a the displacement is sigma * n, n a standard normal from the
+ * Box-Muller transform of two uniforms u = (splitmix64(key) >> 11) * 2^-53,
+ * key = seed ^ splitmix64((config << 40) | (i << 2) | k), k = 0..3; axes x, y
+ * use the cos and sin of the first pair, z the cos of the second.
+ * d_out: double [natom][3]. */
+int msl_phonon_displacements(uint64_t seed, int config, int natom, double sigma, double *d_out);
+
+/* Frozen-phonon CTEM: for each of nconfig configurations displace the atoms
+ * (msl_phonon_displacements), build the potential and transmission functions
+ * of nslice equal slices, run a plane wave through them and image it; image and
+ * exit_intensity (either may be NULL) receive the averages over configurations,
+ * double [nx][ny] (overwritten). */
+int msl_frozen_phonon(msl_ctx *ctx, const msl_atoms *atoms, const double *fparams,
+                      const msl_grid *grid, int nslice, double radius, const msl_optics *optics,
+                      const msl_lens *lens, int nconfig, double sigma, uint64_t seed,
+                      double *image, double *exit_intensity);
+
 /* Probe batch size used by msl_stem_scan (0 = automatic).  Work buffers are
  * sized batch * nx * ny * 8 bytes. */
 int msl_set_probe_batch(msl_ctx *ctx, int batch);

@@ -5,6 +5,7 @@ The compute path is libmsl.so (include/msl.h); this package only binds it
 """
 from . import specimen  # noqa: F401
 from ._abi import MslError  # noqa: F401
-from .api import Context, fparams_table, sigma, wavelength  # noqa: F401
+from .api import Context, fparams_table, phonon_displacements, sigma, wavelength  # noqa: F401
 
-__all__ = ["Context", "MslError", "fparams_table", "sigma", "wavelength", "specimen"]
+__all__ = ["Context", "MslError", "fparams_table", "phonon_displacements", "sigma", "wavelength",
+           "specimen"]

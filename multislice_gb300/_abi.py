@@ -22,6 +22,7 @@ EXPORTS = (
     "msl_fparams_parse", "msl_wavelength", "msl_sigma", "msl_potential_build",
     "msl_transmission_build", "msl_fft2d", "msl_multislice", "msl_stem_scan",
     "msl_set_probe_batch", "msl_profile_enable", "msl_profile_read", "msl_multislice_noalloc",
+    "msl_ctem_image", "msl_phonon_displacements", "msl_frozen_phonon",
 )
 PROF_ROW, PROF_COL, PROF_POTENTIAL, PROF_OTHER = 0, 1, 2, 3
 
@@ -46,6 +47,11 @@ class Probe(ctypes.Structure):
 
 class Detectors(ctypes.Structure):
     _fields_ = [("ndet", c_int), ("k_in", c_void_p), ("k_out", c_void_p)]
+
+
+class Lens(ctypes.Structure):
+    _fields_ = [("cs", c_double), ("df", c_double), ("k_obj", c_double), ("df_spread", c_double),
+                ("df_step", c_double)]
 
 
 class MslError(RuntimeError):
@@ -87,6 +93,12 @@ def load(path=LIB_PATH):
         "msl_profile_read": (c_int, [P, c_int, POINTER(c_int64), POINTER(c_double)]),
         "msl_multislice_noalloc": (c_int, [POINTER(Grid), POINTER(Optics), P, c_int, P, P, c_int,
                                            P, c_int, c_int, P]),
+        "msl_ctem_image": (c_int, [P, POINTER(Grid), POINTER(Optics), P, c_int, P, P, c_int,
+                                   POINTER(Lens), P, c_int, c_int, c_double, P, P]),
+        "msl_phonon_displacements": (c_int, [ctypes.c_uint64, c_int, c_int, c_double, P]),
+        "msl_frozen_phonon": (c_int, [P, POINTER(Atoms), P, POINTER(Grid), c_int, c_double,
+                                      POINTER(Optics), POINTER(Lens), c_int, c_double,
+                                      ctypes.c_uint64, P, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

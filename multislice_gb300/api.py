@@ -23,7 +23,7 @@ import os
 import numpy as np
 
 from . import _abi
-from ._abi import Atoms, Detectors, Grid, MslError, Optics, Probe
+from ._abi import Atoms, Detectors, Grid, Lens, MslError, Optics, Probe
 
 _DATA = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data")
 
@@ -185,6 +185,61 @@ class Context:
                                              batch, 1 if plane else 0))
         return psi
 
+    # ------------------------------------------------------------ CTEM image
+    @staticmethod
+    def _lens(cs, df, k_obj, df_spread=0.0, df_step=0.0):
+        return Lens(float(cs), float(df), float(k_obj), float(df_spread), float(df_step))
+
+    def ctem_image(self, trans, dz, layer_seq, ax, by, kev, cs, df, k_obj, psi=None, batch=1,
+                   df_spread=0.0, df_step=0.0, weight=1.0, image=None, exit_intensity=None,
+                   bandlimit=2.0 / 3.0):
+        """Image intensity (FP64, accumulated into `image`) through an objective lens
+        (mulslice.cpp:539-676); returns (image, exit waves, exit intensity)."""
+        trans = _as(trans, np.complex64)
+        nt, nx, ny = _cshape(trans)
+        dz = np.ascontiguousarray(np.broadcast_to(np.asarray(dz, np.float64), (nt,)))
+        seq = np.ascontiguousarray(layer_seq, np.int32)
+        g = Grid(nx, ny, float(ax), float(by))
+        o = self._optics(kev, bandlimit)
+        ln = self._lens(cs, df, k_obj, df_spread, df_step)
+        plane = psi is None
+        if plane:
+            psi = np.empty((batch, nx, ny), np.complex64)
+        else:
+            shp = _cshape(psi)
+            batch = int(np.prod(shp[:-2])) if len(shp) > 2 else 1
+        if image is None:
+            image = np.zeros((nx, ny), np.float64)
+        eptr = None if exit_intensity is None else _ptr(exit_intensity, np.float64)
+        self._check(self._lib.msl_ctem_image(self._h, ctypes.byref(g), ctypes.byref(o),
+                                             _ptr(trans, np.complex64), nt, _ptr(dz, np.float64),
+                                             _ptr(seq, np.int32), len(seq), ctypes.byref(ln),
+                                             _ptr(psi, np.complex64), batch, 1 if plane else 0,
+                                             float(weight), _ptr(image, np.float64), eptr))
+        return image, psi, exit_intensity
+
+    def frozen_phonon(self, spec, nx, ny, nslice, radius, kev, cs, df, k_obj, nconfig, sigma, seed,
+                      df_spread=0.0, df_step=0.0, fparams=None, bandlimit=2.0 / 3.0,
+                      want_exit=True):
+        """Configuration-averaged image and exit-wave intensity, float64 [nx, ny] each."""
+        fp = np.ascontiguousarray(fparams_table() if fparams is None else fparams, np.float64)
+        x = np.ascontiguousarray(spec.x, np.float64)
+        y = np.ascontiguousarray(spec.y, np.float64)
+        z = np.ascontiguousarray(spec.z, np.float64)
+        Z = np.ascontiguousarray(spec.Z, np.int32)
+        at = Atoms(len(x), x.ctypes.data, y.ctypes.data, z.ctypes.data, Z.ctypes.data, float(spec.cz))
+        g = Grid(int(nx), int(ny), float(spec.ax), float(spec.by))
+        o = self._optics(kev, bandlimit)
+        ln = self._lens(cs, df, k_obj, df_spread, df_step)
+        img = np.empty((nx, ny), np.float64)
+        ex = np.empty((nx, ny), np.float64) if want_exit else None
+        self._check(self._lib.msl_frozen_phonon(self._h, ctypes.byref(at), _ptr(fp, np.float64),
+                                                ctypes.byref(g), int(nslice), float(radius),
+                                                ctypes.byref(o), ctypes.byref(ln), int(nconfig),
+                                                float(sigma), int(seed), _ptr(img, np.float64),
+                                                None if ex is None else _ptr(ex, np.float64)))
+        return img, ex
+
     # ------------------------------------------------------------------ STEM
     def stem_scan(self, trans, dz, layer_seq, ax, by, kev, k_ap, probe_xy, det_k,
                   checkpoints=None, df=0.0, cs=0.0, k_ap_in=0.0, bandlimit=2.0 / 3.0,
@@ -213,6 +268,16 @@ class Context:
                                             _ptr(xy, np.float64), len(xy), ctypes.byref(dets),
                                             _ptr(cps, np.int32), len(cps), _ptr(out, np.float64)))
         return out
+
+
+def phonon_displacements(seed, config, natom, sigma):
+    """Frozen-phonon displacements [natom, 3] of configuration `config` (msl_phonon_displacements)."""
+    d = np.empty((natom, 3), np.float64)
+    rc = _abi.load().msl_phonon_displacements(int(seed), int(config), int(natom), float(sigma),
+                                               ctypes.c_void_p(d.ctypes.data))
+    if rc != _abi.MSL_OK:
+        raise MslError(rc, "msl_phonon_displacements failed")
+    return d
 
 
 def wavelength(kev):

@@ -60,7 +60,7 @@ struct msl_ctx {
     int64_t prof_count[MSL_PROF_KINDS] = {0};
     double prof_ms[MSL_PROF_KINDS] = {0};
     DevBuf wave, in_stage, trans_stage, tabs, apchi, exy, fxy, detmask, partial, detout, pot,
-        atoms;
+        atoms, tmpw, ctf, acc;
     int *dflag = nullptr;  // device flag raised by a kernel whose bounded wait gave up
 };
 
@@ -347,6 +347,109 @@ int check_layers(msl_ctx *c, int ntrans, const double *dz, const int *layer_seq,
     return MSL_OK;
 }
 
+
+// Slice loop plus objective-lens imaging on device buffers (mulslice.cpp:539-676
+// with one illumination angle).  w: [batch][nx][ny] entrance waves (ignored when
+// plane) and, on return, exit waves when want_exit; img_d / exit_d: FP64
+// accumulators (exit_d may be null).
+int ctem_core(msl_ctx *c, const msl_grid *g, const msl_optics *o, const float2 *td, int ntrans,
+              const double *dz, const int *seq, int nslice, const msl_lens *lens, float2 *w,
+              int batch, bool plane, double weight, double *img_d, double *exit_d, bool want_exit) {
+    int rc;
+    const int nx = g->nx, ny = g->ny;
+    const size_t n2 = (size_t)nx * ny;
+    SliceTables st;
+    if ((rc = build_slice_tables(c, g, o, ntrans, dz, st))) return rc;
+    float2 *twr = twiddles(c, ny), *twc = twiddles(c, nx);
+    if (!twr || !twc) return fail(c, MSL_E_NOMEM, "twiddle table allocation failed");
+    for (int s = 0; s < nslice; ++s) {
+        const int l = seq[s];
+        int rf = msl::ROW_TRANS | msl::ROW_FWD;
+        if (s > 0) rf |= msl::ROW_LOAD | msl::ROW_INV;
+        else if (!plane) rf |= msl::ROW_LOAD;
+        RowArgs r = row_args(g, twr, td + (size_t)l * n2, w, batch, rf, c->dflag);
+        LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_row_pass(ny, r, c->stream, c->nsm, &c->launches); }));
+        // the last slice keeps the spectrum: W = Psi(k) / (nx ny) after the propagator
+        int cf = msl::COL_LOAD | msl::COL_FWD | msl::COL_PROP | msl::COL_STORE;
+        if (s + 1 < nslice) cf |= msl::COL_INV;
+        ColArgs ca = col_args(g, st, twc, l, w, batch, cf, c->dflag);
+        LAUNCH_TRY(c, timed(c, MSL_PROF_COL, [&] { return msl::launch_col_pass(nx, ca, c->stream, c->nsm, &c->launches); }));
+    }
+    const size_t wbytes = sizeof(float2) * n2 * batch;
+    CUDA_TRY(c, c->tmpw.ensure(wbytes));
+    float2 *tmp = (float2 *)c->tmpw.p;
+    // defocus values and weights (mulslice.cpp:552, :610-642)
+    std::vector<double> dfs, pw;
+    if (lens->df_spread > 0) {
+        const int ndf = (int)((2.5 * lens->df_spread) / lens->df_step);
+        for (int j = -ndf; j <= ndf; ++j) {
+            const double x = j * lens->df_step / lens->df_spread;
+            dfs.push_back(lens->df + j * lens->df_step);
+            pw.push_back(exp(-0.5 * x * x));
+        }
+    } else {
+        dfs.push_back(lens->df);
+        pw.push_back(1.0);
+    }
+    double psum = 0.0;
+    for (double v : pw) psum += v;
+    CUDA_TRY(c, c->ctf.ensure(sizeof(float2) * n2));
+    float2 *ctf = (float2 *)c->ctf.p;
+    const float kob = (float)lens->k_obj;
+    const float k2obj = kob * kob;
+    const double lam = msl_wavelength(o->kev);
+    const bool exit_needed = want_exit || exit_d != nullptr;
+    for (size_t j = 0; j < dfs.size(); ++j) {
+        // the last image may consume w itself unless the exit wave still needs it
+        const bool last = j + 1 == dfs.size();
+        float2 *target = (last && !exit_needed) ? w : tmp;
+        if (target != w)
+            CUDA_TRY(c, cudaMemcpyAsync(target, w, wbytes, cudaMemcpyDeviceToDevice, c->stream));
+        LAUNCH_TRY(c, timed(c, MSL_PROF_OTHER, [&] {
+                       return msl::launch_ctf_table(nx, ny, st.d_kx2, st.d_ky2, k2obj, lam, lens->cs, dfs[j],
+                                                    1.0f, ctf, c->stream, &c->launches);
+                   }));
+        ColArgs ca = col_args(g, st, twc, 0, target, batch,
+                              msl::COL_LOAD | msl::COL_CTF | msl::COL_INV | msl::COL_STORE, c->dflag);
+        ca.ctf = ctf;
+        LAUNCH_TRY(c, timed(c, MSL_PROF_COL, [&] { return msl::launch_col_pass(nx, ca, c->stream, c->nsm, &c->launches); }));
+        RowArgs r = row_args(g, twr, nullptr, target, batch,
+                             msl::ROW_LOAD | msl::ROW_INV | msl::ROW_ACCUM | msl::ROW_NOSTORE, c->dflag);
+        r.accum = img_d;
+        r.accum_w = weight * pw[j] / psum;
+        LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_row_pass(ny, r, c->stream, c->nsm, &c->launches); }));
+    }
+    if (exit_needed) {  // exit waves: inverse transform of W in place
+        ColArgs ca = col_args(g, st, twc, 0, w, batch, msl::COL_LOAD | msl::COL_INV | msl::COL_STORE, c->dflag);
+        LAUNCH_TRY(c, timed(c, MSL_PROF_COL, [&] { return msl::launch_col_pass(nx, ca, c->stream, c->nsm, &c->launches); }));
+        int rf = msl::ROW_LOAD | msl::ROW_INV;
+        if (exit_d) rf |= msl::ROW_ACCUM;
+        if (!want_exit) rf |= msl::ROW_NOSTORE;
+        RowArgs r = row_args(g, twr, nullptr, w, batch, rf, c->dflag);
+        r.accum = exit_d;
+        r.accum_w = weight;
+        LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_row_pass(ny, r, c->stream, c->nsm, &c->launches); }));
+    }
+    return MSL_OK;
+}
+
+int check_lens(msl_ctx *c, const msl_lens *l) {
+    if (!l) return fail(c, MSL_E_ARG, "lens is null");
+    if (!is_fin(l->cs) || !is_fin(l->df) || !(l->k_obj > 0) || !is_fin(l->k_obj))
+        return fail(c, MSL_E_ARG, "lens: cs, df finite and k_obj > 0 required");
+    if (!(l->df_spread >= 0) || !is_fin(l->df_spread) ||
+        (l->df_spread > 0 && (!(l->df_step > 0) || 2.5 * l->df_spread / l->df_step > 1000)))
+        return fail(c, MSL_E_ARG, "lens: df_spread >= 0 and df_step > 0 (at most 2001 defocus values)");
+    return MSL_OK;
+}
+
+uint64_t splitmix64(uint64_t x) {
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+
 }  // namespace
 
 extern "C" {
@@ -391,7 +494,8 @@ int msl_ctx_destroy(msl_ctx *c) {
     cudaStreamSynchronize(c->stream);
     for (auto &kv : c->tw) cudaFree(kv.second);
     DevBuf *bufs[] = {&c->wave, &c->in_stage, &c->trans_stage, &c->tabs, &c->apchi, &c->exy,
-                      &c->fxy, &c->detmask, &c->partial, &c->detout, &c->pot, &c->atoms};
+                      &c->fxy, &c->detmask, &c->partial, &c->detout, &c->pot, &c->atoms,
+                      &c->tmpw, &c->ctf, &c->acc};
     for (DevBuf *b : bufs) b->release();
     if (c->dflag) cudaFree(c->dflag);
     cudaStreamDestroy(c->stream);
@@ -418,6 +522,149 @@ int msl_profile_read(const msl_ctx *c, int kind, int64_t *launches, double *ms) 
     *launches = c->prof_count[kind];
     *ms = c->prof_ms[kind];
     return MSL_OK;
+}
+
+
+int msl_phonon_displacements(uint64_t seed, int config, int natom, double sigma, double *d) {
+    if (natom < 0 || config < 0 || !(sigma >= 0) || (natom > 0 && !d)) return MSL_E_ARG;
+    const double two_pi = 6.283185307179586477;
+    for (int i = 0; i < natom; ++i) {
+        double u[4];
+        for (int k = 0; k < 4; ++k) {
+            const uint64_t key = ((uint64_t)config << 40) | ((uint64_t)i << 2) | (uint64_t)k;
+            const uint64_t h = splitmix64(seed ^ splitmix64(key));
+            u[k] = (double)(h >> 11) * (1.0 / 9007199254740992.0);
+        }
+        const double r0 = sqrt(-2.0 * log(1.0 - u[0])), r1 = sqrt(-2.0 * log(1.0 - u[2]));
+        d[3 * i + 0] = sigma * r0 * cos(two_pi * u[1]);
+        d[3 * i + 1] = sigma * r0 * sin(two_pi * u[1]);
+        d[3 * i + 2] = sigma * r1 * cos(two_pi * u[3]);
+    }
+    return MSL_OK;
+}
+
+int msl_ctem_image(msl_ctx *c, const msl_grid *g, const msl_optics *o, const float *trans,
+                   int ntrans, const double *dz, const int *layer_seq, int nslice, const msl_lens *lens,
+                   float *psi, int batch, int plane_wave, double weight, double *image,
+                   double *exit_intensity) {
+    if (!c) return MSL_E_ARG;
+    int rc = check_grid(c, g);
+    if (rc) return rc;
+    if ((rc = check_optics(c, o))) return rc;
+    if ((rc = check_layers(c, ntrans, dz, layer_seq, nslice))) return rc;
+    if ((rc = check_lens(c, lens))) return rc;
+    if (!trans || !image || batch < 1 || (!plane_wave && !psi) || !is_fin(weight))
+        return fail(c, MSL_E_ARG, "trans, image required; psi required unless plane_wave; batch >= 1");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    if ((rc = err_reset(c))) return rc;
+    const int nx = g->nx, ny = g->ny;
+    const size_t n2 = (size_t)nx * ny;
+    const float2 *td;
+    if ((rc = stage_in(c, (const float2 *)trans, sizeof(float2) * n2 * ntrans, c->trans_stage, &td)))
+        return rc;
+    const size_t wbytes = sizeof(float2) * n2 * batch;
+    const bool pdev = psi && on_device(psi);
+    float2 *w;
+    if (pdev) {
+        w = (float2 *)psi;
+    } else {
+        CUDA_TRY(c, c->wave.ensure(wbytes));
+        w = (float2 *)c->wave.p;
+        if (!plane_wave) CUDA_TRY(c, cudaMemcpyAsync(w, psi, wbytes, cudaMemcpyHostToDevice, c->stream));
+    }
+    // FP64 accumulators: caller's device buffers, or staged copies of the host ones
+    const size_t ibytes = sizeof(double) * n2;
+    const bool idev = on_device(image), edev = exit_intensity && on_device(exit_intensity);
+    CUDA_TRY(c, c->acc.ensure(2 * ibytes));
+    double *img_d = idev ? image : (double *)c->acc.p;
+    double *exit_d = exit_intensity ? (edev ? exit_intensity : (double *)c->acc.p + n2) : nullptr;
+    if (!idev) CUDA_TRY(c, cudaMemcpyAsync(img_d, image, ibytes, cudaMemcpyHostToDevice, c->stream));
+    if (exit_intensity && !edev)
+        CUDA_TRY(c, cudaMemcpyAsync(exit_d, exit_intensity, ibytes, cudaMemcpyHostToDevice, c->stream));
+    // batch images sum into one accumulator: accumulate image by image
+    for (int b = 0; b < batch; ++b) {
+        if ((rc = ctem_core(c, g, o, td, ntrans, dz, layer_seq, nslice, lens, w + (size_t)b * n2, 1,
+                            plane_wave != 0, weight, img_d, exit_d, psi != nullptr)))
+            return rc;
+    }
+    if (psi && !pdev) CUDA_TRY(c, cudaMemcpyAsync(psi, w, wbytes, cudaMemcpyDeviceToHost, c->stream));
+    if (!idev) CUDA_TRY(c, cudaMemcpyAsync(image, img_d, ibytes, cudaMemcpyDeviceToHost, c->stream));
+    if (exit_intensity && !edev)
+        CUDA_TRY(c, cudaMemcpyAsync(exit_intensity, exit_d, ibytes, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    collect_profile(c);
+    if (c->dflag && (rc = err_check(c))) return rc;
+    return MSL_OK;
+}
+
+int msl_frozen_phonon(msl_ctx *c, const msl_atoms *at, const double *fparams, const msl_grid *g,
+                      int nslice, double radius, const msl_optics *o, const msl_lens *lens, int nconfig,
+                      double sigma, uint64_t seed, double *image, double *exit_intensity) {
+    if (!c) return MSL_E_ARG;
+    int rc = check_grid(c, g);
+    if (rc) return rc;
+    if ((rc = check_optics(c, o))) return rc;
+    if ((rc = check_lens(c, lens))) return rc;
+    if (!at || nconfig < 1 || !(sigma >= 0) || !is_fin(sigma) || nslice < 1)
+        return fail(c, MSL_E_ARG, "atoms required, nconfig >= 1, sigma >= 0, nslice >= 1");
+    if (!image && !exit_intensity) return fail(c, MSL_E_ARG, "nothing to compute: image and exit_intensity null");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    const int nx = g->nx, ny = g->ny, na = at->natom;
+    const size_t n2 = (size_t)nx * ny;
+    // device buffers: potential, transmission, wave, accumulators
+    DevBuf vbuf, tbuf;
+    CUDA_TRY(c, vbuf.ensure(sizeof(float) * n2 * nslice));
+    CUDA_TRY(c, tbuf.ensure(sizeof(float2) * n2 * nslice));
+    CUDA_TRY(c, c->acc.ensure(2 * sizeof(double) * n2));
+    double *img_d = (double *)c->acc.p, *exit_d = img_d + n2;
+    CUDA_TRY(c, cudaMemsetAsync(img_d, 0, 2 * sizeof(double) * n2, c->stream));
+    CUDA_TRY(c, c->wave.ensure(sizeof(float2) * n2));
+    float2 *w = (float2 *)c->wave.p;
+    std::vector<double> x(na), y(na), z(na), d(3 * (size_t)na);
+    std::vector<double> dz(nslice, at->cz / nslice);
+    std::vector<int> seq(nslice);
+    for (int s = 0; s < nslice; ++s) seq[s] = s;
+    msl_atoms jat = *at;
+    jat.x = x.data();
+    jat.y = y.data();
+    jat.z = z.data();
+    int out = MSL_OK;
+    for (int cfg = 0; cfg < nconfig && out == MSL_OK; ++cfg) {
+        msl_phonon_displacements(seed, cfg, na, sigma, d.data());
+        for (int i = 0; i < na; ++i) {
+            x[i] = at->x[i] + d[3 * i];
+            y[i] = at->y[i] + d[3 * i + 1];
+            z[i] = at->z[i] + d[3 * i + 2];
+        }
+        if ((out = msl_potential_build(c, &jat, fparams, g, nslice, radius, (float *)vbuf.p))) break;
+        if ((out = msl_transmission_build(c, g, o, (const float *)vbuf.p, nslice, (float *)tbuf.p))) break;
+        if ((out = err_reset(c))) break;
+        if ((out = ctem_core(c, g, o, (const float2 *)tbuf.p, nslice, dz.data(), seq.data(), nslice, lens,
+                             w, 1, true, 1.0 / nconfig, img_d, exit_intensity ? exit_d : nullptr, false)))
+            break;
+        cudaError_t e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) {
+            out = fail(c, MSL_E_CUDA, std::string("frozen phonon: ") + cudaGetErrorString(e));
+            break;
+        }
+        collect_profile(c);
+        if ((out = err_check(c))) break;
+    }
+    if (out == MSL_OK) {
+        if (image) {
+            cudaError_t e = cudaMemcpyAsync(image, img_d, sizeof(double) * n2, cudaMemcpyDefault, c->stream);
+            if (e != cudaSuccess) out = fail(c, MSL_E_CUDA, "copy of the image failed");
+        }
+        if (out == MSL_OK && exit_intensity) {
+            cudaError_t e = cudaMemcpyAsync(exit_intensity, exit_d, sizeof(double) * n2, cudaMemcpyDefault, c->stream);
+            if (e != cudaSuccess) out = fail(c, MSL_E_CUDA, "copy of the exit intensity failed");
+        }
+        cudaStreamSynchronize(c->stream);
+    }
+    cudaStreamSynchronize(c->stream);
+    vbuf.release();
+    tbuf.release();
+    return out;
 }
 
 int msl_set_probe_batch(msl_ctx *c, int batch) {

@@ -15,6 +15,8 @@ enum RowFlags {
     ROW_INV = 4,     // exp(-i) line transform
     ROW_TRANS = 8,   // multiply by trans[ix][iy]
     ROW_FWD = 16,    // exp(+i) line transform
+    ROW_ACCUM = 32,  // accum[line][iy] += accum_w * |psi|^2 (FP64)
+    ROW_NOSTORE = 64 // do not write the wave back
 };
 
 struct RowArgs {
@@ -29,6 +31,8 @@ struct RowArgs {
     int flags;
     float scale;           // multiplies the output when != 1
     int *err;              // set to 1 when a bounded wait gives up (may be null)
+    double *accum;         // [nlines][ny] (ROW_ACCUM)
+    double accum_w;
 };
 
 // Column pass: strided lines of length nx (one line = one iy of one image).
@@ -40,6 +44,7 @@ enum ColFlags {
     COL_DETECT = 16,  // annular detector partial sums of |psi|^2
     COL_INV = 32,     // exp(-i) line transform
     COL_STORE = 64,   // store to `out`
+    COL_CTF = 128,    // * ctf[ix][iy] (objective lens transfer, full 2D table)
 };
 
 struct ColArgs {
@@ -58,6 +63,7 @@ struct ColArgs {
     int ndet;
     double *partial;          // [batch][ny / C][ndet]
     int *err;                 // set to 1 when a bounded wait gives up (may be null)
+    const float2 *ctf;        // [nx][ny] (COL_CTF)
 };
 
 struct PotArgs {
@@ -94,6 +100,11 @@ cudaError_t launch_probe_shifts(int nx, int ny, int nb, const double *fxy, float
 cudaError_t launch_detector_mask(int nx, int ny, const double *kxd, const double *kyd, int ndet,
                                  const double *kin2, const double *kout2, uint8_t *mask,
                                  cudaStream_t s, int64_t *launches);
+// ctf[ix][iy] = exp(-i chi(k)) * scale for k2 = kx2 + ky2 (float) <= k2obj, else 0;
+// chi = pi lam k2 (cs lam^2 k2 / 2 - df) in FP64
+cudaError_t launch_ctf_table(int nx, int ny, const float *kx2, const float *ky2, float k2obj,
+                             double lam, double cs, double df, float scale, float2 *ctf,
+                             cudaStream_t s, int64_t *launches);
 // out[b * out_stride + d] = scale * sum_t partial[b][t][d]
 cudaError_t launch_detector_finalize(int nb, int ntile, int ndet, const double *partial,
                                      double scale, double *out, int out_stride, cudaStream_t s,

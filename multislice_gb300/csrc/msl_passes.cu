@@ -88,8 +88,16 @@ __global__ void __launch_bounds__(RowCfg<N>::THREADS) row_pass_kernel(RowArgs a)
 #pragma unroll
                 for (int e = 0; e < E; ++e) v[e] = c_scale(v[e], a.scale);
             }
+            if (a.flags & ROW_ACCUM) {
 #pragma unroll
-            for (int e = 0; e < E; ++e) a.out[base + t + T * e] = v[e];
+                for (int e = 0; e < E; ++e)
+                    a.accum[base + t + T * e] +=
+                        a.accum_w * ((double)v[e].x * v[e].x + (double)v[e].y * v[e].y);
+            }
+            if (!(a.flags & ROW_NOSTORE)) {
+#pragma unroll
+                for (int e = 0; e < E; ++e) a.out[base + t + T * e] = v[e];
+            }
         }
     }
 }
@@ -121,6 +129,13 @@ __device__ __forceinline__ void col_propagate(float2 (&v)[P::E], const ColArgs &
         if (k2 < a.k2max) v[e] = c_mul(c_mul(v[e], pyv), a.px[ix]);
         else v[e] = make_float2(0.f, 0.f);
     }
+}
+
+// Objective-lens transfer of mulslice.cpp:613-633 from a precomputed table.
+template <class P>
+__device__ __forceinline__ void col_ctf(float2 (&v)[P::E], const ColArgs &a, int iy, int t) {
+#pragma unroll
+    for (int e = 0; e < P::E; ++e) v[e] = c_mul(v[e], a.ctf[(size_t)(t + P::T * e) * a.ny + iy]);
 }
 
 // Annular detector partial sums of one tile (MSProject.cs:806-829): float per
@@ -187,6 +202,7 @@ __global__ void __launch_bounds__(ColCfg<N>::THREADS) col_pass_kernel(ColArgs a)
         }
         if (a.flags & COL_FWD) fft_line<P, +1>(v, t, ad, tw);
         if (a.flags & COL_PROP) col_propagate<P>(v, a, iy, t);
+        if (a.flags & COL_CTF) col_ctf<P>(v, a, iy, t);
         if (a.flags & COL_DETECT) col_detect<P, NWARP>(v, a, b, iy, t, ty, tiles_per_img, red);
         if (a.flags & COL_INV) fft_line<P, -1>(v, t, ad, tw);
         if (a.flags & COL_STORE) {
@@ -284,6 +300,7 @@ __global__ void __launch_bounds__(ColTmaCfg<PL>::THREADS, MINB)
         }
         if (a.flags & COL_FWD) fft_line<P, +1>(v, t, ad, tw);
         if (a.flags & COL_PROP) col_propagate<P>(v, a, iy, t);
+        if (a.flags & COL_CTF) col_ctf<P>(v, a, iy, t);
         if (a.flags & COL_DETECT) col_detect<P, Cfg::NWARP>(v, a, b, iy, t, ty, tpi, red);
         if (a.flags & COL_INV) fft_line<P, -1>(v, t, ad, tw);
         if (store) {
@@ -407,14 +424,25 @@ __global__ void __launch_bounds__(RowTmaCfg<N, TH>::THREADS, MINB)
 #pragma unroll
             for (int e = 0; e < E; ++e) v[e] = c_scale(v[e], a.scale);
         }
-        __syncthreads();  // every thread is done reading bs
+        if (a.flags & ROW_ACCUM) {
+            double *acc = a.accum + (size_t)line * N;
 #pragma unroll
-        for (int e = 0; e < E; ++e) mine[t + T * e] = v[e];
-        fence_proxy_async();
+            for (int e = 0; e < E; ++e)
+                acc[t + T * e] += a.accum_w * ((double)v[e].x * v[e].x + (double)v[e].y * v[e].y);
+        }
+        const bool st = !(a.flags & ROW_NOSTORE);
+        __syncthreads();  // every thread is done reading bs
+        if (st) {
+#pragma unroll
+            for (int e = 0; e < E; ++e) mine[t + T * e] = v[e];
+            fence_proxy_async();
+        }
         __syncthreads();
         if (tid == 0) {
-            tma_store_3d(&map, 0, 0, tile * L, bs);
-            tma_commit();
+            if (st) {
+                tma_store_3d(&map, 0, 0, tile * L, bs);
+                tma_commit();
+            }
             if (load && k + NBUF - 1 < nmine) {
                 tma_wait_read<1>();        // the store of tile k-1 has left its buffer
                 issue_load(k + NBUF - 1);  // into buffer (k + 2) % 3
@@ -483,6 +511,23 @@ __global__ void detector_mask_kernel(int nx, int ny, const double *kxd, const do
     for (int d = 0; d < ndet; ++d)
         if (s <= kout2[d] && s >= kin2[d]) bits |= 1u << d;
     mask[(size_t)ix * ny + iy] = (uint8_t)bits;
+}
+
+__global__ void ctf_table_kernel(int nx, int ny, const float *kx2, const float *ky2, float k2obj,
+                                 double lam, double cs, double df, float scale, float2 *ctf) {
+    const int iy = blockIdx.x * blockDim.x + threadIdx.x;
+    const int ix = blockIdx.y;
+    if (iy >= ny || ix >= nx) return;
+    const float k2 = __fadd_rn(kx2[ix], ky2[iy]);
+    float2 out = make_float2(0.f, 0.f);
+    if (k2 <= k2obj) {
+        const double q = (double)k2;
+        const double chi = 3.14159265358979323846 * lam * q * (0.5 * cs * lam * lam * q - df);
+        double sn, cn;
+        sincos(chi, &sn, &cn);
+        out = make_float2((float)cn * scale, (float)-sn * scale);
+    }
+    ctf[(size_t)ix * ny + iy] = out;
 }
 
 __global__ void detector_finalize_kernel(int nb, int ntile, int ndet, const double *partial,
@@ -762,6 +807,15 @@ cudaError_t launch_detector_mask(int nx, int ny, const double *kxd, const double
     ++*launches;
     dim3 grid((ny + 255) / 256, nx);
     detector_mask_kernel<<<grid, 256, 0, s>>>(nx, ny, kxd, kyd, ndet, kin2, kout2, mask);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_ctf_table(int nx, int ny, const float *kx2, const float *ky2, float k2obj,
+                             double lam, double cs, double df, float scale, float2 *ctf,
+                             cudaStream_t s, int64_t *launches) {
+    ++*launches;
+    dim3 grid((ny + 255) / 256, nx);
+    ctf_table_kernel<<<grid, 256, 0, s>>>(nx, ny, kx2, ky2, k2obj, lam, cs, df, scale, ctf);
     return cudaGetLastError();
 }
 

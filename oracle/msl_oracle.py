@@ -332,3 +332,60 @@ def rel_l2(a, b):
     a = np.asarray(a)
     b = np.asarray(b)
     return float(np.linalg.norm((a - b).ravel()) / np.linalg.norm(b.ravel()))
+
+
+# ------------------------------------------------------------ CTEM imaging
+def ctf(nx, ny, ax, by, v0, cs, df, k_obj, dtype=np.complex128):
+    """exp(-i chi) inside the objective aperture (mulslice.cpp:556-633); chi in FP64."""
+    kx, kx2 = freqn(nx, ax)
+    ky, ky2 = freqn(ny, by)
+    k2 = (kx2[:, None] + ky2[None, :]).astype(np.float32)
+    kob = np.float32(k_obj)
+    inside = k2 <= np.float32(kob * kob)
+    q = k2.astype(np.float64)
+    lam = wavelength(v0)
+    chi = np.pi * lam * q * (0.5 * cs * lam * lam * q - df)
+    return np.where(inside, np.exp(-1j * chi), 0).astype(dtype)
+
+
+def defocus_weights(df, df_spread, df_step):
+    if df_spread <= 0:
+        return np.array([df]), np.array([1.0])
+    ndf = int((2.5 * df_spread) / df_step)
+    j = np.arange(-ndf, ndf + 1)
+    w = np.exp(-0.5 * (j * df_step / df_spread) ** 2)
+    return df + j * df_step, w / w.sum()
+
+
+def ctem_image(exit_wave, ax, by, v0, cs, df, k_obj, df_spread=0.0, df_step=0.0):
+    """Defocus-averaged image intensity of exit wave(s) [..., nx, ny] (summed over the batch)."""
+    nx, ny = exit_wave.shape[-2:]
+    W = kfft(exit_wave.astype(np.complex128))
+    img = np.zeros((nx, ny))
+    for d, w in zip(*defocus_weights(df, df_spread, df_step)):
+        psi = kifft(W * ctf(nx, ny, ax, by, v0, cs, d, k_obj))
+        I = np.abs(psi) ** 2
+        img += w * (I.sum(axis=0) if I.ndim == 3 else I)
+    return img
+
+
+def _splitmix64(x):
+    x = (x + np.uint64(0x9E3779B97F4A7C15)).astype(np.uint64)
+    x = ((x ^ (x >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)).astype(np.uint64)
+    x = ((x ^ (x >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)).astype(np.uint64)
+    return x ^ (x >> np.uint64(31))
+
+
+def phonon_displacements(seed, config, natom, sigma):
+    """The library's frozen-phonon displacement stream (splitmix64 + Box-Muller)."""
+    with np.errstate(over="ignore"):
+        i = np.arange(natom, dtype=np.uint64)[:, None]
+        k = np.arange(4, dtype=np.uint64)[None, :]
+        key = (np.uint64(config) << np.uint64(40)) | (i << np.uint64(2)) | k
+        h = _splitmix64(np.uint64(seed) ^ _splitmix64(key))
+    u = (h >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+    r0 = np.sqrt(-2.0 * np.log(1.0 - u[:, 0]))
+    r1 = np.sqrt(-2.0 * np.log(1.0 - u[:, 2]))
+    t = 2.0 * np.pi
+    return sigma * np.stack([r0 * np.cos(t * u[:, 1]), r0 * np.sin(t * u[:, 1]),
+                             r1 * np.cos(t * u[:, 3])], axis=1)

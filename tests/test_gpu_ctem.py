@@ -1,0 +1,86 @@
+"""GPU parity of the CTEM imaging epilogue and the frozen-phonon driver
+(objective lens of mulslice.cpp:539-676, jitter of MSUseOnceCalculator.cs:179-199)."""
+import numpy as np
+import pytest
+
+from multislice_gb300 import specimen as S
+from oracle import msl_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+CS = 1.2e7      # 1.2 mm in Angstrom
+DF = -600.0     # -60 nm
+
+
+def test_vacuum_image_is_uniform(ctx):
+    """A plane wave through vacuum images to intensity 1 everywhere (CTF(0) = 1)."""
+    t = np.ones((1, 128, 128), np.complex64)
+    img, psi, ex = ctx.ctem_image(t, 2.0, [0] * 4, 20.0, 20.0, 300.0, CS, DF, 2.0,
+                                  exit_intensity=np.zeros((128, 128)))
+    np.testing.assert_allclose(img, 1.0, atol=1e-6)
+    np.testing.assert_allclose(ex, 1.0, atol=1e-6)
+    img2, _, _ = ctx.ctem_image(t, 2.0, [0] * 4, 20.0, 20.0, 300.0, CS, DF, 2.0, df_spread=50.0,
+                                df_step=25.0)
+    np.testing.assert_allclose(img2, 1.0, atol=1e-6)
+
+
+@pytest.mark.parametrize("spread", [0.0, 50.0])
+def test_ctem_image_vs_oracle(ctx, golden, spread):
+    G = golden("si_small.npz")
+    ax, by, dz = float(G["ax"]), float(G["by"]), float(G["dz"])
+    img, psi, _ = ctx.ctem_image(G["t"], dz, G["seq"], ax, by, 200.0, CS, DF, 1.5,
+                                 df_spread=spread, df_step=25.0)
+    assert O.rel_l2(psi[0], G["wave"]) < 1e-5          # exit wave vs the reference
+    ref = O.ctem_image(G["wave"].astype(np.complex128), ax, by, 200.0, CS, DF, 1.5, spread, 25.0)
+    assert O.rel_l2(img, ref) < 2e-5
+
+
+def _oracle_frozen_phonon(spec, fp, nx, ny, nslice, radius, kev, k_obj, nconfig, sigma, seed):
+    img = np.zeros((nx, ny))
+    exi = np.zeros((nx, ny))
+    mask = O.band_mask(nx, ny, spec.ax, spec.by)
+    props = [O.propagator_tables(nx, ny, spec.ax, spec.by, kev, spec.cz / nslice, precision="f64")]
+    for c in range(nconfig):
+        d = O.phonon_displacements(seed, c, spec.natom, sigma)
+        V = O.potential(spec.x + d[:, 0], spec.y + d[:, 1], spec.z + d[:, 2], spec.Z, fp, spec.ax,
+                        spec.by, spec.cz, nx, ny, nslice, radius)
+        T = O.transmission(V, kev, spec.ax, spec.by, np.complex128)
+        w, _ = O.multislice(np.ones((nx, ny), np.complex128), T, props * nslice, np.arange(nslice), mask)
+        img += O.ctem_image(w, spec.ax, spec.by, kev, CS, DF, k_obj) / nconfig
+        exi += np.abs(w) ** 2 / nconfig
+    return img, exi
+
+
+def test_frozen_phonon_vs_oracle(ctx, fparams):
+    spec = S.fcc_au(2, 2, 4)
+    nx = ny = 128
+    img, exi = ctx.frozen_phonon(spec, nx, ny, 8, 3.0, 300.0, CS, DF, 2.0, nconfig=3, sigma=0.085,
+                                 seed=7)
+    ref_img, ref_exi = _oracle_frozen_phonon(spec, fparams, nx, ny, 8, 3.0, 300.0, 2.0, 3, 0.085, 7)
+    assert O.rel_l2(exi, ref_exi) < 2e-5
+    assert O.rel_l2(img, ref_img) < 2e-5
+
+
+def test_frozen_phonon_zero_sigma_equals_static_image(ctx):
+    spec = S.fcc_au(2, 2, 4)
+    img, exi = ctx.frozen_phonon(spec, 128, 128, 8, 3.0, 300.0, CS, DF, 2.0, nconfig=2, sigma=0.0, seed=1)
+    v = ctx.potential(spec, 128, 128, 8, 3.0)
+    t = ctx.transmission(v, spec.ax, spec.by, 300.0)
+    ref, _, _ = ctx.ctem_image(t, spec.cz / 8, np.arange(8), spec.ax, spec.by, 300.0, CS, DF, 2.0)
+    assert O.rel_l2(img, ref) < 1e-6
+
+
+def test_frozen_phonon_au_2048_full_size(ctx):
+    """fcc Au 16x16x40 cells, 2048^2, 80 slices, 32 configurations, 300 kV, Cs 1.2 mm,
+    df -60 nm: configuration averaging is deterministic and physically bounded."""
+    spec = S.fcc_au()
+    kev = 300.0
+    k_obj = float(S.mrad_to_k(25.0, kev))
+    img, exi = ctx.frozen_phonon(spec, 2048, 2048, 80, 3.0, kev, CS, DF, k_obj, nconfig=32,
+                                 sigma=0.085, seed=2026)
+    assert np.all(np.isfinite(img)) and np.all(img >= 0)
+    assert 0.5 < exi.mean() <= 1.0 + 1e-6          # band limiting only removes intensity
+    assert img.mean() <= exi.mean() + 1e-6          # the aperture only removes intensity
+    img2, _ = ctx.frozen_phonon(spec, 2048, 2048, 80, 3.0, kev, CS, DF, k_obj, nconfig=32,
+                                sigma=0.085, seed=2026, want_exit=False)
+    assert np.array_equal(img, img2)

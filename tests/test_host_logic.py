@@ -62,3 +62,20 @@ def test_stem_raster_and_angles():
 def test_slice_index_drops_outside():
     kz = O.slice_index(np.array([-0.1, 0.0, 1.99, 2.0, 10.0]), 2.0, 4)
     assert kz.tolist() == [-1, 0, 3, -1, -1]
+
+
+def test_phonon_displacement_stream_matches_oracle():
+    from multislice_gb300 import phonon_displacements
+    for seed, cfg, n in ((0, 0, 1), (1234, 5, 1000), (2 ** 63 + 11, 31, 40960)):
+        a = phonon_displacements(seed, cfg, n, 0.085)
+        b = O.phonon_displacements(seed, cfg, n, 0.085)
+        np.testing.assert_allclose(a, b, rtol=0, atol=1e-15)
+    d = phonon_displacements(99, 3, 40960, 0.085)
+    assert abs(d.std() - 0.085) < 0.002 and abs(d.mean()) < 0.002
+    assert not np.allclose(phonon_displacements(99, 4, 10, 0.085), phonon_displacements(99, 3, 10, 0.085))
+
+
+def test_defocus_weights_follow_mulslice_rule():
+    dfs, w = O.defocus_weights(-600.0, 50.0, 25.0)
+    assert len(dfs) == 11 and np.isclose(w.sum(), 1.0)
+    assert np.isclose(dfs[5], -600.0) and w[5] == w.max()
