@@ -105,6 +105,23 @@ int64_t msl_kernel_launches(const msl_ctx *ctx);
  * a1 b1 a2 b2 a3 b3 c1 d1 c2 d2 c3 d3, row 0 is zero. */
 int msl_fparams_parse(const char *text, size_t len, double *tab);
 
+/* Unit cell and atom records of a .coo file. */
+typedef struct {
+    double a, b, c;            /* cell edges, Angstrom */
+    double alpha, beta, gamma; /* cell angles, degrees */
+    int natom;
+} msl_cell;
+
+/* Parse .coo text: a header "a b c alpha beta gamma natoms" then one line per
+ * atom "x y z Z [dw] [ads] [occ]" in fractional coordinates, wrapped into
+ * [0, 1); blank lines are skipped and "//" starts a comment (the C# reader,
+ * MSProject.cs:239-338); a first line that is not a header is taken as a title
+ * (the amodel reader, amodel/include/ModelCoo.cpp:20-90).  Missing dw, ads
+ * default to 0 and occ to 1.  rec receives natom records of 7 doubles
+ * (x y z Z dw ads occ) when it is not NULL and capacity >= natom; call with
+ * rec = NULL first to learn natom from cell->natom. */
+int msl_coo_parse(const char *text, size_t len, msl_cell *cell, double *rec, int capacity);
+
 /* Electron wavelength (A) and interaction constant sigma (rad/(kV*A)):
  * slicelib.cpp:2795-2806 and :2387-2412. */
 double msl_wavelength(double kev);
@@ -230,6 +247,24 @@ int msl_frozen_phonon(msl_ctx *ctx, const msl_atoms *atoms, const double *fparam
 /* Probe batch size used by msl_stem_scan (0 = automatic).  Work buffers are
  * sized batch * nx * ny * 8 bytes. */
 int msl_set_probe_batch(msl_ctx *ctx, int batch);
+
+/* ------------------------------------------------- Muslib-shaped exports */
+
+/* The reference's native STEM library (Musli console 1.3 (STEM) 2/Muslib) with
+ * identical argument lists, so its C# P/Invoke declarations bind unchanged
+ * (Windows ULONG/LONG are 32-bit).  Host arrays in the C# layout: N x M complex
+ * doubles, element (i, j) at gli[2*(j*N + i)].  Run on the current CUDA device
+ * in FP64; return 0 (success) or -1; *cpro is set to 100 on success.
+ * CreatePropagator / ApplyPropagator: Propagator.cpp:5-53 / :55-107.
+ * PG_rs_curve_DW_periodic: PG_RS.cpp:304-446. */
+int CreatePropagator(double a, double b, double gam, double thickness, double E, double Xtilt,
+                     double Ytilt, uint32_t N, uint32_t M, double *gli, float *cpro);
+int ApplyPropagator(double a, double b, double gam, double thickness, double E, double Xtilt,
+                    double Ytilt, uint32_t N, uint32_t M, double *gli, float *cpro);
+int PG_rs_curve_DW_periodic(double a, double b, double gam, double E, double atrad, uint32_t N,
+                            uint32_t M, uint32_t Na, double *xx, double *yy, double *ads, double *occ,
+                            int32_t *type, double *scatentryes, uint32_t Npoints, double dds,
+                            double *gli, float *cpro);
 
 /* ------------------------------------------------- no-allocation variant */
 

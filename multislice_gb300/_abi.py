@@ -22,8 +22,10 @@ EXPORTS = (
     "msl_fparams_parse", "msl_wavelength", "msl_sigma", "msl_potential_build",
     "msl_transmission_build", "msl_fft2d", "msl_multislice", "msl_stem_scan",
     "msl_set_probe_batch", "msl_profile_enable", "msl_profile_read", "msl_multislice_noalloc",
-    "msl_ctem_image", "msl_phonon_displacements", "msl_frozen_phonon",
+    "msl_ctem_image", "msl_phonon_displacements", "msl_frozen_phonon", "msl_coo_parse",
 )
+# Muslib-shaped exports (reference names, no msl_ prefix)
+MUSLIB_EXPORTS = ("CreatePropagator", "ApplyPropagator", "PG_rs_curve_DW_periodic")
 PROF_ROW, PROF_COL, PROF_POTENTIAL, PROF_OTHER = 0, 1, 2, 3
 
 
@@ -47,6 +49,11 @@ class Probe(ctypes.Structure):
 
 class Detectors(ctypes.Structure):
     _fields_ = [("ndet", c_int), ("k_in", c_void_p), ("k_out", c_void_p)]
+
+
+class Cell(ctypes.Structure):
+    _fields_ = [("a", c_double), ("b", c_double), ("c", c_double), ("alpha", c_double),
+                ("beta", c_double), ("gamma", c_double), ("natom", c_int)]
 
 
 class Lens(ctypes.Structure):
@@ -96,6 +103,11 @@ def load(path=LIB_PATH):
         "msl_ctem_image": (c_int, [P, POINTER(Grid), POINTER(Optics), P, c_int, P, P, c_int,
                                    POINTER(Lens), P, c_int, c_int, c_double, P, P]),
         "msl_phonon_displacements": (c_int, [ctypes.c_uint64, c_int, c_int, c_double, P]),
+        "msl_coo_parse": (c_int, [c_char_p, c_size_t, POINTER(Cell), P, c_int]),
+        "CreatePropagator": (c_int, [c_double] * 7 + [ctypes.c_uint32, ctypes.c_uint32, P, P]),
+        "ApplyPropagator": (c_int, [c_double] * 7 + [ctypes.c_uint32, ctypes.c_uint32, P, P]),
+        "PG_rs_curve_DW_periodic": (c_int, [c_double] * 5 + [ctypes.c_uint32] * 3 + [P] * 5 +
+                                    [P, ctypes.c_uint32, c_double, P, P]),
         "msl_frozen_phonon": (c_int, [P, POINTER(Atoms), P, POINTER(Grid), c_int, c_double,
                                       POINTER(Optics), POINTER(Lens), c_int, c_double,
                                       ctypes.c_uint64, P, P]),

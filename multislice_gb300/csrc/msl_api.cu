@@ -699,6 +699,65 @@ int msl_fparams_parse(const char *text, size_t len, double *tab) {
     return seen == 103 ? MSL_OK : MSL_E_ARG;
 }
 
+int msl_coo_parse(const char *text, size_t len, msl_cell *cell, double *rec, int capacity) {
+    if (!text || !cell) return MSL_E_ARG;
+    // split into lines, strip "//" comments, keep non-blank ones
+    std::vector<std::string> lines;
+    size_t p = 0;
+    while (p < len) {
+        size_t e = p;
+        while (e < len && text[e] != '\n') ++e;
+        std::string ln(text + p, e - p);
+        const size_t cm = ln.find("//");
+        if (cm != std::string::npos) ln = ln.substr(0, cm);
+        for (char &ch : ln)
+            if (ch == ',' || ch == '\r' || ch == '\t') ch = ch == ',' ? '.' : ' ';
+        if (ln.find_first_not_of(' ') != std::string::npos) lines.push_back(ln);
+        p = e + 1;
+    }
+    auto numbers = [](const std::string &ln, double *v, int maxn) {
+        const char *q = ln.c_str();
+        int n = 0;
+        while (n < maxn) {
+            char *end = nullptr;
+            const double x = strtod(q, &end);
+            if (end == q) break;
+            v[n++] = x;
+            q = end;
+        }
+        while (*q == ' ') ++q;
+        return *q ? -1 : n;  // trailing junk: not a numeric line
+    };
+    size_t li = 0;
+    double h[8];
+    if (lines.empty()) return MSL_E_ARG;
+    if (numbers(lines[0], h, 8) != 7) li = 1;  // a title line
+    if (li >= lines.size() || numbers(lines[li], h, 8) != 7) return MSL_E_ARG;
+    cell->a = h[0];
+    cell->b = h[1];
+    cell->c = h[2];
+    cell->alpha = h[3];
+    cell->beta = h[4];
+    cell->gamma = h[5];
+    if (!(h[6] >= 0) || h[6] > 2e9) return MSL_E_ARG;
+    const int natom = (int)h[6];
+    cell->natom = natom;
+    if (!rec) return MSL_OK;
+    if (capacity < natom) return MSL_E_ARG;
+    if (lines.size() < li + 1 + (size_t)natom) return MSL_E_ARG;
+    for (int k = 0; k < natom; ++k) {
+        double v[8] = {0, 0, 0, 0, 0, 0, 1, 0};
+        const int n = numbers(lines[li + 1 + k], v, 7);
+        if (n < 4) return MSL_E_ARG;
+        if (n < 5) v[4] = 0;
+        if (n < 6) v[5] = 0;
+        if (n < 7) v[6] = 1;
+        for (int d = 0; d < 3; ++d) v[d] -= std::floor(v[d]);
+        for (int d = 0; d < 7; ++d) rec[(size_t)k * 7 + d] = v[d];
+    }
+    return MSL_OK;
+}
+
 int msl_potential_build(msl_ctx *c, const msl_atoms *at, const double *fparams, const msl_grid *g,
                         int nslice, double radius, float *v_out) {
     if (!c) return MSL_E_ARG;

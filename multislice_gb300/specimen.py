@@ -155,3 +155,43 @@ def config_srtio3_stem(nprobe_side=64):
                 k_ap=float(mrad_to_k(25.0, kev)), probe_xy=xy,
                 det_k=[(float(mrad_to_k(80.0, kev)), float(mrad_to_k(200.0, kev))),
                        (float(mrad_to_k(11.0, kev)), float(mrad_to_k(22.0, kev)))])
+
+
+# ------------------------------------------------------------------- .coo
+def parse_coo(text):
+    """(cell, records) of .coo text via msl_coo_parse; records [natom, 7] =
+    x y z (fractional, wrapped) Z dw ads occ."""
+    import ctypes
+    from . import _abi
+    lib = _abi.load()
+    raw = text.encode() if isinstance(text, str) else bytes(text)
+    cell = _abi.Cell()
+    rc = lib.msl_coo_parse(raw, len(raw), ctypes.byref(cell), None, 0)
+    if rc != 0:
+        raise _abi.MslError(rc, "not a .coo header")
+    rec = np.zeros((max(cell.natom, 1), 7), np.float64)
+    rc = lib.msl_coo_parse(raw, len(raw), ctypes.byref(cell), ctypes.c_void_p(rec.ctypes.data),
+                           cell.natom)
+    if rc != 0:
+        raise _abi.MslError(rc, "malformed .coo atom records")
+    return cell, rec[: cell.natom]
+
+
+def read_coo(path):
+    """Specimen (Cartesian Angstrom, orthogonal cells) from a .coo file."""
+    with open(path, "rb") as f:
+        cell, rec = parse_coo(f.read())
+    if abs(cell.gamma - 90.0) > 1e-9 or abs(cell.alpha - 90.0) > 1e-9 or abs(cell.beta - 90.0) > 1e-9:
+        raise ValueError("only orthogonal cells map onto the slice grid")
+    return Specimen(rec[:, 0] * cell.a, rec[:, 1] * cell.b, rec[:, 2] * cell.c,
+                    rec[:, 3].astype(np.int32), cell.a, cell.b, cell.c)
+
+
+def write_coo(spec, path, title=None):
+    """Write a Specimen as .coo (header line, fractional records x y z Z 0 0 1)."""
+    with open(path, "w") as f:
+        if title:
+            f.write(f"// {title}\n")
+        f.write(f"{spec.ax:.10g} {spec.by:.10g} {spec.cz:.10g} 90 90 90 {spec.natom}\n")
+        for x, y, z, Z in zip(spec.x / spec.ax, spec.y / spec.by, spec.z / spec.cz, spec.Z):
+            f.write(f"{x:.12f} {y:.12f} {z:.12f} {int(Z)} 0 0 1\n")

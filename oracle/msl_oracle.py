@@ -389,3 +389,74 @@ def phonon_displacements(seed, config, natom, sigma):
     t = 2.0 * np.pi
     return sigma * np.stack([r0 * np.cos(t * u[:, 1]), r0 * np.sin(t * u[:, 1]),
                              r1 * np.cos(t * u[:, 3])], axis=1)
+
+
+# ------------------------------------------------- Muslib entry points (C#)
+def cs_lambda(E):
+    """C#/Muslib wavelength, E in volts (Propagator.cpp:17)."""
+    return 0.387818 / np.sqrt(E / 1000.0 * (1.0 + 0.978459e-3 * E / 1000))
+
+
+def muslib_propagator(a, b, gam, thickness, E, tx, ty, N, M):
+    """CreatePropagator (Propagator.cpp:5-53) as complex128 [M, N] (row j, column i)."""
+    A, B = 1.0 / (a * np.sin(gam)), 1.0 / (b * np.sin(gam))
+    GK = np.pi * cs_lambda(E) * thickness
+    smax = min(N * 0.5 / a, M * 0.5 / b) ** 2
+    i = np.where(np.arange(N) < N // 2, np.arange(N), np.arange(N) - N)
+    j = np.where(np.arange(M) < M // 2, np.arange(M), np.arange(M) - M)
+    x = i[None, :] * A
+    y = j[:, None] * B
+    s = x * (x - 2.0 * y * np.cos(gam)) + y * y
+    con = GK * s - 2 * np.pi * thickness * np.tan(tx) * x - 2 * np.pi * thickness * np.tan(ty) * y
+    return np.where(s >= smax, 0, np.exp(1j * con))
+
+
+def muslib_pg_periodic(a, b, gam, E, atrad, N, M, xx, yy, ads, occ, typ, curves, dds):
+    """Multiplicative phase grating of PG_rs_curve_DW_periodic (PG_RS.cpp:304-446),
+    complex128 [M, N]; the nine periodic rectangles with C truncation of bounds."""
+    lam = cs_lambda(E)
+    K = lam * np.sqrt(1.0 + (0.0242621 / lam) ** 2)
+    sg, cg = np.sin(gam), np.cos(gam)
+    drax, dray = atrad * sg / a, atrad * sg / b
+    dxa, dyb = a / N, b / M
+    npts = curves.shape[1]
+    ph = np.zeros((M, N))
+    am = np.zeros((M, N))
+    for k in range(len(xx)):
+        ibb, iee = int((xx[k] - drax) * N), int((xx[k] + drax) * N)
+        jbb, jee = int((yy[k] - dray) * M), int((yy[k] + dray) * M)
+        X, Y = xx[k] * a, yy[k] * b
+        rects = [(max(ibb, 0), min(iee, N), max(jbb, 0), min(jee, M), X, Y)]
+        if jbb < 0:
+            rects.append((max(ibb, 0), min(iee, N), jbb + M, M, X, Y + b))
+        if jee >= M:
+            rects.append((max(ibb, 0), min(iee, N), 0, jee - M + 1, X, Y - b))
+        if ibb < 0:
+            rects.append((ibb + N, N, max(jbb, 0), min(jee, M), X + a, Y))
+        if iee >= N:
+            rects.append((0, iee - N + 1, max(jbb, 0), min(jee, M), X - a, Y))
+        if ibb < 0 and jbb < 0:
+            rects.append((ibb + N, N, jbb + M, M, X + a, Y + b))
+        if iee >= N and jee >= M:
+            rects.append((0, iee - N + 1, 0, jee - M + 1, X - a, Y - b))
+        if iee >= N and jbb < 0:
+            rects.append((0, iee - N + 1, jbb + M, M, X - a, Y + b))
+        if ibb < 0 and jee >= M:
+            rects.append((ibb + N, N, 0, jee - M + 1, X + a, Y - b))
+        cur = curves[typ[k]]
+        for ib, ie, jb, je, x0, y0 in rects:
+            if ie <= ib or je <= jb:
+                continue
+            ii = np.arange(ib, ie)
+            jj = np.arange(jb, je)
+            x = ii[None, :] * dxa - x0
+            y = jj[:, None] * dyb - y0
+            ar2 = np.sqrt(x * (x + 2 * y * cg) + y * y) / dds
+            fl = np.floor(ar2)
+            ok = fl < npts - 1
+            jjj = np.where(ok, fl, 0).astype(np.int64)
+            res = cur[jjj] + (cur[np.minimum(jjj + 1, npts - 1)] - cur[jjj]) * (ar2 - jjj)
+            res = np.where(ok, res, 0.0)
+            ph[jb:je, ib:ie] += K * res * occ[k]
+            am[jb:je, ib:ie] += K * ads[k] * occ[k] * res
+    return np.exp(-am) * np.exp(-1j * ph)

@@ -78,3 +78,48 @@ def test_ctx_create_reports_missing_gpu_as_error():
     rc = lib.msl_ctx_create(0, ctypes.byref(h))
     assert rc in (_abi.MSL_E_CUDA, _abi.MSL_E_ARG)
     assert not h.value
+
+
+def test_library_exports_muslib_entry_points():
+    lib = _lib()
+    text = open(HEADER).read()
+    for name in _abi.MUSLIB_EXPORTS:
+        assert hasattr(lib, name), name
+        assert f"{name}(" in text
+
+
+COO = """// SrTiO3 test cell
+3.905 3.905 3.905 90 90 90 5
+
+0.0 0.0 0.0 38 0.5
+0.5 0.5 0.5 22
+0.5 0.5 0.0 8 0 0.02 1
+1.5 0.0 -0.5 8   // wrapped into [0, 1)
+0.0 0.5 0.5 8 0.1 0.2 0.5
+"""
+
+
+def test_coo_parse_reference_rules():
+    from multislice_gb300.specimen import parse_coo
+    cell, rec = parse_coo(COO)
+    assert (cell.a, cell.gamma, cell.natom) == (3.905, 90.0, 5)
+    np.testing.assert_allclose(rec[0], [0, 0, 0, 38, 0.5, 0, 1])
+    np.testing.assert_allclose(rec[1], [0.5, 0.5, 0.5, 22, 0, 0, 1])
+    np.testing.assert_allclose(rec[3][:3], [0.5, 0.0, 0.5])
+    np.testing.assert_allclose(rec[4], [0, 0.5, 0.5, 8, 0.1, 0.2, 0.5])
+    # amodel style: a title line before the header
+    cell2, rec2 = parse_coo("Fe model\n2.87 2.87 2.87 90 90 90 1\n0.25 0.25 0.25 26\n")
+    assert cell2.natom == 1 and rec2[0][3] == 26
+    with pytest.raises(Exception):
+        parse_coo("1 2 3 90 90 90 4\n0 0 0 8\n")  # fewer records than declared
+
+
+def test_coo_roundtrip(tmp_path):
+    from multislice_gb300 import specimen as S
+    spec = S.srtio3(2, 2, 2)
+    p = tmp_path / "sto.coo"
+    S.write_coo(spec, str(p), "SrTiO3 2x2x2")
+    back = S.read_coo(str(p))
+    np.testing.assert_allclose(back.x, spec.x, atol=1e-9)
+    np.testing.assert_allclose(back.z, spec.z, atol=1e-9)
+    assert np.array_equal(back.Z, spec.Z) and back.cz == spec.cz
