@@ -244,6 +244,37 @@ int msl_frozen_phonon(msl_ctx *ctx, const msl_atoms *atoms, const double *fparam
                       const msl_lens *lens, int nconfig, double sigma, uint64_t seed,
                       double *image, double *exit_intensity);
 
+/* ------------------------------------------------------- uneven batches */
+
+#define MSL_PLANE_WAVE 0
+#define MSL_PROBE 1
+
+/* One multislice job of an uneven batch: its own grid, energy, transmission
+ * stack, slice sequence and illumination (a plane wave of amplitude 1, or the
+ * converged probe of MSProject.cs:458-514 at (probe_x, probe_y)). */
+typedef struct {
+    msl_grid grid;
+    double kev;
+    const float *trans;      /* complex64 [ntrans][nx][ny], host or device */
+    int ntrans;
+    const double *dz;        /* [ntrans] slice thicknesses */
+    const int *layer_seq;    /* [nslice] */
+    int nslice;
+    int illumination;        /* MSL_PLANE_WAVE or MSL_PROBE */
+    msl_probe probe;
+    double probe_x, probe_y; /* Angstrom */
+    float *exit_wave;        /* out: complex64 [nx][ny], host or device */
+} msl_job;
+
+/* Run many independent slice loops at once (the reference runs them one after
+ * another: MSProjectReuse.cs:254-347, MSProjectUseOnce.cs:235-273).  Jobs are
+ * grouped by grid shape; inside a group every slice step is one row-pass and
+ * one column-pass launch over all jobs still running (jobs ordered by
+ * decreasing slice count, so the running ones form a prefix), each image with
+ * its own transmission rows, propagator and band-limit tables.  Results equal
+ * msl_multislice run job by job.  bandlimit as in msl_optics. */
+int msl_run_jobs(msl_ctx *ctx, const msl_job *jobs, int njobs, double bandlimit);
+
 /* Probe batch size used by msl_stem_scan (0 = automatic).  Work buffers are
  * sized batch * nx * ny * 8 bytes. */
 int msl_set_probe_batch(msl_ctx *ctx, int batch);

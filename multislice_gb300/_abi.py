@@ -23,7 +23,9 @@ EXPORTS = (
     "msl_transmission_build", "msl_fft2d", "msl_multislice", "msl_stem_scan",
     "msl_set_probe_batch", "msl_profile_enable", "msl_profile_read", "msl_multislice_noalloc",
     "msl_ctem_image", "msl_phonon_displacements", "msl_frozen_phonon", "msl_coo_parse",
+    "msl_run_jobs",
 )
+PLANE_WAVE, PROBE = 0, 1
 # Muslib-shaped exports (reference names, no msl_ prefix)
 MUSLIB_EXPORTS = ("CreatePropagator", "ApplyPropagator", "PG_rs_curve_DW_periodic")
 PROF_ROW, PROF_COL, PROF_POTENTIAL, PROF_OTHER = 0, 1, 2, 3
@@ -59,6 +61,13 @@ class Cell(ctypes.Structure):
 class Lens(ctypes.Structure):
     _fields_ = [("cs", c_double), ("df", c_double), ("k_obj", c_double), ("df_spread", c_double),
                 ("df_step", c_double)]
+
+
+class Job(ctypes.Structure):
+    _fields_ = [("grid", Grid), ("kev", c_double), ("trans", c_void_p), ("ntrans", c_int),
+                ("dz", c_void_p), ("layer_seq", c_void_p), ("nslice", c_int),
+                ("illumination", c_int), ("probe", Probe), ("probe_x", c_double),
+                ("probe_y", c_double), ("exit_wave", c_void_p)]
 
 
 class MslError(RuntimeError):
@@ -104,6 +113,7 @@ def load(path=LIB_PATH):
                                    POINTER(Lens), P, c_int, c_int, c_double, P, P]),
         "msl_phonon_displacements": (c_int, [ctypes.c_uint64, c_int, c_int, c_double, P]),
         "msl_coo_parse": (c_int, [c_char_p, c_size_t, POINTER(Cell), P, c_int]),
+        "msl_run_jobs": (c_int, [P, P, c_int, c_double]),
         "CreatePropagator": (c_int, [c_double] * 7 + [ctypes.c_uint32, ctypes.c_uint32, P, P]),
         "ApplyPropagator": (c_int, [c_double] * 7 + [ctypes.c_uint32, ctypes.c_uint32, P, P]),
         "PG_rs_curve_DW_periodic": (c_int, [c_double] * 5 + [ctypes.c_uint32] * 3 + [P] * 5 +

@@ -23,7 +23,7 @@ import os
 import numpy as np
 
 from . import _abi
-from ._abi import Atoms, Detectors, Grid, Lens, MslError, Optics, Probe
+from ._abi import Atoms, Detectors, Grid, Job, Lens, MslError, Optics, Probe
 
 _DATA = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data")
 
@@ -239,6 +239,47 @@ class Context:
                                                 float(sigma), int(seed), _ptr(img, np.float64),
                                                 None if ex is None else _ptr(ex, np.float64)))
         return img, ex
+
+    # ---------------------------------------------------------- uneven jobs
+    def run_jobs(self, jobs, bandlimit=2.0 / 3.0):
+        """Run many independent slice loops at once (msl_run_jobs).
+
+        jobs: list of dicts with trans [ntrans, nx, ny] complex64, ax, by, kev, dz, layer_seq
+        and optionally probe=(k_ap, x, y[, df, cs]).  Returns the exit waves."""
+        keep = []
+        arr = (Job * len(jobs))()
+        outs = []
+        for j, d in enumerate(jobs):
+            t = _as(d["trans"], np.complex64)
+            nt, nx, ny = _cshape(t)
+            dz = np.ascontiguousarray(np.broadcast_to(np.asarray(d["dz"], np.float64), (nt,)))
+            seq = np.ascontiguousarray(d["layer_seq"], np.int32)
+            out = d.get("out")
+            if out is None:
+                out = np.empty((nx, ny), np.complex64)
+            keep += [t, dz, seq]
+            outs.append(out)
+            jb = arr[j]
+            jb.grid = Grid(nx, ny, float(d["ax"]), float(d["by"]))
+            jb.kev = float(d["kev"])
+            jb.trans = _ptr(t, np.complex64).value
+            jb.ntrans = nt
+            jb.dz = dz.ctypes.data
+            jb.layer_seq = seq.ctypes.data
+            jb.nslice = len(seq)
+            pr = d.get("probe")
+            if pr is None:
+                jb.illumination = _abi.PLANE_WAVE
+            else:
+                k_ap, x, y = pr[:3]
+                df = pr[3] if len(pr) > 3 else 0.0
+                cs = pr[4] if len(pr) > 4 else 0.0
+                jb.illumination = _abi.PROBE
+                jb.probe = Probe(0.0, float(k_ap), float(df), float(cs))
+                jb.probe_x, jb.probe_y = float(x), float(y)
+            jb.exit_wave = _ptr(out, np.complex64).value
+        self._check(self._lib.msl_run_jobs(self._h, ctypes.byref(arr), len(jobs), float(bandlimit)))
+        return outs
 
     # ------------------------------------------------------------------ STEM
     def stem_scan(self, trans, dz, layer_seq, ax, by, kev, k_ap, probe_xy, det_k,

@@ -60,7 +60,7 @@ struct msl_ctx {
     int64_t prof_count[MSL_PROF_KINDS] = {0};
     double prof_ms[MSL_PROF_KINDS] = {0};
     DevBuf wave, in_stage, trans_stage, tabs, apchi, exy, fxy, detmask, partial, detout, pot,
-        atoms, tmpw, ctf, acc;
+        atoms, tmpw, ctf, acc, jobtab;
     int *dflag = nullptr;  // device flag raised by a kernel whose bounded wait gave up
 };
 
@@ -495,7 +495,7 @@ int msl_ctx_destroy(msl_ctx *c) {
     for (auto &kv : c->tw) cudaFree(kv.second);
     DevBuf *bufs[] = {&c->wave, &c->in_stage, &c->trans_stage, &c->tabs, &c->apchi, &c->exy,
                       &c->fxy, &c->detmask, &c->partial, &c->detout, &c->pot, &c->atoms,
-                      &c->tmpw, &c->ctf, &c->acc};
+                      &c->tmpw, &c->ctf, &c->acc, &c->jobtab};
     for (DevBuf *b : bufs) b->release();
     if (c->dflag) cudaFree(c->dflag);
     cudaStreamDestroy(c->stream);
@@ -665,6 +665,186 @@ int msl_frozen_phonon(msl_ctx *c, const msl_atoms *at, const double *fparams, co
     vbuf.release();
     tbuf.release();
     return out;
+}
+
+
+int msl_run_jobs(msl_ctx *c, const msl_job *jobs, int njobs, double bandlimit) {
+    if (!c) return MSL_E_ARG;
+    if (!jobs || njobs < 1) return fail(c, MSL_E_ARG, "jobs required");
+    if (!(bandlimit > 0) || bandlimit > 1.0) return fail(c, MSL_E_ARG, "bandlimit must lie in (0, 1]");
+    int rc;
+    for (int j = 0; j < njobs; ++j) {
+        const msl_job &jb = jobs[j];
+        msl_optics o = {jb.kev, bandlimit, 0.0, 0.0, 0};
+        if ((rc = check_grid(c, &jb.grid)) || (rc = check_optics(c, &o)) ||
+            (rc = check_layers(c, jb.ntrans, jb.dz, jb.layer_seq, jb.nslice))) {
+            c->err = "job " + std::to_string(j) + ": " + c->err;
+            return rc;
+        }
+        if (!jb.trans || !jb.exit_wave) return fail(c, MSL_E_ARG, "job " + std::to_string(j) + ": trans/exit_wave null");
+        if (jb.illumination != MSL_PLANE_WAVE && jb.illumination != MSL_PROBE)
+            return fail(c, MSL_E_ARG, "job " + std::to_string(j) + ": unknown illumination");
+        if (jb.illumination == MSL_PROBE &&
+            (!(jb.probe.k_in >= 0) || !(jb.probe.k_out > jb.probe.k_in) || !is_fin(jb.probe.k_out) ||
+             !is_fin(jb.probe.df) || !is_fin(jb.probe.cs) || !is_fin(jb.probe_x) || !is_fin(jb.probe_y)))
+            return fail(c, MSL_E_ARG, "job " + std::to_string(j) + ": invalid probe");
+    }
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    if ((rc = err_reset(c))) return rc;
+    // group by grid shape
+    std::map<std::pair<int, int>, std::vector<int>> groups;
+    for (int j = 0; j < njobs; ++j) groups[{jobs[j].grid.nx, jobs[j].grid.ny}].push_back(j);
+    for (auto &kv : groups) {
+        std::vector<int> &ids = kv.second;
+        std::stable_sort(ids.begin(), ids.end(), [&](int x, int y) { return jobs[x].nslice > jobs[y].nslice; });
+        const int nx = kv.first.first, ny = kv.first.second, nb = (int)ids.size();
+        const size_t n2 = (size_t)nx * ny;
+        const int S = jobs[ids[0]].nslice;
+        float2 *twr = twiddles(c, ny), *twc = twiddles(c, nx);
+        if (!twr || !twc) return fail(c, MSL_E_NOMEM, "twiddle table allocation failed");
+        // transmission stacks on the device (staged into one arena when on the host)
+        std::vector<const float2 *> tdev(nb);
+        size_t stage_bytes = 0;
+        for (int b = 0; b < nb; ++b)
+            if (!on_device(jobs[ids[b]].trans)) stage_bytes += sizeof(float2) * n2 * jobs[ids[b]].ntrans;
+        CUDA_TRY(c, c->trans_stage.ensure(stage_bytes));
+        size_t off = 0;
+        for (int b = 0; b < nb; ++b) {
+            const msl_job &jb = jobs[ids[b]];
+            if (on_device(jb.trans)) {
+                tdev[b] = (const float2 *)jb.trans;
+            } else {
+                const size_t bytes = sizeof(float2) * n2 * jb.ntrans;
+                float2 *dst = (float2 *)((unsigned char *)c->trans_stage.p + off);
+                CUDA_TRY(c, cudaMemcpyAsync(dst, jb.trans, bytes, cudaMemcpyHostToDevice, c->stream));
+                tdev[b] = dst;
+                off += bytes;
+            }
+        }
+        // per-job tables: [kx2 ky2] floats, then per layer [px py]; pointer tables per step
+        size_t nprop = 0;
+        for (int b = 0; b < nb; ++b) nprop += (size_t)jobs[ids[b]].ntrans;
+        const size_t kbytes = sizeof(float) * (nx + ny) * nb;
+        const size_t pbytes = sizeof(float2) * (nx + ny) * nprop;
+        std::vector<unsigned char> htab(kbytes + pbytes);
+        std::vector<float> k2max(nb);
+        std::vector<size_t> prop_off(nb);
+        size_t po = 0;
+        for (int b = 0; b < nb; ++b) {
+            const msl_job &jb = jobs[ids[b]];
+            std::vector<float> kx, kx2, ky, ky2;
+            freqn_f32(nx, jb.grid.ax, kx, kx2);
+            freqn_f32(ny, jb.grid.by, ky, ky2);
+            float *kt = (float *)htab.data() + (size_t)b * (nx + ny);
+            memcpy(kt, kx2.data(), sizeof(float) * nx);
+            memcpy(kt + nx, ky2.data(), sizeof(float) * ny);
+            k2max[b] = k2max_f32(nx, ny, jb.grid.ax, jb.grid.by, bandlimit);
+            msl_optics o = {jb.kev, bandlimit, 0.0, 0.0, 0};
+            prop_off[b] = po;
+            for (int l = 0; l < jb.ntrans; ++l) {
+                float2 *pt = (float2 *)(htab.data() + kbytes) + po;
+                prop_tables(nx, ny, jb.grid.ax, jb.grid.by, &o, jb.dz[l], kx, kx2, ky, ky2, pt, pt + nx);
+                po += (size_t)(nx + ny);
+            }
+        }
+        if ((rc = upload(c, c->tabs, htab.data(), htab.size()))) return rc;
+        const float *dk = (const float *)c->tabs.p;
+        const float2 *dp = (const float2 *)((unsigned char *)c->tabs.p + kbytes);
+        // pointer tables: trans[S][nb], prop[S][nb], k2[nb], k2max[nb]
+        std::vector<const void *> ptab((size_t)2 * S * nb + nb);
+        for (int s = 0; s < S; ++s)
+            for (int b = 0; b < nb; ++b) {
+                const msl_job &jb = jobs[ids[b]];
+                const int l = s < jb.nslice ? jb.layer_seq[s] : 0;
+                ptab[(size_t)s * nb + b] = tdev[b] + (size_t)l * n2;
+                ptab[(size_t)(S + s) * nb + b] = dp + prop_off[b] + (size_t)l * (nx + ny);
+            }
+        for (int b = 0; b < nb; ++b) ptab[(size_t)2 * S * nb + b] = dk + (size_t)b * (nx + ny);
+        const size_t ptbytes = sizeof(void *) * ptab.size();
+        CUDA_TRY(c, c->jobtab.ensure(ptbytes + sizeof(float) * nb));
+        CUDA_TRY(c, cudaMemcpyAsync(c->jobtab.p, ptab.data(), ptbytes, cudaMemcpyHostToDevice, c->stream));
+        float *dk2max = (float *)((unsigned char *)c->jobtab.p + ptbytes);
+        CUDA_TRY(c, cudaMemcpyAsync(dk2max, k2max.data(), sizeof(float) * nb, cudaMemcpyHostToDevice, c->stream));
+        const float2 *const *ttab = (const float2 *const *)c->jobtab.p;
+        const float2 *const *ptabd = ttab + (size_t)S * nb;
+        const float *const *ktab = (const float *const *)(ttab + (size_t)2 * S * nb);
+        // entrance waves in the column-inverse representation every job shares:
+        // a plane wave is 1 in the ky = 0 column, a probe is ifft_x of its spectrum
+        CUDA_TRY(c, c->wave.ensure(sizeof(float2) * n2 * nb));
+        float2 *w = (float2 *)c->wave.p;
+        CUDA_TRY(c, cudaMemsetAsync(w, 0, sizeof(float2) * n2 * nb, c->stream));
+        std::vector<float2> ones(nx, make_float2(1.f, 0.f));
+        for (int b = 0; b < nb; ++b) {
+            const msl_job &jb = jobs[ids[b]];
+            float2 *slot = w + (size_t)b * n2;
+            if (jb.illumination == MSL_PLANE_WAVE) {
+                CUDA_TRY(c, cudaMemcpy2DAsync(slot, sizeof(float2) * ny, ones.data(), sizeof(float2),
+                                              sizeof(float2), nx, cudaMemcpyHostToDevice, c->stream));
+                continue;
+            }
+            std::vector<double> hk(nx + ny + 2);
+            for (int i = 0; i < nx; ++i) hk[i] = (double)(i < nx / 2 ? i : i - nx) / jb.grid.ax;
+            for (int i = 0; i < ny; ++i) hk[nx + i] = (double)(i < ny / 2 ? i : i - ny) / jb.grid.by;
+            hk[nx + ny] = jb.probe_x / jb.grid.ax;
+            hk[nx + ny + 1] = jb.probe_y / jb.grid.by;
+            CUDA_TRY(c, c->fxy.ensure(sizeof(double) * hk.size()));
+            CUDA_TRY(c, cudaStreamSynchronize(c->stream));  // fxy/apchi/exy of the previous probe are free
+            CUDA_TRY(c, cudaMemcpyAsync(c->fxy.p, hk.data(), sizeof(double) * hk.size(), cudaMemcpyHostToDevice,
+                                        c->stream));
+            const double *kxd = (const double *)c->fxy.p, *kyd = kxd + nx;
+            CUDA_TRY(c, c->apchi.ensure(sizeof(float2) * n2 + n2));
+            CUDA_TRY(c, c->exy.ensure(sizeof(float2) * (nx + ny)));
+            float2 *apchi = (float2 *)c->apchi.p, *ex = (float2 *)c->exy.p, *ey = ex + nx;
+            LAUNCH_TRY(c, timed(c, MSL_PROF_OTHER, [&] {
+                           return msl::launch_probe_table(nx, ny, kxd, kyd, jb.probe.k_in * jb.probe.k_in,
+                                                          jb.probe.k_out * jb.probe.k_out, msl_wavelength(jb.kev),
+                                                          jb.probe.df, jb.probe.cs, 1.0 / ((double)nx * ny), apchi,
+                                                          c->stream, &c->launches);
+                       }));
+            LAUNCH_TRY(c, timed(c, MSL_PROF_OTHER, [&] {
+                           return msl::launch_probe_shifts(nx, ny, 1, kyd + ny, ex, ey, c->stream, &c->launches);
+                       }));
+            SliceTables none;
+            none.k2max = 0.f;
+            none.d_kx2 = none.d_ky2 = nullptr;
+            none.d_prop = nullptr;
+            ColArgs pa = col_args(&jb.grid, none, twc, 0, slot, 1, msl::COL_PROBE | msl::COL_INV | msl::COL_STORE,
+                                  c->dflag);
+            pa.apchi = apchi;
+            pa.ex = ex;
+            pa.ey = ey;
+            LAUNCH_TRY(c, timed(c, MSL_PROF_COL, [&] { return msl::launch_col_pass(nx, pa, c->stream, c->nsm, &c->launches); }));
+        }
+        // lockstep slice loop over the running prefix
+        msl_grid gg = {nx, ny, 1.0, 1.0};
+        SliceTables none;
+        none.k2max = 0.f;
+        none.d_kx2 = none.d_ky2 = nullptr;
+        none.d_prop = nullptr;
+        for (int s = 0; s < S; ++s) {
+            int nact = 0;
+            while (nact < nb && jobs[ids[nact]].nslice > s) ++nact;
+            RowArgs r = row_args(&gg, twr, nullptr, w, nact,
+                                 msl::ROW_LOAD | msl::ROW_INV | msl::ROW_TRANS | msl::ROW_FWD, c->dflag);
+            r.trans_b = ttab + (size_t)s * nb;
+            LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_row_pass(ny, r, c->stream, c->nsm, &c->launches); }));
+            ColArgs ca = col_args(&gg, none, twc, 0, w, nact,
+                                  msl::COL_LOAD | msl::COL_FWD | msl::COL_PROP | msl::COL_INV | msl::COL_STORE, c->dflag);
+            ca.prop_b = ptabd + (size_t)s * nb;
+            ca.k2_b = ktab;
+            ca.k2max_b = dk2max;
+            LAUNCH_TRY(c, timed(c, MSL_PROF_COL, [&] { return msl::launch_col_pass(nx, ca, c->stream, c->nsm, &c->launches); }));
+        }
+        RowArgs r = row_args(&gg, twr, nullptr, w, nb, msl::ROW_LOAD | msl::ROW_INV, c->dflag);
+        LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_row_pass(ny, r, c->stream, c->nsm, &c->launches); }));
+        for (int b = 0; b < nb; ++b)
+            CUDA_TRY(c, cudaMemcpyAsync(jobs[ids[b]].exit_wave, w + (size_t)b * n2, sizeof(float2) * n2,
+                                        cudaMemcpyDefault, c->stream));
+        CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    }
+    collect_profile(c);
+    if (c->dflag && (rc = err_check(c))) return rc;
+    return MSL_OK;
 }
 
 int msl_set_probe_batch(msl_ctx *c, int batch) {

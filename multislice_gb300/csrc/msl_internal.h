@@ -33,6 +33,7 @@ struct RowArgs {
     int *err;              // set to 1 when a bounded wait gives up (may be null)
     double *accum;         // [nlines][ny] (ROW_ACCUM)
     double accum_w;
+    const float2 *const *trans_b;  // per-image transmission rows (replaces trans when set)
 };
 
 // Column pass: strided lines of length nx (one line = one iy of one image).
@@ -64,6 +65,11 @@ struct ColArgs {
     double *partial;          // [batch][ny / C][ndet]
     int *err;                 // set to 1 when a bounded wait gives up (may be null)
     const float2 *ctf;        // [nx][ny] (COL_CTF)
+    // per-image tables (replace px/py, kx2/ky2, k2max when set): prop_b[b] -> px[nx] py[ny],
+    // k2_b[b] -> kx2[nx] ky2[ny], k2max_b[b]
+    const float2 *const *prop_b;
+    const float *const *k2_b;
+    const float *k2max_b;
 };
 
 struct PotArgs {

@@ -78,7 +78,7 @@ __global__ void __launch_bounds__(RowCfg<N>::THREADS) row_pass_kernel(RowArgs a)
         }
         if (a.flags & ROW_INV) fft_line<P, -1>(v, t, ad, tw);
         if (valid && (a.flags & ROW_TRANS)) {
-            const float2 *tr = a.trans + (size_t)(line % a.nx) * N;
+            const float2 *tr = (a.trans_b ? a.trans_b[line / a.nx] : a.trans) + (size_t)(line % a.nx) * N;
 #pragma unroll
             for (int e = 0; e < E; ++e) v[e] = c_mul(v[e], tr[t + T * e]);
         }
@@ -119,14 +119,24 @@ __device__ __forceinline__ void col_probe(float2 (&v)[P::E], const ColArgs &a, i
 
 // propagate() of slicelib.cpp:744-790: py then px inside the band limit, 0 outside.
 template <class P>
-__device__ __forceinline__ void col_propagate(float2 (&v)[P::E], const ColArgs &a, int iy, int t) {
-    const float ky2 = a.ky2[iy];
-    const float2 pyv = a.py[iy];
+__device__ __forceinline__ void col_propagate(float2 (&v)[P::E], const ColArgs &a, int b, int iy, int t) {
+    const float2 *px = a.px, *py = a.py;
+    const float *kx2 = a.kx2, *ky2t = a.ky2;
+    float k2max = a.k2max;
+    if (a.prop_b) {  // uneven batches: every image has its own tables
+        px = a.prop_b[b];
+        py = px + P::N;
+        kx2 = a.k2_b[b];
+        ky2t = kx2 + P::N;
+        k2max = a.k2max_b[b];
+    }
+    const float ky2 = ky2t[iy];
+    const float2 pyv = py[iy];
 #pragma unroll
     for (int e = 0; e < P::E; ++e) {
         const int ix = t + P::T * e;
-        const float k2 = __fadd_rn(a.kx2[ix], ky2);
-        if (k2 < a.k2max) v[e] = c_mul(c_mul(v[e], pyv), a.px[ix]);
+        const float k2 = __fadd_rn(kx2[ix], ky2);
+        if (k2 < k2max) v[e] = c_mul(c_mul(v[e], pyv), px[ix]);
         else v[e] = make_float2(0.f, 0.f);
     }
 }
@@ -201,7 +211,7 @@ __global__ void __launch_bounds__(ColCfg<N>::THREADS) col_pass_kernel(ColArgs a)
             for (int e = 0; e < E; ++e) v[e] = a.in[base + (size_t)(t + T * e) * a.ny];
         }
         if (a.flags & COL_FWD) fft_line<P, +1>(v, t, ad, tw);
-        if (a.flags & COL_PROP) col_propagate<P>(v, a, iy, t);
+        if (a.flags & COL_PROP) col_propagate<P>(v, a, b, iy, t);
         if (a.flags & COL_CTF) col_ctf<P>(v, a, iy, t);
         if (a.flags & COL_DETECT) col_detect<P, NWARP>(v, a, b, iy, t, ty, tiles_per_img, red);
         if (a.flags & COL_INV) fft_line<P, -1>(v, t, ad, tw);
@@ -299,7 +309,7 @@ __global__ void __launch_bounds__(ColTmaCfg<PL>::THREADS, MINB)
             for (int e = 0; e < E; ++e) v[e] = make_float2(0.f, 0.f);
         }
         if (a.flags & COL_FWD) fft_line<P, +1>(v, t, ad, tw);
-        if (a.flags & COL_PROP) col_propagate<P>(v, a, iy, t);
+        if (a.flags & COL_PROP) col_propagate<P>(v, a, b, iy, t);
         if (a.flags & COL_CTF) col_ctf<P>(v, a, iy, t);
         if (a.flags & COL_DETECT) col_detect<P, Cfg::NWARP>(v, a, b, iy, t, ty, tpi, red);
         if (a.flags & COL_INV) fft_line<P, -1>(v, t, ad, tw);
@@ -396,7 +406,7 @@ __global__ void __launch_bounds__(RowTmaCfg<N, TH>::THREADS, MINB)
         RowXorAddr<P> ad{mine};
         float2 tr[E];
         if (a.flags & ROW_TRANS) {
-            const float2 *trow = a.trans + (size_t)(line % a.nx) * N;
+            const float2 *trow = (a.trans_b ? a.trans_b[line / a.nx] : a.trans) + (size_t)(line % a.nx) * N;
 #pragma unroll
             for (int e = 0; e < E; ++e) tr[e] = __ldg(trow + t + T * e);
         }
