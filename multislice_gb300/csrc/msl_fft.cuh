@@ -249,10 +249,13 @@ __device__ __forceinline__ void fft_stage(float2 (&v)[P::E], int t, const float2
     }
 }
 
-template <class P, int S, class Addr>
+// WARP = true: the line belongs to one warp (T == 32) and the exchange needs
+// only warp-level synchronisation.
+template <class P, int S, bool WARP = false, class Addr>
 __device__ __forceinline__ void fft_exchange(float2 (&v)[P::E], int t, const Addr &ad) {
     constexpr int R = P::radix(S), NS = plan_span<P>(S), E = P::E, Q = E / R, T = P::T;
-    __syncthreads();  // previous readers of the buffer are done
+    static_assert(!WARP || T == 32, "warp-owned lines need 32 threads per line");
+    if constexpr (WARP) __syncwarp(); else __syncthreads();  // previous readers are done
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
         const int j = t + T * q;
@@ -260,19 +263,27 @@ __device__ __forceinline__ void fft_exchange(float2 (&v)[P::E], int t, const Add
 #pragma unroll
         for (int r = 0; r < R; ++r) ad.base[ad(d + r * NS)] = v[q + r * Q];
     }
-    __syncthreads();
+    if constexpr (WARP) __syncwarp(); else __syncthreads();
 #pragma unroll
     for (int e = 0; e < E; ++e) v[e] = ad.base[ad(t + T * e)];
 }
 
-template <class P, int DIR, int S = 0, class Addr>
+template <class P, int DIR, int S = 0, bool WARP = false, class Addr>
 __device__ __forceinline__ void fft_line(float2 (&v)[P::E], int t, const Addr &ad,
                                          const float2 *__restrict__ tw) {
     fft_stage<P, S, DIR>(v, t, tw);
     if constexpr (S + 1 < P::NSTAGE) {
-        fft_exchange<P, S>(v, t, ad);
-        fft_line<P, DIR, S + 1>(v, t, ad, tw);
+        fft_exchange<P, S, WARP>(v, t, ad);
+        fft_line<P, DIR, S + 1, WARP>(v, t, ad, tw);
     }
 }
+
+// Row plan with one warp per line (same radices as Plan<N>).
+template <int N_> struct WarpPlan {
+    using B = Plan<N_>;
+    static constexpr int N = N_, T = 32, E = N_ / 32, NSTAGE = B::NSTAGE;
+    static constexpr int row_swz = B::row_swz, row_sh = B::row_sh, col_c = B::col_c, col_ps = B::col_ps;
+    static constexpr int radix(int s) { return B::radix(s); }
+};
 
 }  // namespace msl

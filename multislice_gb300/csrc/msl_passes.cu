@@ -469,6 +469,123 @@ __global__ void __launch_bounds__(RowTmaCfg<N, TH>::THREADS, MINB)
     }
 }
 
+
+// ------------------------------------------------ warp-per-line row pass
+// Persistent kernel in which every warp owns whole lines: it streams its lines
+// through its own three-line ring in shared memory with 1D bulk copies
+// (cp.async.bulk) and its own mbarriers, and the line transforms exchange
+// through that ring with warp-level synchronisation only.  No CTA-wide barrier
+// runs after the prologue, so a warp waiting on its exchange or its next line
+// never holds up the others.
+template <int N> struct RowWarpCfg {
+    using P = WarpPlan<N>;
+    static constexpr int W = 8, THREADS = 32 * W, NBUF = 3;
+    static constexpr int MINB = P::E <= 8 ? 3 : 2;
+    static constexpr size_t LINE = sizeof(float2) * N;
+    static constexpr size_t OFF_TW = (size_t)W * NBUF * LINE;
+    static constexpr size_t OFF_BAR = OFF_TW + ((sizeof(float2) * plan_tw_size<P>() + 15) / 16) * 16;
+    static constexpr size_t SMEM = OFF_BAR + sizeof(uint64_t) * W * NBUF + 128;
+};
+
+template <int N>
+__global__ void __launch_bounds__(RowWarpCfg<N>::THREADS, RowWarpCfg<N>::MINB) row_warp_kernel(RowArgs a) {
+    using Cfg = RowWarpCfg<N>;
+    using P = WarpPlan<N>;
+    constexpr int E = P::E, NBUF = Cfg::NBUF, W = Cfg::W, TW = plan_tw_size<P>();
+    extern __shared__ unsigned char smraw[];
+    unsigned char *base = smraw + ((128u - (smem_u32(smraw) & 127u)) & 127u);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float2 *ring = reinterpret_cast<float2 *>(base) + (size_t)warp * NBUF * N;
+    float2 *tw = reinterpret_cast<float2 *>(base + Cfg::OFF_TW);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(base + Cfg::OFF_BAR) + warp * NBUF;
+    for (int i = threadIdx.x; i < TW; i += Cfg::THREADS) tw[i] = a.tw[i];
+    if (lane == 0) {
+        for (int s = 0; s < NBUF; ++s) mbar_init(&bar[s], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();  // the only CTA barrier: tables and barriers are ready
+    const bool load = (a.flags & ROW_LOAD) != 0, store = !(a.flags & ROW_NOSTORE);
+    const int G = gridDim.x * W, gw = blockIdx.x * W + warp;
+    const int nmine = gw < a.nlines ? (a.nlines - gw + G - 1) / G : 0;
+    int issued = 0;
+    auto issue = [&](int k) {  // lane 0 only
+        const int line = gw + k * G, s = k % NBUF;
+        fence_proxy_async();
+        mbar_arrive_expect_tx(&bar[s], (uint32_t)Cfg::LINE);
+        bulk_load(ring + (size_t)s * N, a.in + (size_t)line * N, (uint32_t)Cfg::LINE, &bar[s]);
+        issued = k + 1;
+    };
+    if (load && lane == 0)
+        for (int k = 0; k < NBUF - 1 && k < nmine; ++k) issue(k);
+    int k = 0;
+    bool ok = true;
+    for (; k < nmine; ++k) {
+        const int line = gw + k * G, s = k % NBUF;
+        float2 *buf = ring + (size_t)s * N;
+        RowXorAddr<P> ad{buf};
+        float2 tr[E];
+        if (a.flags & ROW_TRANS) {
+            const float2 *trow = (a.trans_b ? a.trans_b[line / a.nx] : a.trans) + (size_t)(line % a.nx) * N;
+#pragma unroll
+            for (int e = 0; e < E; ++e) tr[e] = __ldg(trow + lane + 32 * e);
+        }
+        if (!load && store && lane == 0) tma_wait_read<NBUF - 1>();  // the store of line k-3 left buf
+        float2 v[E];
+        if (load) {
+            const bool got = mbar_wait_bounded(&bar[s], (uint32_t)((k / NBUF) & 1), kWaitLimit);
+            if (__any_sync(0xffffffffu, !got)) {
+                ok = false;
+                break;
+            }
+#pragma unroll
+            for (int e = 0; e < E; ++e) v[e] = buf[lane + 32 * e];
+        } else {
+#pragma unroll
+            for (int e = 0; e < E; ++e) v[e] = make_float2(1.f, 0.f);
+        }
+        if (a.flags & ROW_INV) fft_line<P, -1, 0, true>(v, lane, ad, tw);
+        if (a.flags & ROW_TRANS) {
+#pragma unroll
+            for (int e = 0; e < E; ++e) v[e] = c_mul(v[e], tr[e]);
+        }
+        if (a.flags & ROW_FWD) fft_line<P, +1, 0, true>(v, lane, ad, tw);
+        if (a.scale != 1.0f) {
+#pragma unroll
+            for (int e = 0; e < E; ++e) v[e] = c_scale(v[e], a.scale);
+        }
+        if (a.flags & ROW_ACCUM) {
+            double *acc = a.accum + (size_t)line * N;
+#pragma unroll
+            for (int e = 0; e < E; ++e)
+                acc[lane + 32 * e] += a.accum_w * ((double)v[e].x * v[e].x + (double)v[e].y * v[e].y);
+        }
+        if (store) {
+            __syncwarp();  // every lane is done reading buf
+#pragma unroll
+            for (int e = 0; e < E; ++e) buf[lane + 32 * e] = v[e];
+            fence_proxy_async();
+            __syncwarp();
+            if (lane == 0) {
+                bulk_store(a.out + (size_t)line * N, buf, (uint32_t)Cfg::LINE);
+                tma_commit();
+            }
+        }
+        if (load && lane == 0 && k + NBUF - 1 < nmine) {
+            if (store) tma_wait_read<1>();  // the store of line k-1 has left its buffer
+            issue(k + NBUF - 1);            // into buffer (k + 2) % 3
+        }
+        __syncwarp();
+    }
+    if (lane == 0) {
+        if (store) tma_wait_all();
+        if (!ok) {
+            if (a.err) atomicExch(a.err, 1);
+            for (int j = k; j < issued; ++j)
+                mbar_wait_bounded(&bar[j % NBUF], (uint32_t)((j / NBUF) & 1), kWaitLimit);
+        }
+    }
+}
+
 // ------------------------------------------------------------ set-up kernels
 __global__ void probe_table_kernel(int nx, int ny, const double *kxd, const double *kyd,
                                    double s_in, double s_out, double lam, double df, double cs,
@@ -700,6 +817,33 @@ template <int N> static cudaError_t row_tma_launch(const RowArgs &a, cudaStream_
     return row_tma_launch_v<N, 128, (Plan<N>::E <= 8 ? 6 : 4)>(a, s, nsm);
 }
 
+
+template <int N> static cudaError_t row_warp_launch(const RowArgs &a, cudaStream_t s, int nsm) {
+    using Cfg = RowWarpCfg<N>;
+    static int per_sm = 0;
+    if (!per_sm) {
+        cudaError_t e = cudaFuncSetAttribute(row_warp_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)Cfg::SMEM);
+        if (e != cudaSuccess) return e;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, row_warp_kernel<N>, Cfg::THREADS, Cfg::SMEM);
+        if (e != cudaSuccess) return e;
+        if (per_sm < 1) per_sm = 1;
+    }
+    const int nwarps = (a.nlines + Cfg::W - 1) / Cfg::W;
+    int grid = nsm * per_sm < nwarps ? nsm * per_sm : nwarps;
+    if (grid < 1) grid = 1;
+    row_warp_kernel<N><<<grid, Cfg::THREADS, Cfg::SMEM, s>>>(a);
+    return cudaGetLastError();
+}
+
+// Warp-owned lines for the sides whose plan fits 32 threads per line.
+static bool row_warp_eligible(int ny, const RowArgs &a) {
+    if (ny != 256 && ny != 384 && ny != 512) return false;
+    if (a.flags & ROW_GENT) return false;
+    if (((uintptr_t)a.out & 15u) || ((a.flags & ROW_LOAD) && ((uintptr_t)a.in & 15u))) return false;
+    return true;
+}
+
 #define MSL_FOR_EACH_SIDE(X) X(64) X(128) X(256) X(384) X(512) X(768) X(1024) X(2048)
 
 bool plan_supported(int n) {
@@ -759,6 +903,14 @@ void plan_twiddles(int n, std::vector<float2> &out) {
 
 cudaError_t launch_row_pass(int ny, const RowArgs &a, cudaStream_t s, int nsm, int64_t *launches) {
     ++*launches;
+    if (row_warp_eligible(ny, a)) {
+        switch (ny) {
+            case 256: return row_warp_launch<256>(a, s, nsm);
+            case 384: return row_warp_launch<384>(a, s, nsm);
+            case 512: return row_warp_launch<512>(a, s, nsm);
+            default: break;
+        }
+    }
     if (row_tma_eligible(a)) {
         switch (ny) {
 #define X(N) case N: return row_tma_launch<N>(a, s, nsm);
