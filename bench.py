@@ -137,6 +137,8 @@ def run_ours(args):
     det_k = cfg["det_k"]
 
     ctx = Context(local)
+    if args.batch:
+        ctx.set_probe_batch(args.batch)
     # device-resident inputs for `value`
     v_dev = torch.empty((NSLICE, nx, ny), dtype=torch.float32, device=dev)
     ctx.potential(spec, nx, ny, NSLICE, cfg["radius"], out=v_dev)
@@ -313,6 +315,7 @@ def main():
     ap.add_argument("--probes", type=int, default=4096,
                     help="probes of the 64x64 raster per GPU (smaller cases are for profiling)")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--batch", type=int, default=0, help="probes per launch (0: library default)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
