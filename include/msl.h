@@ -200,8 +200,9 @@ int msl_profile_read(const msl_ctx *ctx, int kind, int64_t *launches, double *ms
 
 /* Objective lens of the CTEM image (mulslice.cpp:539-676): the exit wave's
  * spectrum is multiplied by exp(-i chi(k)) inside the objective aperture
- * k^2 <= k_obj^2, chi = pi lambda k^2 (Cs lambda^2 k^2 / 2 - df) (slicelib.cpp:
- * 258-323, rotationally symmetric terms), and |ifft|^2 is summed over defocus
+ * k^2 <= k_obj^2, chi = pi lambda k^2 (Cs lambda^2 k^2 / 2 - df
+ * + dfa2 sin(2(phi - dfa2phi)) + (2/3) dfa3 lambda |k| sin(3(phi - dfa3phi))),
+ * phi = atan2(ky, kx) (mulslice.cpp:613-619), and |ifft|^2 is summed over defocus
  * values df + j*df_step, |j| <= 2.5 df_spread / df_step, with Gaussian weights
  * exp(-(j df_step / df_spread)^2 / 2) normalised to 1 (df_spread = 0: one
  * coherent image).  chi is evaluated in FP64. */
@@ -211,6 +212,8 @@ typedef struct {
     double k_obj;      /* objective aperture radius, 1/A */
     double df_spread;  /* defocus spread (standard deviation), Angstrom; 0 = none */
     double df_step;    /* defocus integration step, Angstrom (used when df_spread > 0) */
+    double dfa2, dfa2phi; /* 2-fold astigmatism: magnitude (A), angle (rad) */
+    double dfa3, dfa3phi; /* 3-fold astigmatism: magnitude (A), angle (rad) */
 } msl_lens;
 
 /* CTEM image of a batch of waves: runs the slice loop of msl_multislice on psi
@@ -223,6 +226,17 @@ int msl_ctem_image(msl_ctx *ctx, const msl_grid *grid, const msl_optics *optics,
                    const float *trans, int ntrans, const double *dz, const int *layer_seq,
                    int nslice, const msl_lens *lens, float *psi, int batch, int plane_wave,
                    double weight, double *image, double *exit_intensity);
+
+/* Kirkland's partial-coherence CTEM image (mulslice.cpp:539-676): the plane
+ * wave is tilted to every illumination angle (qx, qy) = (i/ax, j/by) with
+ * acmin <= lambda |q| <= acmax (radians), each tilted wave runs the slice loop
+ * (all angles in one batch), is imaged through the lens with the defocus
+ * spread, and image[nx][ny] (FP64, overwritten) receives the average over
+ * angles and defocus values.  n_angles (may be NULL) returns the angle count. */
+int msl_ctem_partial_coherence(msl_ctx *ctx, const msl_grid *grid, const msl_optics *optics,
+                               const float *trans, int ntrans, const double *dz,
+                               const int *layer_seq, int nslice, const msl_lens *lens,
+                               double acmin, double acmax, double *image, int *n_angles);
 
 /* Frozen-phonon displacements (MSUseOnceCalculator.cs:179-199 jitters every atom
  * by a Gaussian per axis; the reference's System.Random stream cannot be

@@ -187,12 +187,13 @@ class Context:
 
     # ------------------------------------------------------------ CTEM image
     @staticmethod
-    def _lens(cs, df, k_obj, df_spread=0.0, df_step=0.0):
-        return Lens(float(cs), float(df), float(k_obj), float(df_spread), float(df_step))
+    def _lens(cs, df, k_obj, df_spread=0.0, df_step=0.0, astig=(0.0, 0.0, 0.0, 0.0)):
+        return Lens(float(cs), float(df), float(k_obj), float(df_spread), float(df_step),
+                    *[float(v) for v in astig])
 
     def ctem_image(self, trans, dz, layer_seq, ax, by, kev, cs, df, k_obj, psi=None, batch=1,
                    df_spread=0.0, df_step=0.0, weight=1.0, image=None, exit_intensity=None,
-                   bandlimit=2.0 / 3.0):
+                   bandlimit=2.0 / 3.0, astig=(0.0, 0.0, 0.0, 0.0)):
         """Image intensity (FP64, accumulated into `image`) through an objective lens
         (mulslice.cpp:539-676); returns (image, exit waves, exit intensity)."""
         trans = _as(trans, np.complex64)
@@ -201,7 +202,7 @@ class Context:
         seq = np.ascontiguousarray(layer_seq, np.int32)
         g = Grid(nx, ny, float(ax), float(by))
         o = self._optics(kev, bandlimit)
-        ln = self._lens(cs, df, k_obj, df_spread, df_step)
+        ln = self._lens(cs, df, k_obj, df_spread, df_step, astig)
         plane = psi is None
         if plane:
             psi = np.empty((batch, nx, ny), np.complex64)
@@ -217,6 +218,26 @@ class Context:
                                              _ptr(psi, np.complex64), batch, 1 if plane else 0,
                                              float(weight), _ptr(image, np.float64), eptr))
         return image, psi, exit_intensity
+
+    def partial_coherence(self, trans, dz, layer_seq, ax, by, kev, cs, df, k_obj, acmin, acmax,
+                          df_spread=0.0, df_step=0.0, astig=(0.0, 0.0, 0.0, 0.0),
+                          bandlimit=2.0 / 3.0):
+        """Kirkland's partial-coherence image (illumination angles acmin..acmax in rad);
+        returns (image float64 [nx, ny], number of angles)."""
+        trans = _as(trans, np.complex64)
+        nt, nx, ny = _cshape(trans)
+        dz = np.ascontiguousarray(np.broadcast_to(np.asarray(dz, np.float64), (nt,)))
+        seq = np.ascontiguousarray(layer_seq, np.int32)
+        g = Grid(nx, ny, float(ax), float(by))
+        o = self._optics(kev, bandlimit)
+        ln = self._lens(cs, df, k_obj, df_spread, df_step, astig)
+        img = np.empty((nx, ny), np.float64)
+        na = ctypes.c_int()
+        self._check(self._lib.msl_ctem_partial_coherence(
+            self._h, ctypes.byref(g), ctypes.byref(o), _ptr(trans, np.complex64), nt,
+            _ptr(dz, np.float64), _ptr(seq, np.int32), len(seq), ctypes.byref(ln), float(acmin),
+            float(acmax), _ptr(img, np.float64), ctypes.byref(na)))
+        return img, int(na.value)
 
     def frozen_phonon(self, spec, nx, ny, nslice, radius, kev, cs, df, k_obj, nconfig, sigma, seed,
                       df_spread=0.0, df_step=0.0, fparams=None, bandlimit=2.0 / 3.0,

@@ -241,8 +241,8 @@ int upload(msl_ctx *c, DevBuf &b, const void *h, size_t bytes) {
 struct SliceTables {
     std::vector<float> kx, kx2, ky, ky2;
     float k2max;
-    // device layout: kx2[nx] ky2[ny] | px py per layer
-    float *d_kx2, *d_ky2;
+    // device layout: kx2[nx] ky2[ny] kx[nx] ky[ny] | px py per layer
+    float *d_kx2, *d_ky2, *d_kx = nullptr, *d_ky = nullptr;
     float2 *d_prop;  // [ntrans][nx + ny]
 };
 
@@ -252,11 +252,13 @@ int build_slice_tables(msl_ctx *c, const msl_grid *g, const msl_optics *o, int n
     freqn_f32(nx, g->ax, st.kx, st.kx2);
     freqn_f32(ny, g->by, st.ky, st.ky2);
     st.k2max = k2max_f32(nx, ny, g->ax, g->by, o->bandlimit);
-    const size_t fbytes = sizeof(float) * (nx + ny);
+    const size_t fbytes = ((sizeof(float) * 2 * (nx + ny) + 15) / 16) * 16;
     const size_t pbytes = sizeof(float2) * (size_t)ntrans * (nx + ny);
     std::vector<unsigned char> h(fbytes + pbytes);
     memcpy(h.data(), st.kx2.data(), sizeof(float) * nx);
     memcpy(h.data() + sizeof(float) * nx, st.ky2.data(), sizeof(float) * ny);
+    memcpy(h.data() + sizeof(float) * (nx + ny), st.kx.data(), sizeof(float) * nx);
+    memcpy(h.data() + sizeof(float) * (2 * nx + ny), st.ky.data(), sizeof(float) * ny);
     float2 *hp = (float2 *)(h.data() + fbytes);
     for (int l = 0; l < ntrans; ++l) {
         if (dz) {
@@ -272,6 +274,8 @@ int build_slice_tables(msl_ctx *c, const msl_grid *g, const msl_optics *o, int n
     if (rc) return rc;
     st.d_kx2 = (float *)c->tabs.p;
     st.d_ky2 = st.d_kx2 + nx;
+    st.d_kx = st.d_ky2 + ny;
+    st.d_ky = st.d_kx + nx;
     st.d_prop = (float2 *)((unsigned char *)c->tabs.p + fbytes);
     return MSL_OK;
 }
@@ -375,8 +379,8 @@ int ctem_core(msl_ctx *c, const msl_grid *g, const msl_optics *o, const float2 *
         ColArgs ca = col_args(g, st, twc, l, w, batch, cf, c->dflag);
         LAUNCH_TRY(c, timed(c, MSL_PROF_COL, [&] { return msl::launch_col_pass(nx, ca, c->stream, c->nsm, &c->launches); }));
     }
-    const size_t wbytes = sizeof(float2) * n2 * batch;
-    CUDA_TRY(c, c->tmpw.ensure(wbytes));
+    const size_t ibytes = sizeof(float2) * n2;  // one image
+    CUDA_TRY(c, c->tmpw.ensure(ibytes));
     float2 *tmp = (float2 *)c->tmpw.p;
     // defocus values and weights (mulslice.cpp:552, :610-642)
     std::vector<double> dfs, pw;
@@ -393,42 +397,56 @@ int ctem_core(msl_ctx *c, const msl_grid *g, const msl_optics *o, const float2 *
     }
     double psum = 0.0;
     for (double v : pw) psum += v;
-    CUDA_TRY(c, c->ctf.ensure(sizeof(float2) * n2));
+    CUDA_TRY(c, c->ctf.ensure(sizeof(float2) * n2 * dfs.size()));
     float2 *ctf = (float2 *)c->ctf.p;
     const float kob = (float)lens->k_obj;
-    const float k2obj = kob * kob;
-    const double lam = msl_wavelength(o->kev);
-    const bool exit_needed = want_exit || exit_d != nullptr;
+    msl::CtfParams cp;
+    cp.lam = msl_wavelength(o->kev);
+    cp.cs = lens->cs;
+    cp.dfa2 = lens->dfa2;
+    cp.dfa2phi = lens->dfa2phi;
+    cp.dfa3 = lens->dfa3;
+    cp.dfa3phi = lens->dfa3phi;
+    cp.k2obj = kob * kob;
+    cp.scale = 1.0f;
     for (size_t j = 0; j < dfs.size(); ++j) {
-        // the last image may consume w itself unless the exit wave still needs it
-        const bool last = j + 1 == dfs.size();
-        float2 *target = (last && !exit_needed) ? w : tmp;
-        if (target != w)
-            CUDA_TRY(c, cudaMemcpyAsync(target, w, wbytes, cudaMemcpyDeviceToDevice, c->stream));
+        cp.df = dfs[j];
         LAUNCH_TRY(c, timed(c, MSL_PROF_OTHER, [&] {
-                       return msl::launch_ctf_table(nx, ny, st.d_kx2, st.d_ky2, k2obj, lam, lens->cs, dfs[j],
-                                                    1.0f, ctf, c->stream, &c->launches);
+                       return msl::launch_ctf_table(nx, ny, st.d_kx2, st.d_ky2, st.d_kx, st.d_ky, cp,
+                                                    ctf + n2 * j, c->stream, &c->launches);
                    }));
-        ColArgs ca = col_args(g, st, twc, 0, target, batch,
-                              msl::COL_LOAD | msl::COL_CTF | msl::COL_INV | msl::COL_STORE, c->dflag);
-        ca.ctf = ctf;
-        LAUNCH_TRY(c, timed(c, MSL_PROF_COL, [&] { return msl::launch_col_pass(nx, ca, c->stream, c->nsm, &c->launches); }));
-        RowArgs r = row_args(g, twr, nullptr, target, batch,
-                             msl::ROW_LOAD | msl::ROW_INV | msl::ROW_ACCUM | msl::ROW_NOSTORE, c->dflag);
-        r.accum = img_d;
-        r.accum_w = weight * pw[j] / psum;
-        LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_row_pass(ny, r, c->stream, c->nsm, &c->launches); }));
     }
-    if (exit_needed) {  // exit waves: inverse transform of W in place
-        ColArgs ca = col_args(g, st, twc, 0, w, batch, msl::COL_LOAD | msl::COL_INV | msl::COL_STORE, c->dflag);
-        LAUNCH_TRY(c, timed(c, MSL_PROF_COL, [&] { return msl::launch_col_pass(nx, ca, c->stream, c->nsm, &c->launches); }));
-        int rf = msl::ROW_LOAD | msl::ROW_INV;
-        if (exit_d) rf |= msl::ROW_ACCUM;
-        if (!want_exit) rf |= msl::ROW_NOSTORE;
-        RowArgs r = row_args(g, twr, nullptr, w, batch, rf, c->dflag);
-        r.accum = exit_d;
-        r.accum_w = weight;
-        LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_row_pass(ny, r, c->stream, c->nsm, &c->launches); }));
+    const bool exit_needed = want_exit || exit_d != nullptr;
+    // every image of the batch: its spectrum W = Psi(k) / (nx ny) sits in its slot
+    for (int b = 0; b < batch; ++b) {
+        float2 *wb = w + (size_t)b * n2;
+        for (size_t j = 0; j < dfs.size(); ++j) {
+            // the last image may consume the slot itself unless the exit wave still needs it
+            const bool last = j + 1 == dfs.size();
+            float2 *target = (last && !exit_needed) ? wb : tmp;
+            if (target != wb)
+                CUDA_TRY(c, cudaMemcpyAsync(target, wb, ibytes, cudaMemcpyDeviceToDevice, c->stream));
+            ColArgs ca = col_args(g, st, twc, 0, target, 1,
+                                  msl::COL_LOAD | msl::COL_CTF | msl::COL_INV | msl::COL_STORE, c->dflag);
+            ca.ctf = ctf + n2 * j;
+            LAUNCH_TRY(c, timed(c, MSL_PROF_COL, [&] { return msl::launch_col_pass(nx, ca, c->stream, c->nsm, &c->launches); }));
+            RowArgs r = row_args(g, twr, nullptr, target, 1,
+                                 msl::ROW_LOAD | msl::ROW_INV | msl::ROW_ACCUM | msl::ROW_NOSTORE, c->dflag);
+            r.accum = img_d;
+            r.accum_w = weight * pw[j] / psum;
+            LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_row_pass(ny, r, c->stream, c->nsm, &c->launches); }));
+        }
+        if (exit_needed) {  // exit wave: inverse transform of W in place
+            ColArgs ca = col_args(g, st, twc, 0, wb, 1, msl::COL_LOAD | msl::COL_INV | msl::COL_STORE, c->dflag);
+            LAUNCH_TRY(c, timed(c, MSL_PROF_COL, [&] { return msl::launch_col_pass(nx, ca, c->stream, c->nsm, &c->launches); }));
+            int rf = msl::ROW_LOAD | msl::ROW_INV;
+            if (exit_d) rf |= msl::ROW_ACCUM;
+            if (!want_exit) rf |= msl::ROW_NOSTORE;
+            RowArgs r = row_args(g, twr, nullptr, wb, 1, rf, c->dflag);
+            r.accum = exit_d;
+            r.accum_w = weight;
+            LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_row_pass(ny, r, c->stream, c->nsm, &c->launches); }));
+        }
     }
     return MSL_OK;
 }
@@ -437,6 +455,8 @@ int check_lens(msl_ctx *c, const msl_lens *l) {
     if (!l) return fail(c, MSL_E_ARG, "lens is null");
     if (!is_fin(l->cs) || !is_fin(l->df) || !(l->k_obj > 0) || !is_fin(l->k_obj))
         return fail(c, MSL_E_ARG, "lens: cs, df finite and k_obj > 0 required");
+    if (!is_fin(l->dfa2) || !is_fin(l->dfa2phi) || !is_fin(l->dfa3) || !is_fin(l->dfa3phi))
+        return fail(c, MSL_E_ARG, "lens: astigmatism terms must be finite");
     if (!(l->df_spread >= 0) || !is_fin(l->df_spread) ||
         (l->df_spread > 0 && (!(l->df_step > 0) || 2.5 * l->df_spread / l->df_step > 1000)))
         return fail(c, MSL_E_ARG, "lens: df_spread >= 0 and df_step > 0 (at most 2001 defocus values)");
@@ -581,12 +601,9 @@ int msl_ctem_image(msl_ctx *c, const msl_grid *g, const msl_optics *o, const flo
     if (!idev) CUDA_TRY(c, cudaMemcpyAsync(img_d, image, ibytes, cudaMemcpyHostToDevice, c->stream));
     if (exit_intensity && !edev)
         CUDA_TRY(c, cudaMemcpyAsync(exit_d, exit_intensity, ibytes, cudaMemcpyHostToDevice, c->stream));
-    // batch images sum into one accumulator: accumulate image by image
-    for (int b = 0; b < batch; ++b) {
-        if ((rc = ctem_core(c, g, o, td, ntrans, dz, layer_seq, nslice, lens, w + (size_t)b * n2, 1,
-                            plane_wave != 0, weight, img_d, exit_d, psi != nullptr)))
-            return rc;
-    }
+    if ((rc = ctem_core(c, g, o, td, ntrans, dz, layer_seq, nslice, lens, w, batch, plane_wave != 0, weight,
+                        img_d, exit_d, psi != nullptr)))
+        return rc;
     if (psi && !pdev) CUDA_TRY(c, cudaMemcpyAsync(psi, w, wbytes, cudaMemcpyDeviceToHost, c->stream));
     if (!idev) CUDA_TRY(c, cudaMemcpyAsync(image, img_d, ibytes, cudaMemcpyDeviceToHost, c->stream));
     if (exit_intensity && !edev)
@@ -842,6 +859,77 @@ int msl_run_jobs(msl_ctx *c, const msl_job *jobs, int njobs, double bandlimit) {
                                         cudaMemcpyDefault, c->stream));
         CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     }
+    collect_profile(c);
+    if (c->dflag && (rc = err_check(c))) return rc;
+    return MSL_OK;
+}
+
+
+int msl_ctem_partial_coherence(msl_ctx *c, const msl_grid *g, const msl_optics *o, const float *trans,
+                               int ntrans, const double *dz, const int *layer_seq, int nslice,
+                               const msl_lens *lens, double acmin, double acmax, double *image,
+                               int *n_angles) {
+    if (!c) return MSL_E_ARG;
+    int rc = check_grid(c, g);
+    if (rc) return rc;
+    if ((rc = check_optics(c, o))) return rc;
+    if ((rc = check_layers(c, ntrans, dz, layer_seq, nslice))) return rc;
+    if ((rc = check_lens(c, lens))) return rc;
+    if (!trans || !image) return fail(c, MSL_E_ARG, "trans and image required");
+    if (!(acmin >= 0) || !(acmax >= acmin) || !is_fin(acmax))
+        return fail(c, MSL_E_ARG, "illumination angles must satisfy 0 <= acmin <= acmax");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    if ((rc = err_reset(c))) return rc;
+    const int nx = g->nx, ny = g->ny;
+    const size_t n2 = (size_t)nx * ny;
+    // illumination angles in float as mulslice.cpp:550-570
+    const float wavlen = (float)msl_wavelength(o->kev);
+    const float ax = (float)g->ax, by = (float)g->by;
+    const float rx = 1.0F / ax, ry = 1.0F / by;
+    const float fac = (float)acmax;
+    const int nacx = (int)((fac / (wavlen * rx)) + 1.5F), nacy = (int)((fac / (wavlen * ry)) + 1.5F);
+    float q2max = fac / wavlen;
+    q2max = q2max * q2max;
+    float q2min = (float)acmin / wavlen;
+    q2min = q2min * q2min;
+    std::vector<float> q;
+    for (int iqy = -nacy; iqy <= nacy; ++iqy) {
+        const float qy = iqy * ry, qy2 = qy * qy;
+        for (int iqx = -nacx; iqx <= nacx; ++iqx) {
+            const float qx = iqx * rx, q2 = qx * qx + qy2;
+            if (q2 <= q2max && q2 >= q2min) {
+                q.push_back(qx);
+                q.push_back(qy);
+            }
+        }
+    }
+    const int na = (int)(q.size() / 2);
+    if (n_angles) *n_angles = na;
+    if (na == 0) return fail(c, MSL_E_ARG, "no illumination angle inside [acmin, acmax]");
+    const float2 *td;
+    if ((rc = stage_in(c, (const float2 *)trans, sizeof(float2) * n2 * ntrans, c->trans_stage, &td))) return rc;
+    // positions xo[i] = (float)(i * a) / (float)(n - 1) of freqn (slicelib.cpp:433-463), and the angles
+    std::vector<float> hp(nx + ny + q.size());
+    for (int i = 0; i < nx; ++i) hp[i] = ((float)(i * g->ax)) / ((float)(nx - 1));
+    for (int i = 0; i < ny; ++i) hp[nx + i] = ((float)(i * g->by)) / ((float)(ny - 1));
+    memcpy(hp.data() + nx + ny, q.data(), sizeof(float) * q.size());
+    if ((rc = upload(c, c->fxy, hp.data(), sizeof(float) * hp.size()))) return rc;
+    const float *dpos = (const float *)c->fxy.p;
+    CUDA_TRY(c, c->wave.ensure(sizeof(float2) * n2 * na));
+    float2 *w = (float2 *)c->wave.p;
+    LAUNCH_TRY(c, timed(c, MSL_PROF_OTHER, [&] {
+                   return msl::launch_tilt_waves(nx, ny, na, dpos, dpos + nx, dpos + nx + ny, w, c->stream,
+                                                 &c->launches);
+               }));
+    const bool idev = on_device(image);
+    CUDA_TRY(c, c->acc.ensure(sizeof(double) * n2));
+    double *img_d = idev ? image : (double *)c->acc.p;
+    CUDA_TRY(c, cudaMemsetAsync(img_d, 0, sizeof(double) * n2, c->stream));
+    if ((rc = ctem_core(c, g, o, td, ntrans, dz, layer_seq, nslice, lens, w, na, false, 1.0 / na, img_d,
+                        nullptr, false)))
+        return rc;
+    if (!idev) CUDA_TRY(c, cudaMemcpyAsync(image, img_d, sizeof(double) * n2, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     collect_profile(c);
     if (c->dflag && (rc = err_check(c))) return rc;
     return MSL_OK;

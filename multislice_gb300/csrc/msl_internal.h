@@ -108,9 +108,17 @@ cudaError_t launch_detector_mask(int nx, int ny, const double *kxd, const double
                                  cudaStream_t s, int64_t *launches);
 // ctf[ix][iy] = exp(-i chi(k)) * scale for k2 = kx2 + ky2 (float) <= k2obj, else 0;
 // chi = pi lam k2 (cs lam^2 k2 / 2 - df) in FP64
-cudaError_t launch_ctf_table(int nx, int ny, const float *kx2, const float *ky2, float k2obj,
-                             double lam, double cs, double df, float scale, float2 *ctf,
-                             cudaStream_t s, int64_t *launches);
+struct CtfParams {
+    double lam, cs, df, dfa2, dfa2phi, dfa3, dfa3phi;
+    float k2obj, scale;
+};
+// phi = atan2(ky, kx) from the float kx / ky tables (astigmatism terms)
+cudaError_t launch_ctf_table(int nx, int ny, const float *kx2, const float *ky2, const float *kx,
+                             const float *ky, const CtfParams &p, float2 *ctf, cudaStream_t s,
+                             int64_t *launches);
+// out[b][ix][iy] = exp(2 pi i (qx[b] xpos[ix] + qy[b] ypos[iy])), the sum in float as mulslice.cpp:573-577
+cudaError_t launch_tilt_waves(int nx, int ny, int nb, const float *xpos, const float *ypos,
+                              const float *q, float2 *out, cudaStream_t s, int64_t *launches);
 // out[b * out_stride + d] = scale * sum_t partial[b][t][d]
 cudaError_t launch_detector_finalize(int nb, int ntile, int ndet, const double *partial,
                                      double scale, double *out, int out_stride, cudaStream_t s,

@@ -640,21 +640,39 @@ __global__ void detector_mask_kernel(int nx, int ny, const double *kxd, const do
     mask[(size_t)ix * ny + iy] = (uint8_t)bits;
 }
 
-__global__ void ctf_table_kernel(int nx, int ny, const float *kx2, const float *ky2, float k2obj,
-                                 double lam, double cs, double df, float scale, float2 *ctf) {
+__global__ void ctf_table_kernel(int nx, int ny, const float *kx2, const float *ky2, const float *kx,
+                                 const float *ky, CtfParams p, float2 *ctf) {
     const int iy = blockIdx.x * blockDim.x + threadIdx.x;
     const int ix = blockIdx.y;
     if (iy >= ny || ix >= nx) return;
     const float k2 = __fadd_rn(kx2[ix], ky2[iy]);
     float2 out = make_float2(0.f, 0.f);
-    if (k2 <= k2obj) {
+    if (k2 <= p.k2obj) {
         const double q = (double)k2;
-        const double chi = 3.14159265358979323846 * lam * q * (0.5 * cs * lam * lam * q - df);
+        double w = 0.5 * p.cs * p.lam * p.lam * q - p.df;
+        if (p.dfa2 != 0.0 || p.dfa3 != 0.0) {
+            const double phi = atan2((double)ky[iy], (double)kx[ix]);
+            w += p.dfa2 * sin(2.0 * (phi - p.dfa2phi)) +
+                 2.0 * p.dfa3 * p.lam * sqrt(q) * sin(3.0 * (phi - p.dfa3phi)) / 3.0;
+        }
+        const double chi = 3.14159265358979323846 * p.lam * q * w;
         double sn, cn;
         sincos(chi, &sn, &cn);
-        out = make_float2((float)cn * scale, (float)-sn * scale);
+        out = make_float2((float)cn * p.scale, (float)-sn * p.scale);
     }
     ctf[(size_t)ix * ny + iy] = out;
+}
+
+__global__ void tilt_wave_kernel(int nx, int ny, const float *xpos, const float *ypos, const float *q,
+                                 float2 *out) {
+    const int iy = blockIdx.x * blockDim.x + threadIdx.x;
+    const int ix = blockIdx.y, b = blockIdx.z;
+    if (iy >= ny || ix >= nx) return;
+    const float s = __fadd_rn(__fmul_rn(q[2 * b], xpos[ix]), __fmul_rn(q[2 * b + 1], ypos[iy]));
+    const double t = 2.0 * (double)3.14159265f * (double)s;
+    double sn, cn;
+    sincos(t, &sn, &cn);
+    out[((size_t)b * nx + ix) * ny + iy] = make_float2((float)cn, (float)sn);
 }
 
 __global__ void detector_finalize_kernel(int nb, int ntile, int ndet, const double *partial,
@@ -972,12 +990,20 @@ cudaError_t launch_detector_mask(int nx, int ny, const double *kxd, const double
     return cudaGetLastError();
 }
 
-cudaError_t launch_ctf_table(int nx, int ny, const float *kx2, const float *ky2, float k2obj,
-                             double lam, double cs, double df, float scale, float2 *ctf,
-                             cudaStream_t s, int64_t *launches) {
+cudaError_t launch_ctf_table(int nx, int ny, const float *kx2, const float *ky2, const float *kx,
+                             const float *ky, const CtfParams &p, float2 *ctf, cudaStream_t s,
+                             int64_t *launches) {
     ++*launches;
     dim3 grid((ny + 255) / 256, nx);
-    ctf_table_kernel<<<grid, 256, 0, s>>>(nx, ny, kx2, ky2, k2obj, lam, cs, df, scale, ctf);
+    ctf_table_kernel<<<grid, 256, 0, s>>>(nx, ny, kx2, ky2, kx, ky, p, ctf);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tilt_waves(int nx, int ny, int nb, const float *xpos, const float *ypos,
+                              const float *q, float2 *out, cudaStream_t s, int64_t *launches) {
+    ++*launches;
+    dim3 grid((ny + 255) / 256, nx, nb);
+    tilt_wave_kernel<<<grid, 256, 0, s>>>(nx, ny, xpos, ypos, q, out);
     return cudaGetLastError();
 }
 

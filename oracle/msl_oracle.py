@@ -335,8 +335,9 @@ def rel_l2(a, b):
 
 
 # ------------------------------------------------------------ CTEM imaging
-def ctf(nx, ny, ax, by, v0, cs, df, k_obj, dtype=np.complex128):
-    """exp(-i chi) inside the objective aperture (mulslice.cpp:556-633); chi in FP64."""
+def ctf(nx, ny, ax, by, v0, cs, df, k_obj, dtype=np.complex128, astig=(0.0, 0.0, 0.0, 0.0)):
+    """exp(-i chi) inside the objective aperture (mulslice.cpp:556-633); chi in FP64,
+    with 2- and 3-fold astigmatism (dfa2, dfa2phi, dfa3, dfa3phi)."""
     kx, kx2 = freqn(nx, ax)
     ky, ky2 = freqn(ny, by)
     k2 = (kx2[:, None] + ky2[None, :]).astype(np.float32)
@@ -344,7 +345,12 @@ def ctf(nx, ny, ax, by, v0, cs, df, k_obj, dtype=np.complex128):
     inside = k2 <= np.float32(kob * kob)
     q = k2.astype(np.float64)
     lam = wavelength(v0)
-    chi = np.pi * lam * q * (0.5 * cs * lam * lam * q - df)
+    w = 0.5 * cs * lam * lam * q - df
+    dfa2, dfa2phi, dfa3, dfa3phi = astig
+    if dfa2 != 0.0 or dfa3 != 0.0:
+        phi = np.arctan2(ky.astype(np.float64)[None, :], kx.astype(np.float64)[:, None])
+        w = w + dfa2 * np.sin(2.0 * (phi - dfa2phi)) + 2.0 * dfa3 * lam * np.sqrt(q) * np.sin(3.0 * (phi - dfa3phi)) / 3.0
+    chi = np.pi * lam * q * w
     return np.where(inside, np.exp(-1j * chi), 0).astype(dtype)
 
 
@@ -357,13 +363,14 @@ def defocus_weights(df, df_spread, df_step):
     return df + j * df_step, w / w.sum()
 
 
-def ctem_image(exit_wave, ax, by, v0, cs, df, k_obj, df_spread=0.0, df_step=0.0):
+def ctem_image(exit_wave, ax, by, v0, cs, df, k_obj, df_spread=0.0, df_step=0.0,
+               astig=(0.0, 0.0, 0.0, 0.0)):
     """Defocus-averaged image intensity of exit wave(s) [..., nx, ny] (summed over the batch)."""
     nx, ny = exit_wave.shape[-2:]
     W = kfft(exit_wave.astype(np.complex128))
     img = np.zeros((nx, ny))
     for d, w in zip(*defocus_weights(df, df_spread, df_step)):
-        psi = kifft(W * ctf(nx, ny, ax, by, v0, cs, d, k_obj))
+        psi = kifft(W * ctf(nx, ny, ax, by, v0, cs, d, k_obj, astig=astig))
         I = np.abs(psi) ** 2
         img += w * (I.sum(axis=0) if I.ndim == 3 else I)
     return img
@@ -460,3 +467,42 @@ def muslib_pg_periodic(a, b, gam, E, atrad, N, M, xx, yy, ads, occ, typ, curves,
             ph[jb:je, ib:ie] += K * res * occ[k]
             am[jb:je, ib:ie] += K * ads[k] * occ[k] * res
     return np.exp(-am) * np.exp(-1j * ph)
+
+
+def illumination_angles(nx, ny, ax, by, v0, acmin, acmax):
+    """Tilt vectors (qx, qy) of mulslice.cpp:550-570, in float."""
+    f32 = np.float32
+    wl = f32(wavelength(v0))
+    rx, ry = f32(1.0) / f32(ax), f32(1.0) / f32(by)
+    fac = f32(acmax)
+    nacx = int((fac / (wl * rx)) + f32(1.5))
+    nacy = int((fac / (wl * ry)) + f32(1.5))
+    q2max = f32(fac / wl) ** 2
+    q2min = f32(f32(acmin) / wl) ** 2
+    out = []
+    for iqy in range(-nacy, nacy + 1):
+        qy = f32(iqy) * ry
+        for iqx in range(-nacx, nacx + 1):
+            qx = f32(iqx) * rx
+            q2 = f32(qx * qx + qy * qy)
+            if q2 <= q2max and q2 >= q2min:
+                out.append((qx, qy))
+    return out
+
+
+def partial_coherence(trans, props, layer_seq, mask, ax, by, v0, cs, df, k_obj, acmin, acmax,
+                      df_spread=0.0, df_step=0.0, astig=(0.0, 0.0, 0.0, 0.0)):
+    """Kirkland's partial-coherence image (mulslice.cpp:539-676), FP64."""
+    nx, ny = trans.shape[-2:]
+    f32 = np.float32
+    xpos = (np.arange(nx) * ax).astype(f32) / f32(nx - 1)
+    ypos = (np.arange(ny) * by).astype(f32) / f32(ny - 1)
+    angles = illumination_angles(nx, ny, ax, by, v0, acmin, acmax)
+    img = np.zeros((nx, ny))
+    for qx, qy in angles:
+        s = (f32(qx) * xpos[:, None] + f32(qy) * ypos[None, :]).astype(f32)
+        t = 2.0 * float(f32(np.pi)) * s.astype(np.float64)
+        w0 = (np.cos(t).astype(f32) + 1j * np.sin(t).astype(f32)).astype(np.complex128)
+        w, _ = multislice(w0, trans, props, layer_seq, mask)
+        img += ctem_image(w, ax, by, v0, cs, df, k_obj, df_spread, df_step, astig)
+    return img / len(angles), len(angles)

@@ -84,3 +84,34 @@ def test_frozen_phonon_au_2048_full_size(ctx):
     img2, _ = ctx.frozen_phonon(spec, 2048, 2048, 80, 3.0, kev, CS, DF, k_obj, nconfig=32,
                                 sigma=0.085, seed=2026, want_exit=False)
     assert np.array_equal(img, img2)
+
+
+def test_astigmatic_image_vs_oracle(ctx, golden):
+    G = golden("si_small.npz")
+    ax, by, dz = float(G["ax"]), float(G["by"]), float(G["dz"])
+    astig = (40.0, 0.3, 300.0, -0.7)
+    img, psi, _ = ctx.ctem_image(G["t"], dz, G["seq"], ax, by, 200.0, CS, DF, 1.5, astig=astig)
+    ref = O.ctem_image(G["wave"].astype(np.complex128), ax, by, 200.0, CS, DF, 1.5, astig=astig)
+    assert O.rel_l2(img, ref) < 2e-5
+
+
+def test_partial_coherence_vs_oracle(ctx, golden):
+    G = golden("si_small.npz")
+    ax, by, dz = float(G["ax"]), float(G["by"]), float(G["dz"])
+    acmax = 0.0012                      # 1.2 mrad condenser
+    img, na = ctx.partial_coherence(G["t"], dz, G["seq"], ax, by, 200.0, CS, DF, 1.5, 0.0, acmax,
+                                    df_spread=40.0, df_step=20.0, astig=(20.0, 0.1, 0.0, 0.0))
+    mask = O.band_mask(64, 64, ax, by)
+    props = [O.propagator_tables(64, 64, ax, by, 200.0, dz, precision="f64")] * 8
+    ref, nref = O.partial_coherence(G["t"].astype(np.complex128), props, G["seq"], mask, ax, by, 200.0,
+                                    CS, DF, 1.5, 0.0, acmax, 40.0, 20.0, (20.0, 0.1, 0.0, 0.0))
+    assert na == nref and na > 1
+    assert O.rel_l2(img, ref) < 2e-5
+
+
+def test_partial_coherence_vacuum_is_uniform(ctx):
+    t = np.ones((1, 128, 128), np.complex64)
+    img, na = ctx.partial_coherence(t, 2.0, [0] * 3, 20.0, 20.0, 200.0, CS, DF, 2.0, 0.0, 0.002,
+                                    df_spread=30.0, df_step=15.0)
+    assert na > 1
+    np.testing.assert_allclose(img, 1.0, atol=1e-5)
