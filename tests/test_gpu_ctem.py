@@ -109,9 +109,13 @@ def test_partial_coherence_vs_oracle(ctx, golden):
     assert O.rel_l2(img, ref) < 2e-5
 
 
-def test_partial_coherence_vacuum_is_uniform(ctx):
-    t = np.ones((1, 128, 128), np.complex64)
-    img, na = ctx.partial_coherence(t, 2.0, [0] * 3, 20.0, 20.0, 200.0, CS, DF, 2.0, 0.0, 0.002,
+def test_partial_coherence_single_angle_equals_coherent_image(ctx, golden):
+    """With the condenser closed to the axis only the untilted wave remains."""
+    G = golden("si_small.npz")
+    ax, by, dz = float(G["ax"]), float(G["by"]), float(G["dz"])
+    img, na = ctx.partial_coherence(G["t"], dz, G["seq"], ax, by, 200.0, CS, DF, 1.5, 0.0, 0.0,
                                     df_spread=30.0, df_step=15.0)
-    assert na > 1
-    np.testing.assert_allclose(img, 1.0, atol=1e-5)
+    ref, _, _ = ctx.ctem_image(G["t"], dz, G["seq"], ax, by, 200.0, CS, DF, 1.5, df_spread=30.0,
+                               df_step=15.0)
+    assert na == 1
+    assert O.rel_l2(img, ref) < 1e-6
