@@ -1,0 +1,77 @@
+"""The reference's XML job files run end to end (LMultiSlice <action>, C# STEM
+<Calculation_parameters>) and agree with the equivalent direct API calls."""
+import numpy as np
+import pytest
+
+from multislice_gb300 import jobs, specimen as S
+from multislice_gb300.mrc import read_mrc
+from oracle import msl_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+LMS = """<?xml version="1.0" ?>
+<action>
+    <io><fileNameInput>si.coo</fileNameInput><fileNameOutput>result/si_64</fileNameOutput></io>
+    <image><nx>64</nx><ny>64</ny><dpa>6.0</dpa></image>
+    <slicing><radiuc>20.0</radiuc><numberslices>8</numberslices></slicing>
+    <microscope><aperture>25</aperture><cs>1.3</cs><defocus>-70</defocus><keV>200</keV></microscope>
+</action>
+"""
+
+MUSLI = """<?xml version="1.0" encoding="utf-8" ?>
+<Calculation_parameters>
+  <ModelFileName>sto.coo</ModelFileName>
+  <NSlices>2</NSlices>
+  <atrad>3</atrad>
+  <ThWaves><double>7.81</double><double>15.62</double></ThWaves>
+  <N>128</N><M>128</M>
+  <E><double>200000</double></E>
+  <IniWaveType>STEMshift</IniWaveType>
+  <BeamShift>
+    <ArrayOfDouble><double>3</double><double>2</double></ArrayOfDouble>
+    <ArrayOfDouble><double>0.1</double><double>0.2</double></ArrayOfDouble>
+    <ArrayOfDouble><double>0.7</double><double>0.6</double></ArrayOfDouble>
+  </BeamShift>
+  <ConvAngles><ArrayOfDouble><double>0.9</double><double>0.0</double></ArrayOfDouble></ConvAngles>
+  <DetectorAngles>
+    <ArrayOfDouble><double>7.9</double><double>3.2</double></ArrayOfDouble>
+    <ArrayOfDouble><double>0.88</double><double>0.44</double></ArrayOfDouble>
+  </DetectorAngles>
+  <Df><double>0</double></Df><Cs><double>0</double></Cs>
+</Calculation_parameters>
+"""
+
+
+def test_lmultislice_action_job(tmp_path, ctx):
+    spec = S.si_diamond(2, 2, 2)
+    S.write_coo(spec, str(tmp_path / "si.coo"))
+    (tmp_path / "result").mkdir()
+    (tmp_path / "job.xml").write_text(LMS)
+    res = jobs.run_job_file(str(tmp_path / "job.xml"))
+    v, _ = read_mrc(res["potential"])
+    img, _ = read_mrc(res["image"])
+    back = S.read_coo(str(tmp_path / "si.coo"))
+    vv = ctx.potential(back, 64, 64, 8, res["radius"])
+    assert np.array_equal(v, vv)
+    t = ctx.transmission(vv, back.ax, back.by, 200.0)
+    k_obj = 25e-3 / O.wavelength(200.0)
+    ref, _, _ = ctx.ctem_image(t, back.cz / 8, np.arange(8), back.ax, back.by, 200.0, 1.3e7, -700.0, k_obj)
+    assert O.rel_l2(img[0], ref) < 1e-6
+
+
+def test_musli_stemshift_job(tmp_path, ctx):
+    spec = S.srtio3(2, 2, 1)
+    S.write_coo(spec, str(tmp_path / "sto.coo"))
+    (tmp_path / "job.xml").write_text(MUSLI)
+    res = jobs.run_job_file(str(tmp_path / "job.xml"))
+    img = res["stem"]
+    assert img.shape == (3, 2, 2, 2) and res["checkpoints"] == [3, 7]
+    back = S.read_coo(str(tmp_path / "sto.coo"))
+    v = ctx.potential(back, 128, 128, 2, 3.0)
+    t = ctx.transmission(v, back.ax, back.by, 200.0)
+    xy = S.raster(0.1 * back.ax, 0.7 * back.ax, 0.2 * back.by, 0.6 * back.by, 3, 2)
+    d = ctx.stem_scan(t, back.cz / 2, np.arange(8) % 2, back.ax, back.by, 200.0, 0.9, xy,
+                      [(3.2, 7.9), (0.44, 0.88)], checkpoints=[3, 7])
+    assert np.array_equal(d.reshape(3, 2, 2, 2), img)
+    f, _ = read_mrc(str(tmp_path / "sto_stem_15.62A_det0.mrc"))
+    assert np.allclose(f[0], img[:, :, 1, 0])
