@@ -289,6 +289,13 @@ typedef struct {
  * msl_multislice run job by job.  bandlimit as in msl_optics. */
 int msl_run_jobs(msl_ctx *ctx, const msl_job *jobs, int njobs, double bandlimit);
 
+/* Check of the failure path of the library's bounded waits: launches a kernel
+ * whose mbarrier wait (polled `polls` times) nothing ever completes.  Returns
+ * MSL_OK when the wait gave up and the kernel raised the context's error flag
+ * as designed -- no fault, no hang, the context stays usable -- and MSL_E_CUDA
+ * otherwise.  Every TMA wait in the pass kernels takes the same path. */
+int msl_check_wait_timeout(msl_ctx *ctx, uint32_t polls);
+
 /* Probe batch size used by msl_stem_scan (0 = automatic).  Work buffers are
  * sized batch * nx * ny * 8 bytes. */
 int msl_set_probe_batch(msl_ctx *ctx, int batch);

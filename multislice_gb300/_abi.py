@@ -23,7 +23,7 @@ EXPORTS = (
     "msl_transmission_build", "msl_fft2d", "msl_multislice", "msl_stem_scan",
     "msl_set_probe_batch", "msl_profile_enable", "msl_profile_read", "msl_multislice_noalloc",
     "msl_ctem_image", "msl_phonon_displacements", "msl_frozen_phonon", "msl_coo_parse",
-    "msl_run_jobs", "msl_ctem_partial_coherence",
+    "msl_run_jobs", "msl_ctem_partial_coherence", "msl_check_wait_timeout",
 )
 PLANE_WAVE, PROBE = 0, 1
 # Muslib-shaped exports (reference names, no msl_ prefix)
@@ -115,6 +115,7 @@ def load(path=LIB_PATH):
         "msl_phonon_displacements": (c_int, [ctypes.c_uint64, c_int, c_int, c_double, P]),
         "msl_coo_parse": (c_int, [c_char_p, c_size_t, POINTER(Cell), P, c_int]),
         "msl_run_jobs": (c_int, [P, P, c_int, c_double]),
+        "msl_check_wait_timeout": (c_int, [P, ctypes.c_uint32]),
         "msl_ctem_partial_coherence": (c_int, [P, POINTER(Grid), POINTER(Optics), P, c_int, P, P, c_int,
                                                POINTER(Lens), c_double, c_double, P, P]),
         "CreatePropagator": (c_int, [c_double] * 7 + [ctypes.c_uint32, ctypes.c_uint32, P, P]),

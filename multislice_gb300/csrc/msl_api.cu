@@ -935,6 +935,21 @@ int msl_ctem_partial_coherence(msl_ctx *c, const msl_grid *g, const msl_optics *
     return MSL_OK;
 }
 
+int msl_check_wait_timeout(msl_ctx *c, uint32_t polls) {
+    if (!c) return MSL_E_ARG;
+    if (polls == 0 || polls > (1u << 20)) return fail(c, MSL_E_ARG, "polls must lie in [1, 2^20]");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    int rc;
+    if ((rc = err_reset(c))) return rc;
+    LAUNCH_TRY(c, msl::launch_wait_timeout(c->dflag, polls, c->stream, &c->launches));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    int h = 0;
+    CUDA_TRY(c, cudaMemcpy(&h, c->dflag, sizeof(int), cudaMemcpyDeviceToHost));
+    CUDA_TRY(c, cudaMemsetAsync(c->dflag, 0, sizeof(int), c->stream));
+    if (h != 1) return fail(c, MSL_E_CUDA, "the bounded wait did not report its timeout");
+    return MSL_OK;
+}
+
 int msl_set_probe_batch(msl_ctx *c, int batch) {
     if (!c || batch < 0) return fail(c, MSL_E_ARG, "probe batch must be >= 0");
     c->probe_batch = batch;

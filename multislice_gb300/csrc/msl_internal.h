@@ -119,6 +119,8 @@ cudaError_t launch_ctf_table(int nx, int ny, const float *kx2, const float *ky2,
 // out[b][ix][iy] = exp(2 pi i (qx[b] xpos[ix] + qy[b] ypos[iy])), the sum in float as mulslice.cpp:573-577
 cudaError_t launch_tilt_waves(int nx, int ny, int nb, const float *xpos, const float *ypos,
                               const float *q, float2 *out, cudaStream_t s, int64_t *launches);
+// a kernel whose mbarrier wait must run out: raises *err
+cudaError_t launch_wait_timeout(int *err, uint32_t polls, cudaStream_t s, int64_t *launches);
 // out[b * out_stride + d] = scale * sum_t partial[b][t][d]
 cudaError_t launch_detector_finalize(int nb, int ntile, int ndet, const double *partial,
                                      double scale, double *out, int out_stride, cudaStream_t s,

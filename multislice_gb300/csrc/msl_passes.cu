@@ -675,6 +675,19 @@ __global__ void tilt_wave_kernel(int nx, int ny, const float *xpos, const float 
     out[((size_t)b * nx + ix) * ny + iy] = make_float2((float)cn, (float)sn);
 }
 
+// Self-test of the bounded waits: an mbarrier that nothing ever arrives on is
+// polled `polls` times; the wait gives up, the kernel raises *err and returns.
+__global__ void wait_timeout_kernel(int *err, uint32_t polls) {
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    const bool got = mbar_wait_bounded(&bar, 0u, polls);
+    if (__syncthreads_or(!got) && threadIdx.x == 0) atomicExch(err, 1);
+}
+
 __global__ void detector_finalize_kernel(int nb, int ntile, int ndet, const double *partial,
                                          double scale, double *out, int out_stride) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1004,6 +1017,12 @@ cudaError_t launch_tilt_waves(int nx, int ny, int nb, const float *xpos, const f
     ++*launches;
     dim3 grid((ny + 255) / 256, nx, nb);
     tilt_wave_kernel<<<grid, 256, 0, s>>>(nx, ny, xpos, ypos, q, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_wait_timeout(int *err, uint32_t polls, cudaStream_t s, int64_t *launches) {
+    ++*launches;
+    wait_timeout_kernel<<<1, 64, 0, s>>>(err, polls);
     return cudaGetLastError();
 }
 

@@ -210,3 +210,12 @@ def test_device_buffers_match_host_buffers(ctx, golden):
     d_host = ctx.stem_scan(t_host, dz, np.arange(20), ax, by, kev, float(G["k_ap"]), G["xy"],
                            G["det_k"])
     assert np.array_equal(out_dev.cpu().numpy(), d_host)
+
+
+def test_bounded_wait_reports_timeout_and_context_survives(ctx):
+    """A wait that nothing completes gives up, raises the error flag, and leaves the
+    context usable (failure detection without a GPU fault)."""
+    assert ctx._lib.msl_check_wait_timeout(ctx._h, 256) == 0
+    t = np.ones((1, 64, 64), np.complex64)
+    w = ctx.multislice(t, 1.0, [0, 0], 10.0, 10.0, 200.0)
+    np.testing.assert_allclose(w, 1.0, atol=1e-6)
