@@ -14,6 +14,8 @@ Two formats exist in the reference:
   STEMshift), BeamShift, ConvAngles and DetectorAngles (1/A, outer then inner),
   Df, Cs (A), ThWaves (thickness checkpoints, A).  The unit cell is repeated
   along the beam until the last checkpoint (MSReuseCalculator.cs:36-92).
+  Results are written in the driver's own .wav / .stem formats (csfiles.py) and
+  as MRC.
 
 What differs from the reference, by design: the potential is always Kirkland's
 FPARAMS form (the C# PotType families are not rebuilt here); the cutoff radius
@@ -30,6 +32,7 @@ import numpy as np
 
 from . import specimen as S
 from .api import Context, wavelength
+from .csfiles import write_stem, write_wav
 from .mrc import write_mrc
 
 
@@ -136,9 +139,10 @@ def run_musli(root, base_dir, ctx):
         img = d.reshape(int(npx), int(npy), len(cps), len(dets))
         for ic, th in enumerate(ths):
             for k in range(len(dets)):
-                path = f"{stem}_stem_{th:g}A_det{k}.mrc"
-                write_mrc(path, img[:, :, ic, k].astype(np.float32), (spec.ax, spec.by, th),
+                path = f"{stem}_stem_{th:g}A_det{k}"
+                write_mrc(path + ".mrc", img[:, :, ic, k].astype(np.float32), (spec.ax, spec.by, th),
                           [f"STEM detector {k}, thickness {th:g} A"])
+                write_stem(path + ".stem", img[:, :, ic, k], (x1 - x0, y1 - y0), th, kev)
         results["stem"] = img
         return results
     waves = []
@@ -152,8 +156,9 @@ def run_musli(root, base_dir, ctx):
             w = ctx.run_jobs([job])[0]
         else:
             w = ctx.multislice(t, dz, seq[:n], spec.ax, spec.by, kev)[0]
-        path = f"{stem}_wave_{th:g}A.mrc"
-        write_mrc(path, w, (spec.ax, spec.by, th), [f"exit wave at {th:g} A"])
+        path = f"{stem}_wave_{th:g}A"
+        write_mrc(path + ".mrc", w, (spec.ax, spec.by, th), [f"exit wave at {th:g} A"])
+        write_wav(path + ".wav", w, spec.ax, spec.by, th, kev)
         waves.append(w)
     results["waves"] = waves
     return results
