@@ -308,7 +308,9 @@ int msl_set_probe_batch(msl_ctx *ctx, int batch);
  * doubles, element (i, j) at gli[2*(j*N + i)].  Run on the current CUDA device
  * in FP64; return 0 (success) or -1; *cpro is set to 100 on success.
  * CreatePropagator / ApplyPropagator: Propagator.cpp:5-53 / :55-107.
- * PG_rs_curve_DW_periodic: PG_RS.cpp:304-446. */
+ * PG_rs_curve_DW_periodic: PG_RS.cpp:304-446 (multiplies gli by the phase
+ * grating exp(-K B) exp(-i K A), A = sum res occ, B = sum res occ ads over the
+ * atoms, res the linearly interpolated radial curve of the atom's type). */
 int CreatePropagator(double a, double b, double gam, double thickness, double E, double Xtilt,
                      double Ytilt, uint32_t N, uint32_t M, double *gli, float *cpro);
 int ApplyPropagator(double a, double b, double gam, double thickness, double E, double Xtilt,
@@ -317,6 +319,20 @@ int PG_rs_curve_DW_periodic(double a, double b, double gam, double E, double atr
                             uint32_t M, uint32_t Na, double *xx, double *yy, double *ads, double *occ,
                             int32_t *type, double *scatentryes, uint32_t Npoints, double dds,
                             double *gli, float *cpro);
+/* PG_RS.cpp:57-119: the same grating with each atom clipped at the cell edge. */
+int PG_rs_curve_DW_cutpot(double a, double b, double gam, double E, double atrad, uint32_t N, uint32_t M,
+                          uint32_t Na, double *xx, double *yy, double *ads, double *occ, int32_t *type,
+                          double *scatentryes, uint32_t Npoints, double dds, double *gli, float *cpro);
+/* Pot_RS.cpp:209-348 / :5-55: add the potential (real part) and absorption
+ * (imaginary part) of the atoms to gli, periodic / clipped. */
+int Potential_rs_curve_DW_periodic(double a, double b, double gam, double atrad, uint32_t N, uint32_t M,
+                                   uint32_t Na, double *xx, double *yy, double *ads, double *occ,
+                                   int32_t *type, double *scatentryes, uint32_t Npoints, double dds,
+                                   double *gli, float *cpro);
+int Potential_rs_curve_DW_cutpot(double a, double b, double gam, double atrad, uint32_t N, uint32_t M,
+                                 uint32_t Na, double *xx, double *yy, double *ads, double *occ,
+                                 int32_t *type, double *scatentryes, uint32_t Npoints, double dds,
+                                 double *gli, float *cpro);
 
 /* ------------------------------------------------- no-allocation variant */
 

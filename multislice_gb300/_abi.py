@@ -27,7 +27,9 @@ EXPORTS = (
 )
 PLANE_WAVE, PROBE = 0, 1
 # Muslib-shaped exports (reference names, no msl_ prefix)
-MUSLIB_EXPORTS = ("CreatePropagator", "ApplyPropagator", "PG_rs_curve_DW_periodic")
+MUSLIB_EXPORTS = ("CreatePropagator", "ApplyPropagator", "PG_rs_curve_DW_periodic",
+                  "PG_rs_curve_DW_cutpot", "Potential_rs_curve_DW_periodic",
+                  "Potential_rs_curve_DW_cutpot")
 PROF_ROW, PROF_COL, PROF_POTENTIAL, PROF_OTHER = 0, 1, 2, 3
 
 
@@ -122,6 +124,12 @@ def load(path=LIB_PATH):
         "ApplyPropagator": (c_int, [c_double] * 7 + [ctypes.c_uint32, ctypes.c_uint32, P, P]),
         "PG_rs_curve_DW_periodic": (c_int, [c_double] * 5 + [ctypes.c_uint32] * 3 + [P] * 5 +
                                     [P, ctypes.c_uint32, c_double, P, P]),
+        "PG_rs_curve_DW_cutpot": (c_int, [c_double] * 5 + [ctypes.c_uint32] * 3 + [P] * 5 +
+                                  [P, ctypes.c_uint32, c_double, P, P]),
+        "Potential_rs_curve_DW_periodic": (c_int, [c_double] * 4 + [ctypes.c_uint32] * 3 + [P] * 5 +
+                                           [P, ctypes.c_uint32, c_double, P, P]),
+        "Potential_rs_curve_DW_cutpot": (c_int, [c_double] * 4 + [ctypes.c_uint32] * 3 + [P] * 5 +
+                                         [P, ctypes.c_uint32, c_double, P, P]),
         "msl_frozen_phonon": (c_int, [P, POINTER(Atoms), P, POINTER(Grid), c_int, c_double,
                                       POINTER(Optics), POINTER(Lens), c_int, c_double,
                                       ctypes.c_uint64, P, P]),

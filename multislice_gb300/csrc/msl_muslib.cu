@@ -79,10 +79,11 @@ int propagator(double a, double b, double gam, double thickness, double E, doubl
     return rc;
 }
 
-// One block per (atom, periodic image); the rectangle of pixels and the image
-// shift follow the nine cases of PG_RS.cpp:333-420 (integer bounds by C
-// truncation, as there).  Exponents are summed per pixel in FP64:
-// ph += K res occ, am += K ads occ res, with res the linear interpolation of the
+// One block per (atom, image rectangle); the rectangle of pixels and the image
+// shift follow the nine periodic cases of PG_RS.cpp:333-420, or the single
+// clipped case of the "cutpot" variants (PG_RS.cpp:57-119, Pot_RS.cpp:5-55),
+// integer bounds by C truncation as there.  Per pixel, in FP64:
+// A += res occ and B += res occ ads, with res the linear interpolation of the
 // atom type's radial curve at r / dds (r beyond the curve contributes nothing).
 struct Rect {
     int32_t ib, ie, jb, je;
@@ -92,7 +93,7 @@ struct Rect {
 __global__ void pg_accumulate_kernel(const Rect *rects, const int32_t *atom_of, const double *occ,
                                      const double *ads, const int32_t *type, const double *curves,
                                      uint32_t Npoints, double dds, double dxa, double dyb, double cos_g,
-                                     double K, uint32_t N, double *ph, double *am) {
+                                     uint32_t N, double *A, double *Bacc) {
     const Rect r = rects[blockIdx.x];
     const int k = atom_of[blockIdx.x];
     const double *curk = curves + (size_t)type[k] * Npoints;
@@ -109,53 +110,48 @@ __global__ void pg_accumulate_kernel(const Rect *rects, const int32_t *atom_of, 
         const double rem = ar2 - jjj;
         const double res = curk[jjj] + (curk[jjj + 1] - curk[jjj]) * rem;
         const size_t p = (size_t)j * N + i;
-        atomicAdd(ph + p, K * res * o);
-        atomicAdd(am + p, K * ad * o * res);
+        atomicAdd(A + p, res * o);
+        atomicAdd(Bacc + p, res * o * ad);
     }
 }
 
-__global__ void pg_apply_kernel(const double *ph, const double *am, size_t n, double *gli) {
+// Phase grating (PG_RS.cpp:434-441): gli *= exp(-K B) (cos K A - i sin K A).
+__global__ void pg_apply_kernel(const double *A, const double *Bacc, double K, size_t n, double *gli) {
     const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
     double sn, cn;
-    sincos(ph[p], &sn, &cn);
-    const double aI = exp(-am[p]);
+    sincos(K * A[p], &sn, &cn);
+    const double aI = exp(-K * Bacc[p]);
     const double rr = cn * aI, ri = -sn * aI;
     const double wr = gli[2 * p], wi = gli[2 * p + 1];
     gli[2 * p] = wr * rr - wi * ri;
     gli[2 * p + 1] = wr * ri + wi * rr;
 }
 
-}  // namespace
-
-extern "C" {
-
-// Propagator.cpp:5-53: gli <- exp(i (pi lambda dz s - 2 pi dz (tan tx x + tan ty y))) inside
-// s < min(N/2a, M/2b)^2, 0 outside.
-int CreatePropagator(double a, double b, double gam, double thickness, double E, double Xtilt,
-                     double Ytilt, uint32_t N, uint32_t M, double *gli, float *cpro) {
-    return propagator(a, b, gam, thickness, E, Xtilt, Ytilt, N, M, gli, cpro, 0);
+// Potential (Pot_RS.cpp:44-45): gli += (A, B).
+__global__ void pot_apply_kernel(const double *A, const double *Bacc, size_t n, double *gli) {
+    const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    gli[2 * p] += A[p];
+    gli[2 * p + 1] += Bacc[p];
 }
 
-// Propagator.cpp:55-107: gli <- gli * the same factor (0 outside).
-int ApplyPropagator(double a, double b, double gam, double thickness, double E, double Xtilt,
-                    double Ytilt, uint32_t N, uint32_t M, double *gli, float *cpro) {
-    return propagator(a, b, gam, thickness, E, Xtilt, Ytilt, N, M, gli, cpro, 1);
-}
+// Shared body of the curve-based real-space exports.  periodic: nine image
+// rectangles, else the clipped one; phase_grating: multiply gli by the grating
+// with interaction constant K, else add the potential.
+int curve_rs(double a, double b, double gam, double K, double atrad, uint32_t N, uint32_t M, uint32_t Na,
+             const double *xx, const double *yy, const double *ads, const double *occ, const int32_t *type,
+             const double *scatentryes, uint32_t Npoints, double dds, double *gli, float *cpro, bool periodic,
+             bool phase_grating);
 
-// PG_RS.cpp:304-446: multiply gli by the phase grating of Na atoms, each a
-// tabulated radial potential curve (Npoints samples spaced dds) with absorption
-// ads and occupancy occ, periodic over the cell, within atrad of the atom.
-int PG_rs_curve_DW_periodic(double a, double b, double gam, double E, double atrad, uint32_t N,
-                            uint32_t M, uint32_t Na, double *xx, double *yy, double *ads, double *occ,
-                            int32_t *type, double *scatentryes, uint32_t Npoints, double dds,
-                            double *gli, float *cpro) {
+int curve_rs(double a, double b, double gam, double K, double atrad, uint32_t N, uint32_t M, uint32_t Na,
+             const double *xx, const double *yy, const double *ads, const double *occ, const int32_t *type,
+             const double *scatentryes, uint32_t Npoints, double dds, double *gli, float *cpro, bool periodic,
+             bool phase_grating) {
     if (cpro) *cpro = 0;
     if (!gli || N == 0 || M == 0 || Npoints < 2 || !(dds > 0)) return -1;
     if (Na > 0 && (!xx || !yy || !ads || !occ || !type || !scatentryes)) return -1;
     const double sin_gam = sin(gam), cos_gam = cos(gam);
-    const double lambda = cs_lambda(E);
-    const double K = lambda * sqrt(1.0 + pow((0.0242621 / lambda), 2));
     const double drax = atrad * sin_gam / a, dray = atrad * sin_gam / b;
     const double dxa = a / (double)N, dyb = b / (double)M;
     int32_t maxtype = 0;
@@ -173,6 +169,7 @@ int PG_rs_curve_DW_periodic(double a, double b, double gam, double E, double atr
             owner.push_back((int32_t)k);
         };
         add(ibb > 0 ? ibb : 0, iee < LN ? iee : LN, jbb > 0 ? jbb : 0, jee < LM ? jee : LM, X, Y);
+        if (!periodic) continue;
         if (jbb < 0) add(ibb > 0 ? ibb : 0, iee < LN ? iee : LN, jbb + LM, LM, X, Y + b);
         if (jee >= LM) add(ibb > 0 ? ibb : 0, iee < LN ? iee : LN, 0, jee - LM + 1, X, Y - b);
         if (ibb < 0) add(ibb + LN, LN, jbb > 0 ? jbb : 0, jee < LM ? jee : LM, X + a, Y);
@@ -207,8 +204,11 @@ int PG_rs_curve_DW_periodic(double a, double b, double gam, double E, double atr
                      ok(cudaMemcpy(d_own, owner.data(), sizeof(int32_t) * nr, cudaMemcpyHostToDevice))))) {
         if (nr > 0)
             pg_accumulate_kernel<<<(unsigned)nr, 256>>>(d_rect, d_own, d_occ, d_ads, d_type, d_cur, Npoints, dds,
-                                                        dxa, dyb, cos_gam, K, N, d_ph, d_ph + n);
-        pg_apply_kernel<<<(unsigned)((n + 255) / 256), 256>>>(d_ph, d_ph + n, n, d_gli);
+                                                        dxa, dyb, cos_gam, N, d_ph, d_ph + n);
+        if (phase_grating)
+            pg_apply_kernel<<<(unsigned)((n + 255) / 256), 256>>>(d_ph, d_ph + n, K, n, d_gli);
+        else
+            pot_apply_kernel<<<(unsigned)((n + 255) / 256), 256>>>(d_ph, d_ph + n, n, d_gli);
         if (ok(cudaGetLastError())) ok(cudaMemcpy(gli, d_gli, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost));
     }
     cudaFree(d_gli);
@@ -221,6 +221,63 @@ int PG_rs_curve_DW_periodic(double a, double b, double gam, double E, double atr
     cudaFree(d_own);
     if (!rc && cpro) *cpro = 100;
     return rc;
+}
+
+
+}  // namespace
+
+extern "C" {
+
+// Propagator.cpp:5-53: gli <- exp(i (pi lambda dz s - 2 pi dz (tan tx x + tan ty y))) inside
+// s < min(N/2a, M/2b)^2, 0 outside.
+int CreatePropagator(double a, double b, double gam, double thickness, double E, double Xtilt,
+                     double Ytilt, uint32_t N, uint32_t M, double *gli, float *cpro) {
+    return propagator(a, b, gam, thickness, E, Xtilt, Ytilt, N, M, gli, cpro, 0);
+}
+
+// Propagator.cpp:55-107: gli <- gli * the same factor (0 outside).
+int ApplyPropagator(double a, double b, double gam, double thickness, double E, double Xtilt,
+                    double Ytilt, uint32_t N, uint32_t M, double *gli, float *cpro) {
+    return propagator(a, b, gam, thickness, E, Xtilt, Ytilt, N, M, gli, cpro, 1);
+}
+
+// PG_RS.cpp:304-446: multiply gli by the phase grating of Na atoms, each a
+// tabulated radial potential curve (Npoints samples spaced dds) with absorption
+// ads and occupancy occ, periodic over the cell, within atrad of the atom.
+int PG_rs_curve_DW_periodic(double a, double b, double gam, double E, double atrad, uint32_t N,
+                            uint32_t M, uint32_t Na, double *xx, double *yy, double *ads, double *occ,
+                            int32_t *type, double *scatentryes, uint32_t Npoints, double dds,
+                            double *gli, float *cpro) {
+    const double lambda = cs_lambda(E);
+    const double K = lambda * sqrt(1.0 + pow((0.0242621 / lambda), 2));
+    return curve_rs(a, b, gam, K, atrad, N, M, Na, xx, yy, ads, occ, type, scatentryes, Npoints, dds, gli,
+                    cpro, true, true);
+}
+
+// PG_RS.cpp:57-119: the same grating, each atom clipped at the cell edge.
+int PG_rs_curve_DW_cutpot(double a, double b, double gam, double E, double atrad, uint32_t N, uint32_t M,
+                          uint32_t Na, double *xx, double *yy, double *ads, double *occ, int32_t *type,
+                          double *scatentryes, uint32_t Npoints, double dds, double *gli, float *cpro) {
+    const double lambda = cs_lambda(E);
+    const double K = lambda * sqrt(1.0 + pow((0.0242621 / lambda), 2));
+    return curve_rs(a, b, gam, K, atrad, N, M, Na, xx, yy, ads, occ, type, scatentryes, Npoints, dds, gli,
+                    cpro, false, true);
+}
+
+// Pot_RS.cpp:209-348: add the potential (real) and absorption (imaginary) of the atoms, periodic.
+int Potential_rs_curve_DW_periodic(double a, double b, double gam, double atrad, uint32_t N, uint32_t M,
+                                   uint32_t Na, double *xx, double *yy, double *ads, double *occ, int32_t *type,
+                                   double *scatentryes, uint32_t Npoints, double dds, double *gli, float *cpro) {
+    return curve_rs(a, b, gam, 1.0, atrad, N, M, Na, xx, yy, ads, occ, type, scatentryes, Npoints, dds, gli,
+                    cpro, true, false);
+}
+
+// Pot_RS.cpp:5-55: the same, each atom clipped at the cell edge.
+int Potential_rs_curve_DW_cutpot(double a, double b, double gam, double atrad, uint32_t N, uint32_t M,
+                                 uint32_t Na, double *xx, double *yy, double *ads, double *occ, int32_t *type,
+                                 double *scatentryes, uint32_t Npoints, double dds, double *gli, float *cpro) {
+    return curve_rs(a, b, gam, 1.0, atrad, N, M, Na, xx, yy, ads, occ, type, scatentryes, Npoints, dds, gli,
+                    cpro, false, false);
 }
 
 }  // extern "C"

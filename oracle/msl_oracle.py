@@ -418,11 +418,18 @@ def muslib_propagator(a, b, gam, thickness, E, tx, ty, N, M):
     return np.where(s >= smax, 0, np.exp(1j * con))
 
 
-def muslib_pg_periodic(a, b, gam, E, atrad, N, M, xx, yy, ads, occ, typ, curves, dds):
-    """Multiplicative phase grating of PG_rs_curve_DW_periodic (PG_RS.cpp:304-446),
-    complex128 [M, N]; the nine periodic rectangles with C truncation of bounds."""
+def muslib_pg_periodic(a, b, gam, E, atrad, N, M, xx, yy, ads, occ, typ, curves, dds, periodic=True):
+    """Multiplicative phase grating of PG_rs_curve_DW_periodic (PG_RS.cpp:304-446)
+    or, periodic=False, PG_rs_curve_DW_cutpot (:57-119); complex128 [M, N]."""
     lam = cs_lambda(E)
     K = lam * np.sqrt(1.0 + (0.0242621 / lam) ** 2)
+    A, B = muslib_curve_sums(a, b, gam, atrad, N, M, xx, yy, ads, occ, typ, curves, dds, periodic)
+    return np.exp(-K * B) * np.exp(-1j * K * A)
+
+
+def muslib_curve_sums(a, b, gam, atrad, N, M, xx, yy, ads, occ, typ, curves, dds, periodic=True):
+    """(sum res occ, sum res occ ads) per pixel [M, N]: the nine periodic rectangles
+    (PG_RS.cpp:333-420) or the single clipped one, C truncation of bounds."""
     sg, cg = np.sin(gam), np.cos(gam)
     drax, dray = atrad * sg / a, atrad * sg / b
     dxa, dyb = a / N, b / M
@@ -434,21 +441,21 @@ def muslib_pg_periodic(a, b, gam, E, atrad, N, M, xx, yy, ads, occ, typ, curves,
         jbb, jee = int((yy[k] - dray) * M), int((yy[k] + dray) * M)
         X, Y = xx[k] * a, yy[k] * b
         rects = [(max(ibb, 0), min(iee, N), max(jbb, 0), min(jee, M), X, Y)]
-        if jbb < 0:
+        if periodic and jbb < 0:
             rects.append((max(ibb, 0), min(iee, N), jbb + M, M, X, Y + b))
-        if jee >= M:
+        if periodic and jee >= M:
             rects.append((max(ibb, 0), min(iee, N), 0, jee - M + 1, X, Y - b))
-        if ibb < 0:
+        if periodic and ibb < 0:
             rects.append((ibb + N, N, max(jbb, 0), min(jee, M), X + a, Y))
-        if iee >= N:
+        if periodic and iee >= N:
             rects.append((0, iee - N + 1, max(jbb, 0), min(jee, M), X - a, Y))
-        if ibb < 0 and jbb < 0:
+        if periodic and ibb < 0 and jbb < 0:
             rects.append((ibb + N, N, jbb + M, M, X + a, Y + b))
-        if iee >= N and jee >= M:
+        if periodic and iee >= N and jee >= M:
             rects.append((0, iee - N + 1, 0, jee - M + 1, X - a, Y - b))
-        if iee >= N and jbb < 0:
+        if periodic and iee >= N and jbb < 0:
             rects.append((0, iee - N + 1, jbb + M, M, X - a, Y + b))
-        if ibb < 0 and jee >= M:
+        if periodic and ibb < 0 and jee >= M:
             rects.append((ibb + N, N, 0, jee - M + 1, X + a, Y - b))
         cur = curves[typ[k]]
         for ib, ie, jb, je, x0, y0 in rects:
@@ -464,9 +471,9 @@ def muslib_pg_periodic(a, b, gam, E, atrad, N, M, xx, yy, ads, occ, typ, curves,
             jjj = np.where(ok, fl, 0).astype(np.int64)
             res = cur[jjj] + (cur[np.minimum(jjj + 1, npts - 1)] - cur[jjj]) * (ar2 - jjj)
             res = np.where(ok, res, 0.0)
-            ph[jb:je, ib:ie] += K * res * occ[k]
-            am[jb:je, ib:ie] += K * ads[k] * occ[k] * res
-    return np.exp(-am) * np.exp(-1j * ph)
+            ph[jb:je, ib:ie] += res * occ[k]
+            am[jb:je, ib:ie] += res * occ[k] * ads[k]
+    return ph, am
 
 
 def illumination_angles(nx, ny, ax, by, v0, acmin, acmax):
