@@ -306,33 +306,79 @@ int msl_set_probe_batch(msl_ctx *ctx, int batch);
  * identical argument lists, so its C# P/Invoke declarations bind unchanged
  * (Windows ULONG/LONG are 32-bit).  Host arrays in the C# layout: N x M complex
  * doubles, element (i, j) at gli[2*(j*N + i)].  Run on the current CUDA device
- * in FP64; return 0 (success) or -1; *cpro is set to 100 on success.
- * CreatePropagator / ApplyPropagator: Propagator.cpp:5-53 / :55-107.
- * PG_rs_curve_DW_periodic: PG_RS.cpp:304-446 (multiplies gli by the phase
- * grating exp(-K B) exp(-i K A), A = sum res occ, B = sum res occ ads over the
- * atoms, res the linearly interpolated radial curve of the atom's type). */
+ * in FP64; return 0 (success) or -1.  *cpro advances as the reference's does
+ * (periodic forms end at 100, clipped forms add 100/Na per atom).
+ * CreatePropagator / ApplyPropagator: Propagator.cpp:5-53 / :55-107. */
 int CreatePropagator(double a, double b, double gam, double thickness, double E, double Xtilt,
                      double Ytilt, uint32_t N, uint32_t M, double *gli, float *cpro);
 int ApplyPropagator(double a, double b, double gam, double thickness, double E, double Xtilt,
                     double Ytilt, uint32_t N, uint32_t M, double *gli, float *cpro);
-int PG_rs_curve_DW_periodic(double a, double b, double gam, double E, double atrad, uint32_t N,
-                            uint32_t M, uint32_t Na, double *xx, double *yy, double *ads, double *occ,
-                            int32_t *type, double *scatentryes, uint32_t Npoints, double dds,
-                            double *gli, float *cpro);
-/* PG_RS.cpp:57-119: the same grating with each atom clipped at the cell edge. */
-int PG_rs_curve_DW_cutpot(double a, double b, double gam, double E, double atrad, uint32_t N, uint32_t M,
-                          uint32_t Na, double *xx, double *yy, double *ads, double *occ, int32_t *type,
-                          double *scatentryes, uint32_t Npoints, double dds, double *gli, float *cpro);
-/* Pot_RS.cpp:209-348 / :5-55: add the potential (real part) and absorption
- * (imaginary part) of the atoms to gli, periodic / clipped. */
-int Potential_rs_curve_DW_periodic(double a, double b, double gam, double atrad, uint32_t N, uint32_t M,
-                                   uint32_t Na, double *xx, double *yy, double *ads, double *occ,
-                                   int32_t *type, double *scatentryes, uint32_t Npoints, double dds,
-                                   double *gli, float *cpro);
-int Potential_rs_curve_DW_cutpot(double a, double b, double gam, double atrad, uint32_t N, uint32_t M,
-                                 uint32_t Na, double *xx, double *yy, double *ads, double *occ,
-                                 int32_t *type, double *scatentryes, uint32_t Npoints, double dds,
-                                 double *gli, float *cpro);
+
+/* Real-space atoms (PG_RS.cpp, Pot_RS.cpp).  Per pixel A = sum res occ and
+ * B = sum res occ ads over the atoms whose box (radius atrad) covers it.  PG_*
+ * multiply gli by the phase grating exp(-K B) exp(-i K A), K the relativistic
+ * interaction constant at E volts; Potential_* add (A, B) to gli.  res is a
+ * tabulated radial curve of the atom's type interpolated at r/dds ("curve"), or
+ * the Doyle-Turner potential of Z = type with a per-atom Debye-Waller factor dw
+ * ("DT_DW") or none ("DT_TV").  "DW" forms take fractional coordinates, "TV"
+ * forms Angstrom; "periodic" forms wrap each atom's box over the cell edges,
+ * "cutpot" forms clip it. */
+#define MSL_MUSLIB_CURVE_ARGS                                                              \
+    uint32_t N, uint32_t M, uint32_t Na, double *xx, double *yy, double *ads, double *occ, \
+        int32_t *type, double *scatentryes, uint32_t Npoints, double dds, double *gli, float *cpro
+#define MSL_MUSLIB_DTDW_ARGS                                                               \
+    uint32_t N, uint32_t M, uint32_t Na, double *xx, double *yy, double *dw, double *ads,  \
+        double *occ, int32_t *type, double *gli, float *cpro
+#define MSL_MUSLIB_DTTV_ARGS                                                               \
+    uint32_t N, uint32_t M, uint32_t Na, double *xx, double *yy, double *ads, double *occ, \
+        int32_t *type, double *gli, float *cpro
+int PG_rs_curve_DW_cutpot(double a, double b, double gam, double E, double atrad, MSL_MUSLIB_CURVE_ARGS);   /* PG_RS.cpp:57-119 */
+int PG_rs_curve_TV_cutpot(double a, double b, double gam, double E, double atrad, MSL_MUSLIB_CURVE_ARGS);   /* :121-186 */
+int PG_rs_DT_DW_cutpot(double a, double b, double gam, double E, double atrad, MSL_MUSLIB_DTDW_ARGS);       /* :188-241 */
+int PG_rs_DT_TV_cutpot(double a, double b, double gam, double E, double atrad, MSL_MUSLIB_DTTV_ARGS);       /* :243-300 */
+int PG_rs_curve_DW_periodic(double a, double b, double gam, double E, double atrad, MSL_MUSLIB_CURVE_ARGS); /* :304-452 */
+int PG_rs_DT_DW_periodic(double a, double b, double gam, double E, double atrad, MSL_MUSLIB_DTDW_ARGS);     /* :454-598 */
+int PG_rs_curve_TV_periodic(double a, double b, double gam, double E, double atrad, MSL_MUSLIB_CURVE_ARGS); /* :602-751 */
+int PG_rs_DT_TV_periodic(double a, double b, double gam, double E, double atrad, MSL_MUSLIB_DTTV_ARGS);     /* :754-897 */
+int Potential_rs_curve_DW_cutpot(double a, double b, double gam, double atrad, MSL_MUSLIB_CURVE_ARGS);      /* Pot_RS.cpp:5-55 */
+int Potential_rs_curve_TV_cutpot(double a, double b, double gam, double atrad, MSL_MUSLIB_CURVE_ARGS);      /* :57-109 */
+int Potential_rs_DT_DW_cutpot(double a, double b, double gam, double atrad, MSL_MUSLIB_DTDW_ARGS);          /* :111-155 */
+int Potential_rs_DT_TV_cutpot(double a, double b, double gam, double atrad, MSL_MUSLIB_DTTV_ARGS);          /* :157-207 */
+int Potential_rs_curve_DW_periodic(double a, double b, double gam, double atrad, MSL_MUSLIB_CURVE_ARGS);    /* :209-348 */
+int Potential_rs_DT_DW_periodic(double a, double b, double gam, double atrad, MSL_MUSLIB_DTDW_ARGS);        /* :350-486 */
+int Potential_rs_curve_TV_periodic(double a, double b, double gam, double atrad, MSL_MUSLIB_CURVE_ARGS);    /* :488-627 */
+int Potential_rs_DT_TV_periodic(double a, double b, double gam, double atrad, MSL_MUSLIB_DTTV_ARGS);        /* :629-763 */
+/* PG_RS.cpp:5-55: the curve grating of one atom over every pixel, K given. */
+int PG_rs_curve_DW_cutpot_oneatom(double a, double b, double gam, double K, double atrad, uint32_t N,
+                                  uint32_t M, double xx, double yy, double ads, double occ,
+                                  double *scatentry, uint32_t Npoints, double dds, double *gli);
+
+/* Reciprocal-space potential (Pot_rec_DT_DW.cpp:3-134, Pot_rec_curve_DW.cpp:7-164):
+ * adds to gli, rows SL..EL-1 of an M-row grid (EL - SL rows of N complex
+ * doubles), the Fourier coefficients of the atoms' potential on the
+ * reflections (+-i Nmult, +-j Mmult) with i Nmult < N/2 and j Mmult < M/2:
+ * sum over atoms of res(|g|/2) occ (1 + i ads) exp(-2 pi i (h x + k y)), res the
+ * Doyle-Turner factor f(s) exp(-DW s^2) / cell area, or the type's curve. */
+int Potential_rec_DT_DW(double a, double b, double gam, uint32_t Nmult, uint32_t Mmult, uint32_t N,
+                        uint32_t M, uint32_t Na, uint32_t SL, uint32_t EL, double *xx, double *yy,
+                        double *DW, double *ads, double *occ, int32_t *type, double *gli, float *cpro);
+int Potential_rec_curve_DW(double a, double b, double gam, uint32_t Nmult, uint32_t Mmult, uint32_t N,
+                           uint32_t M, uint32_t Na, uint32_t SL, uint32_t EL, double *xx, double *yy,
+                           double *ads, double *occ, int32_t *type, double *scatentryes,
+                           uint32_t Npoints, double dds, double *gli, float *cpro);
+
+/* Doyle-Turner scattering factors and radial curves (Curves.cpp:3-81), host
+ * code: i is Z (1..92).  scat_ampl_rs_DT_DW: projected potential at radius s;
+ * scat_ampl_rs2_*: at squared radius s; CreatePots_rec_DT_DW / _rs_DT_DW fill
+ * sc[Ntypes][Npoints] at s = 0, dds, 2 dds, ... (reciprocal with cell factor
+ * _Vol / real space). */
+double scat_ampl_rs_DT_DW(int i, double s, double dw);
+double scat_ampl_rs2_DT_DW(int i, double s, double dw);
+double scat_ampl_rs2_DT_DW0(int i, double s);
+void CreatePots_rec_DT_DW(uint32_t Ntypes, uint32_t Npoints, double dds, int32_t *types, double *DW,
+                          double _Vol, double *sc);
+void CreatePots_rs_DT_DW(uint32_t Ntypes, uint32_t Npoints, double dds, int32_t *types, double *DW,
+                         double *sc);
 
 /* ------------------------------------------------- no-allocation variant */
 

@@ -27,9 +27,13 @@ EXPORTS = (
 )
 PLANE_WAVE, PROBE = 0, 1
 # Muslib-shaped exports (reference names, no msl_ prefix)
-MUSLIB_EXPORTS = ("CreatePropagator", "ApplyPropagator", "PG_rs_curve_DW_periodic",
-                  "PG_rs_curve_DW_cutpot", "Potential_rs_curve_DW_periodic",
-                  "Potential_rs_curve_DW_cutpot")
+_RS_FORMS = [(kind, src, coord, wrap) for kind in ("PG", "Potential") for src in ("curve", "DT")
+             for coord in ("DW", "TV") for wrap in ("cutpot", "periodic")]
+MUSLIB_RS = tuple(f"{k}_rs_{s}_{c}_{w}" for k, s, c, w in _RS_FORMS)
+MUSLIB_EXPORTS = ("CreatePropagator", "ApplyPropagator", *MUSLIB_RS, "PG_rs_curve_DW_cutpot_oneatom",
+                  "Potential_rec_DT_DW", "Potential_rec_curve_DW", "scat_ampl_rs_DT_DW",
+                  "scat_ampl_rs2_DT_DW", "scat_ampl_rs2_DT_DW0", "CreatePots_rec_DT_DW",
+                  "CreatePots_rs_DT_DW")
 PROF_ROW, PROF_COL, PROF_POTENTIAL, PROF_OTHER = 0, 1, 2, 3
 
 
@@ -122,18 +126,30 @@ def load(path=LIB_PATH):
                                                POINTER(Lens), c_double, c_double, P, P]),
         "CreatePropagator": (c_int, [c_double] * 7 + [ctypes.c_uint32, ctypes.c_uint32, P, P]),
         "ApplyPropagator": (c_int, [c_double] * 7 + [ctypes.c_uint32, ctypes.c_uint32, P, P]),
-        "PG_rs_curve_DW_periodic": (c_int, [c_double] * 5 + [ctypes.c_uint32] * 3 + [P] * 5 +
-                                    [P, ctypes.c_uint32, c_double, P, P]),
-        "PG_rs_curve_DW_cutpot": (c_int, [c_double] * 5 + [ctypes.c_uint32] * 3 + [P] * 5 +
-                                  [P, ctypes.c_uint32, c_double, P, P]),
-        "Potential_rs_curve_DW_periodic": (c_int, [c_double] * 4 + [ctypes.c_uint32] * 3 + [P] * 5 +
-                                           [P, ctypes.c_uint32, c_double, P, P]),
-        "Potential_rs_curve_DW_cutpot": (c_int, [c_double] * 4 + [ctypes.c_uint32] * 3 + [P] * 5 +
-                                         [P, ctypes.c_uint32, c_double, P, P]),
         "msl_frozen_phonon": (c_int, [P, POINTER(Atoms), P, POINTER(Grid), c_int, c_double,
                                       POINTER(Optics), POINTER(Lens), c_int, c_double,
                                       ctypes.c_uint64, P, P]),
     }
+    U = ctypes.c_uint32
+    for kind, src, coord, wrap in _RS_FORMS:
+        head = [c_double] * (5 if kind == "PG" else 4) + [U] * 3 + [P, P]
+        if src == "curve":
+            tail = [P, P, P, P, U, c_double, P, P]        # ads occ type curves Npoints dds gli cpro
+        elif coord == "DW":
+            tail = [P, P, P, P, P, P]                     # dw ads occ type gli cpro
+        else:
+            tail = [P, P, P, P, P]                        # ads occ type gli cpro
+        sig[f"{kind}_rs_{src}_{coord}_{wrap}"] = (c_int, head + tail)
+    sig["PG_rs_curve_DW_cutpot_oneatom"] = (c_int, [c_double] * 5 + [U, U] + [c_double] * 4 +
+                                            [P, U, c_double, P])
+    rec_head = [c_double] * 3 + [U] * 7 + [P, P]
+    sig["Potential_rec_DT_DW"] = (c_int, rec_head + [P, P, P, P, P, P])
+    sig["Potential_rec_curve_DW"] = (c_int, rec_head + [P, P, P, P, U, c_double, P, P])
+    sig["scat_ampl_rs_DT_DW"] = (c_double, [c_int, c_double, c_double])
+    sig["scat_ampl_rs2_DT_DW"] = (c_double, [c_int, c_double, c_double])
+    sig["scat_ampl_rs2_DT_DW0"] = (c_double, [c_int, c_double])
+    sig["CreatePots_rec_DT_DW"] = (None, [U, U, c_double, P, P, c_double, P])
+    sig["CreatePots_rs_DT_DW"] = (None, [U, U, c_double, P, P, P])
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
         fn.restype = res

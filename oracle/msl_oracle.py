@@ -418,62 +418,255 @@ def muslib_propagator(a, b, gam, thickness, E, tx, ty, N, M):
     return np.where(s >= smax, 0, np.exp(1j * con))
 
 
-def muslib_pg_periodic(a, b, gam, E, atrad, N, M, xx, yy, ads, occ, typ, curves, dds, periodic=True):
-    """Multiplicative phase grating of PG_rs_curve_DW_periodic (PG_RS.cpp:304-446)
-    or, periodic=False, PG_rs_curve_DW_cutpot (:57-119); complex128 [M, N]."""
-    lam = cs_lambda(E)
-    K = lam * np.sqrt(1.0 + (0.0242621 / lam) ** 2)
-    A, B = muslib_curve_sums(a, b, gam, atrad, N, M, xx, yy, ads, occ, typ, curves, dds, periodic)
+def doyle_turner():
+    """Doyle & Turner (1968) table of the Muslib bank (Curves.cpp:86-179), [93, 8]."""
+    import os
+    path = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                        "multislice_gb300", "data", "doyle_turner.npy")
+    return np.load(path)
+
+
+def dt_rec(z, s, tab=None):
+    """Curves.cpp:3-10: sum_j a_j exp(-b_j s^2)."""
+    tab = doyle_turner() if tab is None else tab
+    s = np.asarray(s, np.float64) * s
+    return sum(tab[z, 2 * j] * np.exp(-tab[z, 2 * j + 1] * s) for j in range(4))
+
+
+def dt_rs2(z, r2, dw, tab=None):
+    """Curves.cpp:23-32: 4 pi sum_{b_j>0} a_j/(b_j+dw) exp(-4 pi^2 r2/(b_j+dw))."""
+    tab = doyle_turner() if tab is None else tab
+    r2 = np.asarray(r2, np.float64) * (-4.0 * np.pi * np.pi)
+    sf = np.zeros_like(r2)
+    for j in range(4):
+        bj = tab[z, 2 * j + 1]
+        if bj > 0:
+            sf = sf + tab[z, 2 * j] / (bj + dw) * np.exp(r2 / (bj + dw))
+    return sf * 4 * np.pi
+
+
+def dt_rs(z, s, dw, tab=None):
+    """Curves.cpp:12-21: the same at radius s."""
+    s = np.asarray(s, np.float64)
+    return dt_rs2(z, s * s, dw, tab)
+
+
+def create_pots(types, DW, npoints, dds, vol=None):
+    """CreatePots_rec_DT_DW (vol given, Curves.cpp:45-61) or CreatePots_rs_DT_DW
+    (Curves.cpp:63-81); the sample points accumulate s += dds as there."""
+    s = np.empty(npoints)
+    acc = 0.0
+    for i in range(npoints):
+        s[i] = acc
+        acc += dds
+    out = np.empty((len(types), npoints))
+    for nt, (ty, dw) in enumerate(zip(types, DW)):
+        if vol is None:
+            out[nt] = dt_rs(ty, s, dw)
+        else:
+            out[nt] = dt_rec(ty, s) * np.exp(-dw * s * s) * vol
+    return out
+
+
+def _umin(v, n):
+    """min(long, ULONG) of the Windows build: an unsigned compare."""
+    return v if 0 <= v < n else n
+
+
+def _rs_rects(k, a, b, atrad, N, M, xx, yy, sg, source, angstrom, periodic, whole):
+    """Pixel rectangles (ib, ie, jb, je, x0, y0) of atom k, bounds formula by
+    formula as each variant of PG_RS.cpp / Pot_RS.cpp writes them."""
+    xk, yk = float(xx[k]), float(yy[k])
+    X, Y = (xk, yk) if angstrom else (xk * a, yk * b)
+    if whole:
+        return [(0, N, 0, M, X, Y)]
+    drax = atrad * sg if angstrom else atrad * sg / a
+    dray = atrad * sg if angstrom else atrad * sg / b
+    if not periodic:
+        if not angstrom:                              # PG_RS.cpp:81-84
+            r = (max(int((xk - drax) * N), 0), _umin(int((xk + drax) * N), N),
+                 max(int((yk - dray) * M), 0), _umin(int((yk + dray) * M), M))
+        elif source == "curve":                       # PG_RS.cpp:149-152
+            t = lambda v: int(v) if v > 0 else 0
+            r = (t(int((xk - drax) * N) / a), t(min(int((xk + drax) * N) / a, N)),
+                 t(int((yk - dray) * M) / b), t(min(int((yk + dray) * M) / b, M)))
+        else:                                         # PG_RS.cpp:269-272
+            r = (max(int((xk - drax) * N / a), 0), _umin(int((xk + drax) * N / a), N),
+                 max(int((yk - dray) * M / b), 0), _umin(int((yk + dray) * M / b), M))
+        return [r + (X, Y)]
+    if not angstrom:                                  # PG_RS.cpp:327-330
+        ibb, iee = int((xk - drax) * N), int((xk + drax) * N)
+        jbb, jee = int((yk - dray) * M), int((yk + dray) * M)
+    else:                                             # PG_RS.cpp:625-628
+        ibb, iee = int((xk - drax) / a * N), int((xk + drax) / a * N)
+        jbb, jee = int((yk - dray) / b * M), int((yk + dray) / b * M)
+    ib0, ie0, jb0, je0 = max(ibb, 0), _umin(iee, N), max(jbb, 0), _umin(jee, M)
+    rects = [(ib0, ie0, jb0, je0, X, Y)]          # the nine cases of PG_RS.cpp:337-417
+    if jbb < 0:
+        rects.append((ib0, ie0, jbb + M, M, X, Y + b))
+    if jee >= M:
+        rects.append((ib0, ie0, 0, jee - M + 1, X, Y - b))
+    if ibb < 0:
+        rects.append((ibb + N, N, jb0, je0, X + a, Y))
+    if iee >= N:
+        rects.append((0, iee - N + 1, jb0, je0, X - a, Y))
+    if ibb < 0 and jbb < 0:
+        rects.append((ibb + N, N, jbb + M, M, X + a, Y + b))
+    if iee >= N and jee >= M:
+        rects.append((0, iee - N + 1, 0, jee - M + 1, X - a, Y - b))
+    if iee >= N and jbb < 0:
+        rects.append((0, iee - N + 1, jbb + M, M, X - a, Y + b))
+    if ibb < 0 and jee >= M:
+        rects.append((ibb + N, N, 0, jee - M + 1, X + a, Y - b))
+    return rects
+
+
+def muslib_rs_sums(a, b, gam, atrad, N, M, xx, yy, ads, occ, typ, curves=None, dds=None, dw=None,
+                   source="curve", angstrom=False, periodic=True, whole=False):
+    """(A, B) = (sum res occ, sum res occ ads) per pixel [M, N] of the real-space
+    Muslib forms (PG_RS.cpp, Pot_RS.cpp).  source: "curve" (the type's curve at
+    r/dds, nothing beyond it), "DT_DW" (Doyle-Turner at r^2 with dw[k]) or
+    "DT_TV" (no Debye-Waller term); angstrom: "TV" coordinates."""
+    sg, cg = np.sin(gam), np.cos(gam)
+    dxa, dyb = a / N, b / M
+    tab = doyle_turner() if source != "curve" else None
+    A = np.zeros((M, N))
+    B = np.zeros((M, N))
+    for k in range(len(xx)):
+        for ib, ie, jb, je, x0, y0 in _rs_rects(k, a, b, atrad, N, M, xx, yy, sg, source, angstrom,
+                                                periodic, whole):
+            ib, jb, ie, je = max(ib, 0), max(jb, 0), min(ie, N), min(je, M)
+            if ie <= ib or je <= jb:
+                continue
+            x = np.arange(ib, ie)[None, :] * dxa - x0
+            y = np.arange(jb, je)[:, None] * dyb - y0
+            r2 = x * (x + 2 * y * cg) + y * y
+            if source == "curve":
+                npts = curves.shape[1]
+                cur = curves[typ[k]]
+                ar2 = np.sqrt(r2) / dds
+                fl = np.floor(ar2)
+                ok = fl < npts - 1
+                jjj = np.where(ok, fl, 0).astype(np.int64)
+                res = cur[jjj] + (cur[np.minimum(jjj + 1, npts - 1)] - cur[jjj]) * (ar2 - jjj)
+                res = np.where(ok, res, 0.0)
+            else:
+                res = dt_rs2(int(typ[k]), r2, float(dw[k]) if source == "DT_DW" else 0.0, tab)
+            A[jb:je, ib:ie] += res * occ[k]
+            B[jb:je, ib:ie] += res * occ[k] * ads[k]
+    return A, B
+
+
+def muslib_pg(A, B, E, K=None):
+    """Phase grating exp(-K B) exp(-i K A) of PG_RS.cpp:433-441 (K from E volts)."""
+    if K is None:
+        lam = cs_lambda(E)
+        K = lam * np.sqrt(1.0 + (0.0242621 / lam) ** 2)
     return np.exp(-K * B) * np.exp(-1j * K * A)
 
 
+def muslib_pg_periodic(a, b, gam, E, atrad, N, M, xx, yy, ads, occ, typ, curves, dds, periodic=True):
+    """Multiplicative phase grating of PG_rs_curve_DW_periodic (PG_RS.cpp:304-446)
+    or, periodic=False, PG_rs_curve_DW_cutpot (:57-119); complex128 [M, N]."""
+    A, B = muslib_curve_sums(a, b, gam, atrad, N, M, xx, yy, ads, occ, typ, curves, dds, periodic)
+    return muslib_pg(A, B, E)
+
+
 def muslib_curve_sums(a, b, gam, atrad, N, M, xx, yy, ads, occ, typ, curves, dds, periodic=True):
-    """(sum res occ, sum res occ ads) per pixel [M, N]: the nine periodic rectangles
-    (PG_RS.cpp:333-420) or the single clipped one, C truncation of bounds."""
-    sg, cg = np.sin(gam), np.cos(gam)
-    drax, dray = atrad * sg / a, atrad * sg / b
-    dxa, dyb = a / N, b / M
-    npts = curves.shape[1]
-    ph = np.zeros((M, N))
-    am = np.zeros((M, N))
-    for k in range(len(xx)):
-        ibb, iee = int((xx[k] - drax) * N), int((xx[k] + drax) * N)
-        jbb, jee = int((yy[k] - dray) * M), int((yy[k] + dray) * M)
-        X, Y = xx[k] * a, yy[k] * b
-        rects = [(max(ibb, 0), min(iee, N), max(jbb, 0), min(jee, M), X, Y)]
-        if periodic and jbb < 0:
-            rects.append((max(ibb, 0), min(iee, N), jbb + M, M, X, Y + b))
-        if periodic and jee >= M:
-            rects.append((max(ibb, 0), min(iee, N), 0, jee - M + 1, X, Y - b))
-        if periodic and ibb < 0:
-            rects.append((ibb + N, N, max(jbb, 0), min(jee, M), X + a, Y))
-        if periodic and iee >= N:
-            rects.append((0, iee - N + 1, max(jbb, 0), min(jee, M), X - a, Y))
-        if periodic and ibb < 0 and jbb < 0:
-            rects.append((ibb + N, N, jbb + M, M, X + a, Y + b))
-        if periodic and iee >= N and jee >= M:
-            rects.append((0, iee - N + 1, 0, jee - M + 1, X - a, Y - b))
-        if periodic and iee >= N and jbb < 0:
-            rects.append((0, iee - N + 1, jbb + M, M, X - a, Y + b))
-        if periodic and ibb < 0 and jee >= M:
-            rects.append((ibb + N, N, 0, jee - M + 1, X + a, Y - b))
-        cur = curves[typ[k]]
-        for ib, ie, jb, je, x0, y0 in rects:
-            if ie <= ib or je <= jb:
-                continue
-            ii = np.arange(ib, ie)
-            jj = np.arange(jb, je)
-            x = ii[None, :] * dxa - x0
-            y = jj[:, None] * dyb - y0
-            ar2 = np.sqrt(x * (x + 2 * y * cg) + y * y) / dds
-            fl = np.floor(ar2)
-            ok = fl < npts - 1
-            jjj = np.where(ok, fl, 0).astype(np.int64)
-            res = cur[jjj] + (cur[np.minimum(jjj + 1, npts - 1)] - cur[jjj]) * (ar2 - jjj)
-            res = np.where(ok, res, 0.0)
-            ph[jb:je, ib:ie] += res * occ[k]
-            am[jb:je, ib:ie] += res * occ[k] * ads[k]
-    return ph, am
+    """(sum res occ, sum res occ ads) of the curve forms in fractional coordinates."""
+    return muslib_rs_sums(a, b, gam, atrad, N, M, xx, yy, ads, occ, typ, curves=curves, dds=dds,
+                          periodic=periodic)
+
+
+def muslib_rec_potential(a, b, gam, Nmult, Mmult, N, M, SL, EL, xx, yy, ads, occ, typ, DW=None,
+                         curves=None, dds=None):
+    """Coefficients Potential_rec_DT_DW (Pot_rec_DT_DW.cpp:3-134, DW given) or
+    Potential_rec_curve_DW (Pot_rec_curve_DW.cpp:7-164, curves given) add to the
+    rows [SL, EL) of an M x N grid; complex128 [EL - SL, N].  Follows the
+    reference's loops: row 0, then rows j Mmult < M/2 with their mirrors."""
+    cos_gam = -np.cos(gam)
+    A_, B_ = 1.0 / (a * np.sin(gam)), 1.0 / (b * np.sin(gam))
+    vol = 1.0 / (a * b * np.sin(gam))
+    out = np.zeros((EL - SL, N), np.complex128)
+    tab = doyle_turner() if curves is None else None
+    ds = 1.0 / dds if curves is not None else 0.0
+    npts = curves.shape[1] if curves is not None else 0
+    ii = np.arange(1, N)
+    ii = ii[ii * Nmult < N // 2]
+    x = ii * A_
+    cols, mcols = ii * Nmult, N - ii * Nmult
+
+    def lookup(k, t):
+        """curve value at index position t (array) and the in-range mask."""
+        t = np.asarray(t, np.float64)
+        fl = np.floor(t)
+        ok = fl < npts - 1
+        jj = np.where(ok, fl, 0).astype(np.int64)
+        c = curves[typ[k]]
+        return c[jj] + (c[np.minimum(jj + 1, npts - 1)] - c[jj]) * (t - jj), ok
+
+    def dt(k, s, ss):
+        return dt_rec(int(typ[k]), s, tab) * np.exp(-DW[k] * ss) * vol * occ[k]
+
+    if SL == 0:
+        for k in range(len(xx)):
+            if curves is None:
+                res0 = dt_rec(int(typ[k]), 0.0, tab) * vol * occ[k]
+            else:
+                res0 = curves[typ[k], 0] * occ[k]
+            out[0, 0] += res0 * (1 + 1j * ads[k])
+            if curves is None:
+                res, ok = dt(k, x * 0.5, x * x * 0.25), np.ones(len(x), bool)
+            else:
+                res, ok = lookup(k, x * 0.5 * ds)
+                res = res * occ[k]
+            ph = np.exp(1j * (-2. * np.pi * xx[k] * ii.astype(np.float64)))
+            out[0, cols[ok]] += (res * ph * (1 + 1j * ads[k]))[ok]
+            out[0, mcols[ok]] += (res * np.conj(ph) * (1 + 1j * ads[k]))[ok]
+    j = 1
+    while j * Mmult < M // 2:
+        jj = j * Mmult
+        isup = SL <= jj < EL
+        islow = SL <= M - jj < EL
+        if not (isup or islow):
+            j += 1
+            continue
+        y = j * B_
+        y_pow2 = y * y
+        y_cosgam = y * cos_gam * 2.
+        for k in range(len(xx)):
+            pj = np.exp(1j * (-2. * np.pi * yy[k] * float(j)))
+            if curves is None:
+                r0 = dt(k, np.sqrt(y_pow2 * 0.25), y_pow2 * 0.25)
+            else:
+                r0, ok0 = lookup(k, y * ds * 0.5)
+                if not ok0:
+                    continue
+                r0 = r0 * occ[k]
+            if isup:
+                out[jj - SL, 0] += r0 * pj * (1 + 1j * ads[k])
+            if islow:
+                out[M - jj - SL, 0] += r0 * np.conj(pj) * (1 + 1j * ads[k])
+            ss = (x * x + y_pow2 + x * y_cosgam) * 0.25
+            ss1 = ss - x * y_cosgam * 0.5
+            if curves is None:
+                res, res1 = dt(k, np.sqrt(ss), ss), dt(k, np.sqrt(ss1), ss1)
+                ok = np.ones(len(x), bool)
+            else:
+                res, ok1 = lookup(k, np.sqrt(ss) * ds)
+                res1, ok2 = lookup(k, np.sqrt(ss1) * ds)
+                ok = ok1 & ok2
+                res, res1 = res * occ[k], res1 * occ[k]
+            pi_ = np.exp(1j * (-2. * np.pi * xx[k] * ii.astype(np.float64)))
+            f = 1 + 1j * ads[k]
+            if isup:
+                out[jj - SL, cols[ok]] += (res * pi_ * pj * f)[ok]
+                out[jj - SL, mcols[ok]] += (res1 * np.conj(pi_) * pj * f)[ok]
+            if islow:
+                out[M - jj - SL, cols[ok]] += (res1 * pi_ * np.conj(pj) * f)[ok]
+                out[M - jj - SL, mcols[ok]] += (res * np.conj(pi_ * pj) * f)[ok]
+        j += 1
+    return out
 
 
 def illumination_angles(nx, ny, ax, by, v0, acmin, acmax):

@@ -88,3 +88,124 @@ def test_potential_curve(periodic, gam):
     np.testing.assert_allclose(gli[..., 0] - base[..., 0], A, atol=1e-11)
     np.testing.assert_allclose(gli[..., 1] - base[..., 1], B, atol=1e-11)
     assert A.max() > 1.0
+
+
+def _rs_inputs(src, coord, seed=9):
+    rng = np.random.default_rng(seed)
+    a, b, E, atrad, N, M, na = 9.0, 10.5, 200e3, 1.8, 80, 96, 30
+    xx, yy = rng.random(na), rng.random(na)
+    xx[:4] = [0.01, 0.985, 0.5, 0.03]              # boxes that cross the cell edges
+    yy[:4] = [0.02, 0.97, 0.995, 0.5]
+    if coord == "TV":
+        xx, yy = xx * a, yy * b                    # Angstrom coordinates
+    ads = rng.random(na) * 0.05
+    occ = 0.5 + 0.5 * rng.random(na)
+    dw = 0.2 + 0.6 * rng.random(na)
+    if src == "curve":
+        typ = rng.integers(0, 3, na).astype(np.int32)
+        r = np.arange(300) * 0.01
+        curves = np.ascontiguousarray(np.stack([z * np.exp(-r / 0.35) for z in (1.0, 2.0, 3.5)]))
+    else:
+        typ = rng.choice(np.array([8, 22, 38], np.int32), na)
+        curves = None
+    return a, b, E, atrad, N, M, na, xx, yy, ads, occ, dw, typ, curves
+
+
+@pytest.mark.parametrize("name", _abi.MUSLIB_RS)
+@pytest.mark.parametrize("gam", [np.pi / 2, 1.8])
+def test_real_space_forms(name, gam):
+    """Every PG_rs_* / Potential_rs_* export against the restatement of its own
+    box bounds, radial source and wrap rule."""
+    import torch  # noqa: F401
+    lib = _abi.load()
+    kind, _, src, coord, wrap = name.split("_")
+    a, b, E, atrad, N, M, na, xx, yy, ads, occ, dw, typ, curves = _rs_inputs(src, coord)
+    rng = np.random.default_rng(1)
+    base = rng.standard_normal((M, N, 2))
+    gli = base.copy()
+    cpro = ctypes.c_float(0)
+    head = (a, b, gam, E, atrad) if kind == "PG" else (a, b, gam, atrad)
+    common = (N, M, na, _p(xx), _p(yy))
+    if src == "curve":
+        tail = (_p(ads), _p(occ), _p(typ), _p(curves), curves.shape[1], 0.01, _p(gli), ctypes.byref(cpro))
+    elif coord == "DW":
+        tail = (_p(dw), _p(ads), _p(occ), _p(typ), _p(gli), ctypes.byref(cpro))
+    else:
+        tail = (_p(ads), _p(occ), _p(typ), _p(gli), ctypes.byref(cpro))
+    assert getattr(lib, name)(*head, *common, *tail) == 0
+    source = "curve" if src == "curve" else f"DT_{coord}"
+    A, B = O.muslib_rs_sums(a, b, gam, atrad, N, M, xx, yy, ads, occ, typ, curves=curves, dds=0.01,
+                            dw=dw, source=source, angstrom=coord == "TV", periodic=wrap == "periodic")
+    assert A.max() > 0.5
+    got = gli[..., 0] + 1j * gli[..., 1]
+    b0 = base[..., 0] + 1j * base[..., 1]
+    if kind == "PG":
+        assert O.rel_l2(got, b0 * O.muslib_pg(A, B, E)) < 1e-12
+    else:
+        np.testing.assert_allclose(gli[..., 0] - base[..., 0], A, atol=1e-10)
+        np.testing.assert_allclose(gli[..., 1] - base[..., 1], B, atol=1e-10)
+    if wrap == "periodic":
+        assert cpro.value == 100.0
+    else:
+        ref = np.float32(0)
+        for _ in range(na):
+            ref = np.float32(np.float64(ref) + 100.0 / na)
+        assert cpro.value == ref
+
+
+def test_one_atom_grating():
+    import torch  # noqa: F401
+    lib = _abi.load()
+    a, b, gam, K, N, M = 8.0, 8.0, 1.9, 0.025, 64, 64
+    r = np.arange(500) * 0.01
+    cur = np.ascontiguousarray(4.0 * np.exp(-r / 0.5))
+    gli = np.zeros((M, N, 2))
+    gli[..., 0] = 1.0
+    assert lib.PG_rs_curve_DW_cutpot_oneatom(a, b, gam, K, 1.0, N, M, 0.3, 0.7, 0.04, 0.9, _p(cur), 500,
+                                             0.01, _p(gli)) == 0
+    A, B = O.muslib_rs_sums(a, b, gam, 1.0, N, M, np.array([0.3]), np.array([0.7]), np.array([0.04]),
+                            np.array([0.9]), np.array([0]), curves=cur[None], dds=0.01, periodic=False,
+                            whole=True)
+    assert O.rel_l2(gli[..., 0] + 1j * gli[..., 1], O.muslib_pg(A, B, 0, K=K)) < 1e-12
+
+
+@pytest.mark.parametrize("form", ["DT", "curve"])
+@pytest.mark.parametrize("gam,mult,band", [(np.pi / 2, (1, 1), (0, 64)), (1.75, (2, 1), (0, 40)),
+                                           (np.pi / 2, (1, 3), (10, 60))])
+def test_reciprocal_space_potential(form, gam, mult, band):
+    import torch  # noqa: F401
+    lib = _abi.load()
+    rng = np.random.default_rng(21)
+    a, b, N, M, na = 11.0, 12.0, 48, 64, 40
+    Nmult, Mmult = mult
+    SL, EL = band
+    xx, yy = rng.random(na), rng.random(na)
+    ads, occ = rng.random(na) * 0.05, 0.5 + 0.5 * rng.random(na)
+    zs = np.array([8, 22, 38], np.int32)
+    pick = rng.integers(0, 3, na)
+    dwv = np.array([0.3, 0.45, 0.6])
+    base = rng.standard_normal((EL - SL, N, 2))
+    gli = base.copy()
+    cpro = ctypes.c_float(0)
+    if form == "DT":
+        typ, DW = zs[pick], dwv[pick]
+        rc = lib.Potential_rec_DT_DW(a, b, gam, Nmult, Mmult, N, M, na, SL, EL, _p(xx), _p(yy), _p(DW),
+                                     _p(ads), _p(occ), _p(typ), _p(gli), ctypes.byref(cpro))
+        ref = O.muslib_rec_potential(a, b, gam, Nmult, Mmult, N, M, SL, EL, xx, yy, ads, occ, typ, DW=DW)
+    else:
+        typ = pick.astype(np.int32)
+        curves = np.ascontiguousarray(O.create_pots(zs, dwv, 60, 0.02, vol=1 / (a * b * np.sin(gam))))
+        rc = lib.Potential_rec_curve_DW(a, b, gam, Nmult, Mmult, N, M, na, SL, EL, _p(xx), _p(yy), _p(ads),
+                                        _p(occ), _p(typ), _p(curves), 60, 0.02, _p(gli), ctypes.byref(cpro))
+        ref = O.muslib_rec_potential(a, b, gam, Nmult, Mmult, N, M, SL, EL, xx, yy, ads, occ, typ,
+                                     curves=curves, dds=0.02)
+    assert rc == 0
+    got = (gli[..., 0] - base[..., 0]) + 1j * (gli[..., 1] - base[..., 1])
+    assert np.abs(ref).max() > 0.1
+    np.testing.assert_allclose(got, ref, atol=1e-12 * np.abs(ref).max())
+    rows = (SL == 0) + sum(1 for j in range(1, M) if j * Mmult < M // 2 and
+                           (SL <= j * Mmult < EL or SL <= M - j * Mmult < EL))
+    ref_p = np.float32(0)
+    for _ in range(rows):
+        ref_p = np.float32(np.float64(ref_p) + 200.0 / M)
+    assert cpro.value == ref_p

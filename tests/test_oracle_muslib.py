@@ -1,11 +1,14 @@
 """The vectorised Muslib restatement (nine clipped rectangles per atom) against
 a literal per-pixel loop over the same index ranges, PG_RS.cpp:57-119 (clipped)
 and :304-446 (periodic), on a small cell."""
+import ctypes
 import math
+import os
 
 import numpy as np
 import pytest
 
+from multislice_gb300 import _abi
 from oracle import msl_oracle as O
 
 
@@ -75,3 +78,75 @@ def test_periodic_grating_adds_only_the_wrapped_parts():
     per = O.muslib_curve_sums(*args, True)[0]
     cut = O.muslib_curve_sums(*args, False)[0]
     assert np.all(per >= cut - 1e-12) and (per - cut).max() > 0.1
+
+
+def _lib():
+    if not os.path.exists(_abi.LIB_PATH):
+        from multislice_gb300 import build
+        build.build()
+    return _abi.load()
+
+
+def test_doyle_turner_table_shape():
+    tab = O.doyle_turner()
+    assert tab.shape == (93, 8) and np.all(tab[0] == 0)
+    assert tab[14, 0] == 2.1293 and tab[79, 7] == 0.3067   # Si a1, Au b4
+
+
+def test_host_scattering_functions_match_oracle():
+    """Curves.cpp host exports (no GPU needed) against the restatement."""
+    lib = _lib()
+    for z in (1, 6, 14, 38, 79, 92):
+        for s, dw in ((0.0, 0.0), (0.05, 0.3), (0.7, 1.1)):
+            assert lib.scat_ampl_rs2_DT_DW(z, s, dw) == pytest.approx(float(O.dt_rs2(z, s, dw)), rel=1e-14)
+            assert lib.scat_ampl_rs_DT_DW(z, s, dw) == pytest.approx(float(O.dt_rs(z, s, dw)), rel=1e-14)
+        assert lib.scat_ampl_rs2_DT_DW0(z, 0.2) == pytest.approx(float(O.dt_rs2(z, 0.2, 0.0)), rel=1e-14)
+    types = np.array([6, 14, 79], np.int32)
+    dw = np.array([0.3, 0.5, 0.0])
+    npts, dds = 300, 0.01
+    sc = np.zeros((3, npts))
+    lib.CreatePots_rs_DT_DW(3, npts, dds, types.ctypes.data, dw.ctypes.data, sc.ctypes.data)
+    np.testing.assert_allclose(sc, O.create_pots(types, dw, npts, dds), rtol=1e-13)
+    lib.CreatePots_rec_DT_DW(3, npts, dds, types.ctypes.data, dw.ctypes.data, 0.02, sc.ctypes.data)
+    np.testing.assert_allclose(sc, O.create_pots(types, dw, npts, dds, vol=0.02), rtol=1e-13)
+
+
+def test_rec_potential_single_atom_closed_form():
+    """One atom: the coefficient of reflection (h, k) is f(|g|/2) exp(-DW |g|^2/4)
+    occ (1 + i ads) / area * exp(-2 pi i (h x + k y)), |g| on the reciprocal lattice
+    of the oblique cell (angle pi - gam between a* and b*)."""
+    a, b, gam, N, M = 7.0, 9.0, 1.7, 16, 20
+    xx, yy = np.array([0.23]), np.array([0.61])
+    ads, occ, typ, DW = np.array([0.07]), np.array([0.8]), np.array([29]), np.array([0.4])
+    got = O.muslib_rec_potential(a, b, gam, 1, 1, N, M, 0, M, xx, yy, ads, occ, typ, DW=DW)
+    A_, B_ = 1 / (a * math.sin(gam)), 1 / (b * math.sin(gam))
+    vol = 1 / (a * b * math.sin(gam))
+    for h in range(-N // 2 + 1, N // 2):
+        for k in range(-M // 2 + 1, M // 2):
+            g2 = (h * A_) ** 2 + (k * B_) ** 2 - 2 * h * k * A_ * B_ * math.cos(gam)
+            s = math.sqrt(g2) / 2
+            ref = (O.dt_rec(29, s) * math.exp(-DW[0] * s * s) * vol * occ[0] * (1 + 1j * ads[0]) *
+                   np.exp(-2j * math.pi * (h * xx[0] + k * yy[0])))
+            assert abs(got[k % M, h % N] - ref) < 1e-12 * max(1.0, abs(ref)), (h, k)
+    assert np.all(got[M // 2] == 0) and np.all(got[:, N // 2] == 0)   # Nyquist lines are never written
+
+
+def test_rec_potential_curve_band_and_symmetry():
+    """Without absorption the coefficients are Hermitian, and a row band [SL, EL)
+    equals the same rows of the full grid."""
+    rng = np.random.default_rng(5)
+    a, b, gam, N, M, na = 8.0, 8.0, math.pi / 2, 24, 24, 6
+    xx, yy = rng.random(na), rng.random(na)
+    occ, typ = 0.5 + 0.5 * rng.random(na), rng.integers(0, 2, na)
+    curves = O.create_pots([8, 38], [0.2, 0.4], 500, 0.005, vol=1 / (a * b))
+    full = O.muslib_rec_potential(a, b, gam, 1, 1, N, M, 0, M, xx, yy, np.zeros(na), occ, typ,
+                                  curves=curves, dds=0.005)
+    for jj in range(1, M // 2):
+        for ii in range(1, N // 2):
+            assert abs(full[M - jj, N - ii] - np.conj(full[jj, ii])) < 1e-12
+    band = O.muslib_rec_potential(a, b, gam, 1, 1, N, M, 5, 19, xx, yy, np.zeros(na), occ, typ,
+                                  curves=curves, dds=0.005)
+    np.testing.assert_allclose(band, full[5:19], atol=1e-13)
+    dt = O.muslib_rec_potential(a, b, gam, 1, 1, N, M, 0, M, xx, yy, np.zeros(na), occ,
+                                np.array([8, 38])[typ], DW=np.array([0.2, 0.4])[typ])
+    assert O.rel_l2(full, dt) < 1e-4      # the tabulated curve approximates the DT form
