@@ -14,8 +14,10 @@ Two formats exist in the reference:
   STEMshift), BeamShift, ConvAngles and DetectorAngles (1/A, outer then inner),
   Df, Cs (A), ThWaves (thickness checkpoints, A).  The unit cell is repeated
   along the beam until the last checkpoint (MSReuseCalculator.cs:36-92).
-  Results are written in the driver's own .wav / .stem formats (csfiles.py) and
-  as MRC.
+  Results are written in the driver's own formats (csfiles.py) and as MRC:
+  .wav exit waves (IsSaveWaves, default on), .cbed diffraction patterns
+  (IsSaveDiffractions), .stem images, and the slices' phase gratings as .slice
+  files under "Slice stack" (SaveSlices, MSProjectReuse.cs:443, :527-560).
 
 What differs from the reference, by design: the potential is always Kirkland's
 FPARAMS form (the C# PotType families are not rebuilt here); the cutoff radius
@@ -32,7 +34,7 @@ import numpy as np
 
 from . import specimen as S
 from .api import Context, wavelength
-from .csfiles import write_stem, write_wav
+from .csfiles import write_cbed, write_slice, write_stem, write_wav
 from .mrc import write_mrc
 
 
@@ -43,6 +45,13 @@ def _f(node, path, default=None, cast=float):
             raise ValueError(f"job file: <{path}> is required")
         return default
     return cast(el.text.strip().replace(",", "."))
+
+
+def _bool(node, path, default):
+    el = node.find(path)
+    if el is None or el.text is None or not el.text.strip():
+        return default
+    return el.text.strip().lower() in ("true", "1")
 
 
 def _doubles(node, path):
@@ -128,6 +137,12 @@ def run_musli(root, base_dir, ctx):
     t = ctx.transmission(v, spec.ax, spec.by, kev)
     seq, cps = _slices_to(ths, dz, nsl)
     results = {"checkpoints": cps, "thickness": ths}
+    if _bool(root, "SaveSlices", False):
+        sdir = os.path.join(os.path.dirname(stem), "Slice stack")
+        os.makedirs(sdir, exist_ok=True)
+        for i in range(nsl):
+            write_slice(os.path.join(sdir, f"Slice_{i:04d}.slice"), t[i], spec.ax, spec.by, dz, i, nsl)
+        results["slices"] = sdir
     if kind == "STEMshift":
         bs = _pairs(root, "BeamShift")
         (npx, npy), (x0, y0), (x1, y1) = bs[0], bs[1], bs[2]
@@ -146,6 +161,8 @@ def run_musli(root, base_dir, ctx):
         results["stem"] = img
         return results
     waves = []
+    save_waves = _bool(root, "IsSaveWaves", True)
+    save_diff = _bool(root, "IsSaveDiffractions", False)
     for ic, th in enumerate(ths):
         n = cps[ic] + 1
         if kind == "Converged":
@@ -158,7 +175,12 @@ def run_musli(root, base_dir, ctx):
             w = ctx.multislice(t, dz, seq[:n], spec.ax, spec.by, kev)[0]
         path = f"{stem}_wave_{th:g}A"
         write_mrc(path + ".mrc", w, (spec.ax, spec.by, th), [f"exit wave at {th:g} A"])
-        write_wav(path + ".wav", w, spec.ax, spec.by, th, kev)
+        if save_waves:
+            write_wav(path + ".wav", w, spec.ax, spec.by, th, kev)
+        if save_diff:
+            # the spectrum after the checkpoint slice's propagator = forward transform of the exit wave
+            spec_k = ctx.fft2d(np.ascontiguousarray(w[None]), spec.ax, spec.by, +1)[0]
+            write_cbed(f"{stem}_diffraction_{th:g}A.cbed", spec_k, spec.ax, spec.by, th, kev)
         waves.append(w)
     results["waves"] = waves
     return results

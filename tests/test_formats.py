@@ -43,3 +43,32 @@ def test_csharp_wav_and_stem_roundtrip(tmp_path):
     write_stem(tmp_path / "s.stem", img, (0.6, 0.4), 15.62, 200.0)
     back, meta = read_stem(tmp_path / "s.stem")
     assert np.array_equal(back, img) and (meta["n"], meta["m"]) == (4, 3)
+
+
+def test_csharp_cbed_slice_and_slice_coo(tmp_path):
+    from multislice_gb300 import csfiles as C
+    rng = np.random.default_rng(2)
+    n, m = 8, 6
+    spec = rng.standard_normal((n, m)) + 1j * rng.standard_normal((n, m))
+    C.write_cbed(tmp_path / "d.cbed", spec, 10.0, 12.0, 50.0, 300.0)
+    raw = open(tmp_path / "d.cbed", "rb").read()
+    assert len(raw) == n * m * 8 + 160 and raw[-160:].startswith(b"~~~ ")
+    out = np.frombuffer(raw[: n * m * 8], np.float64).reshape(m, n)
+    # zero frequency at (row M/2, column N/2), as MSProject.cs:658-667 writes it
+    assert out[m // 2, n // 2] == abs(spec[0, 0]) ** 2
+    assert out[0, 0] == abs(spec[n // 2, m // 2]) ** 2
+    assert out[m // 2, n // 2 + 1] == abs(spec[1, 0]) ** 2
+    back, meta = C.read_cbed(tmp_path / "d.cbed")
+    assert np.array_equal(back, np.abs(spec) ** 2) and meta["kev"] == 300.0
+    t = np.exp(1j * rng.standard_normal((n, m))).astype(np.complex64)
+    C.write_slice(tmp_path / "s.slice", t, 3.905, 3.905, 1.9525, 7, 100, nmult=8, mmult=8)
+    tb, meta = C.read_slice(tmp_path / "s.slice")
+    assert np.array_equal(tb, t.astype(np.complex128))
+    assert meta["kev"] == -1.0 and meta["f9"] == 7 and meta["f10"] == 100 and abs(meta["a"] - 31.24) < 1e-9
+    atoms = {"x": rng.random(5), "y": rng.random(5), "z": rng.random(5) * 2, "DW": rng.random(5),
+             "ads": rng.random(5) * 0.1, "occ": np.ones(5), "type": np.arange(5, dtype=np.int32),
+             "type_": np.array([8, 8, 22, 38, 8], np.int32)}
+    C.write_slice_coo(tmp_path / "a.slice_coo", 1.9525, atoms)
+    assert len(open(tmp_path / "a.slice_coo", "rb").read()) == 4 + 8 + 5 * (6 * 8 + 2 * 4)
+    th, back = C.read_slice_coo(tmp_path / "a.slice_coo")
+    assert th == 1.9525 and all(np.array_equal(back[k], atoms[k]) for k in atoms)

@@ -75,3 +75,38 @@ def test_musli_stemshift_job(tmp_path, ctx):
     assert np.array_equal(d.reshape(3, 2, 2, 2), img)
     f, _ = read_mrc(str(tmp_path / "sto_stem_15.62A_det0.mrc"))
     assert np.allclose(f[0], img[:, :, 1, 0])
+
+
+MUSLI_PW = """<?xml version="1.0" encoding="utf-8" ?>
+<Calculation_parameters>
+  <ModelFileName>sto.coo</ModelFileName>
+  <NSlices>2</NSlices>
+  <SaveSlices>true</SaveSlices>
+  <IsSaveDiffractions>true</IsSaveDiffractions>
+  <atrad>3</atrad>
+  <ThWaves><double>7.81</double></ThWaves>
+  <N>128</N><M>128</M>
+  <E><double>200000</double></E>
+  <IniWaveType>PlaneWave</IniWaveType>
+</Calculation_parameters>
+"""
+
+
+def test_musli_planewave_job_writes_csharp_files(tmp_path, ctx):
+    from multislice_gb300 import csfiles as C
+    spec = S.srtio3(2, 2, 1)
+    S.write_coo(spec, str(tmp_path / "sto.coo"))
+    (tmp_path / "job.xml").write_text(MUSLI_PW)
+    res = jobs.run_job_file(str(tmp_path / "job.xml"))
+    back = S.read_coo(str(tmp_path / "sto.coo"))
+    v = ctx.potential(back, 128, 128, 2, 3.0)
+    t = ctx.transmission(v, back.ax, back.by, 200.0)
+    w = ctx.multislice(t, back.cz / 2, np.arange(4) % 2, back.ax, back.by, 200.0)[0]
+    wav, meta = C.read_wav(str(tmp_path / "sto_wave_7.81A.wav"))
+    assert np.array_equal(wav, w.astype(np.complex128)) and res["checkpoints"] == [3]
+    cbed, _ = C.read_cbed(str(tmp_path / "sto_diffraction_7.81A.cbed"))
+    ref = O.kfft(w.astype(np.complex128)[None])[0]
+    assert O.rel_l2(cbed, np.abs(ref) ** 2) < 1e-5
+    assert abs(cbed.sum() - (128 * 128) ** 2 * np.mean(np.abs(w) ** 2)) < 1e-4 * cbed.sum()   # Parseval
+    sl, meta = C.read_slice(str(tmp_path / "Slice stack" / "Slice_0001.slice"))
+    assert np.array_equal(sl, t[1].astype(np.complex128)) and meta["f9"] == 1 and meta["f10"] == 2
