@@ -28,6 +28,7 @@
 
 #include "cfpix.hpp"
 #include "slicelib.hpp"
+#include "floatTIFF.hpp"
 
 extern double **fparams;   // slicelib.cpp:138
 extern int feTableRead;    // slicelib.cpp:137
@@ -317,6 +318,39 @@ int kref_stem(int nx, int ny, double ax, double by, double v0, int nlayer,
     }
     kfree(S);
     return 0;
+}
+
+// floatTIFF round trip: the reference's own reader and writer of Kirkland's
+// TIFF files (floatTIFF.cpp:324-350, :1263-1840).  data is [ny][nx] (row iy,
+// column ix); params holds PMAX = 512 floats.
+int kref_tiff_write(const char *path, const float *data, int nx, int ny, int npix, const float *params,
+                    float rmin, float rmax, float imin, float imax, float dx, float dy) {
+    floatTIFF f;
+    f.resize(nx, ny);
+    f.setnpix(npix);
+    for (int i = 0; i < f.maxParam(); ++i) f.setParam(i, params[i]);
+    for (int iy = 0; iy < ny; ++iy)
+        for (int ix = 0; ix < nx; ++ix) f(ix, iy) = data[(size_t)iy * nx + ix];
+    return f.write(path, rmin, rmax, imin, imax, dx, dy);
+}
+
+int kref_tiff_read(const char *path, float *data, int cap, int *nx, int *ny, int *npix, float *params) {
+    floatTIFF f;
+    const int rc = f.read(path);
+    if (rc != 1) return rc;
+    *nx = f.nx();
+    *ny = f.ny();
+    *npix = f.getnpix();
+    for (int i = 0; i < f.maxParam(); ++i) params[i] = f.getParam(i);
+    if ((long)(*nx) * (*ny) > cap) return -100;
+    for (int iy = 0; iy < *ny; ++iy)
+        for (int ix = 0; ix < *nx; ++ix) data[(size_t)iy * (*nx) + ix] = f(ix, iy);
+    return 1;
+}
+
+// The reference's stacking-sequence parser (slicelib.cpp:620-720).
+int kref_parlay(const char *c, int *islice, int nsmax, int lmax, int *nslice) {
+    return parlay(c, islice, nsmax, lmax, nslice, 0);
 }
 
 }  // extern "C"

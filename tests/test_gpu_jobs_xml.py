@@ -110,3 +110,29 @@ def test_musli_planewave_job_writes_csharp_files(tmp_path, ctx):
     assert abs(cbed.sum() - (128 * 128) ** 2 * np.mean(np.abs(w) ** 2)) < 1e-4 * cbed.sum()   # Parseval
     sl, meta = C.read_slice(str(tmp_path / "Slice stack" / "Slice_0001.slice"))
     assert np.array_equal(sl, t[1].astype(np.complex128)) and meta["f9"] == 1 and meta["f10"] == 2
+
+
+def test_kirkland_mulslice_from_tiff_layers(tmp_path, ctx):
+    """Layer potentials as floatTIFF files (vz with phase lambda mm0 vz) and a
+    stacking sequence -> exit wave TIFF, against the direct library calls."""
+    from multislice_gb300 import floattiff as FT, kirkland as K
+    spec = S.si_diamond(2, 2, 1)
+    v = ctx.potential(spec, 64, 64, 2, 3.0)
+    kev = 200.0
+    f32 = np.float32
+    scale = f32(f32(O.wavelength(kev)) * (f32(1.0) + f32(kev) / f32(511.0)))
+    files = []
+    for i in range(2):
+        vz = (v[i].astype(np.float64) * O.sigma(kev) / float(scale)).astype(np.float32)
+        par = np.zeros(512, np.float32)
+        par[FT.P["C"]] = spec.cz / 2
+        par[FT.P["DX"]], par[FT.P["DY"]] = spec.ax / 64, spec.by / 64
+        FT.write_float_tiff(tmp_path / f"l{i}.tif", vz, params=par, dx=spec.ax / 64, dy=spec.by / 64)
+        files.append(str(tmp_path / f"l{i}.tif"))
+    w, seq = K.mulslice(ctx, files, "6(ab)", kev, str(tmp_path / "w.tif"))
+    assert seq == [0, 1] * 6
+    back, par = FT.read_exit_wave(str(tmp_path / "w.tif"))
+    assert np.array_equal(back, w) and par[FT.P["NSLICES"]] == 12
+    t = ctx.transmission(v, spec.ax, spec.by, kev)
+    ref = ctx.multislice(t, spec.cz / 2, seq, spec.ax, spec.by, kev)[0]
+    assert O.rel_l2(back, ref) < 2e-6
