@@ -212,6 +212,30 @@ template <class P> struct RowXorAddr {
     float2 *base;
     __device__ __forceinline__ int operator()(int i) const { return i ^ ((i >> P::row_sh) & 15); }
 };
+// Contiguous lines addressed through 32-bit shared addresses.  The slot map
+// f(i) = i ^ ((i >> sh) & 15) (the RowXorAddr layout) is linear over xor:
+// f(a ^ b) = f(a) ^ f(b).  An exchange index splits into a thread part and a
+// compile-time part with disjoint bits, i = T | K, so with the line buffer
+// aligned to its own size (a power of two) the byte address of slot i is
+// (base + 8 f(T)) ^ 8 f(K): one xor with an immediate per access, the
+// thread parts computed once per exchange.  Same layout, same bank behaviour
+// as RowXorAddr.
+template <class P> struct RowXorLin {
+    uint32_t base;  // shared address of the line, aligned to N * 8 bytes
+    static __host__ __device__ constexpr int f(int i) { return i ^ ((i >> P::row_sh) & 15); }
+};
+template <class A> struct is_xor_lin { static constexpr bool value = false; };
+template <class P> struct is_xor_lin<RowXorLin<P>> { static constexpr bool value = true; };
+
+__device__ __forceinline__ void sts_f2(uint32_t addr, float2 v) {
+    asm volatile("st.shared.v2.f32 [%0], {%1, %2};" ::"r"(addr), "f"(v.x), "f"(v.y) : "memory");
+}
+__device__ __forceinline__ float2 lds_f2(uint32_t addr) {
+    float2 v;
+    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(addr) : "memory");
+    return v;
+}
+
 // Column tiles: C interleaved columns, slot = perm(i) * C + c.
 template <class P> struct ColAddr {
     float2 *base;
@@ -222,6 +246,27 @@ template <class P> struct ColAddr {
         else return (i ^ ((i >> P::col_ps) & (16 / C - 1))) * C + c;
     }
 };
+
+// Column tiles addressed through 32-bit shared addresses: slot = g(i) * C + c
+// with g(i) = i ^ ((i >> ps) & M) (the ColAddr layout, M = 16/C - 1 or none).
+// g is linear over xor, so for an exchange index i = T | K (thread part T,
+// compile-time part K, disjoint bits) g(i) = g(T) ^ g(K).  Split g(K) into O,
+// its bits inside the range of g(T) (always within the M bits), and the rest:
+// g(i) = (g(T) ^ O) + (g(K) ^ O), two disjoint terms.  Each thread keeps one
+// base per value of O (M + 1 of them), so every access is base + immediate.
+template <class P> struct ColXorLin {
+    uint32_t base;  // shared address of the tile plus 8 c
+    static constexpr int C = P::col_c;
+    static constexpr int M = (C >= 16 || P::col_ps >= 30) ? 0 : 16 / C - 1;
+    static __host__ __device__ constexpr int g(int i) { return M ? i ^ ((i >> P::col_ps) & M) : i; }
+};
+template <class A> struct is_col_lin { static constexpr bool value = false; };
+template <class P> struct is_col_lin<ColXorLin<P>> { static constexpr bool value = true; };
+
+// Bits g(T) can occupy when T ranges over [0, 2^tb) shifted left by ts bits.
+template <class P> __host__ __device__ constexpr int col_lin_mask(int tbits_mask) {
+    return tbits_mask | ColXorLin<P>::M;
+}
 
 // ------------------------------------------------------------ the transform
 // tw: this plan's stage tables (exp(+2 pi i r k / (NS R)) at [r][k]).
@@ -268,12 +313,80 @@ __device__ __forceinline__ void fft_exchange(float2 (&v)[P::E], int t, const Add
     for (int e = 0; e < E; ++e) v[e] = ad.base[ad(t + T * e)];
 }
 
+// The same exchange on RowXorLin addressing (warp-owned lines, power-of-two
+// radices and spans).  Write index of (q, r): with j = t + T q,
+// i = (j / NS) NS R + j % NS + r NS, i.e. T-part (t / NS) NS R + t % NS and
+// K-part T R q + NS r when NS <= T; T-part t and K-part
+// (q / (NS/T)) NS R + T (q % (NS/T)) + NS r when NS > T.  Read index t + T e.
+template <class P, int S>
+__device__ __forceinline__ void fft_exchange_xl(float2 (&v)[P::E], int t, const RowXorLin<P> &ad) {
+    constexpr int R = P::radix(S), NS = plan_span<P>(S), E = P::E, Q = E / R, T = P::T;
+    static_assert(T == 32 && (NS & (NS - 1)) == 0 && (R & (R - 1)) == 0 && (P::N & (P::N - 1)) == 0,
+                  "xor-linear exchange needs warp-owned lines and power-of-two radices");
+    using F = RowXorLin<P>;
+    const int tw_part = NS <= T ? (t / NS) * NS * R + t % NS : t;
+    const uint32_t wb = ad.base + 8u * (uint32_t)F::f(tw_part);
+    const uint32_t rb = ad.base + 8u * (uint32_t)F::f(t);
+    __syncwarp();  // previous readers are done
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int K = NS <= T ? q * T * R + r * NS : (q / (NS / T)) * NS * R + T * (q % (NS / T)) + r * NS;
+            sts_f2(wb ^ (8u * (uint32_t)F::f(K)), v[q + r * Q]);
+        }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int e = 0; e < E; ++e) v[e] = lds_f2(rb ^ (8u * (uint32_t)F::f(T * e)));
+}
+
+// The column exchange on ColXorLin addressing (T threads per column spread
+// over the CTA, so CTA barriers; power-of-two T, radices and spans).  Index
+// split as in fft_exchange_xl.
+template <class P, int S>
+__device__ __forceinline__ void fft_exchange_cl(float2 (&v)[P::E], int t, const ColXorLin<P> &ad) {
+    constexpr int R = P::radix(S), NS = plan_span<P>(S), E = P::E, Q = E / R, T = P::T, C = P::col_c;
+    static_assert((T & (T - 1)) == 0 && (NS & (NS - 1)) == 0 && (R & (R - 1)) == 0 && (P::N & (P::N - 1)) == 0,
+                  "xor-linear column exchange needs power-of-two sizes");
+    using G = ColXorLin<P>;
+    constexpr int NB = G::M + 1;
+    // write pattern: thread part and the bits it can occupy
+    const int tw_part = NS <= T ? (t / NS) * NS * R + t % NS : t;
+    constexpr int WMASK = col_lin_mask<P>(NS <= T ? ((T / NS - 1) * NS * R) | (NS - 1) : (T - 1));
+    constexpr int RMASK = col_lin_mask<P>(T - 1);
+    uint32_t wb[NB], rb[NB];
+#pragma unroll
+    for (int o = 0; o < NB; ++o) {
+        wb[o] = ad.base + 8u * C * (uint32_t)(G::g(tw_part) ^ o);
+        rb[o] = ad.base + 8u * C * (uint32_t)(G::g(t) ^ o);
+    }
+    __syncthreads();  // previous readers are done
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int K = NS <= T ? q * T * R + r * NS : (q / (NS / T)) * NS * R + T * (q % (NS / T)) + r * NS;
+            const int gk = G::g(K), o = gk & WMASK;
+            sts_f2(wb[o] + 8u * C * (uint32_t)(gk ^ o), v[q + r * Q]);
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+        const int gk = G::g(T * e), o = gk & RMASK;
+        v[e] = lds_f2(rb[o] + 8u * C * (uint32_t)(gk ^ o));
+    }
+}
+
 template <class P, int DIR, int S = 0, bool WARP = false, class Addr>
 __device__ __forceinline__ void fft_line(float2 (&v)[P::E], int t, const Addr &ad,
                                          const float2 *__restrict__ tw) {
     fft_stage<P, S, DIR>(v, t, tw);
     if constexpr (S + 1 < P::NSTAGE) {
-        fft_exchange<P, S, WARP>(v, t, ad);
+        if constexpr (is_xor_lin<Addr>::value) fft_exchange_xl<P, S>(v, t, ad);
+        else if constexpr (is_col_lin<Addr>::value) fft_exchange_cl<P, S>(v, t, ad);
+        else fft_exchange<P, S, WARP>(v, t, ad);
         fft_line<P, DIR, S + 1, WARP>(v, t, ad, tw);
     }
 }

@@ -10,6 +10,7 @@
 // probe-slice), and every pointwise step of the reference runs in registers
 // between two line transforms.  Kirkland's 1/(nx ny) ifft scale rides in py.
 #include <cuda_runtime.h>
+#include <type_traits>
 #include <math.h>
 #include <stdint.h>
 
@@ -234,6 +235,11 @@ __global__ void __launch_bounds__(ColCfg<N>::THREADS) col_pass_kernel(ColArgs a)
 // waits (bounded) for its loads still in flight and leaves.
 constexpr uint32_t kWaitLimit = 1u << 22;
 
+template <class A> __device__ __forceinline__ A make_col_addr(float2 *bs, int c) {
+    if constexpr (is_col_lin<A>::value) return A{smem_u32(bs) + 8u * (uint32_t)c};
+    else return A{bs, c};
+}
+
 template <class PL> struct ColTmaCfg {
     using P = PL;
     static constexpr int N = P::N;
@@ -291,7 +297,8 @@ __global__ void __launch_bounds__(ColTmaCfg<PL>::THREADS, MINB)
         const int tile = blockIdx.x + k * gridDim.x, b = tile / tpi, ty = tile % tpi;
         const int iy = ty * C + c, s = k % NBUF;
         float2 *bs = buf0 + (size_t)s * N * C;
-        ColAddr<P> ad{bs, c};
+        using Addr = typename std::conditional<(N & (N - 1)) == 0, ColXorLin<P>, ColAddr<P>>::type;
+        Addr ad = make_col_addr<Addr>(bs, c);
         float2 v[E];
         if (!load && store && tid == 0) tma_wait_read<NBUF - 1>();  // store of tile k-3 left bs
         if (load) {
@@ -477,14 +484,29 @@ __global__ void __launch_bounds__(RowTmaCfg<N, TH>::THREADS, MINB)
 // through that ring with warp-level synchronisation only.  No CTA-wide barrier
 // runs after the prologue, so a warp waiting on its exchange or its next line
 // never holds up the others.
+template <class A> __device__ __forceinline__ A make_row_addr(float2 *buf);
+template <> __device__ __forceinline__ RowXorLin<WarpPlan<256>> make_row_addr(float2 *buf) {
+    return RowXorLin<WarpPlan<256>>{smem_u32(buf)};
+}
+template <> __device__ __forceinline__ RowXorLin<WarpPlan<512>> make_row_addr(float2 *buf) {
+    return RowXorLin<WarpPlan<512>>{smem_u32(buf)};
+}
+template <> __device__ __forceinline__ RowXorAddr<WarpPlan<384>> make_row_addr(float2 *buf) {
+    return RowXorAddr<WarpPlan<384>>{buf};
+}
+
 template <int N> struct RowWarpCfg {
     using P = WarpPlan<N>;
     static constexpr int W = 8, THREADS = 32 * W, NBUF = 3;
     static constexpr int MINB = P::E <= 8 ? 3 : 2;
     static constexpr size_t LINE = sizeof(float2) * N;
+    // power-of-two sides address their exchanges xor-linearly (RowXorLin), which
+    // needs every line buffer aligned to its size
+    static constexpr bool XL = (N & (N - 1)) == 0;
+    static constexpr uint32_t ALIGN = XL ? (uint32_t)LINE : 128u;
     static constexpr size_t OFF_TW = (size_t)W * NBUF * LINE;
     static constexpr size_t OFF_BAR = OFF_TW + ((sizeof(float2) * plan_tw_size<P>() + 15) / 16) * 16;
-    static constexpr size_t SMEM = OFF_BAR + sizeof(uint64_t) * W * NBUF + 128;
+    static constexpr size_t SMEM = OFF_BAR + sizeof(uint64_t) * W * NBUF + ALIGN;
 };
 
 template <int N>
@@ -492,8 +514,9 @@ __global__ void __launch_bounds__(RowWarpCfg<N>::THREADS, RowWarpCfg<N>::MINB) r
     using Cfg = RowWarpCfg<N>;
     using P = WarpPlan<N>;
     constexpr int E = P::E, NBUF = Cfg::NBUF, W = Cfg::W, TW = plan_tw_size<P>();
+    constexpr uint32_t AL = Cfg::ALIGN;
     extern __shared__ unsigned char smraw[];
-    unsigned char *base = smraw + ((128u - (smem_u32(smraw) & 127u)) & 127u);
+    unsigned char *base = smraw + ((AL - (smem_u32(smraw) & (AL - 1u))) & (AL - 1u));
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     float2 *ring = reinterpret_cast<float2 *>(base) + (size_t)warp * NBUF * N;
     float2 *tw = reinterpret_cast<float2 *>(base + Cfg::OFF_TW);
@@ -522,7 +545,8 @@ __global__ void __launch_bounds__(RowWarpCfg<N>::THREADS, RowWarpCfg<N>::MINB) r
     for (; k < nmine; ++k) {
         const int line = gw + k * G, s = k % NBUF;
         float2 *buf = ring + (size_t)s * N;
-        RowXorAddr<P> ad{buf};
+        using Addr = typename std::conditional<Cfg::XL, RowXorLin<P>, RowXorAddr<P>>::type;
+        Addr ad = make_row_addr<Addr>(buf);
         float2 tr[E];
         if (a.flags & ROW_TRANS) {
             const float2 *trow = (a.trans_b ? a.trans_b[line / a.nx] : a.trans) + (size_t)(line % a.nx) * N;
