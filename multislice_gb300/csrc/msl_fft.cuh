@@ -63,7 +63,7 @@ template <> struct ColPlan<64> : ColPlanT<64, 8, 16, 30, 4> {};
 template <> struct ColPlan<128> : ColPlanT<128, 16, 16, 30, 2> {};
 template <> struct ColPlan<256> : ColPlanT<256, 32, 8, 3, 2> {};
 template <> struct ColPlan<384> : ColPlanT<384, 32, 8, 30, 2> {};
-template <> struct ColPlan<512> : ColPlanT<512, 32, 8, 3, 2> {};
+template <> struct ColPlan<512> : ColPlanT<512, 32, 4, 3, 4> {};
 template <> struct ColPlan<768> : ColPlanT<768, 64, 4, 30, 2> {};
 template <> struct ColPlan<1024> : ColPlanT<1024, 64, 8, 4, 1> {};
 template <> struct ColPlan<2048> : ColPlanT<2048, 128, 4, 4, 1> {};
