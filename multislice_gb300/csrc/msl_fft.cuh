@@ -294,6 +294,39 @@ __device__ __forceinline__ void fft_stage(float2 (&v)[P::E], int t, const float2
     }
 }
 
+// The same stage with the twiddles w^r, r = 2..R-1, formed in registers from
+// the table's w^1 (one shared load per distinct k instead of R - 1): w^r =
+// w^(r/2) w^(r - r/2), at most three products deep.  Trades shared-memory
+// bandwidth, which bounds the line transforms, for FMA work.
+template <class P, int S, int DIR>
+__device__ __forceinline__ void fft_stage_cw(float2 (&v)[P::E], int t, const float2 *__restrict__ tw) {
+    constexpr int R = P::radix(S), NS = plan_span<P>(S), E = P::E, Q = E / R, T = P::T;
+    const float2 *tws = tw + plan_tw_offset<P>(S);
+    constexpr bool SHARED_K = NS > 1 && T % NS == 0;  // every q of a thread has the same k
+    float2 w[R];
+    auto powers = [&](int k) {
+        w[1] = tws[NS + k];
+        if constexpr (DIR < 0) w[1].y = -w[1].y;
+#pragma unroll
+        for (int r = 2; r < R; ++r) w[r] = c_mul(w[r / 2], w[r - r / 2]);
+    };
+    if constexpr (SHARED_K) powers(t % NS);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        float2 a[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) a[r] = v[q + r * Q];
+        if constexpr (NS > 1) {
+            if constexpr (!SHARED_K) powers((t + T * q) % NS);
+#pragma unroll
+            for (int r = 1; r < R; ++r) a[r] = c_mul(a[r], w[r]);
+        }
+        dft<R, DIR>(a);
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[q + r * Q] = a[r];
+    }
+}
+
 // WARP = true: the line belongs to one warp (T == 32) and the exchange needs
 // only warp-level synchronisation.
 template <class P, int S, bool WARP = false, class Addr>
@@ -382,7 +415,8 @@ __device__ __forceinline__ void fft_exchange_cl(float2 (&v)[P::E], int t, const 
 template <class P, int DIR, int S = 0, bool WARP = false, class Addr>
 __device__ __forceinline__ void fft_line(float2 (&v)[P::E], int t, const Addr &ad,
                                          const float2 *__restrict__ tw) {
-    fft_stage<P, S, DIR>(v, t, tw);
+    if constexpr (is_xor_lin<Addr>::value) fft_stage_cw<P, S, DIR>(v, t, tw);
+    else fft_stage<P, S, DIR>(v, t, tw);
     if constexpr (S + 1 < P::NSTAGE) {
         if constexpr (is_xor_lin<Addr>::value) fft_exchange_xl<P, S>(v, t, ad);
         else if constexpr (is_col_lin<Addr>::value) fft_exchange_cl<P, S>(v, t, ad);
