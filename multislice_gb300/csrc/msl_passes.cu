@@ -497,8 +497,8 @@ template <> __device__ __forceinline__ RowXorAddr<WarpPlan<384>> make_row_addr(f
 
 template <int N> struct RowWarpCfg {
     using P = WarpPlan<N>;
-    static constexpr int W = 8, THREADS = 32 * W, NBUF = 3;
-    static constexpr int MINB = P::E <= 8 ? 3 : 2;
+    static constexpr int W = 8, THREADS = 32 * W, NBUF = N == 512 ? 2 : 3;
+    static constexpr int MINB = N == 512 ? 3 : P::E <= 8 ? 3 : 2;
     static constexpr size_t LINE = sizeof(float2) * N;
     // power-of-two sides address their exchanges xor-linearly (RowXorLin), which
     // needs every line buffer aligned to its size
@@ -547,13 +547,18 @@ __global__ void __launch_bounds__(RowWarpCfg<N>::THREADS, RowWarpCfg<N>::MINB) r
         float2 *buf = ring + (size_t)s * N;
         using Addr = typename std::conditional<Cfg::XL, RowXorLin<P>, RowXorAddr<P>>::type;
         Addr ad = make_row_addr<Addr>(buf);
-        float2 tr[E];
-        if (a.flags & ROW_TRANS) {
-            const float2 *trow = (a.trans_b ? a.trans_b[line / a.nx] : a.trans) + (size_t)(line % a.nx) * N;
-#pragma unroll
-            for (int e = 0; e < E; ++e) tr[e] = __ldg(trow + lane + 32 * e);
+        const float2 *trow = (a.flags & ROW_TRANS)
+                                 ? (a.trans_b ? a.trans_b[line / a.nx] : a.trans) + (size_t)(line % a.nx) * N
+                                 : nullptr;
+        if (!load && store && lane == 0) tma_wait_read<NBUF - 1>();  // the store of line k-NBUF left buf
+        if constexpr (NBUF == 2) {
+            // two buffers: the next line goes into the buffer of line k-1 as soon as
+            // that line's store has read it, so it loads while line k is transformed
+            if (load && lane == 0 && k + 1 < nmine) {
+                if (store) tma_wait_read<0>();
+                issue(k + 1);
+            }
         }
-        if (!load && store && lane == 0) tma_wait_read<NBUF - 1>();  // the store of line k-3 left buf
         float2 v[E];
         if (load) {
             const bool got = mbar_wait_bounded(&bar[s], (uint32_t)((k / NBUF) & 1), kWaitLimit);
@@ -570,7 +575,7 @@ __global__ void __launch_bounds__(RowWarpCfg<N>::THREADS, RowWarpCfg<N>::MINB) r
         if (a.flags & ROW_INV) fft_line<P, -1, 0, true>(v, lane, ad, tw);
         if (a.flags & ROW_TRANS) {
 #pragma unroll
-            for (int e = 0; e < E; ++e) v[e] = c_mul(v[e], tr[e]);
+            for (int e = 0; e < E; ++e) v[e] = c_mul(v[e], __ldg(trow + lane + 32 * e));
         }
         if (a.flags & ROW_FWD) fft_line<P, +1, 0, true>(v, lane, ad, tw);
         if (a.scale != 1.0f) {
@@ -594,9 +599,11 @@ __global__ void __launch_bounds__(RowWarpCfg<N>::THREADS, RowWarpCfg<N>::MINB) r
                 tma_commit();
             }
         }
-        if (load && lane == 0 && k + NBUF - 1 < nmine) {
-            if (store) tma_wait_read<1>();  // the store of line k-1 has left its buffer
-            issue(k + NBUF - 1);            // into buffer (k + 2) % 3
+        if constexpr (NBUF == 3) {
+            if (load && lane == 0 && k + NBUF - 1 < nmine) {
+                if (store) tma_wait_read<1>();  // the store of line k-1 has left its buffer
+                issue(k + NBUF - 1);            // into buffer (k + 2) % 3
+            }
         }
         __syncwarp();
     }
