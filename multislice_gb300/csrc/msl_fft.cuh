@@ -50,9 +50,9 @@ MSL_PLAN(768,  64, 5,  3,  4, 4, 4, 4,  0,  5,  8, 3)
 // Column-pass plan of the TMA-fed kernel: same radices (and so the same twiddle
 // tables) as Plan<N>, its own threads per line T, columns per tile C, exchange
 // row permutation shift PS (>= 30: none) and CTAs per SM the registers allow.
-template <int N_, int T_, int C_, int PS_, int MINB_> struct ColPlanT {
+template <int N_, int T_, int C_, int PS_, int MINB_, int NBUF_ = 3> struct ColPlanT {
     using B = Plan<N_>;
-    static constexpr int N = N_, T = T_, E = N_ / T_, NSTAGE = B::NSTAGE, MINB = MINB_;
+    static constexpr int N = N_, T = T_, E = N_ / T_, NSTAGE = B::NSTAGE, MINB = MINB_, NBUF = NBUF_;
     static constexpr int row_swz = B::row_swz, row_sh = B::row_sh;
     static constexpr int col_c = C_, col_ps = PS_;
     static constexpr int radix(int s) { return B::radix(s); }

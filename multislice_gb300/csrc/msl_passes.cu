@@ -244,7 +244,8 @@ template <class PL> struct ColTmaCfg {
     using P = PL;
     static constexpr int N = P::N;
     static constexpr int C = P::col_c, T = P::T, THREADS = T * C, NWARP = THREADS / 32;
-    static constexpr int NBUF = 3;
+    static constexpr int NBUF = P::NBUF;
+    static_assert(NBUF == 2 || NBUF == 3, "tile ring of two or three buffers");
     // rows per TMA box: the largest divisor of N not above 256 (the box limit)
     static constexpr int BOXR = N <= 256 ? N : (N % 256 == 0 ? 256 : N / 2), NBOX = N / BOXR;
     static_assert(BOXR <= 256 && BOXR * NBOX == N, "TMA boxes must tile the column");
@@ -300,12 +301,21 @@ __global__ void __launch_bounds__(ColTmaCfg<PL>::THREADS, MINB)
         using Addr = typename std::conditional<(N & (N - 1)) == 0, ColXorLin<P>, ColAddr<P>>::type;
         Addr ad = make_col_addr<Addr>(bs, c);
         float2 v[E];
-        if (!load && store && tid == 0) tma_wait_read<NBUF - 1>();  // store of tile k-3 left bs
+        if (!load && store && tid == 0) tma_wait_read<NBUF - 1>();  // store of tile k-NBUF left bs
         if (load) {
             const bool got = mbar_wait_bounded(&bar[s], (uint32_t)((k / NBUF) & 1), kWaitLimit);
             if (__syncthreads_or(!got)) {
                 ok = false;
                 break;
+            }
+            if constexpr (NBUF == 2) {
+                // two buffers: tile k+1 goes into the buffer of tile k-1 once every
+                // thread is past it (the barrier above) and its store has read it,
+                // so it loads while tile k is transformed
+                if (tid == 0 && k + 1 < nmine) {
+                    if (store) tma_wait_read<0>();
+                    issue_load(k + 1);
+                }
             }
 #pragma unroll
             for (int e = 0; e < E; ++e) v[e] = bs[(t + T * e) * C + c];
@@ -333,9 +343,11 @@ __global__ void __launch_bounds__(ColTmaCfg<PL>::THREADS, MINB)
                 tma_commit();
             }
         }
-        if (load && tid == 0 && k + NBUF - 1 < nmine) {
-            if (store) tma_wait_read<1>();  // the store of tile k-1 has left its buffer
-            issue_load(k + NBUF - 1);       // into buffer (k + 2) % 3 == (k - 1) % 3
+        if constexpr (NBUF == 3) {
+            if (load && tid == 0 && k + NBUF - 1 < nmine) {
+                if (store) tma_wait_read<1>();  // the store of tile k-1 has left its buffer
+                issue_load(k + NBUF - 1);       // into buffer (k + 2) % 3 == (k - 1) % 3
+            }
         }
     }
     if (tid == 0) {
