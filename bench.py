@@ -199,7 +199,7 @@ def run_ours(args):
         tt = torch.tensor([e_el], dtype=torch.float64, device=dev)
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         e_el = float(tt.item())
-    e2e_value = units / e_el
+    e2e_value = units / e_el if e_el == e_el else None   # None (JSON null) with --no-e2e
     h2d = spec.natom * (3 * 8 + 4) + 104 * 12 * 8 + nprobe * 2 * 8
     d2h = res_host.nbytes
 
