@@ -14,6 +14,10 @@ Two formats exist in the reference:
   STEMshift), BeamShift, ConvAngles and DetectorAngles (1/A, outer then inner),
   Df, Cs (A), ThWaves (thickness checkpoints, A).  The unit cell is repeated
   along the beam until the last checkpoint (MSReuseCalculator.cs:36-92).
+  IniWaveType Precalculated resumes from a saved .wav (IniWaveFileName): its
+  trailer must match the cell (a, b, gamma within 1e-5) and the grid, and sets
+  the energy and the start thickness; the checkpoints stay absolute
+  (MSProject.cs:423-440, MSProjectReuse.cs:337).
   Results are written in the driver's own formats (csfiles.py) and as MRC:
   .wav exit waves (IsSaveWaves, default on), .cbed diffraction patterns
   (IsSaveDiffractions), .stem images, and the slices' phase gratings as .slice
@@ -27,6 +31,7 @@ ModelSimulated.cu / kernel.cu:86-92).
 """
 from __future__ import annotations
 
+import math
 import os
 import xml.etree.ElementTree as ET
 
@@ -34,7 +39,7 @@ import numpy as np
 
 from . import specimen as S
 from .api import Context, wavelength
-from .csfiles import write_cbed, write_slice, write_stem, write_wav
+from .csfiles import read_wav, write_cbed, write_slice, write_stem, write_wav
 from .mrc import write_mrc
 
 
@@ -130,12 +135,20 @@ def run_musli(root, base_dir, ctx):
     kev = E[0] / 1000.0
     ths = _doubles(root, "ThWaves") or [spec.cz]
     kind = _f(root, "IniWaveType", "PlaneWave", cast=str)
+    start_wave, start_th = None, 0.0
+    if kind == "Precalculated":
+        start_wave, meta = read_wav(_resolve(base_dir, _f(root, "IniWaveFileName", cast=str)))
+        if (abs(meta["a"] - spec.ax) > 1e-5 or abs(meta["b"] - spec.by) > 1e-5
+                or abs(meta["gamma"] - math.pi / 2) > 1e-5 or (meta["n"], meta["m"]) != (nx, ny)):
+            raise ValueError("parameters of the preloaded initial wave do not fit those of the model")
+        kev = meta["kev"]
+        start_th = meta["f9"]
     df = (_doubles(root, "Df") or [0.0])[0]
     cs = (_doubles(root, "Cs") or [0.0])[0]
     dz = spec.cz / nsl
     v = ctx.potential(spec, nx, ny, nsl, radius)
     t = ctx.transmission(v, spec.ax, spec.by, kev)
-    seq, cps = _slices_to(ths, dz, nsl)
+    seq, cps = _slices_to([max(th - start_th, 0.0) for th in ths], dz, nsl)
     results = {"checkpoints": cps, "thickness": ths}
     if _bool(root, "SaveSlices", False):
         sdir = os.path.join(os.path.dirname(stem), "Slice stack")
@@ -165,7 +178,13 @@ def run_musli(root, base_dir, ctx):
     save_diff = _bool(root, "IsSaveDiffractions", False)
     for ic, th in enumerate(ths):
         n = cps[ic] + 1
-        if kind == "Converged":
+        if start_wave is not None:
+            if th <= start_th + 1e-9:          # already reached: the loaded wave itself
+                w = start_wave.astype(np.complex64)
+            else:
+                psi = np.ascontiguousarray(start_wave.astype(np.complex64)[None])
+                w = ctx.multislice(t, dz, seq[:n], spec.ax, spec.by, kev, psi=psi)[0]
+        elif kind == "Converged":
             conv = _pairs(root, "ConvAngles")[0]
             x, y = _pairs(root, "BeamShift")[0]
             job = dict(trans=t, ax=spec.ax, by=spec.by, kev=kev, dz=dz, layer_seq=seq[:n],

@@ -136,3 +136,41 @@ def test_kirkland_mulslice_from_tiff_layers(tmp_path, ctx):
     t = ctx.transmission(v, spec.ax, spec.by, kev)
     ref = ctx.multislice(t, spec.cz / 2, seq, spec.ax, spec.by, kev)[0]
     assert O.rel_l2(back, ref) < 2e-6
+
+
+def _musli_job(kind, ths, extra=""):
+    return f"""<?xml version="1.0" encoding="utf-8" ?>
+<Calculation_parameters>
+  <ModelFileName>sto.coo</ModelFileName>
+  <NSlices>2</NSlices>
+  <atrad>3</atrad>
+  <ThWaves>{''.join(f'<double>{t}</double>' for t in ths)}</ThWaves>
+  <N>128</N><M>128</M>
+  <E><double>200000</double></E>
+  <IniWaveType>{kind}</IniWaveType>{extra}
+</Calculation_parameters>
+"""
+
+
+def test_musli_precalculated_wave_resumes_the_run(tmp_path, ctx):
+    """Checkpoint / resume: a run stopped at 7.81 A and continued from its .wav
+    equals the uninterrupted run to 15.62 A (MSProject.cs:423-440)."""
+    from multislice_gb300 import csfiles as C
+    S.write_coo(S.srtio3(2, 2, 2), str(tmp_path / "sto.coo"))
+    ax = S.read_coo(str(tmp_path / "sto.coo")).ax
+    (tmp_path / "a.xml").write_text(_musli_job("PlaneWave", [7.81]))
+    jobs.run_job_file(str(tmp_path / "a.xml"))
+    (tmp_path / "b.xml").write_text(_musli_job("Precalculated", [15.62],
+                                               "\n  <IniWaveFileName>sto_wave_7.81A.wav</IniWaveFileName>"))
+    resumed = jobs.run_job_file(str(tmp_path / "b.xml"))["waves"][0]
+    (tmp_path / "c.xml").write_text(_musli_job("PlaneWave", [15.62]))
+    whole = jobs.run_job_file(str(tmp_path / "c.xml"))["waves"][0]
+    assert O.rel_l2(resumed, whole) < 1e-6
+    _, meta = C.read_wav(str(tmp_path / "sto_wave_15.62A.wav"))
+    assert meta["f9"] == 15.62
+    # a start wave on another grid is refused before any work
+    C.write_wav(str(tmp_path / "bad.wav"), np.ones((64, 64), np.complex64), ax, ax, 7.81, 200.0)
+    (tmp_path / "d.xml").write_text(_musli_job("Precalculated", [15.62],
+                                               "\n  <IniWaveFileName>bad.wav</IniWaveFileName>"))
+    with pytest.raises(ValueError):
+        jobs.run_job_file(str(tmp_path / "d.xml"))
