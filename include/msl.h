@@ -300,6 +300,16 @@ int msl_check_wait_timeout(msl_ctx *ctx, uint32_t polls);
  * sized batch * nx * ny * 8 bytes. */
 int msl_set_probe_batch(msl_ctx *ctx, int batch);
 
+/* Cap on the device memory the context keeps in its work buffers (0 = none,
+ * the default), for GPUs shared with other work.  A call whose buffers would
+ * grow past the cap returns MSL_E_NOMEM before it frees or allocates anything
+ * and leaves the context usable; the automatic probe batch of msl_stem_scan
+ * shrinks to half the cap.  Caller-owned buffers are not counted.  The
+ * reference has no counterpart (its buffers are sized by the calculation). */
+int msl_set_memory_limit(msl_ctx *ctx, size_t bytes);
+/* Bytes the context's work buffers hold now. */
+int msl_memory_in_use(msl_ctx *ctx, size_t *bytes);
+
 /* ------------------------------------------------- Muslib-shaped exports */
 
 /* The reference's native STEM library (Musli console 1.3 (STEM) 2/Muslib) with

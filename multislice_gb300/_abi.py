@@ -23,7 +23,8 @@ EXPORTS = (
     "msl_transmission_build", "msl_fft2d", "msl_multislice", "msl_stem_scan",
     "msl_set_probe_batch", "msl_profile_enable", "msl_profile_read", "msl_multislice_noalloc",
     "msl_ctem_image", "msl_phonon_displacements", "msl_frozen_phonon", "msl_coo_parse",
-    "msl_run_jobs", "msl_ctem_partial_coherence", "msl_check_wait_timeout",
+    "msl_run_jobs", "msl_ctem_partial_coherence", "msl_check_wait_timeout", "msl_set_memory_limit",
+    "msl_memory_in_use",
 )
 PLANE_WAVE, PROBE = 0, 1
 # Muslib-shaped exports (reference names, no msl_ prefix)
@@ -112,6 +113,8 @@ def load(path=LIB_PATH):
         "msl_stem_scan": (c_int, [P, POINTER(Grid), POINTER(Optics), P, c_int, P, P, c_int,
                                   POINTER(Probe), P, c_int, POINTER(Detectors), P, c_int, P]),
         "msl_set_probe_batch": (c_int, [P, c_int]),
+        "msl_set_memory_limit": (c_int, [P, c_size_t]),
+        "msl_memory_in_use": (c_int, [P, POINTER(c_size_t)]),
         "msl_profile_enable": (c_int, [P, c_int]),
         "msl_profile_read": (c_int, [P, c_int, POINTER(c_int64), POINTER(c_double)]),
         "msl_multislice_noalloc": (c_int, [POINTER(Grid), POINTER(Optics), P, c_int, P, P, c_int,

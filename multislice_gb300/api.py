@@ -117,6 +117,15 @@ class Context:
     def set_probe_batch(self, batch):
         self._check(self._lib.msl_set_probe_batch(self._h, int(batch)))
 
+    def set_memory_limit(self, nbytes):
+        """Cap the device memory of the context's work buffers (0: no cap)."""
+        self._check(self._lib.msl_set_memory_limit(self._h, int(nbytes)))
+
+    def memory_in_use(self):
+        n = ctypes.c_size_t(0)
+        self._check(self._lib.msl_memory_in_use(self._h, ctypes.byref(n)))
+        return n.value
+
     @staticmethod
     def _optics(kev, bandlimit=2.0 / 3.0, tilt=(0.0, 0.0), f32_prop_args=False):
         return Optics(float(kev), float(bandlimit), float(tilt[0]), float(tilt[1]),

@@ -23,20 +23,39 @@ namespace {
 
 const char kVersion[] = "msl 0.1 (sm_103a)";
 
+// Device memory held by a context's work buffers, against an optional cap
+// (msl_set_memory_limit).
+struct MemBudget {
+    size_t limit = 0;  // 0: no cap
+    size_t used = 0;
+};
+
 struct DevBuf {
     void *p = nullptr;
     size_t cap = 0;
+    MemBudget *mb = nullptr;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf() { release(); }
+    // Grow to at least `bytes`; a growth the context's cap would not allow fails
+    // before anything is freed or allocated.
     cudaError_t ensure(size_t bytes) {
         if (bytes <= cap) return cudaSuccess;
-        if (p) cudaFree(p);
-        p = nullptr;
-        cap = 0;
+        if (mb && mb->limit && mb->used - cap + bytes > mb->limit) return cudaErrorMemoryAllocation;
+        release();
         cudaError_t e = cudaMalloc(&p, bytes ? bytes : 1);
-        if (e == cudaSuccess) cap = bytes;
+        if (e == cudaSuccess) {
+            cap = bytes;
+            if (mb) mb->used += bytes;
+        } else {
+            p = nullptr;
+        }
         return e;
     }
     void release() {
         if (p) cudaFree(p);
+        if (mb) mb->used -= cap;
         p = nullptr;
         cap = 0;
     }
@@ -59,9 +78,15 @@ struct msl_ctx {
     std::vector<Pending> pending;
     int64_t prof_count[MSL_PROF_KINDS] = {0};
     double prof_ms[MSL_PROF_KINDS] = {0};
+    MemBudget mem;
     DevBuf wave, in_stage, trans_stage, tabs, apchi, exy, fxy, detmask, partial, detout, pot,
         atoms, tmpw, ctf, acc, jobtab;
     int *dflag = nullptr;  // device flag raised by a kernel whose bounded wait gave up
+    msl_ctx() {
+        DevBuf *bufs[] = {&wave, &in_stage, &trans_stage, &tabs, &apchi, &exy, &fxy, &detmask,
+                          &partial, &detout, &pot, &atoms, &tmpw, &ctf, &acc, &jobtab};
+        for (DevBuf *b : bufs) b->mb = &mem;
+    }
 };
 
 namespace {
@@ -630,6 +655,7 @@ int msl_frozen_phonon(msl_ctx *c, const msl_atoms *at, const double *fparams, co
     const size_t n2 = (size_t)nx * ny;
     // device buffers: potential, transmission, wave, accumulators
     DevBuf vbuf, tbuf;
+    vbuf.mb = tbuf.mb = &c->mem;
     CUDA_TRY(c, vbuf.ensure(sizeof(float) * n2 * nslice));
     CUDA_TRY(c, tbuf.ensure(sizeof(float2) * n2 * nslice));
     CUDA_TRY(c, c->acc.ensure(2 * sizeof(double) * n2));
@@ -947,6 +973,18 @@ int msl_check_wait_timeout(msl_ctx *c, uint32_t polls) {
     CUDA_TRY(c, cudaMemcpy(&h, c->dflag, sizeof(int), cudaMemcpyDeviceToHost));
     CUDA_TRY(c, cudaMemsetAsync(c->dflag, 0, sizeof(int), c->stream));
     if (h != 1) return fail(c, MSL_E_CUDA, "the bounded wait did not report its timeout");
+    return MSL_OK;
+}
+
+int msl_set_memory_limit(msl_ctx *c, size_t bytes) {
+    if (!c) return MSL_E_ARG;
+    c->mem.limit = bytes;
+    return MSL_OK;
+}
+
+int msl_memory_in_use(msl_ctx *c, size_t *bytes) {
+    if (!c || !bytes) return MSL_E_ARG;
+    *bytes = c->mem.used;
     return MSL_OK;
 }
 
@@ -1340,7 +1378,9 @@ int msl_stem_scan(msl_ctx *c, const msl_grid *g, const msl_optics *o, const floa
                                             c->stream, &c->launches); }));
     int B = c->probe_batch;
     if (B <= 0) {
-        const size_t budget = (size_t)8 << 30;  // wave buffer budget, bytes
+        // wave buffer budget: 8 GiB, or half the context's memory cap when one is set
+        size_t budget = (size_t)8 << 30;
+        if (c->mem.limit && c->mem.limit / 2 < budget) budget = c->mem.limit / 2;
         B = (int)std::max<size_t>(1, std::min<size_t>(budget / (sizeof(float2) * n2), 65536));
     }
     if (B > nprobe) B = nprobe;
