@@ -245,7 +245,7 @@ template <class PL> struct ColTmaCfg {
     static constexpr int N = P::N;
     static constexpr int C = P::col_c, T = P::T, THREADS = T * C, NWARP = THREADS / 32;
     static constexpr int NBUF = P::NBUF;
-    static_assert(NBUF == 2 || NBUF == 3, "tile ring of two or three buffers");
+    static_assert(NBUF >= 2 && NBUF <= 4, "tile ring of two to four buffers");
     // rows per TMA box: the largest divisor of N not above 256 (the box limit)
     static constexpr int BOXR = N <= 256 ? N : (N % 256 == 0 ? 256 : N / 2), NBOX = N / BOXR;
     static_assert(BOXR <= 256 && BOXR * NBOX == N, "TMA boxes must tile the column");
@@ -343,10 +343,10 @@ __global__ void __launch_bounds__(ColTmaCfg<PL>::THREADS, MINB)
                 tma_commit();
             }
         }
-        if constexpr (NBUF == 3) {
+        if constexpr (NBUF >= 3) {
             if (load && tid == 0 && k + NBUF - 1 < nmine) {
                 if (store) tma_wait_read<1>();  // the store of tile k-1 has left its buffer
-                issue_load(k + NBUF - 1);       // into buffer (k + 2) % 3 == (k - 1) % 3
+                issue_load(k + NBUF - 1);       // into the buffer of tile k-1
             }
         }
     }
