@@ -122,6 +122,31 @@ def amorphous(box, thickness, density, dmin, Zs, weights, rng, max_tries=60):
                     float(box[0]), float(box[1]), float(thickness))
 
 
+def uneven_jobs(seed, njobs, max_slices=300, max_box=None):
+    """Job descriptions of the uneven-batch workload: grid side from
+    {256, 384, 512, 768, 1024}, 20..max_slices slices of 1-2 A, an amorphous
+    specimen of 0.05 atoms/A^3 with 1.5 A minimum separation and Z from
+    {6, 14, 29, 79} (weights 0.4, 0.3, 0.2, 0.1), 80/200/300 kV, plane-wave or
+    probe illumination.  The lateral box is 0.1 A per pixel, capped at max_box A.
+    Returns dicts with spec, n, nslice, dz, kev and probe (k_ap, x, y) or None;
+    everything follows from the seed."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for j in range(njobs):
+        n = int(rng.choice([256, 384, 512, 768, 1024]))
+        nslice = int(rng.integers(20, max(max_slices, 20) + 1))
+        dz = float(rng.uniform(1.0, 2.0))
+        box = 0.1 * n if max_box is None else min(0.1 * n, float(max_box))
+        spec = amorphous((box, box), nslice * dz, 0.05, 1.5, [6, 14, 29, 79], [0.4, 0.3, 0.2, 0.1], rng)
+        kev = float(rng.choice([80.0, 200.0, 300.0]))
+        probe = None
+        if rng.random() < 0.5:
+            probe = (float(mrad_to_k(rng.uniform(10.0, 30.0), kev)), float(rng.uniform(0, box)),
+                     float(rng.uniform(0, box)))
+        out.append(dict(spec=spec, n=n, nslice=nslice, dz=dz, kev=kev, probe=probe))
+    return out
+
+
 def raster(x0, x1, y0, y1, nx, ny):
     """Probe positions of an nx x ny raster over [x0, x1) x [y0, y1), x-major."""
     xs = x0 + (x1 - x0) * np.arange(nx) / nx

@@ -57,3 +57,43 @@ def test_uneven_batch_rejects_bad_job(ctx):
     with pytest.raises(MslError) as e:
         ctx.run_jobs(jobs)
     assert "job" in str(e.value)
+
+
+def test_uneven_workload_every_side(ctx):
+    """The uneven-batch workload at reduced thickness: amorphous specimens on every
+    grid side 256-1024, 80-300 kV, plane waves and probes mixed, built on the GPU
+    and run in one lockstep loop; each job equals its own run, the smallest also
+    the FP64 oracle."""
+    from multislice_gb300 import specimen as S
+    descs = S.uneven_jobs(3, 10, max_slices=26, max_box=32.0)
+    assert sorted({d["n"] for d in descs}) == [256, 384, 512, 768, 1024]
+    jobs = []
+    for d in descs:
+        s, n = d["spec"], d["n"]
+        v = ctx.potential(s, n, n, d["nslice"], 3.0)
+        t = ctx.transmission(v, s.ax, s.by, d["kev"])
+        job = dict(trans=t, ax=s.ax, by=s.by, kev=d["kev"], dz=d["dz"], layer_seq=np.arange(d["nslice"]))
+        if d["probe"] is not None:
+            job["probe"] = d["probe"]
+        jobs.append(job)
+    outs = ctx.run_jobs(jobs)
+    for job, w in zip(jobs, outs):
+        if "probe" in job:
+            alone = ctx.run_jobs([job])[0]
+            assert O.rel_l2(w, alone) < 1e-6
+        else:
+            alone = ctx.multislice(job["trans"], job["dz"], job["layer_seq"], job["ax"], job["by"], job["kev"])[0]
+            assert np.array_equal(w, alone)
+        assert np.isfinite(w).all()
+    j = min(range(len(jobs)), key=lambda i: descs[i]["n"] * descs[i]["nslice"])
+    job = jobs[j]
+    nt, nx, ny = job["trans"].shape
+    props = [O.propagator_tables(nx, ny, job["ax"], job["by"], job["kev"], job["dz"], precision="f64")] * nt
+    if "probe" in job:
+        k_ap, x, y = job["probe"]
+        psi0 = O.probe(nx, ny, job["ax"], job["by"], job["kev"], 0.0, k_ap, 0.0, 0.0, [[x, y]], np.complex128)[0]
+    else:
+        psi0 = np.ones((nx, ny), np.complex128)
+    ref, _ = O.multislice(psi0, job["trans"].astype(np.complex128), props, job["layer_seq"],
+                          O.band_mask(nx, ny, job["ax"], job["by"]))
+    assert O.rel_l2(outs[j], ref) < 2e-5

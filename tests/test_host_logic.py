@@ -79,3 +79,17 @@ def test_defocus_weights_follow_mulslice_rule():
     dfs, w = O.defocus_weights(-600.0, 50.0, 25.0)
     assert len(dfs) == 11 and np.isclose(w.sum(), 1.0)
     assert np.isclose(dfs[5], -600.0) and w[5] == w.max()
+
+
+def test_uneven_jobs_follow_the_workload_rules():
+    from multislice_gb300 import specimen as S
+    a = S.uneven_jobs(11, 6, max_slices=30, max_box=30.0)
+    b = S.uneven_jobs(11, 6, max_slices=30, max_box=30.0)
+    for x, y in zip(a, b):                       # seeded
+        assert (x["n"], x["nslice"], x["kev"]) == (y["n"], y["nslice"], y["kev"])
+        assert np.array_equal(x["spec"].x, y["spec"].x)
+    for j in a:
+        assert j["n"] in (256, 384, 512, 768, 1024) and 20 <= j["nslice"] <= 30 and 1 <= j["dz"] <= 2
+        s = j["spec"]
+        vol = s.ax * s.by * s.cz
+        assert abs(s.natom / vol - 0.05) < 0.005 and set(np.unique(s.Z)) <= {6, 14, 29, 79}
