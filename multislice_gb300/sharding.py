@@ -1,4 +1,4 @@
-"""Probe sharding across ranks (one process per GPU).
+"""Probe and job sharding across ranks (one process per GPU).
 
 STEM probes (and frozen-phonon configurations) are independent: the reference
 runs them in a serial loop (MSProjectReuse.cs:254-347, MSProjectUseOnce.cs:235-273).
@@ -19,6 +19,30 @@ def probe_shard(nprobe, rank, world):
     lo = rank * base + min(rank, extra)
     hi = lo + base + (1 if rank < extra else 0)
     return lo, hi
+
+
+def job_cost(n, nslice):
+    """Relative cost of one job of the uneven batch: two passes of N log N line
+    transforms over N lines per slice."""
+    return float(n) * float(n) * np.log2(float(n)) * float(nslice)
+
+
+def job_shard(costs, rank, world):
+    """Indices of the jobs rank `rank` of `world` runs: jobs of very different
+    sizes and thicknesses are dealt largest first to the least-loaded rank (the
+    same on every rank, so no communication is needed).  Each rank then runs its
+    jobs as one uneven batch (msl_run_jobs)."""
+    if world < 1 or not (0 <= rank < world):
+        raise ValueError("rank must lie in [0, world)")
+    costs = np.asarray(costs, dtype=np.float64)
+    order = sorted(range(len(costs)), key=lambda i: (-costs[i], i))
+    load = [0.0] * world
+    owner = np.empty(len(costs), dtype=np.int64)
+    for i in order:
+        r = min(range(world), key=lambda q: (load[q], q))
+        owner[i] = r
+        load[r] += costs[i]
+    return np.nonzero(owner == rank)[0]
 
 
 def gather_detector_sums(local, nprobe, group=None):

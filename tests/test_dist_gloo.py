@@ -79,3 +79,20 @@ def test_two_gloo_ranks_match_single_rank(tmp_path):
     P = O.probe(n, n, a, a, kev, 0.0, 0.8, 0.0, 0.0, xy, np.complex128)
     ref = O.stem(T, props, [0, 1, 0, 1], mask, P, dm, [3])
     np.testing.assert_allclose(full, ref, rtol=1e-12, atol=1e-12)
+
+
+def test_job_shard_covers_every_job_once_and_balances():
+
+    from multislice_gb300.sharding import job_cost, job_shard
+    rng = np.random.default_rng(0)
+    sides = rng.choice([256, 384, 512, 768, 1024], 256)
+    slices = rng.integers(20, 301, 256)
+    costs = [job_cost(n, s) for n, s in zip(sides, slices)]
+    for world in (1, 2, 4, 8):
+        parts = [job_shard(costs, r, world) for r in range(world)]
+        allidx = np.sort(np.concatenate(parts))
+        assert np.array_equal(allidx, np.arange(256))
+        loads = [sum(costs[i] for i in p) for p in parts]
+        assert max(loads) <= sum(costs) / world + max(costs)      # greedy bound
+        assert max(loads) / (sum(costs) / world) < 1.05            # near even at 256 jobs
+
