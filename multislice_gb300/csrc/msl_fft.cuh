@@ -425,6 +425,77 @@ __device__ __forceinline__ void fft_line(float2 (&v)[P::E], int t, const Addr &a
     }
 }
 
+// ------------------------------------------ compact base-twiddle table
+// Stages that form their twiddle powers in registers read only w^1 of each k:
+// a compact table of those bases, stage s at offset sum_{1 <= i < s} NS_i.
+template <class P> __host__ __device__ constexpr int plan_cw_offset(int s) {
+    int off = 0;
+    for (int i = 1; i < s; ++i) off += plan_span<P>(i);
+    return off;
+}
+template <class P> __host__ __device__ constexpr int plan_cw_size() { return plan_cw_offset<P>(P::NSTAGE); }
+
+template <class P, int S, int DIR>
+__device__ __forceinline__ void fft_stage_cwc(float2 (&v)[P::E], int t, const float2 *__restrict__ twb) {
+    constexpr int R = P::radix(S), NS = plan_span<P>(S), E = P::E, Q = E / R, T = P::T;
+    constexpr bool SHARED_K = NS > 1 && T % NS == 0;
+    float2 w[R];
+    auto powers = [&](int k) {
+        w[1] = twb[plan_cw_offset<P>(S) + k];
+        if constexpr (DIR < 0) w[1].y = -w[1].y;
+#pragma unroll
+        for (int r = 2; r < R; ++r) w[r] = c_mul(w[r / 2], w[r - r / 2]);
+    };
+    if constexpr (SHARED_K) powers(t % NS);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        float2 a[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) a[r] = v[q + r * Q];
+        if constexpr (NS > 1) {
+            if constexpr (!SHARED_K) powers((t + T * q) % NS);
+#pragma unroll
+            for (int r = 1; r < R; ++r) a[r] = c_mul(a[r], w[r]);
+        }
+        dft<R, DIR>(a);
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[q + r * Q] = a[r];
+    }
+}
+
+// Exchange after stage S between two thread-to-line mappings of 512-point
+// lines held 32 threads x 16 elements (WarpPlan layout): the writer role is
+// thread tw of line space rw, the reader role thread tr of line space rr (a
+// line space: a 4096-byte aligned shared region holding one line as
+// f(i) ^ m, f the RowXorLin swizzle, m a per-line mask).  Addresses as in
+// fft_exchange_xl: (base + 8 (f(T) ^ m)) ^ 8 f(K).  PRE / POST select the
+// synchronisation before the writes and between writes and reads (1: warp,
+// 2: CTA), so the same routine serves exchanges inside a warp and exchanges
+// that move a line between warps.
+template <class P, int S, int PRE, int POST>
+__device__ __forceinline__ void fft_exchange_map(float2 (&v)[P::E], int tw, uint32_t rw, uint32_t mw, int tr,
+                                                 uint32_t rr, uint32_t mr) {
+    constexpr int R = P::radix(S), NS = plan_span<P>(S), E = P::E, Q = E / R, T = P::T;
+    static_assert(T == 32 && (NS & (NS - 1)) == 0 && (R & (R - 1)) == 0 && (P::N & (P::N - 1)) == 0,
+                  "mapped exchange needs 32 threads per line and power-of-two radices");
+    using F = RowXorLin<P>;
+    const int tw_part = NS <= T ? (tw / NS) * NS * R + tw % NS : tw;
+    const uint32_t wb = rw + 8u * ((uint32_t)F::f(tw_part) ^ mw);
+    const uint32_t rb = rr + 8u * ((uint32_t)F::f(tr) ^ mr);
+    if constexpr (PRE == 2) __syncthreads(); else if constexpr (PRE == 1) __syncwarp();
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int K = NS <= T ? q * T * R + r * NS : (q / (NS / T)) * NS * R + T * (q % (NS / T)) + r * NS;
+            sts_f2(wb ^ (8u * (uint32_t)F::f(K)), v[q + r * Q]);
+        }
+    }
+    if constexpr (POST == 2) __syncthreads(); else __syncwarp();
+#pragma unroll
+    for (int e = 0; e < E; ++e) v[e] = lds_f2(rb ^ (8u * (uint32_t)F::f(T * e)));
+}
+
 // Row plan with one warp per line (same radices as Plan<N>).
 template <int N_> struct WarpPlan {
     using B = Plan<N_>;
