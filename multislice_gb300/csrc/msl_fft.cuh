@@ -188,12 +188,58 @@ template <int DIR> __device__ __forceinline__ void dft16(float2 *a) {
         }
 }
 
+// exp(DIR * i * 2 pi m / 32), m a compile-time constant after unrolling
+template <int DIR> __device__ __forceinline__ float2 w32(int m) {
+    const float c[9] = {1.0f, 0.98078528040323044913f, 0.92387953251128675613f, 0.83146961230254523708f,
+                        0.70710678118654752440f, 0.55557023301960222474f, 0.38268343236508977173f,
+                        0.19509032201612826785f, 0.0f};
+    m &= 31;
+    const int q = m >> 3, r = m & 7;
+    const float cr = q == 0 ? c[r] : q == 1 ? -c[8 - r] : q == 2 ? -c[r] : c[8 - r];
+    const float sr = q == 0 ? c[8 - r] : q == 1 ? c[r] : q == 2 ? -c[8 - r] : -c[r];
+    return make_float2(cr, DIR * sr);
+}
+
+template <int DIR> __device__ __forceinline__ void dft32(float2 *a) {
+    // n = 4 n1 + n2: 8-point transforms over n1 for each n2, Y[n2][k1] at a[4 k1 + n2]
+#pragma unroll
+    for (int n2 = 0; n2 < 4; ++n2) {
+        float2 t[8];
+#pragma unroll
+        for (int n1 = 0; n1 < 8; ++n1) t[n1] = a[4 * n1 + n2];
+        dft8<DIR>(t);
+#pragma unroll
+        for (int k1 = 0; k1 < 8; ++k1) a[4 * k1 + n2] = t[k1];
+    }
+    // twiddle by w32^(n2 k1)
+#pragma unroll
+    for (int k1 = 1; k1 < 8; ++k1)
+#pragma unroll
+        for (int n2 = 1; n2 < 4; ++n2) {
+            const int m = n2 * k1;
+            if (m == 8) a[4 * k1 + n2] = c_muli<DIR>(a[4 * k1 + n2]);
+            else if (m == 16) a[4 * k1 + n2] = make_float2(-a[4 * k1 + n2].x, -a[4 * k1 + n2].y);
+            else a[4 * k1 + n2] = c_mul(a[4 * k1 + n2], w32<DIR>(m));
+        }
+    // 4-point transforms over n2 for each k1: X[k1 + 8 k2] at a[4 k1 + k2]
+#pragma unroll
+    for (int k1 = 0; k1 < 8; ++k1) dft4<DIR>(a[4 * k1], a[4 * k1 + 1], a[4 * k1 + 2], a[4 * k1 + 3]);
+    float2 o[32];
+#pragma unroll
+    for (int k1 = 0; k1 < 8; ++k1)
+#pragma unroll
+        for (int k2 = 0; k2 < 4; ++k2) o[k1 + 8 * k2] = a[4 * k1 + k2];
+#pragma unroll
+    for (int k = 0; k < 32; ++k) a[k] = o[k];
+}
+
 template <int R, int DIR> __device__ __forceinline__ void dft(float2 *a) {
     if constexpr (R == 2) dft2<DIR>(a[0], a[1]);
     else if constexpr (R == 3) dft3<DIR>(a[0], a[1], a[2]);
     else if constexpr (R == 4) dft4<DIR>(a[0], a[1], a[2], a[3]);
     else if constexpr (R == 8) dft8<DIR>(a);
     else if constexpr (R == 16) dft16<DIR>(a);
+    else if constexpr (R == 32) dft32<DIR>(a);
     else static_assert(R == 2, "unsupported radix");
 }
 
@@ -354,8 +400,9 @@ __device__ __forceinline__ void fft_exchange(float2 (&v)[P::E], int t, const Add
 template <class P, int S>
 __device__ __forceinline__ void fft_exchange_xl(float2 (&v)[P::E], int t, const RowXorLin<P> &ad) {
     constexpr int R = P::radix(S), NS = plan_span<P>(S), E = P::E, Q = E / R, T = P::T;
-    static_assert(T == 32 && (NS & (NS - 1)) == 0 && (R & (R - 1)) == 0 && (P::N & (P::N - 1)) == 0,
-                  "xor-linear exchange needs warp-owned lines and power-of-two radices");
+    static_assert((T == 32 || T == 16) && (NS & (NS - 1)) == 0 && (R & (R - 1)) == 0 &&
+                      (P::N & (P::N - 1)) == 0,
+                  "xor-linear exchange needs warp- or half-warp-owned lines and power-of-two radices");
     using F = RowXorLin<P>;
     const int tw_part = NS <= T ? (t / NS) * NS * R + t % NS : t;
     const uint32_t wb = ad.base + 8u * (uint32_t)F::f(tw_part);
@@ -494,6 +541,27 @@ __device__ __forceinline__ void fft_exchange_map(float2 (&v)[P::E], int tw, uint
     if constexpr (POST == 2) __syncthreads(); else __syncwarp();
 #pragma unroll
     for (int e = 0; e < E; ++e) v[e] = lds_f2(rb ^ (8u * (uint32_t)F::f(T * e)));
+}
+
+// Two-stage plan for 512-point lines, 16 threads x 32 elements (two lines per
+// warp, one per half-warp): radix 16 then radix 32, a single exchange per
+// transform.  Twiddle table: stage 1 only, [r][k] = exp(+2 pi i r k / 512),
+// r < 32, k < 16.
+struct HalfWarpPlan512 {
+    static constexpr int N = 512, T = 16, E = 32, NSTAGE = 2;
+    static constexpr int row_swz = 1, row_sh = 4, col_c = 4, col_ps = 30;
+    static constexpr int radix(int s) { return s == 0 ? 16 : 32; }
+};
+
+// Warp- or half-warp-owned line with table twiddles and xor-linear exchanges.
+template <class P, int DIR, int S = 0>
+__device__ __forceinline__ void fft_line_tab(float2 (&v)[P::E], int t, const RowXorLin<P> &ad,
+                                             const float2 *__restrict__ tw) {
+    fft_stage<P, S, DIR>(v, t, tw);
+    if constexpr (S + 1 < P::NSTAGE) {
+        fft_exchange_xl<P, S>(v, t, ad);
+        fft_line_tab<P, DIR, S + 1>(v, t, ad, tw);
+    }
 }
 
 // Row plan with one warp per line (same radices as Plan<N>).

@@ -761,6 +761,144 @@ __global__ void __launch_bounds__(RowWarpCfg<N>::THREADS, RowWarpCfg<N>::MINB) r
     }
 }
 
+// ---------------------------------------------- half-warp row pass, 512
+// Row pass for 512-point lines in the two-stage layout (HalfWarpPlan512): each
+// warp transforms two consecutive lines at a time, one per half-warp, with a
+// radix-16 and a radix-32 stage and a single exchange per transform (the
+// three-stage warp layout needs two).  Lines arrive in pairs (8 KB) by 1D bulk
+// copy into a private two-slot ring per warp; the next pair is requested once
+// the previous pair's store has read its slot.  The stage-1 twiddle table is
+// formed in shared memory at start-up.
+struct RowHalfCfg {
+    using P = HalfWarpPlan512;
+    static constexpr int N = 512, W = 4, THREADS = 32 * W, NBUF = 2, MINB = 3;
+    static constexpr size_t LINE = sizeof(float2) * N, SLOT = 2 * LINE;
+    static constexpr uint32_t ALIGN = (uint32_t)LINE;  // each line's exchange space is line-aligned
+    static constexpr int TW = 32 * 16;
+    static constexpr size_t OFF_TW = (size_t)W * NBUF * SLOT;
+    static constexpr size_t OFF_BAR = OFF_TW + sizeof(float2) * TW;
+    static constexpr size_t SMEM = OFF_BAR + sizeof(uint64_t) * W * NBUF + ALIGN;
+};
+
+__global__ void __launch_bounds__(RowHalfCfg::THREADS, RowHalfCfg::MINB) row_half_kernel(RowArgs a) {
+    using Cfg = RowHalfCfg;
+    using P = Cfg::P;
+    constexpr int N = Cfg::N, E = P::E, NBUF = Cfg::NBUF, W = Cfg::W;
+    constexpr uint32_t AL = Cfg::ALIGN;
+    extern __shared__ unsigned char smraw[];
+    unsigned char *base = smraw + ((AL - (smem_u32(smraw) & (AL - 1u))) & (AL - 1u));
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, h = lane >> 4, t = lane & 15;
+    float2 *ring = reinterpret_cast<float2 *>(base) + (size_t)warp * NBUF * 2 * N;
+    float2 *tw = reinterpret_cast<float2 *>(base + Cfg::OFF_TW);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(base + Cfg::OFF_BAR) + warp * NBUF;
+    for (int i = threadIdx.x; i < Cfg::TW; i += Cfg::THREADS) {
+        float sn, cn;
+        sincospif((float)(2 * (i >> 4) * (i & 15)) / (float)N, &sn, &cn);  // exp(2 pi i r k / 512), [r][k]
+        tw[i] = make_float2(cn, sn);
+    }
+    if (lane == 0) {
+        for (int s = 0; s < NBUF; ++s) mbar_init(&bar[s], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();  // the only CTA barrier: tables and barriers are ready
+    const bool load = (a.flags & ROW_LOAD) != 0, store = !(a.flags & ROW_NOSTORE);
+    const int npairs = a.nlines / 2;
+    const int G = gridDim.x * W, gw = blockIdx.x * W + warp;
+    const int nmine = gw < npairs ? (npairs - gw + G - 1) / G : 0;
+    int issued = 0;
+    auto issue = [&](int k) {  // lane 0 only
+        const int pair = gw + k * G, s = k % NBUF;
+        fence_proxy_async();
+        mbar_arrive_expect_tx(&bar[s], (uint32_t)Cfg::SLOT);
+        bulk_load(ring + (size_t)s * 2 * N, a.in + (size_t)pair * 2 * N, (uint32_t)Cfg::SLOT, &bar[s]);
+        issued = k + 1;
+    };
+    if (load && lane == 0 && nmine > 0) issue(0);
+    int k = 0;
+    bool ok = true;
+    for (; k < nmine; ++k) {
+        const int pair = gw + k * G, s = k % NBUF, line = 2 * pair + h;
+        float2 *slot = ring + (size_t)s * 2 * N;
+        float2 *buf = slot + (size_t)h * N;
+        const RowXorLin<P> ad{smem_u32(buf)};
+        const float2 *trow = (a.flags & ROW_TRANS)
+                                 ? (a.trans_b ? a.trans_b[line / a.nx] : a.trans) + (size_t)(line % a.nx) * N
+                                 : nullptr;
+        if (!load && store && lane == 0) tma_wait_read<NBUF - 1>();  // the store of pair k-2 left the slot
+        if (load && lane == 0 && k + 1 < nmine) {
+            if (store) tma_wait_read<0>();  // the store of pair k-1 has read the other slot
+            issue(k + 1);
+        }
+        float2 v[E];
+        if (load) {
+            const bool got = mbar_wait_bounded(&bar[s], (uint32_t)((k / NBUF) & 1), kWaitLimit);
+            if (__any_sync(0xffffffffu, !got)) {
+                ok = false;
+                break;
+            }
+#pragma unroll
+            for (int e = 0; e < E; ++e) v[e] = buf[t + 16 * e];
+        } else {
+#pragma unroll
+            for (int e = 0; e < E; ++e) v[e] = make_float2(1.f, 0.f);
+        }
+        if (a.flags & ROW_INV) fft_line_tab<P, -1>(v, t, ad, tw);
+        if (a.flags & ROW_TRANS) {
+#pragma unroll
+            for (int e = 0; e < E; ++e) v[e] = c_mul(v[e], __ldg(trow + t + 16 * e));
+        }
+        if (a.flags & ROW_FWD) fft_line_tab<P, +1>(v, t, ad, tw);
+        if (a.scale != 1.0f) {
+#pragma unroll
+            for (int e = 0; e < E; ++e) v[e] = c_scale(v[e], a.scale);
+        }
+        if (a.flags & ROW_ACCUM) {
+            double *acc = a.accum + (size_t)line * N;
+#pragma unroll
+            for (int e = 0; e < E; ++e)
+                acc[t + 16 * e] += a.accum_w * ((double)v[e].x * v[e].x + (double)v[e].y * v[e].y);
+        }
+        if (store) {
+            __syncwarp();  // every lane is done reading the slot
+#pragma unroll
+            for (int e = 0; e < E; ++e) buf[t + 16 * e] = v[e];
+            fence_proxy_async();
+            __syncwarp();
+            if (lane == 0) {
+                bulk_store(a.out + (size_t)pair * 2 * N, slot, (uint32_t)Cfg::SLOT);
+                tma_commit();
+            }
+        }
+        __syncwarp();
+    }
+    if (lane == 0) {
+        if (store) tma_wait_all();
+        if (!ok) {
+            if (a.err) atomicExch(a.err, 1);
+            for (int j = k; j < issued; ++j)
+                mbar_wait_bounded(&bar[j % NBUF], (uint32_t)((j / NBUF) & 1), kWaitLimit);
+        }
+    }
+}
+
+static cudaError_t row_half_launch(const RowArgs &a, cudaStream_t s, int nsm) {
+    using Cfg = RowHalfCfg;
+    static int per_sm = 0;
+    if (!per_sm) {
+        cudaError_t e = cudaFuncSetAttribute(row_half_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)Cfg::SMEM);
+        if (e != cudaSuccess) return e;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, row_half_kernel, Cfg::THREADS, Cfg::SMEM);
+        if (e != cudaSuccess) return e;
+        if (per_sm < 1) per_sm = 1;
+    }
+    const int nwarps = (a.nlines / 2 + Cfg::W - 1) / Cfg::W;
+    int grid = nsm * per_sm < nwarps ? nsm * per_sm : nwarps;
+    if (grid < 1) grid = 1;
+    row_half_kernel<<<grid, Cfg::THREADS, Cfg::SMEM, s>>>(a);
+    return cudaGetLastError();
+}
+
 // ------------------------------------------------------------ set-up kernels
 __global__ void probe_table_kernel(int nx, int ny, const double *kxd, const double *kyd,
                                    double s_in, double s_out, double lam, double df, double cs,
@@ -1139,7 +1277,10 @@ cudaError_t launch_row_pass(int ny, const RowArgs &a, cudaStream_t s, int nsm, i
         switch (ny) {
             case 256: return row_warp_launch<256>(a, s, nsm);
             case 384: return row_warp_launch<384>(a, s, nsm);
-            case 512: return row_warp_launch<512>(a, s, nsm);
+            case 512:
+                if (a.nlines % 2 == 0 && !(((uintptr_t)a.out | (uintptr_t)a.in) & 15u))
+                    return row_half_launch(a, s, nsm);
+                return row_warp_launch<512>(a, s, nsm);
             default: break;
         }
     }
