@@ -32,6 +32,7 @@ template <int N> struct Plan;
         static constexpr int N = N_, T = T_, E = N_ / T_, NSTAGE = NST_;         \
         static constexpr int row_swz = RSWZ, row_sh = RSH;                      \
         static constexpr int col_c = CC, col_ps = CPS;                          \
+        static constexpr bool PK = false;                                       \
         static constexpr int radix(int s) {                                     \
             return s == 0 ? R0 : s == 1 ? R1 : s == 2 ? R2 : s == 3 ? R3 : R4;  \
         }                                                                       \
@@ -55,6 +56,7 @@ template <int N_, int T_, int C_, int PS_, int MINB_, int NBUF_ = 3> struct ColP
     static constexpr int N = N_, T = T_, E = N_ / T_, NSTAGE = B::NSTAGE, MINB = MINB_, NBUF = NBUF_;
     static constexpr int row_swz = B::row_swz, row_sh = B::row_sh;
     static constexpr int col_c = C_, col_ps = PS_;
+    static constexpr bool PK = true;
     static constexpr int radix(int s) { return B::radix(s); }
 };
 // Tile shapes chosen by a shared-memory bank model and by timing the 512 case.
@@ -88,8 +90,27 @@ template <class P> __host__ __device__ constexpr int row_line_slots() {
 }
 
 // --------------------------------------------------------- complex helpers
-__device__ __forceinline__ float2 c_add(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ float2 c_sub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+// Complex add / subtract.  PK = true issues each as one packed FP32 pair
+// instruction (the sm_100-family f32x2 add, round to nearest like the scalar
+// form; the negation of b folds into the instruction), halving the issue slots
+// of a butterfly.  Plans choose PK (the `PK` member): measured 11 % faster in the
+// 512 row pass and 3-4 % in the 256 / 384 passes, but 3 % slower in the
+// two-mapping 512 column pass (`col_map_kernel`), which keeps scalar adds.
+template <bool PK> __device__ __forceinline__ float2 c_add(float2 a, float2 b) {
+    if constexpr (PK) return __fadd2_rn(a, b);
+    else return make_float2(a.x + b.x, a.y + b.y);
+}
+template <bool PK> __device__ __forceinline__ float2 c_sub(float2 a, float2 b) {
+    if constexpr (PK) return __fadd2_rn(a, make_float2(-b.x, -b.y));
+    else return make_float2(a.x - b.x, a.y - b.y);
+}
+// a + DIR i u and a - DIR i u, scalar: the swapped operand needs no register pair.
+template <int DIR> __device__ __forceinline__ float2 c_add_muli(float2 a, float2 u) {
+    return DIR > 0 ? make_float2(a.x - u.y, a.y + u.x) : make_float2(a.x + u.y, a.y - u.x);
+}
+template <int DIR> __device__ __forceinline__ float2 c_sub_muli(float2 a, float2 u) {
+    return DIR > 0 ? make_float2(a.x + u.y, a.y - u.x) : make_float2(a.x - u.y, a.y + u.x);
+}
 __device__ __forceinline__ float2 c_mul(float2 a, float2 b) {
     return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
@@ -100,50 +121,49 @@ template <int DIR> __device__ __forceinline__ float2 c_muli(float2 a) {
 }
 
 // ---------------------------------------------------------- radix kernels
-template <int DIR> __device__ __forceinline__ void dft2(float2 &a, float2 &b) {
+template <int DIR, bool PK> __device__ __forceinline__ void dft2(float2 &a, float2 &b) {
     float2 t = a;
-    a = c_add(t, b);
-    b = c_sub(t, b);
+    a = c_add<PK>(t, b);
+    b = c_sub<PK>(t, b);
 }
 
-template <int DIR> __device__ __forceinline__ void dft3(float2 &x0, float2 &x1, float2 &x2) {
+template <int DIR, bool PK> __device__ __forceinline__ void dft3(float2 &x0, float2 &x1, float2 &x2) {
     const float s3 = 0.86602540378443864676f;
-    float2 t = c_add(x1, x2), u = c_sub(x1, x2);
+    float2 t = c_add<PK>(x1, x2), u = c_sub<PK>(x1, x2);
     float2 m = make_float2(x0.x - 0.5f * t.x, x0.y - 0.5f * t.y);
-    x0 = c_add(x0, t);
+    x0 = c_add<PK>(x0, t);
     float2 v = c_muli<DIR>(c_scale(u, s3));
-    x1 = c_add(m, v);
-    x2 = c_sub(m, v);
+    x1 = c_add<PK>(m, v);
+    x2 = c_sub<PK>(m, v);
 }
 
-template <int DIR>
+template <int DIR, bool PK>
 __device__ __forceinline__ void dft4(float2 &x0, float2 &x1, float2 &x2, float2 &x3) {
-    float2 t0 = c_add(x0, x2), t1 = c_sub(x0, x2);
-    float2 t2 = c_add(x1, x3), t3 = c_muli<DIR>(c_sub(x1, x3));
-    x0 = c_add(t0, t2);
-    x2 = c_sub(t0, t2);
-    x1 = c_add(t1, t3);
-    x3 = c_sub(t1, t3);
+    float2 t0 = c_add<PK>(x0, x2), t1 = c_sub<PK>(x0, x2);
+    float2 t2 = c_add<PK>(x1, x3), u = c_sub<PK>(x1, x3);
+    x0 = c_add<PK>(t0, t2);
+    x2 = c_sub<PK>(t0, t2);
+    x1 = c_add_muli<DIR>(t1, u);
+    x3 = c_sub_muli<DIR>(t1, u);
 }
 
-template <int DIR> __device__ __forceinline__ void dft8(float2 *a) {
+template <int DIR, bool PK> __device__ __forceinline__ void dft8(float2 *a) {
     float2 e0 = a[0], e1 = a[2], e2 = a[4], e3 = a[6];
     float2 o0 = a[1], o1 = a[3], o2 = a[5], o3 = a[7];
-    dft4<DIR>(e0, e1, e2, e3);
-    dft4<DIR>(o0, o1, o2, o3);
+    dft4<DIR, PK>(e0, e1, e2, e3);
+    dft4<DIR, PK>(o0, o1, o2, o3);
     const float h = 0.70710678118654752440f;
     // w8^1 = (1 + DIR i) h, w8^2 = DIR i, w8^3 = (-1 + DIR i) h
     float2 t1 = make_float2(h * (o1.x - DIR * o1.y), h * (o1.y + DIR * o1.x));
-    float2 t2 = c_muli<DIR>(o2);
     float2 t3 = make_float2(h * (-o3.x - DIR * o3.y), h * (-o3.y + DIR * o3.x));
-    a[0] = c_add(e0, o0);
-    a[4] = c_sub(e0, o0);
-    a[1] = c_add(e1, t1);
-    a[5] = c_sub(e1, t1);
-    a[2] = c_add(e2, t2);
-    a[6] = c_sub(e2, t2);
-    a[3] = c_add(e3, t3);
-    a[7] = c_sub(e3, t3);
+    a[0] = c_add<PK>(e0, o0);
+    a[4] = c_sub<PK>(e0, o0);
+    a[1] = c_add<PK>(e1, t1);
+    a[5] = c_sub<PK>(e1, t1);
+    a[2] = c_add_muli<DIR>(e2, o2);
+    a[6] = c_sub_muli<DIR>(e2, o2);
+    a[3] = c_add<PK>(e3, t3);
+    a[7] = c_sub<PK>(e3, t3);
 }
 
 // exp(DIR * i * 2 pi m / 16) for m in 0..9
@@ -166,17 +186,17 @@ template <int DIR> __device__ __forceinline__ float2 w16(int m) {
     return make_float2(re, DIR * im);
 }
 
-template <int DIR> __device__ __forceinline__ void dft16(float2 *a) {
+template <int DIR, bool PK> __device__ __forceinline__ void dft16(float2 *a) {
     // n = 4 n1 + n2, k = k1 + 4 k2
 #pragma unroll
-    for (int n2 = 0; n2 < 4; ++n2) dft4<DIR>(a[n2], a[4 + n2], a[8 + n2], a[12 + n2]);
+    for (int n2 = 0; n2 < 4; ++n2) dft4<DIR, PK>(a[n2], a[4 + n2], a[8 + n2], a[12 + n2]);
     // a[4 k1 + n2] = Y[n2][k1]; twiddle by w16^(n2 k1)
 #pragma unroll
     for (int k1 = 1; k1 < 4; ++k1)
 #pragma unroll
         for (int n2 = 1; n2 < 4; ++n2) a[4 * k1 + n2] = c_mul(a[4 * k1 + n2], w16<DIR>(n2 * k1));
 #pragma unroll
-    for (int k1 = 0; k1 < 4; ++k1) dft4<DIR>(a[4 * k1], a[4 * k1 + 1], a[4 * k1 + 2], a[4 * k1 + 3]);
+    for (int k1 = 0; k1 < 4; ++k1) dft4<DIR, PK>(a[4 * k1], a[4 * k1 + 1], a[4 * k1 + 2], a[4 * k1 + 3]);
     // X[k1 + 4 k2] sits at a[4 k1 + k2]: transpose the 4x4 block
 #pragma unroll
     for (int i = 0; i < 4; ++i)
@@ -200,14 +220,14 @@ template <int DIR> __device__ __forceinline__ float2 w32(int m) {
     return make_float2(cr, DIR * sr);
 }
 
-template <int DIR> __device__ __forceinline__ void dft32(float2 *a) {
+template <int DIR, bool PK> __device__ __forceinline__ void dft32(float2 *a) {
     // n = 4 n1 + n2: 8-point transforms over n1 for each n2, Y[n2][k1] at a[4 k1 + n2]
 #pragma unroll
     for (int n2 = 0; n2 < 4; ++n2) {
         float2 t[8];
 #pragma unroll
         for (int n1 = 0; n1 < 8; ++n1) t[n1] = a[4 * n1 + n2];
-        dft8<DIR>(t);
+        dft8<DIR, PK>(t);
 #pragma unroll
         for (int k1 = 0; k1 < 8; ++k1) a[4 * k1 + n2] = t[k1];
     }
@@ -223,7 +243,7 @@ template <int DIR> __device__ __forceinline__ void dft32(float2 *a) {
         }
     // 4-point transforms over n2 for each k1: X[k1 + 8 k2] at a[4 k1 + k2]
 #pragma unroll
-    for (int k1 = 0; k1 < 8; ++k1) dft4<DIR>(a[4 * k1], a[4 * k1 + 1], a[4 * k1 + 2], a[4 * k1 + 3]);
+    for (int k1 = 0; k1 < 8; ++k1) dft4<DIR, PK>(a[4 * k1], a[4 * k1 + 1], a[4 * k1 + 2], a[4 * k1 + 3]);
     float2 o[32];
 #pragma unroll
     for (int k1 = 0; k1 < 8; ++k1)
@@ -233,13 +253,13 @@ template <int DIR> __device__ __forceinline__ void dft32(float2 *a) {
     for (int k = 0; k < 32; ++k) a[k] = o[k];
 }
 
-template <int R, int DIR> __device__ __forceinline__ void dft(float2 *a) {
-    if constexpr (R == 2) dft2<DIR>(a[0], a[1]);
-    else if constexpr (R == 3) dft3<DIR>(a[0], a[1], a[2]);
-    else if constexpr (R == 4) dft4<DIR>(a[0], a[1], a[2], a[3]);
-    else if constexpr (R == 8) dft8<DIR>(a);
-    else if constexpr (R == 16) dft16<DIR>(a);
-    else if constexpr (R == 32) dft32<DIR>(a);
+template <int R, int DIR, bool PK> __device__ __forceinline__ void dft(float2 *a) {
+    if constexpr (R == 2) dft2<DIR, PK>(a[0], a[1]);
+    else if constexpr (R == 3) dft3<DIR, PK>(a[0], a[1], a[2]);
+    else if constexpr (R == 4) dft4<DIR, PK>(a[0], a[1], a[2], a[3]);
+    else if constexpr (R == 8) dft8<DIR, PK>(a);
+    else if constexpr (R == 16) dft16<DIR, PK>(a);
+    else if constexpr (R == 32) dft32<DIR, PK>(a);
     else static_assert(R == 2, "unsupported radix");
 }
 
@@ -334,7 +354,7 @@ __device__ __forceinline__ void fft_stage(float2 (&v)[P::E], int t, const float2
                 a[r] = c_mul(a[r], w);
             }
         }
-        dft<R, DIR>(a);
+        dft<R, DIR, P::PK>(a);
 #pragma unroll
         for (int r = 0; r < R; ++r) v[q + r * Q] = a[r];
     }
@@ -367,7 +387,7 @@ __device__ __forceinline__ void fft_stage_cw(float2 (&v)[P::E], int t, const flo
 #pragma unroll
             for (int r = 1; r < R; ++r) a[r] = c_mul(a[r], w[r]);
         }
-        dft<R, DIR>(a);
+        dft<R, DIR, P::PK>(a);
 #pragma unroll
         for (int r = 0; r < R; ++r) v[q + r * Q] = a[r];
     }
@@ -504,7 +524,7 @@ __device__ __forceinline__ void fft_stage_cwc(float2 (&v)[P::E], int t, const fl
 #pragma unroll
             for (int r = 1; r < R; ++r) a[r] = c_mul(a[r], w[r]);
         }
-        dft<R, DIR>(a);
+        dft<R, DIR, P::PK>(a);
 #pragma unroll
         for (int r = 0; r < R; ++r) v[q + r * Q] = a[r];
     }
@@ -550,6 +570,7 @@ __device__ __forceinline__ void fft_exchange_map(float2 (&v)[P::E], int tw, uint
 struct HalfWarpPlan512 {
     static constexpr int N = 512, T = 16, E = 32, NSTAGE = 2;
     static constexpr int row_swz = 1, row_sh = 4, col_c = 4, col_ps = 30;
+    static constexpr bool PK = true;
     static constexpr int radix(int s) { return s == 0 ? 16 : 32; }
 };
 
@@ -564,11 +585,12 @@ __device__ __forceinline__ void fft_line_tab(float2 (&v)[P::E], int t, const Row
     }
 }
 
-// Row plan with one warp per line (same radices as Plan<N>).
-template <int N_> struct WarpPlan {
+// Plan with one warp per line (same radices as Plan<N>); PK as in the complex helpers.
+template <int N_, bool PK_ = true> struct WarpPlan {
     using B = Plan<N_>;
     static constexpr int N = N_, T = 32, E = N_ / 32, NSTAGE = B::NSTAGE;
     static constexpr int row_swz = B::row_swz, row_sh = B::row_sh, col_c = B::col_c, col_ps = B::col_ps;
+    static constexpr bool PK = PK_;
     static constexpr int radix(int s) { return B::radix(s); }
 };
 

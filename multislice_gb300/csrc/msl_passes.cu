@@ -378,7 +378,7 @@ __global__ void __launch_bounds__(ColTmaCfg<PL>::THREADS, MINB)
 // CTA barriers per tile: 6 (tile arrival, the two cross exchanges, results
 // into the store layout, store), against 11 in col_tma_kernel.
 template <int N> struct ColMapCfg {
-    using P = WarpPlan<N>;
+    using P = WarpPlan<N, false>;  // scalar complex adds: measured faster here
     static constexpr int C = 4, THREADS = 32 * C, NWARP = C, NBUF = 3, MINB = 4;
     static constexpr int BOXR = 256, NBOX = N / BOXR;
     static constexpr size_t TILE_BYTES = sizeof(float2) * (size_t)N * C;
