@@ -574,6 +574,46 @@ struct HalfWarpPlan512 {
     static constexpr int radix(int s) { return s == 0 ? 16 : 32; }
 };
 
+// Half-warp-owned 512-point columns inside a tile of 8 columns x 512 rows laid
+// out by the TMA 64-byte swizzle: element (r, c) at byte 64 r + (8 c ^ 16 ((r >> 1) & 3)),
+// i.e. B(r) ^ 8 c with B(p) = 64 p | 16 ((p >> 1) & 3).  The exchange keeps
+// logical slot i of column c at row pi(i) = i ^ ((i >> 4) & 7) of the same
+// column, so its address is L(i) ^ 8 c with L = B o pi.  B and pi are linear
+// over xor; with the tile aligned to 32 KB (every L(i) ^ 8 c is below 32 KB)
+// an access is a per-thread base xor a compile-time constant.  Two columns per
+// warp, lane l on column l & 1 as thread t = l >> 1: each half-warp's sixteen
+// 64-bit accesses (8 rows of both columns) then hit sixteen distinct bank pairs
+// for the natural-order accesses (row t + 16 e) and for the exchange writes
+// (16 t + 256 q + r) and reads (t + 16 e), one wavefront per half-warp.
+struct ColHalfLin {
+    static __host__ __device__ constexpr uint32_t B(uint32_t p) { return (p << 6) | (((p >> 1) & 3u) << 4); }
+    static __host__ __device__ constexpr uint32_t pi(uint32_t i) { return i ^ ((i >> 4) & 7u); }
+    static __host__ __device__ constexpr uint32_t L(uint32_t i) { return B(pi(i)); }
+};
+
+// Exchange after stage S of a HalfWarpPlan512 column; cb = tile address ^ 8 c.
+// Index split as in fft_exchange_xl.
+template <class P, int S>
+__device__ __forceinline__ void fft_exchange_ch(float2 (&v)[P::E], int t, uint32_t cb) {
+    constexpr int R = P::radix(S), NS = plan_span<P>(S), E = P::E, Q = E / R, T = P::T;
+    static_assert(T == 16 && P::N == 512, "half-warp column exchange: 512-point columns, 16 threads");
+    const int tw_part = NS <= T ? (t / NS) * NS * R + t % NS : t;
+    const uint32_t wb = cb ^ ColHalfLin::L((uint32_t)tw_part);
+    const uint32_t rb = cb ^ ColHalfLin::L((uint32_t)t);
+    __syncwarp();  // previous readers of the column are done
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int K = NS <= T ? q * T * R + r * NS : (q / (NS / T)) * NS * R + T * (q % (NS / T)) + r * NS;
+            sts_f2(wb ^ ColHalfLin::L((uint32_t)K), v[q + r * Q]);
+        }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int e = 0; e < E; ++e) v[e] = lds_f2(rb ^ ColHalfLin::L((uint32_t)(T * e)));
+}
+
 // Warp- or half-warp-owned line with table twiddles and xor-linear exchanges.
 template <class P, int DIR, int S = 0>
 __device__ __forceinline__ void fft_line_tab(float2 (&v)[P::E], int t, const RowXorLin<P> &ad,

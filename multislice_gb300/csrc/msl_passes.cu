@@ -494,6 +494,166 @@ __global__ void __launch_bounds__(ColMapCfg<N>::THREADS, ColMapCfg<N>::MINB)
     }
 }
 
+// ------------------------------------- column pass, half-warp columns, 512
+// The slice loop's column transform pair at N = 512 built like the half-warp
+// row pass: each column is one half-warp's line (16 threads x 32 elements,
+// radix 16 x 32, one warp-synchronous exchange per transform; the two columns
+// of a warp interleave lane by lane).  Tiles of 8
+// columns x 512 rows arrive by TMA with the 64-byte swizzle, so the
+// natural-order reads and writes of two columns per warp are conflict-free; the
+// exchange reuses the column's own slots in the permuted order of ColHalfLin.
+// One CTA per SM runs G groups of 4 warps; each group streams its own tiles
+// through a two-slot ring of 32 KB-aligned slots (every exchange address is a
+// per-thread base xor a constant).  Group barriers per tile: the arrival vote
+// and the one before the TMA store (two more at detector checkpoints).
+// Detector partial sums are written per 4 columns, the tile layout of the other
+// column passes at 512.
+struct ColHalfCfg {
+    using P = HalfWarpPlan512;
+    static constexpr int N = 512, C = 8, G = 3, GT = 128, THREADS = GT * G, NBUF = 2, BOXR = 256;
+    static constexpr uint32_t SLOT = sizeof(float2) * N * C;  // 32 KB, also the slot alignment
+    static constexpr int TW = 32 * 16;
+    static constexpr size_t OFF_RED = sizeof(float2) * TW;
+    static constexpr size_t OFF_BAR = OFF_RED + sizeof(double) * G * 4 * kMaxDet;
+    static constexpr size_t HEADER = OFF_BAR + sizeof(uint64_t) * G * NBUF;
+    static constexpr size_t SMEM = 227 * 1024;  // the header, then 2 G slots from the next 32 KB boundary
+    static_assert(SLOT == 32768 && N % BOXR == 0, "32 KB tiles of two TMA boxes");
+};
+
+__global__ void __launch_bounds__(ColHalfCfg::THREADS, 1)
+    col_half_kernel(const __grid_constant__ CUtensorMap map, ColArgs a) {
+    using Cfg = ColHalfCfg;
+    using P = Cfg::P;
+    constexpr int N = Cfg::N, C = Cfg::C, E = P::E, G = Cfg::G, GT = Cfg::GT, NBUF = Cfg::NBUF;
+    constexpr uint32_t SLOT = Cfg::SLOT;
+    extern __shared__ unsigned char smraw[];
+    const uint32_t sbase = smem_u32(smraw);
+    const uint32_t slot0 = (sbase + (uint32_t)Cfg::HEADER + SLOT - 1u) & ~(SLOT - 1u);
+    if (slot0 + (uint32_t)(NBUF * G) * SLOT > sbase + (uint32_t)Cfg::SMEM) {  // uniform over the CTA
+        if (threadIdx.x == 0 && a.err) atomicExch(a.err, 1);
+        return;
+    }
+    float2 *tw = reinterpret_cast<float2 *>(smraw);
+    double *redall = reinterpret_cast<double *>(smraw + Cfg::OFF_RED);
+    uint64_t *barall = reinterpret_cast<uint64_t *>(smraw + Cfg::OFF_BAR);
+    for (int i = threadIdx.x; i < Cfg::TW; i += Cfg::THREADS) {
+        float sn, cn;
+        sincospif((float)(2 * (i >> 4) * (i & 15)) / (float)N, &sn, &cn);  // exp(2 pi i r k / 512), [r][k]
+        tw[i] = make_float2(cn, sn);
+    }
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < G * NBUF; ++s) mbar_init(&barall[s], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();  // the only CTA-wide barrier
+    const int g = threadIdx.x / GT, gt = threadIdx.x % GT, wg = gt >> 5, lane = gt & 31;
+    // two columns per warp, lanes alternating between them: each half-warp then
+    // touches 8 rows of both, which is what keeps its 64-bit accesses on 16 bank pairs
+    const int t = lane >> 1, c = 2 * wg + (lane & 1);
+    const uint32_t barid = 1u + (uint32_t)g;
+    uint64_t *bar = barall + g * NBUF;
+    double *red = redall + g * 4 * kMaxDet;
+    const uint32_t gslot = slot0 + (uint32_t)(g * NBUF) * SLOT;
+    const bool store = (a.flags & COL_STORE) != 0;
+    const int tpi = a.ny / C, ntiles = a.batch * tpi;
+    const int NG = gridDim.x * G, gid = blockIdx.x * G + g;
+    const int nmine = gid < ntiles ? (ntiles - gid + NG - 1) / NG : 0;
+    int issued = 0;
+    auto issue = [&](int k) {  // group thread 0 only
+        const int tile = gid + k * NG, b = tile / tpi, ty = tile % tpi, s = k % NBUF;
+        unsigned char *dst = smraw + (gslot + (uint32_t)s * SLOT - sbase);
+        fence_proxy_async();
+        mbar_arrive_expect_tx(&bar[s], SLOT);
+#pragma unroll
+        for (int q = 0; q < N / Cfg::BOXR; ++q)
+            tma_load_2d(dst + (size_t)q * Cfg::BOXR * C * sizeof(float2), &map, ty * C, b * N + q * Cfg::BOXR,
+                        &bar[s]);
+        issued = k + 1;
+    };
+    if (gt == 0 && nmine > 0) issue(0);
+    int k = 0;
+    bool ok = true;
+    for (; k < nmine; ++k) {
+        const int tile = gid + k * NG, b = tile / tpi, ty = tile % tpi, s = k % NBUF;
+        if (gt == 0 && k + 1 < nmine) {
+            if (store) tma_wait_read<0>();  // the store of tile k-1 has read the other slot
+            issue(k + 1);
+        }
+        const bool got = mbar_wait_bounded(&bar[s], (uint32_t)((k / NBUF) & 1), kWaitLimit);
+        if (bar_group_or(barid, GT, !got)) {
+            ok = false;
+            break;
+        }
+        const uint32_t cb = (gslot + (uint32_t)s * SLOT) ^ (8u * (uint32_t)c);
+        const uint32_t nb = cb ^ ColHalfLin::B((uint32_t)t);  // row t + 16 e at nb + 1024 e
+        float2 v[E];
+#pragma unroll
+        for (int e = 0; e < E; ++e) v[e] = lds_f2(nb + 1024u * (uint32_t)e);
+        fft_stage<P, 0, +1>(v, t, tw);
+        fft_exchange_ch<P, 0>(v, t, cb);
+        fft_stage<P, 1, +1>(v, t, tw);
+        const int iy = ty * C + c;
+        if (a.flags & COL_PROP) col_propagate<P>(v, a, b, iy, t);
+        if (a.flags & COL_CTF) col_ctf<P>(v, a, iy, t);
+        if (a.flags & COL_DETECT) {
+            float acc[kMaxDet];
+#pragma unroll
+            for (int d = 0; d < kMaxDet; ++d) acc[d] = 0.f;
+#pragma unroll
+            for (int e = 0; e < E; ++e) {
+                const unsigned bits = a.detmask[(size_t)(t + 16 * e) * a.ny + iy];
+                const float p = v[e].x * v[e].x + v[e].y * v[e].y;
+#pragma unroll
+                for (int d = 0; d < kMaxDet; ++d)
+                    if (bits & (1u << d)) acc[d] += p;
+            }
+            bar_group(barid, GT);  // red[] of the previous tile has been consumed
+#pragma unroll
+            for (int d = 0; d < kMaxDet; ++d) {
+                if (d < a.ndet) {
+                    double x = (double)acc[d];
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+                    if (lane == 0) red[wg * kMaxDet + d] = x;
+                }
+            }
+            bar_group(barid, GT);
+            if (gt < 2 * a.ndet) {  // warps 2h, 2h + 1 hold columns 4h .. 4h + 3
+                const int hq = gt / a.ndet, d = gt % a.ndet;
+                const double sum = red[(2 * hq) * kMaxDet + d] + red[(2 * hq + 1) * kMaxDet + d];
+                a.partial[((size_t)b * (a.ny / 4) + 2 * ty + hq) * a.ndet + d] = sum;
+            }
+        }
+        fft_stage<P, 0, -1>(v, t, tw);
+        fft_exchange_ch<P, 0>(v, t, cb);
+        fft_stage<P, 1, -1>(v, t, tw);
+        if (store) {
+            __syncwarp();  // every lane of the warp is done reading its columns
+#pragma unroll
+            for (int e = 0; e < E; ++e) sts_f2(nb + 1024u * (uint32_t)e, v[e]);
+            fence_proxy_async();
+            bar_group(barid, GT);
+            if (gt == 0) {
+                const unsigned char *src = smraw + (gslot + (uint32_t)s * SLOT - sbase);
+#pragma unroll
+                for (int q = 0; q < N / Cfg::BOXR; ++q)
+                    tma_store_2d(&map, ty * C, b * N + q * Cfg::BOXR, src + (size_t)q * Cfg::BOXR * C * sizeof(float2));
+                tma_commit();
+            }
+        } else {
+            bar_group(barid, GT);  // the slot is free before the load of tile k + 2 lands in it
+        }
+    }
+    if (gt == 0) {
+        if (store) tma_wait_all();
+        if (!ok) {
+            if (a.err) atomicExch(a.err, 1);
+            for (int j = k; j < issued; ++j)
+                mbar_wait_bounded(&bar[j % NBUF], (uint32_t)((j / NBUF) & 1), kWaitLimit);
+        }
+    }
+}
+
 // ---------------------------------------------------- TMA-fed row pass
 // Persistent kernel, one CTA per SM, 512 threads = L lines x T threads.  Tiles
 // of L consecutive lines (L * N * 8 bytes, contiguous) arrive by TMA into a ring
@@ -1138,6 +1298,32 @@ template <int N> static cudaError_t col_map_launch(const ColArgs &a, cudaStream_
     col_map_kernel<N><<<grid, Cfg::THREADS, Cfg::SMEM, s>>>(map, a);
     return cudaGetLastError();
 }
+static cudaError_t col_half_launch(const ColArgs &a, cudaStream_t s, int nsm) {
+    using Cfg = ColHalfCfg;
+    static int per_sm = 0;
+    if (!per_sm) {
+        cudaError_t e = cudaFuncSetAttribute(col_half_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)Cfg::SMEM);
+        if (e != cudaSuccess) return e;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, col_half_kernel, Cfg::THREADS, Cfg::SMEM);
+        if (e != cudaSuccess) return e;
+        if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    }
+    CUtensorMap map;
+    const cuuint64_t gdim[2] = {(cuuint64_t)a.ny, (cuuint64_t)a.batch * Cfg::N};
+    const cuuint64_t gstride[1] = {(cuuint64_t)a.ny * sizeof(float2)};
+    const cuuint32_t box[2] = {(cuuint32_t)Cfg::C, (cuuint32_t)Cfg::BOXR};
+    const cuuint32_t estride[2] = {1, 1};
+    CUresult r = encode_fn()(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, (void *)a.out, gdim, gstride, box,
+                             estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                             CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
+    const int ngroups = (a.batch * (a.ny / Cfg::C) + Cfg::G - 1) / Cfg::G;
+    int grid = nsm * per_sm < ngroups ? nsm * per_sm : ngroups;
+    if (grid < 1) grid = 1;
+    col_half_kernel<<<grid, Cfg::THREADS, Cfg::SMEM, s>>>(map, a);
+    return cudaGetLastError();
+}
 template <int N> static cudaError_t col_tma_launch(const ColArgs &a, cudaStream_t s, int nsm) {
     return col_tma_launch_v<ColPlan<N>, ColPlan<N>::MINB>(a, s, nsm);
 }
@@ -1306,7 +1492,7 @@ cudaError_t launch_col_pass(int nx, const ColArgs &a, cudaStream_t s, int nsm, i
         // the slice loop's transform pair at 512: the two-mapping kernel
         if (nx == 512 && (a.flags & COL_LOAD) && (a.flags & COL_FWD) && (a.flags & COL_INV) &&
             !(a.flags & COL_PROBE))
-            return col_map_launch<512>(a, s, nsm);
+            return a.ny % ColHalfCfg::C == 0 ? col_half_launch(a, s, nsm) : col_map_launch<512>(a, s, nsm);
         switch (nx) {
 #define X(N) case N: return col_tma_launch<N>(a, s, nsm);
             MSL_FOR_EACH_SIDE(X)

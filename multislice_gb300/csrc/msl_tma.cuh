@@ -102,6 +102,24 @@ template <int N> __device__ __forceinline__ void tma_wait_read() {
 // Wait until every committed store group has completed.
 __device__ __forceinline__ void tma_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 
+// Named CTA barrier over the n threads (a multiple of 32) of one thread group.
+__device__ __forceinline__ void bar_group(uint32_t id, uint32_t n) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+// The same barrier, returning whether any participating thread passed pred = true.
+__device__ __forceinline__ bool bar_group_or(uint32_t id, uint32_t n, bool pred) {
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 p, %1, 0;\n\t"
+        "bar.red.or.pred q, %2, %3, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}"
+        : "=r"(r)
+        : "r"((uint32_t)pred), "r"(id), "r"(n)
+        : "memory");
+    return r != 0;
+}
+
 // Order this thread's generic-proxy shared-memory accesses with async-proxy (TMA) ones.
 __device__ __forceinline__ void fence_proxy_async() {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
