@@ -32,7 +32,7 @@ template <int N> struct Plan;
         static constexpr int N = N_, T = T_, E = N_ / T_, NSTAGE = NST_;         \
         static constexpr int row_swz = RSWZ, row_sh = RSH;                      \
         static constexpr int col_c = CC, col_ps = CPS;                          \
-        static constexpr bool PK = false;                                       \
+        static constexpr bool PK = false, PKMUL = false;                        \
         static constexpr int radix(int s) {                                     \
             return s == 0 ? R0 : s == 1 ? R1 : s == 2 ? R2 : s == 3 ? R3 : R4;  \
         }                                                                       \
@@ -56,7 +56,7 @@ template <int N_, int T_, int C_, int PS_, int MINB_, int NBUF_ = 3> struct ColP
     static constexpr int N = N_, T = T_, E = N_ / T_, NSTAGE = B::NSTAGE, MINB = MINB_, NBUF = NBUF_;
     static constexpr int row_swz = B::row_swz, row_sh = B::row_sh;
     static constexpr int col_c = C_, col_ps = PS_;
-    static constexpr bool PK = true;
+    static constexpr bool PK = true, PKMUL = false;
     static constexpr int radix(int s) { return B::radix(s); }
 };
 // Tile shapes chosen by a shared-memory bank model and by timing the 512 case.
@@ -94,8 +94,8 @@ template <class P> __host__ __device__ constexpr int row_line_slots() {
 // instruction (the sm_100-family f32x2 add, round to nearest like the scalar
 // form; the negation of b folds into the instruction), halving the issue slots
 // of a butterfly.  Plans choose PK (the `PK` member): measured 11 % faster in the
-// 512 row pass and 3-4 % in the 256 / 384 passes, but 3 % slower in the
-// two-mapping 512 column pass (`col_map_kernel`), which keeps scalar adds.
+// 512 row pass and 3-4 % in the 256 / 384 passes; the register-only passes
+// (Plan<N>) keep scalar adds.
 template <bool PK> __device__ __forceinline__ float2 c_add(float2 a, float2 b) {
     if constexpr (PK) return __fadd2_rn(a, b);
     else return make_float2(a.x + b.x, a.y + b.y);
@@ -113,6 +113,16 @@ template <int DIR> __device__ __forceinline__ float2 c_sub_muli(float2 a, float2
 }
 __device__ __forceinline__ float2 c_mul(float2 a, float2 b) {
     return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// Complex product by a run-time factor (a table twiddle).  PK: two packed pair
+// operations, a.x (w.x, w.y) + a.y (-w.y, w.x); the operand pairs cost moves,
+// so it pays only where it shortens a pass's critical path (measured: the
+// half-warp column pass 7 % faster, the half-warp row pass 2 % slower).  Plans
+// choose it with their `PKMUL` member.
+template <bool PK> __device__ __forceinline__ float2 c_mul_rt(float2 a, float2 w) {
+    if constexpr (PK)
+        return __ffma2_rn(make_float2(a.y, a.y), make_float2(-w.y, w.x), __fmul2_rn(make_float2(a.x, a.x), w));
+    else return c_mul(a, w);
 }
 __device__ __forceinline__ float2 c_scale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
 // multiply by DIR * i
@@ -351,7 +361,7 @@ __device__ __forceinline__ void fft_stage(float2 (&v)[P::E], int t, const float2
             for (int r = 1; r < R; ++r) {
                 float2 w = tws[r * NS + k];
                 if constexpr (DIR < 0) w.y = -w.y;
-                a[r] = c_mul(a[r], w);
+                a[r] = c_mul_rt<P::PKMUL>(a[r], w);
             }
         }
         dft<R, DIR, P::PK>(a);
@@ -492,77 +502,6 @@ __device__ __forceinline__ void fft_line(float2 (&v)[P::E], int t, const Addr &a
     }
 }
 
-// ------------------------------------------ compact base-twiddle table
-// Stages that form their twiddle powers in registers read only w^1 of each k:
-// a compact table of those bases, stage s at offset sum_{1 <= i < s} NS_i.
-template <class P> __host__ __device__ constexpr int plan_cw_offset(int s) {
-    int off = 0;
-    for (int i = 1; i < s; ++i) off += plan_span<P>(i);
-    return off;
-}
-template <class P> __host__ __device__ constexpr int plan_cw_size() { return plan_cw_offset<P>(P::NSTAGE); }
-
-template <class P, int S, int DIR>
-__device__ __forceinline__ void fft_stage_cwc(float2 (&v)[P::E], int t, const float2 *__restrict__ twb) {
-    constexpr int R = P::radix(S), NS = plan_span<P>(S), E = P::E, Q = E / R, T = P::T;
-    constexpr bool SHARED_K = NS > 1 && T % NS == 0;
-    float2 w[R];
-    auto powers = [&](int k) {
-        w[1] = twb[plan_cw_offset<P>(S) + k];
-        if constexpr (DIR < 0) w[1].y = -w[1].y;
-#pragma unroll
-        for (int r = 2; r < R; ++r) w[r] = c_mul(w[r / 2], w[r - r / 2]);
-    };
-    if constexpr (SHARED_K) powers(t % NS);
-#pragma unroll
-    for (int q = 0; q < Q; ++q) {
-        float2 a[R];
-#pragma unroll
-        for (int r = 0; r < R; ++r) a[r] = v[q + r * Q];
-        if constexpr (NS > 1) {
-            if constexpr (!SHARED_K) powers((t + T * q) % NS);
-#pragma unroll
-            for (int r = 1; r < R; ++r) a[r] = c_mul(a[r], w[r]);
-        }
-        dft<R, DIR, P::PK>(a);
-#pragma unroll
-        for (int r = 0; r < R; ++r) v[q + r * Q] = a[r];
-    }
-}
-
-// Exchange after stage S between two thread-to-line mappings of 512-point
-// lines held 32 threads x 16 elements (WarpPlan layout): the writer role is
-// thread tw of line space rw, the reader role thread tr of line space rr (a
-// line space: a 4096-byte aligned shared region holding one line as
-// f(i) ^ m, f the RowXorLin swizzle, m a per-line mask).  Addresses as in
-// fft_exchange_xl: (base + 8 (f(T) ^ m)) ^ 8 f(K).  PRE / POST select the
-// synchronisation before the writes and between writes and reads (1: warp,
-// 2: CTA), so the same routine serves exchanges inside a warp and exchanges
-// that move a line between warps.
-template <class P, int S, int PRE, int POST>
-__device__ __forceinline__ void fft_exchange_map(float2 (&v)[P::E], int tw, uint32_t rw, uint32_t mw, int tr,
-                                                 uint32_t rr, uint32_t mr) {
-    constexpr int R = P::radix(S), NS = plan_span<P>(S), E = P::E, Q = E / R, T = P::T;
-    static_assert(T == 32 && (NS & (NS - 1)) == 0 && (R & (R - 1)) == 0 && (P::N & (P::N - 1)) == 0,
-                  "mapped exchange needs 32 threads per line and power-of-two radices");
-    using F = RowXorLin<P>;
-    const int tw_part = NS <= T ? (tw / NS) * NS * R + tw % NS : tw;
-    const uint32_t wb = rw + 8u * ((uint32_t)F::f(tw_part) ^ mw);
-    const uint32_t rb = rr + 8u * ((uint32_t)F::f(tr) ^ mr);
-    if constexpr (PRE == 2) __syncthreads(); else if constexpr (PRE == 1) __syncwarp();
-#pragma unroll
-    for (int q = 0; q < Q; ++q) {
-#pragma unroll
-        for (int r = 0; r < R; ++r) {
-            const int K = NS <= T ? q * T * R + r * NS : (q / (NS / T)) * NS * R + T * (q % (NS / T)) + r * NS;
-            sts_f2(wb ^ (8u * (uint32_t)F::f(K)), v[q + r * Q]);
-        }
-    }
-    if constexpr (POST == 2) __syncthreads(); else __syncwarp();
-#pragma unroll
-    for (int e = 0; e < E; ++e) v[e] = lds_f2(rb ^ (8u * (uint32_t)F::f(T * e)));
-}
-
 // Two-stage plan for 512-point lines, 16 threads x 32 elements (two lines per
 // warp, one per half-warp): radix 16 then radix 32, a single exchange per
 // transform.  Twiddle table: stage 1 only, [r][k] = exp(+2 pi i r k / 512),
@@ -570,8 +509,12 @@ __device__ __forceinline__ void fft_exchange_map(float2 (&v)[P::E], int tw, uint
 struct HalfWarpPlan512 {
     static constexpr int N = 512, T = 16, E = 32, NSTAGE = 2;
     static constexpr int row_swz = 1, row_sh = 4, col_c = 4, col_ps = 30;
-    static constexpr bool PK = true;
+    static constexpr bool PK = true, PKMUL = false;
     static constexpr int radix(int s) { return s == 0 ? 16 : 32; }
+};
+// The same plan for the half-warp column pass, with packed twiddle products.
+struct HalfWarpColPlan512 : HalfWarpPlan512 {
+    static constexpr bool PKMUL = true;
 };
 
 // Half-warp-owned 512-point columns inside a tile of 8 columns x 512 rows laid
@@ -625,12 +568,12 @@ __device__ __forceinline__ void fft_line_tab(float2 (&v)[P::E], int t, const Row
     }
 }
 
-// Plan with one warp per line (same radices as Plan<N>); PK as in the complex helpers.
-template <int N_, bool PK_ = true> struct WarpPlan {
+// Plan with one warp per line (same radices as Plan<N>).
+template <int N_> struct WarpPlan {
     using B = Plan<N_>;
     static constexpr int N = N_, T = 32, E = N_ / 32, NSTAGE = B::NSTAGE;
     static constexpr int row_swz = B::row_swz, row_sh = B::row_sh, col_c = B::col_c, col_ps = B::col_ps;
-    static constexpr bool PK = PK_;
+    static constexpr bool PK = true, PKMUL = false;
     static constexpr int radix(int s) { return B::radix(s); }
 };
 

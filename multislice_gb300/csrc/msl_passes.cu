@@ -362,138 +362,6 @@ __global__ void __launch_bounds__(ColTmaCfg<PL>::THREADS, MINB)
 }
 
 
-// ------------------------------------------ column pass, two mappings
-// Column pass for the slice loop (forward transform, pointwise work, inverse
-// transform) at N = 512 that keeps the TMA-fed kernel's conflict-free tile
-// access but needs fewer CTA barriers.  Tiles are C = 4 columns x 512 rows.
-// Two thread-to-column mappings are used: "tile" (column tid % 4, thread
-// tid / 4: the tile reads and writes touch 32 contiguous bytes per row) and
-// "warp" (column = warp, thread = lane: exchanges need only the warp).  Each
-// transform's first radix-8 stage runs where its data already is, the
-// exchanges that move a column between mappings (forward: tile -> warp after
-// stage 0; inverse: warp -> tile after stage 1) cross warps, the other two are
-// warp-synchronous.  The buffer's quarter at 4096 c is column c's exchange
-// space, laid out f(i) ^ 4c: the per-column mask makes the cross-warp
-// exchanges conflict-free (a bank model checked every access pattern).
-// CTA barriers per tile: 6 (tile arrival, the two cross exchanges, results
-// into the store layout, store), against 11 in col_tma_kernel.
-template <int N> struct ColMapCfg {
-    using P = WarpPlan<N, false>;  // scalar complex adds: measured faster here
-    static constexpr int C = 4, THREADS = 32 * C, NWARP = C, NBUF = 3, MINB = 4;
-    static constexpr int BOXR = 256, NBOX = N / BOXR;
-    static constexpr size_t TILE_BYTES = sizeof(float2) * (size_t)N * C;
-    static constexpr uint32_t ALIGN = sizeof(float2) * N;
-    static constexpr size_t OFF_TW = NBUF * TILE_BYTES;
-    static constexpr size_t OFF_RED = OFF_TW + ((sizeof(float2) * plan_cw_size<P>() + 15) / 16) * 16;
-    static constexpr size_t OFF_BAR = OFF_RED + sizeof(double) * NWARP * kMaxDet;
-    static constexpr size_t SMEM = OFF_BAR + sizeof(uint64_t) * NBUF + ALIGN;
-    static_assert(N == 512 && P::NSTAGE == 3 && BOXR * NBOX == N, "two-mapping column pass: 512 = 8 x 8 x 8");
-};
-
-template <int N>
-__global__ void __launch_bounds__(ColMapCfg<N>::THREADS, ColMapCfg<N>::MINB)
-    col_map_kernel(const __grid_constant__ CUtensorMap map, ColArgs a) {
-    using Cfg = ColMapCfg<N>;
-    using P = typename Cfg::P;
-    constexpr int C = Cfg::C, E = P::E, NBUF = Cfg::NBUF;
-    constexpr uint32_t AL = Cfg::ALIGN;
-    extern __shared__ unsigned char smraw[];
-    unsigned char *base = smraw + ((AL - (smem_u32(smraw) & (AL - 1u))) & (AL - 1u));
-    float2 *buf0 = reinterpret_cast<float2 *>(base);
-    float2 *twb = reinterpret_cast<float2 *>(base + Cfg::OFF_TW);
-    double *red = reinterpret_cast<double *>(base + Cfg::OFF_RED);
-    uint64_t *bar = reinterpret_cast<uint64_t *>(base + Cfg::OFF_BAR);
-    const int tid = threadIdx.x;
-    const int cT = tid % C, tT = tid / C;        // tile mapping
-    const int cW = tid >> 5, tW = tid & 31;      // warp mapping
-    const bool store = (a.flags & COL_STORE) != 0;
-    const int tpi = a.ny / C, ntiles = a.batch * tpi;
-    const int nmine = (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
-    for (int s = 1; s < P::NSTAGE; ++s) {
-        const int NS = plan_span<P>(s);
-        for (int k = tid; k < NS; k += Cfg::THREADS)
-            twb[plan_cw_offset<P>(s) + k] = a.tw[plan_tw_offset<P>(s) + NS + k];
-    }
-    if (tid == 0) {
-        for (int s = 0; s < NBUF; ++s) mbar_init(&bar[s], 1);
-        mbar_fence_init();
-    }
-    __syncthreads();
-    const uint32_t mT = 4u * (uint32_t)cT, mW = 4u * (uint32_t)cW;
-    int issued = 0;
-    auto issue_load = [&](int k) {
-        const int tile = blockIdx.x + k * gridDim.x, b = tile / tpi, ty = tile % tpi, s = k % NBUF;
-        float2 *dst = buf0 + (size_t)s * N * C;
-        fence_proxy_async();
-        mbar_arrive_expect_tx(&bar[s], (uint32_t)Cfg::TILE_BYTES);
-#pragma unroll
-        for (int q = 0; q < Cfg::NBOX; ++q)
-            tma_load_2d(dst + (size_t)q * Cfg::BOXR * C, &map, ty * C, b * N + q * Cfg::BOXR, &bar[s]);
-        issued = k + 1;
-    };
-    if (tid == 0)
-        for (int k = 0; k < NBUF - 1 && k < nmine; ++k) issue_load(k);
-    int k = 0;
-    bool ok = true;
-    for (; k < nmine; ++k) {
-        const int tile = blockIdx.x + k * gridDim.x, b = tile / tpi, ty = tile % tpi, s = k % NBUF;
-        float2 *bs = buf0 + (size_t)s * N * C;
-        const uint32_t bsa = smem_u32(bs);
-        const uint32_t regT = bsa + AL * (uint32_t)cT, regW = bsa + AL * (uint32_t)cW;
-        float2 v[E];
-        const bool got = mbar_wait_bounded(&bar[s], (uint32_t)((k / NBUF) & 1), kWaitLimit);
-        if (__syncthreads_or(!got)) {
-            ok = false;
-            break;
-        }
-#pragma unroll
-        for (int e = 0; e < E; ++e) v[e] = bs[(tT + 32 * e) * C + cT];
-        // forward transform: stage 0 in the tile mapping, then into the warp mapping
-        fft_stage_cwc<P, 0, +1>(v, tT, twb);
-        fft_exchange_map<P, 0, 2, 2>(v, tT, regT, mT, tW, regW, mW);
-        fft_stage_cwc<P, 1, +1>(v, tW, twb);
-        fft_exchange_map<P, 1, 1, 1>(v, tW, regW, mW, tW, regW, mW);
-        fft_stage_cwc<P, 2, +1>(v, tW, twb);
-        const int iy = ty * C + cW;
-        if (a.flags & COL_PROP) col_propagate<P>(v, a, b, iy, tW);
-        if (a.flags & COL_CTF) col_ctf<P>(v, a, iy, tW);
-        if (a.flags & COL_DETECT) col_detect<P, Cfg::NWARP>(v, a, b, iy, tW, ty, tpi, red);
-        // inverse transform: stages 0-1 in the warp mapping, then back to the tile mapping
-        fft_stage_cwc<P, 0, -1>(v, tW, twb);
-        fft_exchange_map<P, 0, 1, 1>(v, tW, regW, mW, tW, regW, mW);
-        fft_stage_cwc<P, 1, -1>(v, tW, twb);
-        fft_exchange_map<P, 1, 1, 2>(v, tW, regW, mW, tT, regT, mT);
-        fft_stage_cwc<P, 2, -1>(v, tT, twb);
-        if (store) {
-            __syncthreads();  // every thread is done reading the exchange spaces
-#pragma unroll
-            for (int e = 0; e < E; ++e) bs[(tT + 32 * e) * C + cT] = v[e];
-            fence_proxy_async();
-            __syncthreads();
-            if (tid == 0) {
-#pragma unroll
-                for (int q = 0; q < Cfg::NBOX; ++q)
-                    tma_store_2d(&map, ty * C, b * N + q * Cfg::BOXR, bs + (size_t)q * Cfg::BOXR * C);
-                tma_commit();
-            }
-        } else {
-            __syncthreads();  // the buffer is free before the next load lands in it
-        }
-        if (tid == 0 && k + NBUF - 1 < nmine) {
-            if (store) tma_wait_read<1>();  // the store of tile k-1 has left its buffer
-            issue_load(k + NBUF - 1);       // into the buffer of tile k-1
-        }
-    }
-    if (tid == 0) {
-        if (store) tma_wait_all();
-        if (!ok) {
-            if (a.err) atomicExch(a.err, 1);
-            for (int j = k; j < issued; ++j)
-                mbar_wait_bounded(&bar[j % NBUF], (uint32_t)((j / NBUF) & 1), kWaitLimit);
-        }
-    }
-}
-
 // ------------------------------------- column pass, half-warp columns, 512
 // The slice loop's column transform pair at N = 512 built like the half-warp
 // row pass: each column is one half-warp's line (16 threads x 32 elements,
@@ -509,7 +377,7 @@ __global__ void __launch_bounds__(ColMapCfg<N>::THREADS, ColMapCfg<N>::MINB)
 // Detector partial sums are written per 4 columns, the tile layout of the other
 // column passes at 512.
 struct ColHalfCfg {
-    using P = HalfWarpPlan512;
+    using P = HalfWarpColPlan512;
     static constexpr int N = 512, C = 8, G = 3, GT = 128, THREADS = GT * G, NBUF = 2, BOXR = 256;
     static constexpr uint32_t SLOT = sizeof(float2) * N * C;  // 32 KB, also the slot alignment
     static constexpr int TW = 32 * 16;
@@ -1272,32 +1140,6 @@ template <class PL, int MINB> static cudaError_t col_tma_launch_v(const ColArgs 
     return cudaGetLastError();
 }
 
-template <int N> static cudaError_t col_map_launch(const ColArgs &a, cudaStream_t s, int nsm) {
-    using Cfg = ColMapCfg<N>;
-    static int per_sm = 0;
-    if (!per_sm) {
-        cudaError_t e = cudaFuncSetAttribute(col_map_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)Cfg::SMEM);
-        if (e != cudaSuccess) return e;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, col_map_kernel<N>, Cfg::THREADS, Cfg::SMEM);
-        if (e != cudaSuccess) return e;
-        if (per_sm < 1) per_sm = 1;
-    }
-    CUtensorMap map;
-    const cuuint64_t gdim[2] = {(cuuint64_t)a.ny, (cuuint64_t)a.batch * N};
-    const cuuint64_t gstride[1] = {(cuuint64_t)a.ny * sizeof(float2)};
-    const cuuint32_t box[2] = {(cuuint32_t)Cfg::C, (cuuint32_t)Cfg::BOXR};
-    const cuuint32_t estride[2] = {1, 1};
-    CUresult r = encode_fn()(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, (void *)a.out, gdim, gstride, box,
-                             estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                             CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
-    const int ntiles = a.batch * (a.ny / Cfg::C);
-    int grid = nsm * per_sm < ntiles ? nsm * per_sm : ntiles;
-    if (grid < 1) grid = 1;
-    col_map_kernel<N><<<grid, Cfg::THREADS, Cfg::SMEM, s>>>(map, a);
-    return cudaGetLastError();
-}
 static cudaError_t col_half_launch(const ColArgs &a, cudaStream_t s, int nsm) {
     using Cfg = ColHalfCfg;
     static int per_sm = 0;
@@ -1489,10 +1331,10 @@ cudaError_t launch_row_pass(int ny, const RowArgs &a, cudaStream_t s, int nsm, i
 cudaError_t launch_col_pass(int nx, const ColArgs &a, cudaStream_t s, int nsm, int64_t *launches) {
     ++*launches;
     if (tma_eligible(a)) {
-        // the slice loop's transform pair at 512: the two-mapping kernel
+        // the slice loop's transform pair at 512: half-warp columns
         if (nx == 512 && (a.flags & COL_LOAD) && (a.flags & COL_FWD) && (a.flags & COL_INV) &&
-            !(a.flags & COL_PROBE))
-            return a.ny % ColHalfCfg::C == 0 ? col_half_launch(a, s, nsm) : col_map_launch<512>(a, s, nsm);
+            !(a.flags & COL_PROBE) && a.ny % ColHalfCfg::C == 0)
+            return col_half_launch(a, s, nsm);
         switch (nx) {
 #define X(N) case N: return col_tma_launch<N>(a, s, nsm);
             MSL_FOR_EACH_SIDE(X)
