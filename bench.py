@@ -203,7 +203,7 @@ def run_ours(args):
     h2d = spec.natom * (3 * 8 + 4) + 104 * 12 * 8 + nprobe * 2 * 8
     d2h = res_host.nbytes
 
-    # roofline of the dominant kernel (the column pass; row pass reported beside it)
+    # roofline of the dominant kernel (the pass with the larger device time; the other beside it)
     hbm, peak_kind = peaks()
     rows = {}
     for kind in ("row", "col"):
