@@ -398,7 +398,7 @@ __global__ void __launch_bounds__(ColHalfCfg::THREADS, 1)
     const uint32_t sbase = smem_u32(smraw);
     const uint32_t slot0 = (sbase + (uint32_t)Cfg::HEADER + SLOT - 1u) & ~(SLOT - 1u);
     if (slot0 + (uint32_t)(NBUF * G) * SLOT > sbase + (uint32_t)Cfg::SMEM) {  // uniform over the CTA
-        if (threadIdx.x == 0 && a.err) atomicExch(a.err, 1);
+        if (threadIdx.x == 0 && a.err) atomicExch(a.err, 2);                  // layout error, not a timeout
         return;
     }
     float2 *tw = reinterpret_cast<float2 *>(smraw);
