@@ -509,8 +509,20 @@ __device__ __forceinline__ void fft_line(float2 (&v)[P::E], int t, const Addr &a
 struct HalfWarpPlan512 {
     static constexpr int N = 512, T = 16, E = 32, NSTAGE = 2;
     static constexpr int row_swz = 1, row_sh = 4, col_c = 4, col_ps = 30;
-    static constexpr bool PK = true, PKMUL = false;
+    static constexpr bool PK = true, PKMUL = false, CW = false;
     static constexpr int radix(int s) { return s == 0 ? 16 : 32; }
+};
+// Two-stage plan for 1024-point lines, one warp per line (32 threads x 32
+// elements): radix 32 then radix 32, a single exchange per transform.  The
+// exchange swizzle i ^ ((i >> 5) & 15) keeps both of its access patterns
+// (32 t + r and t + 32 e) on 16 distinct bank pairs per half-warp.
+// Its stage-1 twiddles are formed in registers from w^k (CW, fft_stage_cw), so
+// the kernel's table is two rows of 32 instead of 32 x 32 entries.
+struct WarpPlan1024x2 {
+    static constexpr int N = 1024, T = 32, E = 32, NSTAGE = 2;
+    static constexpr int row_swz = 1, row_sh = 5, col_c = 4, col_ps = 30;
+    static constexpr bool PK = true, PKMUL = false, CW = true;
+    static constexpr int radix(int) { return 32; }
 };
 // The same plan for the half-warp column pass, with packed twiddle products.
 struct HalfWarpColPlan512 : HalfWarpPlan512 {
@@ -561,7 +573,8 @@ __device__ __forceinline__ void fft_exchange_ch(float2 (&v)[P::E], int t, uint32
 template <class P, int DIR, int S = 0>
 __device__ __forceinline__ void fft_line_tab(float2 (&v)[P::E], int t, const RowXorLin<P> &ad,
                                              const float2 *__restrict__ tw) {
-    fft_stage<P, S, DIR>(v, t, tw);
+    if constexpr (P::CW) fft_stage_cw<P, S, DIR>(v, t, tw);
+    else fft_stage<P, S, DIR>(v, t, tw);
     if constexpr (S + 1 < P::NSTAGE) {
         fft_exchange_xl<P, S>(v, t, ad);
         fft_line_tab<P, DIR, S + 1>(v, t, ad, tw);

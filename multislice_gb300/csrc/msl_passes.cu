@@ -797,31 +797,36 @@ __global__ void __launch_bounds__(RowWarpCfg<N>::THREADS, RowWarpCfg<N>::MINB) r
 // copy into a private two-slot ring per warp; the next pair is requested once
 // the previous pair's store has read its slot.  The stage-1 twiddle table is
 // formed in shared memory at start-up.
-struct RowHalfCfg {
-    using P = HalfWarpPlan512;
-    static constexpr int N = 512, W = 4, THREADS = 32 * W, NBUF = 2, MINB = 3;
-    static constexpr size_t LINE = sizeof(float2) * N, SLOT = 2 * LINE;
+template <class P_> struct RowTwoCfg {
+    using P = P_;
+    static constexpr int N = P::N, W = 4, THREADS = 32 * W, NBUF = 2, MINB = 3;
+    static constexpr int LPW = 32 / P::T;  // lines per warp: 2 (half-warp lines) or 1
+    static constexpr int R0 = P::radix(0), R1 = P::radix(1);
+    static constexpr size_t LINE = sizeof(float2) * N, SLOT = LPW * LINE;
     static constexpr uint32_t ALIGN = (uint32_t)LINE;  // each line's exchange space is line-aligned
-    static constexpr int TW = 32 * 16;
+    // stage 1 table [r][k], k < R0: every r < R1, or rows 0 and 1 when the
+    // plan forms the powers w^r in registers (CW)
+    static constexpr int TW = (P::CW ? 2 : R1) * R0;
+    static_assert(P::NSTAGE == 2 && R0 * R1 == N && (P::T == 16 || P::T == 32), "two-stage warp-owned lines");
     static constexpr size_t OFF_TW = (size_t)W * NBUF * SLOT;
     static constexpr size_t OFF_BAR = OFF_TW + sizeof(float2) * TW;
     static constexpr size_t SMEM = OFF_BAR + sizeof(uint64_t) * W * NBUF + ALIGN;
 };
 
-__global__ void __launch_bounds__(RowHalfCfg::THREADS, RowHalfCfg::MINB) row_half_kernel(RowArgs a) {
-    using Cfg = RowHalfCfg;
-    using P = Cfg::P;
-    constexpr int N = Cfg::N, E = P::E, NBUF = Cfg::NBUF, W = Cfg::W;
+template <class P>
+__global__ void __launch_bounds__(RowTwoCfg<P>::THREADS, RowTwoCfg<P>::MINB) row_two_kernel(RowArgs a) {
+    using Cfg = RowTwoCfg<P>;
+    constexpr int N = Cfg::N, E = P::E, T = P::T, NBUF = Cfg::NBUF, W = Cfg::W, LPW = Cfg::LPW, R0 = Cfg::R0;
     constexpr uint32_t AL = Cfg::ALIGN;
     extern __shared__ unsigned char smraw[];
     unsigned char *base = smraw + ((AL - (smem_u32(smraw) & (AL - 1u))) & (AL - 1u));
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, h = lane >> 4, t = lane & 15;
-    float2 *ring = reinterpret_cast<float2 *>(base) + (size_t)warp * NBUF * 2 * N;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, h = lane / T, t = lane % T;
+    float2 *ring = reinterpret_cast<float2 *>(base) + (size_t)warp * NBUF * LPW * N;
     float2 *tw = reinterpret_cast<float2 *>(base + Cfg::OFF_TW);
     uint64_t *bar = reinterpret_cast<uint64_t *>(base + Cfg::OFF_BAR) + warp * NBUF;
     for (int i = threadIdx.x; i < Cfg::TW; i += Cfg::THREADS) {
         float sn, cn;
-        sincospif((float)(2 * (i >> 4) * (i & 15)) / (float)N, &sn, &cn);  // exp(2 pi i r k / 512), [r][k]
+        sincospif((float)(2 * (i / R0) * (i % R0)) / (float)N, &sn, &cn);  // exp(2 pi i r k / N), [r][k]
         tw[i] = make_float2(cn, sn);
     }
     if (lane == 0) {
@@ -830,7 +835,7 @@ __global__ void __launch_bounds__(RowHalfCfg::THREADS, RowHalfCfg::MINB) row_hal
     }
     __syncthreads();  // the only CTA barrier: tables and barriers are ready
     const bool load = (a.flags & ROW_LOAD) != 0, store = !(a.flags & ROW_NOSTORE);
-    const int npairs = a.nlines / 2;
+    const int npairs = a.nlines / LPW;  // units of LPW consecutive lines
     const int G = gridDim.x * W, gw = blockIdx.x * W + warp;
     const int nmine = gw < npairs ? (npairs - gw + G - 1) / G : 0;
     int issued = 0;
@@ -838,15 +843,15 @@ __global__ void __launch_bounds__(RowHalfCfg::THREADS, RowHalfCfg::MINB) row_hal
         const int pair = gw + k * G, s = k % NBUF;
         fence_proxy_async();
         mbar_arrive_expect_tx(&bar[s], (uint32_t)Cfg::SLOT);
-        bulk_load(ring + (size_t)s * 2 * N, a.in + (size_t)pair * 2 * N, (uint32_t)Cfg::SLOT, &bar[s]);
+        bulk_load(ring + (size_t)s * LPW * N, a.in + (size_t)pair * LPW * N, (uint32_t)Cfg::SLOT, &bar[s]);
         issued = k + 1;
     };
     if (load && lane == 0 && nmine > 0) issue(0);
     int k = 0;
     bool ok = true;
     for (; k < nmine; ++k) {
-        const int pair = gw + k * G, s = k % NBUF, line = 2 * pair + h;
-        float2 *slot = ring + (size_t)s * 2 * N;
+        const int pair = gw + k * G, s = k % NBUF, line = LPW * pair + h;
+        float2 *slot = ring + (size_t)s * LPW * N;
         float2 *buf = slot + (size_t)h * N;
         const RowXorLin<P> ad{smem_u32(buf)};
         const float2 *trow = (a.flags & ROW_TRANS)
@@ -865,7 +870,7 @@ __global__ void __launch_bounds__(RowHalfCfg::THREADS, RowHalfCfg::MINB) row_hal
                 break;
             }
 #pragma unroll
-            for (int e = 0; e < E; ++e) v[e] = buf[t + 16 * e];
+            for (int e = 0; e < E; ++e) v[e] = buf[t + T * e];
         } else {
 #pragma unroll
             for (int e = 0; e < E; ++e) v[e] = make_float2(1.f, 0.f);
@@ -873,7 +878,7 @@ __global__ void __launch_bounds__(RowHalfCfg::THREADS, RowHalfCfg::MINB) row_hal
         if (a.flags & ROW_INV) fft_line_tab<P, -1>(v, t, ad, tw);
         if (a.flags & ROW_TRANS) {
 #pragma unroll
-            for (int e = 0; e < E; ++e) v[e] = c_mul(v[e], __ldg(trow + t + 16 * e));
+            for (int e = 0; e < E; ++e) v[e] = c_mul(v[e], __ldg(trow + t + T * e));
         }
         if (a.flags & ROW_FWD) fft_line_tab<P, +1>(v, t, ad, tw);
         if (a.scale != 1.0f) {
@@ -884,16 +889,16 @@ __global__ void __launch_bounds__(RowHalfCfg::THREADS, RowHalfCfg::MINB) row_hal
             double *acc = a.accum + (size_t)line * N;
 #pragma unroll
             for (int e = 0; e < E; ++e)
-                acc[t + 16 * e] += a.accum_w * ((double)v[e].x * v[e].x + (double)v[e].y * v[e].y);
+                acc[t + T * e] += a.accum_w * ((double)v[e].x * v[e].x + (double)v[e].y * v[e].y);
         }
         if (store) {
             __syncwarp();  // every lane is done reading the slot
 #pragma unroll
-            for (int e = 0; e < E; ++e) buf[t + 16 * e] = v[e];
+            for (int e = 0; e < E; ++e) buf[t + T * e] = v[e];
             fence_proxy_async();
             __syncwarp();
             if (lane == 0) {
-                bulk_store(a.out + (size_t)pair * 2 * N, slot, (uint32_t)Cfg::SLOT);
+                bulk_store(a.out + (size_t)pair * LPW * N, slot, (uint32_t)Cfg::SLOT);
                 tma_commit();
             }
         }
@@ -909,21 +914,21 @@ __global__ void __launch_bounds__(RowHalfCfg::THREADS, RowHalfCfg::MINB) row_hal
     }
 }
 
-static cudaError_t row_half_launch(const RowArgs &a, cudaStream_t s, int nsm) {
-    using Cfg = RowHalfCfg;
+template <class P> static cudaError_t row_two_launch(const RowArgs &a, cudaStream_t s, int nsm) {
+    using Cfg = RowTwoCfg<P>;
     static int per_sm = 0;
     if (!per_sm) {
-        cudaError_t e = cudaFuncSetAttribute(row_half_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaError_t e = cudaFuncSetAttribute(row_two_kernel<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)Cfg::SMEM);
         if (e != cudaSuccess) return e;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, row_half_kernel, Cfg::THREADS, Cfg::SMEM);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, row_two_kernel<P>, Cfg::THREADS, Cfg::SMEM);
         if (e != cudaSuccess) return e;
         if (per_sm < 1) per_sm = 1;
     }
-    const int nwarps = (a.nlines / 2 + Cfg::W - 1) / Cfg::W;
+    const int nwarps = (a.nlines / Cfg::LPW + Cfg::W - 1) / Cfg::W;
     int grid = nsm * per_sm < nwarps ? nsm * per_sm : nwarps;
     if (grid < 1) grid = 1;
-    row_half_kernel<<<grid, Cfg::THREADS, Cfg::SMEM, s>>>(a);
+    row_two_kernel<P><<<grid, Cfg::THREADS, Cfg::SMEM, s>>>(a);
     return cudaGetLastError();
 }
 
@@ -1236,7 +1241,7 @@ template <int N> static cudaError_t row_warp_launch(const RowArgs &a, cudaStream
 
 // Warp-owned lines for the sides whose plan fits 32 threads per line.
 static bool row_warp_eligible(int ny, const RowArgs &a) {
-    if (ny != 256 && ny != 384 && ny != 512) return false;
+    if (ny != 256 && ny != 384 && ny != 512 && ny != 1024) return false;
     if (a.flags & ROW_GENT) return false;
     if (((uintptr_t)a.out & 15u) || ((a.flags & ROW_LOAD) && ((uintptr_t)a.in & 15u))) return false;
     return true;
@@ -1307,8 +1312,9 @@ cudaError_t launch_row_pass(int ny, const RowArgs &a, cudaStream_t s, int nsm, i
             case 384: return row_warp_launch<384>(a, s, nsm);
             case 512:
                 if (a.nlines % 2 == 0 && !(((uintptr_t)a.out | (uintptr_t)a.in) & 15u))
-                    return row_half_launch(a, s, nsm);
+                    return row_two_launch<HalfWarpPlan512>(a, s, nsm);
                 return row_warp_launch<512>(a, s, nsm);
+            case 1024: return row_two_launch<WarpPlan1024x2>(a, s, nsm);
             default: break;
         }
     }
