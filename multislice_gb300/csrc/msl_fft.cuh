@@ -524,49 +524,65 @@ struct WarpPlan1024x2 {
     static constexpr bool PK = true, PKMUL = false, CW = true;
     static constexpr int radix(int) { return 32; }
 };
-// The same plan for the half-warp column pass, with packed twiddle products.
+// The same plans for the column passes: table twiddles with packed products.
 struct HalfWarpColPlan512 : HalfWarpPlan512 {
     static constexpr bool PKMUL = true;
 };
+struct WarpPairColPlan1024 : WarpPlan1024x2 {
+    static constexpr bool PKMUL = true, CW = false;
+};
 
-// Half-warp-owned 512-point columns inside a tile of 8 columns x 512 rows laid
-// out by the TMA 64-byte swizzle: element (r, c) at byte 64 r + (8 c ^ 16 ((r >> 1) & 3)),
-// i.e. B(r) ^ 8 c with B(p) = 64 p | 16 ((p >> 1) & 3).  The exchange keeps
-// logical slot i of column c at row pi(i) = i ^ ((i >> 4) & 7) of the same
-// column, so its address is L(i) ^ 8 c with L = B o pi.  B and pi are linear
-// over xor; with the tile aligned to 32 KB (every L(i) ^ 8 c is below 32 KB)
-// an access is a per-thread base xor a compile-time constant.  Two columns per
-// warp, lane l on column l & 1 as thread t = l >> 1: each half-warp's sixteen
-// 64-bit accesses (8 rows of both columns) then hit sixteen distinct bank pairs
-// for the natural-order accesses (row t + 16 e) and for the exchange writes
-// (16 t + 256 q + r) and reads (t + 16 e), one wavefront per half-warp.
-struct ColHalfLin {
+
+// Column tiles of C columns x N rows laid out by a TMA swizzle, and the exchange
+// that reuses each column's own slots.
+//
+// ColLin64 (512-point columns, C = 8, 64-byte rows, 64-byte swizzle): element
+// (r, c) at byte 64 r + (8 c ^ 16 ((r >> 1) & 3)), i.e. B(r) ^ 8 c with
+// B(p) = 64 p | 16 ((p >> 1) & 3); the exchange keeps logical slot i at row
+// pi(i) = i ^ ((i >> 4) & 7).  ColLin32 (1024-point columns, C = 4, 32-byte
+// rows, 32-byte swizzle): B(p) = 32 p | 16 ((p >> 2) & 1), pi(i) = i ^ ((i >> 5) & 7).
+// Slot i of column c is at L(i) ^ 8 c, L = B o pi.  B and pi are linear over
+// xor; with the tile aligned to 32 KB (every L(i) ^ 8 c is below 32 KB) an
+// access is a per-thread base xor a compile-time constant.  A column's threads
+// sit in one warp (512: lane l on column l & 1 as thread l >> 1) or in a warp
+// pair (1024: 16 lanes of each warp, alternating between the pair's two
+// columns); either way each half-warp's sixteen 64-bit accesses cover 8 rows of
+// two columns, which for the natural order (row t + T e), the exchange writes
+// (T t + r) and reads (t + T e) hits sixteen distinct bank pairs: one wavefront
+// per half-warp (a CPU bank model checked every pattern).
+struct ColLin64 {
     static __host__ __device__ constexpr uint32_t B(uint32_t p) { return (p << 6) | (((p >> 1) & 3u) << 4); }
     static __host__ __device__ constexpr uint32_t pi(uint32_t i) { return i ^ ((i >> 4) & 7u); }
     static __host__ __device__ constexpr uint32_t L(uint32_t i) { return B(pi(i)); }
 };
+struct ColLin32 {
+    static __host__ __device__ constexpr uint32_t B(uint32_t p) { return (p << 5) | (((p >> 2) & 1u) << 4); }
+    static __host__ __device__ constexpr uint32_t pi(uint32_t i) { return i ^ ((i >> 5) & 7u); }
+    static __host__ __device__ constexpr uint32_t L(uint32_t i) { return B(pi(i)); }
+};
 
-// Exchange after stage S of a HalfWarpPlan512 column; cb = tile address ^ 8 c.
-// Index split as in fft_exchange_xl.
-template <class P, int S>
-__device__ __forceinline__ void fft_exchange_ch(float2 (&v)[P::E], int t, uint32_t cb) {
+// Exchange after stage S of a column held T threads x E elements in such a tile;
+// cb = tile address ^ 8 c; sync() orders the column's threads (a warp or a
+// warp pair).  Index split as in fft_exchange_xl.
+template <class P, int S, class Lin, class Sync>
+__device__ __forceinline__ void fft_exchange_ch(float2 (&v)[P::E], int t, uint32_t cb, const Sync &sync) {
     constexpr int R = P::radix(S), NS = plan_span<P>(S), E = P::E, Q = E / R, T = P::T;
-    static_assert(T == 16 && P::N == 512, "half-warp column exchange: 512-point columns, 16 threads");
+    static_assert((T == 16 || T == 32) && (NS & (NS - 1)) == 0 && (R & (R - 1)) == 0, "power-of-two column plans");
     const int tw_part = NS <= T ? (t / NS) * NS * R + t % NS : t;
-    const uint32_t wb = cb ^ ColHalfLin::L((uint32_t)tw_part);
-    const uint32_t rb = cb ^ ColHalfLin::L((uint32_t)t);
-    __syncwarp();  // previous readers of the column are done
+    const uint32_t wb = cb ^ Lin::L((uint32_t)tw_part);
+    const uint32_t rb = cb ^ Lin::L((uint32_t)t);
+    sync();  // previous readers of the column are done
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             const int K = NS <= T ? q * T * R + r * NS : (q / (NS / T)) * NS * R + T * (q % (NS / T)) + r * NS;
-            sts_f2(wb ^ ColHalfLin::L((uint32_t)K), v[q + r * Q]);
+            sts_f2(wb ^ Lin::L((uint32_t)K), v[q + r * Q]);
         }
     }
-    __syncwarp();
+    sync();
 #pragma unroll
-    for (int e = 0; e < E; ++e) v[e] = lds_f2(rb ^ ColHalfLin::L((uint32_t)(T * e)));
+    for (int e = 0; e < E; ++e) v[e] = lds_f2(rb ^ Lin::L((uint32_t)(T * e)));
 }
 
 // Warp- or half-warp-owned line with table twiddles and xor-linear exchanges.

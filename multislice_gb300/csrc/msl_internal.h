@@ -84,8 +84,10 @@ struct PotArgs {
 };
 
 bool plan_supported(int n);
-// Columns per tile of the column pass that will run for this call (TMA-fed
-// kernel when the wave buffer allows it, else the register-only kernel).
+// Columns per detector-partial tile of the slice loop's column pass for this
+// call's buffers: 4 for the two-stage kernels (512, 1024), the TMA-fed
+// kernel's tile width where the wave buffer allows TMA, else the register-only
+// kernel's.
 int plan_col_c(int n);
 int plan_col_c_launch(int n, const ColArgs &a);
 // Per-stage twiddle tables for side n (exp(+2 pi i r k / (NS R)) at [r][k]).

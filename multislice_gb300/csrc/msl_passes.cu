@@ -362,37 +362,62 @@ __global__ void __launch_bounds__(ColTmaCfg<PL>::THREADS, MINB)
 }
 
 
-// ------------------------------------- column pass, half-warp columns, 512
-// The slice loop's column transform pair at N = 512 built like the half-warp
-// row pass: each column is one half-warp's line (16 threads x 32 elements,
-// radix 16 x 32, one warp-synchronous exchange per transform; the two columns
-// of a warp interleave lane by lane).  Tiles of 8
-// columns x 512 rows arrive by TMA with the 64-byte swizzle, so the
-// natural-order reads and writes of two columns per warp are conflict-free; the
-// exchange reuses the column's own slots in the permuted order of ColHalfLin.
-// One CTA per SM runs G groups of 4 warps; each group streams its own tiles
-// through a two-slot ring of 32 KB-aligned slots (every exchange address is a
-// per-thread base xor a constant).  Group barriers per tile: the arrival vote
-// and the one before the TMA store (two more at detector checkpoints).
-// Detector partial sums are written per 4 columns, the tile layout of the other
-// column passes at 512.
-struct ColHalfCfg {
+// ------------------------------- column pass, two-stage columns, 512 / 1024
+// The slice loop's column transform pair at N = 512 and 1024 built like the
+// two-stage row pass: each column is one line of T threads x 32 elements
+// (radix 16 x 32 at 512, 32 x 32 at 1024), one exchange per transform.  Tiles
+// of C columns x N rows (32 KB) arrive by TMA with a swizzle (ColLin64,
+// ColLin32) under which the natural-order reads and writes of the tile are
+// conflict-free; the exchange reuses each column's own slots in a permuted
+// order, conflict-free too.  At 512 a warp owns two columns (16 lanes each,
+// alternating) and its exchanges need only the warp; at 1024 a warp pair owns
+// two columns (16 lanes of each warp per column) and syncs on a named barrier
+// of 64 threads.  One CTA per SM runs G groups of 4 warps; each group streams
+// its own tiles through a two-slot ring of 32 KB-aligned slots (every exchange
+// address is a per-thread base xor a constant).  Group barriers per tile: the
+// arrival vote and the one before the TMA store (two more at detector
+// checkpoints).  Detector partial sums are written per 4 columns.
+struct ColHalfL512 {  // 512: 8 columns, a warp per column pair
     using P = HalfWarpColPlan512;
-    static constexpr int N = 512, C = 8, G = 3, GT = 128, THREADS = GT * G, NBUF = 2, BOXR = 256;
+    using Lin = ColLin64;
+    static constexpr int N = 512, C = 8;
+    static constexpr bool PAIR = false;
+    static constexpr CUtensorMapSwizzle SWZ = CU_TENSOR_MAP_SWIZZLE_64B;
+    __device__ static int col(int wg, int lane) { return 2 * wg + (lane & 1); }
+    __device__ static int thr(int wg, int lane) { return lane >> 1; }
+};
+struct ColPairL1024 {  // 1024: 4 columns, a warp pair per column pair
+    using P = WarpPairColPlan1024;
+    using Lin = ColLin32;
+    static constexpr int N = 1024, C = 4;
+    static constexpr bool PAIR = true;
+    static constexpr CUtensorMapSwizzle SWZ = CU_TENSOR_MAP_SWIZZLE_32B;
+    __device__ static int col(int wg, int lane) { return 2 * (wg >> 1) + (lane & 1); }
+    __device__ static int thr(int wg, int lane) { return 16 * (wg & 1) + (lane >> 1); }
+};
+
+template <class L> struct ColHalfCfg {
+    using P = typename L::P;
+    static constexpr int N = L::N, C = L::C, G = 3, GT = 128, THREADS = GT * G, NBUF = 2, BOXR = 256;
     static constexpr uint32_t SLOT = sizeof(float2) * N * C;  // 32 KB, also the slot alignment
-    static constexpr int TW = 32 * 16;
+    static constexpr int TW = P::radix(1) * P::radix(0);      // stage 1 table [r][k]
     static constexpr size_t OFF_RED = sizeof(float2) * TW;
     static constexpr size_t OFF_BAR = OFF_RED + sizeof(double) * G * 4 * kMaxDet;
     static constexpr size_t HEADER = OFF_BAR + sizeof(uint64_t) * G * NBUF;
     static constexpr size_t SMEM = 227 * 1024;  // the header, then 2 G slots from the next 32 KB boundary
-    static_assert(SLOT == 32768 && N % BOXR == 0, "32 KB tiles of two TMA boxes");
+    static_assert(SLOT == 32768 && N % BOXR == 0 && P::NSTAGE == 2 && C % 4 == 0, "32 KB tiles, two stages");
+    static_assert(L::Lin::B(P::T) == 1024 && L::Lin::B(P::T - 1) < 1024, "natural order: row t + T e at + 1024 e");
+    static_assert(HEADER <= SLOT, "the header fits before the first slot");
 };
 
-__global__ void __launch_bounds__(ColHalfCfg::THREADS, 1)
+template <class L>
+__global__ void __launch_bounds__(ColHalfCfg<L>::THREADS, 1)
     col_half_kernel(const __grid_constant__ CUtensorMap map, ColArgs a) {
-    using Cfg = ColHalfCfg;
-    using P = Cfg::P;
-    constexpr int N = Cfg::N, C = Cfg::C, E = P::E, G = Cfg::G, GT = Cfg::GT, NBUF = Cfg::NBUF;
+    using Cfg = ColHalfCfg<L>;
+    using P = typename Cfg::P;
+    using Lin = typename L::Lin;
+    constexpr int N = Cfg::N, C = Cfg::C, E = P::E, T = P::T, G = Cfg::G, GT = Cfg::GT, NBUF = Cfg::NBUF;
+    constexpr int R0 = P::radix(0);
     constexpr uint32_t SLOT = Cfg::SLOT;
     extern __shared__ unsigned char smraw[];
     const uint32_t sbase = smem_u32(smraw);
@@ -406,7 +431,7 @@ __global__ void __launch_bounds__(ColHalfCfg::THREADS, 1)
     uint64_t *barall = reinterpret_cast<uint64_t *>(smraw + Cfg::OFF_BAR);
     for (int i = threadIdx.x; i < Cfg::TW; i += Cfg::THREADS) {
         float sn, cn;
-        sincospif((float)(2 * (i >> 4) * (i & 15)) / (float)N, &sn, &cn);  // exp(2 pi i r k / 512), [r][k]
+        sincospif((float)(2 * (i / R0) * (i % R0)) / (float)N, &sn, &cn);  // exp(2 pi i r k / N), [r][k]
         tw[i] = make_float2(cn, sn);
     }
     if (threadIdx.x == 0) {
@@ -415,9 +440,14 @@ __global__ void __launch_bounds__(ColHalfCfg::THREADS, 1)
     }
     __syncthreads();  // the only CTA-wide barrier
     const int g = threadIdx.x / GT, gt = threadIdx.x % GT, wg = gt >> 5, lane = gt & 31;
-    // two columns per warp, lanes alternating between them: each half-warp then
-    // touches 8 rows of both, which is what keeps its 64-bit accesses on 16 bank pairs
-    const int t = lane >> 1, c = 2 * wg + (lane & 1);
+    // lanes alternate between two columns: each half-warp then touches 8 rows of
+    // both, which is what keeps its 64-bit accesses on 16 bank pairs
+    const int t = L::thr(wg, lane), c = L::col(wg, lane);
+    const uint32_t pairid = 4u + 2u * (uint32_t)g + (uint32_t)(wg >> 1);  // the warp pair's barrier (1024)
+    auto colsync = [&]() {
+        if constexpr (L::PAIR) bar_group(pairid, 64);
+        else __syncwarp();
+    };
     const uint32_t barid = 1u + (uint32_t)g;
     uint64_t *bar = barall + g * NBUF;
     double *red = redall + g * 4 * kMaxDet;
@@ -453,12 +483,12 @@ __global__ void __launch_bounds__(ColHalfCfg::THREADS, 1)
             break;
         }
         const uint32_t cb = (gslot + (uint32_t)s * SLOT) ^ (8u * (uint32_t)c);
-        const uint32_t nb = cb ^ ColHalfLin::B((uint32_t)t);  // row t + 16 e at nb + 1024 e
+        const uint32_t nb = cb ^ Lin::B((uint32_t)t);  // row t + T e at nb + 1024 e
         float2 v[E];
 #pragma unroll
         for (int e = 0; e < E; ++e) v[e] = lds_f2(nb + 1024u * (uint32_t)e);
         fft_stage<P, 0, +1>(v, t, tw);
-        fft_exchange_ch<P, 0>(v, t, cb);
+        fft_exchange_ch<P, 0, Lin>(v, t, cb, colsync);
         fft_stage<P, 1, +1>(v, t, tw);
         const int iy = ty * C + c;
         if (a.flags & COL_PROP) col_propagate<P>(v, a, b, iy, t);
@@ -469,7 +499,7 @@ __global__ void __launch_bounds__(ColHalfCfg::THREADS, 1)
             for (int d = 0; d < kMaxDet; ++d) acc[d] = 0.f;
 #pragma unroll
             for (int e = 0; e < E; ++e) {
-                const unsigned bits = a.detmask[(size_t)(t + 16 * e) * a.ny + iy];
+                const unsigned bits = a.detmask[(size_t)(t + T * e) * a.ny + iy];
                 const float p = v[e].x * v[e].x + v[e].y * v[e].y;
 #pragma unroll
                 for (int d = 0; d < kMaxDet; ++d)
@@ -486,17 +516,22 @@ __global__ void __launch_bounds__(ColHalfCfg::THREADS, 1)
                 }
             }
             bar_group(barid, GT);
-            if (gt < 2 * a.ndet) {  // warps 2h, 2h + 1 hold columns 4h .. 4h + 3
+            constexpr int NBLK = C / 4, WPB = 4 / NBLK;  // 4-column blocks per tile, warps per block
+            if (gt < NBLK * a.ndet) {                   // warps WPB hq .. WPB hq + WPB - 1 hold block hq
                 const int hq = gt / a.ndet, d = gt % a.ndet;
-                const double sum = red[(2 * hq) * kMaxDet + d] + red[(2 * hq + 1) * kMaxDet + d];
-                a.partial[((size_t)b * (a.ny / 4) + 2 * ty + hq) * a.ndet + d] = sum;
+                double sum = 0.0;
+#pragma unroll
+                for (int w = 0; w < WPB; ++w) sum += red[(WPB * hq + w) * kMaxDet + d];
+                a.partial[((size_t)b * (a.ny / 4) + NBLK * ty + hq) * a.ndet + d] = sum;
             }
         }
-        fft_stage<P, 0, -1>(v, t, tw);
-        fft_exchange_ch<P, 0>(v, t, cb);
-        fft_stage<P, 1, -1>(v, t, tw);
+        if (a.flags & COL_INV) {  // absent on a scan's last slice (detection only)
+            fft_stage<P, 0, -1>(v, t, tw);
+            fft_exchange_ch<P, 0, Lin>(v, t, cb, colsync);
+            fft_stage<P, 1, -1>(v, t, tw);
+        }
         if (store) {
-            __syncwarp();  // every lane of the warp is done reading its columns
+            colsync();  // every thread of the columns is done reading them
 #pragma unroll
             for (int e = 0; e < E; ++e) sts_f2(nb + 1024u * (uint32_t)e, v[e]);
             fence_proxy_async();
@@ -1145,14 +1180,14 @@ template <class PL, int MINB> static cudaError_t col_tma_launch_v(const ColArgs 
     return cudaGetLastError();
 }
 
-static cudaError_t col_half_launch(const ColArgs &a, cudaStream_t s, int nsm) {
-    using Cfg = ColHalfCfg;
+template <class L> static cudaError_t col_half_launch(const ColArgs &a, cudaStream_t s, int nsm) {
+    using Cfg = ColHalfCfg<L>;
     static int per_sm = 0;
     if (!per_sm) {
-        cudaError_t e = cudaFuncSetAttribute(col_half_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaError_t e = cudaFuncSetAttribute(col_half_kernel<L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)Cfg::SMEM);
         if (e != cudaSuccess) return e;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, col_half_kernel, Cfg::THREADS, Cfg::SMEM);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, col_half_kernel<L>, Cfg::THREADS, Cfg::SMEM);
         if (e != cudaSuccess) return e;
         if (per_sm < 1) return cudaErrorInvalidConfiguration;
     }
@@ -1162,14 +1197,24 @@ static cudaError_t col_half_launch(const ColArgs &a, cudaStream_t s, int nsm) {
     const cuuint32_t box[2] = {(cuuint32_t)Cfg::C, (cuuint32_t)Cfg::BOXR};
     const cuuint32_t estride[2] = {1, 1};
     CUresult r = encode_fn()(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, (void *)a.out, gdim, gstride, box,
-                             estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                             estride, CU_TENSOR_MAP_INTERLEAVE_NONE, L::SWZ,
                              CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
     const int ngroups = (a.batch * (a.ny / Cfg::C) + Cfg::G - 1) / Cfg::G;
     int grid = nsm * per_sm < ngroups ? nsm * per_sm : ngroups;
     if (grid < 1) grid = 1;
-    col_half_kernel<<<grid, Cfg::THREADS, Cfg::SMEM, s>>>(map, a);
+    col_half_kernel<L><<<grid, Cfg::THREADS, Cfg::SMEM, s>>>(map, a);
     return cudaGetLastError();
+}
+// The column pass the slice loop takes at side n (0: col_tma_kernel): every
+// pass that loads the wave and starts with the forward transform, with or
+// without the inverse (a scan's last slice detects only), so all detector
+// passes of a scan write partials per 4 columns.
+static int col_half_side(int n, const ColArgs &a) {
+    if (!(a.flags & COL_LOAD) || !(a.flags & COL_FWD) || (a.flags & COL_PROBE)) return 0;
+    if (n == 512 && a.ny % ColHalfL512::C == 0) return 512;
+    if (n == 1024 && a.ny % ColPairL1024::C == 0) return 1024;
+    return 0;
 }
 template <int N> static cudaError_t col_tma_launch(const ColArgs &a, cudaStream_t s, int nsm) {
     return col_tma_launch_v<ColPlan<N>, ColPlan<N>::MINB>(a, s, nsm);
@@ -1270,6 +1315,11 @@ int plan_col_c(int n) {
 
 int plan_col_c_launch(int n, const ColArgs &a) {
     if (tma_eligible(a)) {
+        // the slice loop's column pass (load, forward, inverse) on two-stage
+        // columns writes detector partials per 4 columns
+        ColArgs f = a;
+        f.flags = (f.flags | COL_LOAD | COL_FWD) & ~COL_PROBE;
+        if (col_half_side(n, f)) return 4;
         switch (n) {
 #define X(N) case N: return ColPlan<N>::col_c;
             MSL_FOR_EACH_SIDE(X)
@@ -1337,10 +1387,12 @@ cudaError_t launch_row_pass(int ny, const RowArgs &a, cudaStream_t s, int nsm, i
 cudaError_t launch_col_pass(int nx, const ColArgs &a, cudaStream_t s, int nsm, int64_t *launches) {
     ++*launches;
     if (tma_eligible(a)) {
-        // the slice loop's transform pair at 512: half-warp columns
-        if (nx == 512 && (a.flags & COL_LOAD) && (a.flags & COL_FWD) && (a.flags & COL_INV) &&
-            !(a.flags & COL_PROBE) && a.ny % ColHalfCfg::C == 0)
-            return col_half_launch(a, s, nsm);
+        // the slice loop's transform pair at 512 and 1024: two-stage columns
+        switch (col_half_side(nx, a)) {
+            case 512: return col_half_launch<ColHalfL512>(a, s, nsm);
+            case 1024: return col_half_launch<ColPairL1024>(a, s, nsm);
+            default: break;
+        }
         switch (nx) {
 #define X(N) case N: return col_tma_launch<N>(a, s, nsm);
             MSL_FOR_EACH_SIDE(X)

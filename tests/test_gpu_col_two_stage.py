@@ -1,7 +1,8 @@
-"""The slice loop's column pass at nx = 512 (half-warp columns in 8-column TMA
-tiles, three independent thread groups per CTA): non-square grids, batches that
-leave groups without tiles, several detectors and checkpoints, against the FP64
-oracle."""
+"""The slice loop's two-stage column passes at nx = 512 and 1024 (columns of 32
+elements per thread in swizzled 32 KB TMA tiles, three independent thread groups
+per CTA; at 1024 a column is shared by a warp pair): non-square grids, batches
+that leave groups without tiles, several detectors and checkpoints, against the
+FP64 oracle."""
 import numpy as np
 import pytest
 
@@ -19,10 +20,11 @@ def _layers(rng, nt, nx, ny, ax, by, kev):
     return O.transmission(v, kev, ax, by, np.complex64)
 
 
-@pytest.mark.parametrize("ny,batch", [(64, 1), (384, 3), (1024, 2), (512, 5)])
-def test_ctem_nx512_matches_oracle(ctx, ny, batch):
-    rng = np.random.default_rng(ny + batch)
-    nx, ax, by, kev = 512, 30.0, 30.0 * ny / 512, 200.0
+@pytest.mark.parametrize("nx,ny,batch", [(512, 64, 1), (512, 384, 3), (512, 1024, 2), (512, 512, 5),
+                                         (1024, 64, 1), (1024, 256, 3), (1024, 1024, 2)])
+def test_ctem_two_stage_columns_match_oracle(ctx, nx, ny, batch):
+    rng = np.random.default_rng(nx + ny + batch)
+    ax, by, kev = 30.0, 30.0 * ny / nx, 200.0
     t = _layers(rng, 3, nx, ny, ax, by, kev)
     dz = np.array([1.2, 1.9, 1.5])
     seq = [0, 1, 2, 1, 0, 2, 2]
@@ -34,9 +36,11 @@ def test_ctem_nx512_matches_oracle(ctx, ny, batch):
     assert O.rel_l2(got, ref) < 2e-5
 
 
-def test_stem_nx512_detectors_and_checkpoints(ctx):
+@pytest.mark.parametrize("nx,ny", [(512, 384), (1024, 256)])
+def test_stem_two_stage_columns_detectors_and_checkpoints(ctx, nx, ny):
     rng = np.random.default_rng(11)
-    nx, ny, ax, by, kev = 512, 384, 31.0, 23.25, 200.0
+    ax, kev = 31.0, 200.0
+    by = ax * ny / nx
     t = _layers(rng, 2, nx, ny, ax, by, kev)
     seq = [0, 1, 0, 1, 1, 0]
     k_ap = 1.5
