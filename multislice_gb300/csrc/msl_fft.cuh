@@ -512,6 +512,14 @@ struct HalfWarpPlan512 {
     static constexpr bool PK = true, PKMUL = false, CW = false;
     static constexpr int radix(int s) { return s == 0 ? 16 : 32; }
 };
+// Two-stage plan for 256-point lines, 16 threads x 16 elements (two lines per
+// warp): radix 16 then radix 16, the exchange swizzle of the 512 plan.
+struct HalfWarpPlan256 {
+    static constexpr int N = 256, T = 16, E = 16, NSTAGE = 2;
+    static constexpr int row_swz = 1, row_sh = 4, col_c = 4, col_ps = 30;
+    static constexpr bool PK = true, PKMUL = false, CW = false;
+    static constexpr int radix(int) { return 16; }
+};
 // Two-stage plan for 1024-point lines, one warp per line (32 threads x 32
 // elements): radix 32 then radix 32, a single exchange per transform.  The
 // exchange swizzle i ^ ((i >> 5) & 15) keeps both of its access patterns
@@ -526,6 +534,9 @@ struct WarpPlan1024x2 {
 };
 // The same plans for the column passes: table twiddles with packed products.
 struct HalfWarpColPlan512 : HalfWarpPlan512 {
+    static constexpr bool PKMUL = true;
+};
+struct HalfWarpColPlan256 : HalfWarpPlan256 {
     static constexpr bool PKMUL = true;
 };
 struct WarpPairColPlan1024 : WarpPlan1024x2 {

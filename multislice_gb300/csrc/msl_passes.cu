@@ -380,7 +380,16 @@ __global__ void __launch_bounds__(ColTmaCfg<PL>::THREADS, MINB)
 struct ColHalfL512 {  // 512: 8 columns, a warp per column pair
     using P = HalfWarpColPlan512;
     using Lin = ColLin64;
-    static constexpr int N = 512, C = 8;
+    static constexpr int N = 512, C = 8, G = 3;
+    static constexpr bool PAIR = false;
+    static constexpr CUtensorMapSwizzle SWZ = CU_TENSOR_MAP_SWIZZLE_64B;
+    __device__ static int col(int wg, int lane) { return 2 * wg + (lane & 1); }
+    __device__ static int thr(int wg, int lane) { return lane >> 1; }
+};
+struct ColHalfL256 {  // 256: 8 columns, a warp per column pair, four groups per CTA
+    using P = HalfWarpColPlan256;
+    using Lin = ColLin64;
+    static constexpr int N = 256, C = 8, G = 4;
     static constexpr bool PAIR = false;
     static constexpr CUtensorMapSwizzle SWZ = CU_TENSOR_MAP_SWIZZLE_64B;
     __device__ static int col(int wg, int lane) { return 2 * wg + (lane & 1); }
@@ -389,7 +398,7 @@ struct ColHalfL512 {  // 512: 8 columns, a warp per column pair
 struct ColPairL1024 {  // 1024: 4 columns, a warp pair per column pair
     using P = WarpPairColPlan1024;
     using Lin = ColLin32;
-    static constexpr int N = 1024, C = 4;
+    static constexpr int N = 1024, C = 4, G = 3;
     static constexpr bool PAIR = true;
     static constexpr CUtensorMapSwizzle SWZ = CU_TENSOR_MAP_SWIZZLE_32B;
     __device__ static int col(int wg, int lane) { return 2 * (wg >> 1) + (lane & 1); }
@@ -398,14 +407,17 @@ struct ColPairL1024 {  // 1024: 4 columns, a warp pair per column pair
 
 template <class L> struct ColHalfCfg {
     using P = typename L::P;
-    static constexpr int N = L::N, C = L::C, G = 3, GT = 128, THREADS = GT * G, NBUF = 2, BOXR = 256;
-    static constexpr uint32_t SLOT = sizeof(float2) * N * C;  // 32 KB, also the slot alignment
+    static constexpr int N = L::N, C = L::C, G = L::G, GT = 128, THREADS = GT * G, NBUF = 2, BOXR = 256;
+    static constexpr uint32_t SLOT = sizeof(float2) * N * C;  // 16 or 32 KB, also the slot alignment
     static constexpr int TW = P::radix(1) * P::radix(0);      // stage 1 table [r][k]
     static constexpr size_t OFF_RED = sizeof(float2) * TW;
     static constexpr size_t OFF_BAR = OFF_RED + sizeof(double) * G * 4 * kMaxDet;
     static constexpr size_t HEADER = OFF_BAR + sizeof(uint64_t) * G * NBUF;
-    static constexpr size_t SMEM = 227 * 1024;  // the header, then 2 G slots from the next 32 KB boundary
-    static_assert(SLOT == 32768 && N % BOXR == 0 && P::NSTAGE == 2 && C % 4 == 0, "32 KB tiles, two stages");
+    // the header, then 2 G slots from the next slot boundary
+    static constexpr size_t SMEM = HEADER + SLOT - 1 + (size_t)NBUF * G * SLOT + 1024 <= 227 * 1024
+                                       ? HEADER + SLOT - 1 + (size_t)NBUF * G * SLOT + 1024 : 227 * 1024;
+    static_assert((SLOT & (SLOT - 1)) == 0 && N % BOXR == 0 && P::NSTAGE == 2 && C % 4 == 0, "two stages");
+    static_assert(1 + G + 2 * G <= 16, "named barriers: one per group, one per warp pair");
     static_assert(L::Lin::B(P::T) == 1024 && L::Lin::B(P::T - 1) < 1024, "natural order: row t + T e at + 1024 e");
     static_assert(HEADER <= SLOT, "the header fits before the first slot");
 };
@@ -443,7 +455,7 @@ __global__ void __launch_bounds__(ColHalfCfg<L>::THREADS, 1)
     // lanes alternate between two columns: each half-warp then touches 8 rows of
     // both, which is what keeps its 64-bit accesses on 16 bank pairs
     const int t = L::thr(wg, lane), c = L::col(wg, lane);
-    const uint32_t pairid = 4u + 2u * (uint32_t)g + (uint32_t)(wg >> 1);  // the warp pair's barrier (1024)
+    const uint32_t pairid = 1u + G + 2u * (uint32_t)g + (uint32_t)(wg >> 1);  // the warp pair's barrier (1024)
     auto colsync = [&]() {
         if constexpr (L::PAIR) bar_group(pairid, 64);
         else __syncwarp();
@@ -834,7 +846,8 @@ __global__ void __launch_bounds__(RowWarpCfg<N>::THREADS, RowWarpCfg<N>::MINB) r
 // formed in shared memory at start-up.
 template <class P_> struct RowTwoCfg {
     using P = P_;
-    static constexpr int N = P::N, W = 4, THREADS = 32 * W, NBUF = 2, MINB = 3;
+    // CTAs per SM: 3 at 32 elements per thread (registers), 5 at 16
+    static constexpr int N = P::N, W = 4, THREADS = 32 * W, NBUF = 2, MINB = P::E >= 32 ? 3 : 5;
     static constexpr int LPW = 32 / P::T;  // lines per warp: 2 (half-warp lines) or 1
     static constexpr int R0 = P::radix(0), R1 = P::radix(1);
     static constexpr size_t LINE = sizeof(float2) * N, SLOT = LPW * LINE;
@@ -1212,6 +1225,7 @@ template <class L> static cudaError_t col_half_launch(const ColArgs &a, cudaStre
 // passes of a scan write partials per 4 columns.
 static int col_half_side(int n, const ColArgs &a) {
     if (!(a.flags & COL_LOAD) || !(a.flags & COL_FWD) || (a.flags & COL_PROBE)) return 0;
+    if (n == 256 && a.ny % ColHalfL256::C == 0) return 256;
     if (n == 512 && a.ny % ColHalfL512::C == 0) return 512;
     if (n == 1024 && a.ny % ColPairL1024::C == 0) return 1024;
     return 0;
@@ -1358,7 +1372,10 @@ cudaError_t launch_row_pass(int ny, const RowArgs &a, cudaStream_t s, int nsm, i
     ++*launches;
     if (row_warp_eligible(ny, a)) {
         switch (ny) {
-            case 256: return row_warp_launch<256>(a, s, nsm);
+            case 256:
+                if (a.nlines % 2 == 0 && !(((uintptr_t)a.out | (uintptr_t)a.in) & 15u))
+                    return row_two_launch<HalfWarpPlan256>(a, s, nsm);
+                return row_warp_launch<256>(a, s, nsm);
             case 384: return row_warp_launch<384>(a, s, nsm);
             case 512:
                 if (a.nlines % 2 == 0 && !(((uintptr_t)a.out | (uintptr_t)a.in) & 15u))
@@ -1387,8 +1404,9 @@ cudaError_t launch_row_pass(int ny, const RowArgs &a, cudaStream_t s, int nsm, i
 cudaError_t launch_col_pass(int nx, const ColArgs &a, cudaStream_t s, int nsm, int64_t *launches) {
     ++*launches;
     if (tma_eligible(a)) {
-        // the slice loop's transform pair at 512 and 1024: two-stage columns
+        // the slice loop's passes at 256, 512 and 1024: two-stage columns
         switch (col_half_side(nx, a)) {
+            case 256: return col_half_launch<ColHalfL256>(a, s, nsm);
             case 512: return col_half_launch<ColHalfL512>(a, s, nsm);
             case 1024: return col_half_launch<ColPairL1024>(a, s, nsm);
             default: break;

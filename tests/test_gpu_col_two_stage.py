@@ -1,8 +1,8 @@
-"""The slice loop's two-stage column passes at nx = 512 and 1024 (columns of 32
-elements per thread in swizzled 32 KB TMA tiles, three independent thread groups
-per CTA; at 1024 a column is shared by a warp pair): non-square grids, batches
-that leave groups without tiles, several detectors and checkpoints, against the
-FP64 oracle."""
+"""The slice loop's two-stage passes at nx = 256, 512 and 1024 (columns in
+swizzled TMA tiles, independent thread groups per CTA; at 1024 a column is
+shared by a warp pair; rows of 256 and 512 two per warp): non-square grids,
+batches that leave groups without tiles, several detectors and checkpoints,
+against the FP64 oracle."""
 import numpy as np
 import pytest
 
@@ -20,7 +20,8 @@ def _layers(rng, nt, nx, ny, ax, by, kev):
     return O.transmission(v, kev, ax, by, np.complex64)
 
 
-@pytest.mark.parametrize("nx,ny,batch", [(512, 64, 1), (512, 384, 3), (512, 1024, 2), (512, 512, 5),
+@pytest.mark.parametrize("nx,ny,batch", [(256, 64, 1), (256, 384, 3), (256, 256, 7),
+                                         (512, 64, 1), (512, 384, 3), (512, 1024, 2), (512, 512, 5),
                                          (1024, 64, 1), (1024, 256, 3), (1024, 1024, 2)])
 def test_ctem_two_stage_columns_match_oracle(ctx, nx, ny, batch):
     rng = np.random.default_rng(nx + ny + batch)
@@ -36,10 +37,10 @@ def test_ctem_two_stage_columns_match_oracle(ctx, nx, ny, batch):
     assert O.rel_l2(got, ref) < 2e-5
 
 
-@pytest.mark.parametrize("nx,ny", [(512, 384), (1024, 256)])
+@pytest.mark.parametrize("nx,ny", [(256, 256), (512, 384), (1024, 256)])
 def test_stem_two_stage_columns_detectors_and_checkpoints(ctx, nx, ny):
     rng = np.random.default_rng(11)
-    ax, kev = 31.0, 200.0
+    ax, kev = 31.0 * nx / 512, 200.0  # 0.06 A pixels: every detector inside the band limit
     by = ax * ny / nx
     t = _layers(rng, 2, nx, ny, ax, by, kev)
     seq = [0, 1, 0, 1, 1, 0]
