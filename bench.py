@@ -304,6 +304,48 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_sides(args):
+    """Per-pass device time of the slice loop at every supported side from 256 up
+    (batched plane waves, 20 slices over 4 random phase layers, waves larger than
+    L2): one JSON line per side with each pass's algorithmic bandwidth and its
+    fraction of the measured HBM copy bandwidth."""
+    import ctypes
+
+    import torch
+
+    from multislice_gb300 import Context
+
+    hbm, peak_kind = peaks()
+    with Context(0) as c:
+        for n, batch in ((256, 1024), (384, 512), (512, 256), (768, 128), (1024, 64), (2048, 16)):
+            nt = 4
+            rng = np.random.default_rng(1)
+            t = np.exp(1j * rng.uniform(0, 0.3, (nt, n, n))).astype(np.complex64)
+            td = torch.from_numpy(t.view(np.float32).reshape(nt, n, n, 2)).cuda()
+            psi = torch.zeros((batch, n, n, 2), dtype=torch.float32, device="cuda")
+            psi[..., 0] = 1
+            seq = np.arange(20) % nt
+            dz = np.full(nt, 1.5)
+            for _ in range(max(args.warmup, 3)):
+                c.multislice(td, dz, seq, 20.0, 20.0, 200.0, psi=psi)
+            torch.cuda.synchronize()
+            c._lib.msl_profile_enable(c._h, 1)
+            for _ in range(max(args.steps, 1)):
+                c.multislice(td, dz, seq, 20.0, 20.0, 200.0, psi=psi)
+            torch.cuda.synchronize()
+            line = {"side": n, "batch": batch, "peak_gbs": hbm, "peak_source": peak_kind}
+            for k, name in ((0, "row"), (1, "col")):
+                cnt, ms = ctypes.c_int64(), ctypes.c_double()
+                c._lib.msl_profile_read(c._h, k, ctypes.byref(cnt), ctypes.byref(ms))
+                per = ms.value / max(cnt.value, 1)
+                gbs = 16.0 * n * n * batch / (per * 1e-3) / 1e9
+                line[name] = {"ms_per_launch": per, "achieved_gbs": gbs, "frac": gbs / hbm}
+            c._lib.msl_profile_enable(c._h, 0)
+            print(json.dumps(line), flush=True)
+            del psi, td
+            torch.cuda.empty_cache()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -316,8 +358,12 @@ def main():
                     help="probes of the 64x64 raster per GPU (smaller cases are for profiling)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--batch", type=int, default=0, help="probes per launch (0: library default)")
+    ap.add_argument("--sides", action="store_true",
+                    help="per-pass bandwidth of the slice loop at every side instead of the scan")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.sides:
+        run_sides(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)
