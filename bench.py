@@ -243,7 +243,12 @@ def run_ours(args):
     }
     if rank == 0:
         if world == 1 and not args.no_cpu:
-            line["cpu_baseline"] = cpu_baseline(cfg, args.cpu_probes)
+            chk = out_dev[: args.cpu_probes].cpu().numpy() if nprobe >= args.cpu_probes else None
+            cb = cpu_baseline(cfg, args.cpu_probes, check=chk)
+            acc = cb.pop("accuracy", None)
+            line["cpu_baseline"] = cb
+            if acc is not None:
+                line["accuracy"] = acc
         line["clocks"] = clk.summary()
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -252,8 +257,11 @@ def run_ours(args):
 
 
 # ------------------------------------------------------------- CPU baseline
-def cpu_baseline(cfg, nprobe, spawn_pool=False):
-    """Oracle port of the reference CPU loop on a bounded probe sample."""
+def cpu_baseline(cfg, nprobe, spawn_pool=False, check=None, check_fp64=4):
+    """Oracle port of the reference CPU loop on a bounded probe sample.  With
+    `check` (the GPU's detector sums of the same raster) it also reports their
+    relative L2 error per detector against this run and against an FP64 run of
+    the first `check_fp64` probes."""
     from oracle import msl_oracle as O
     spec = cfg["spec"]
     nx = ny = 512
@@ -269,11 +277,27 @@ def cpu_baseline(cfg, nprobe, spawn_pool=False):
     xy = cfg["probe_xy"][:nprobe]
     t0 = time.perf_counter()
     P = O.probe(nx, ny, spec.ax, spec.by, 200.0, 0.0, cfg["k_ap"], 0.0, 0.0, xy, np.complex64)
-    O.stem(T, props, np.arange(NSLICE), mask, P, dm, [NSLICE - 1], workers=workers)
+    det = O.stem(T, props, np.arange(NSLICE), mask, P, dm, [NSLICE - 1], workers=workers)
     el = time.perf_counter() - t0
-    return {"value": nprobe * NSLICE / el, "unit": UNIT, "cores": workers, "kind": "port",
-            "sample": f"{nprobe} probes x {NSLICE} slices of the 512^2 SrTiO3 scan "
-                      f"(numpy/scipy oracle, FFT workers={workers}), {el:.1f} s"}
+    res = {"value": nprobe * NSLICE / el, "unit": UNIT, "cores": workers, "kind": "port",
+           "sample": f"{nprobe} probes x {NSLICE} slices of the 512^2 SrTiO3 scan "
+                     f"(numpy/scipy oracle, FFT workers={workers}), {el:.1f} s"}
+    if check is not None:
+        # the checker (not timed): the GPU's detector sums for the same probes
+        # against this FP32 CPU run and against an FP64 run of the first few
+        got = np.asarray(check)
+        nf = min(check_fp64, nprobe)
+        T64 = O.transmission(V, 200.0, spec.ax, spec.by, np.complex128)
+        props64 = [O.propagator_tables(nx, ny, spec.ax, spec.by, 200.0, spec.cz / NSLICE, precision="f64")] * NSLICE
+        P64 = O.probe(nx, ny, spec.ax, spec.by, 200.0, 0.0, cfg["k_ap"], 0.0, 0.0, xy[:nf], np.complex128)
+        det64 = O.stem(T64, props64, np.arange(NSLICE), mask, P64, dm, [NSLICE - 1], workers=workers)
+        names = ("HAADF", "ABF")
+        res["accuracy"] = {
+            "rel_l2_vs_fp64": {n: O.rel_l2(got[:nf, 0, k], det64[:, 0, k]) for k, n in enumerate(names)},
+            "probes_fp64": nf,
+            "rel_l2_vs_cpu_f32": {n: O.rel_l2(got[:nprobe, 0, k], det[:, 0, k]) for k, n in enumerate(names)},
+            "probes_f32": nprobe, "bar": 1e-3}
+    return res
 
 
 def run_reference(args):
