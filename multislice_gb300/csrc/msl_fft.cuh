@@ -263,10 +263,58 @@ template <int DIR, bool PK> __device__ __forceinline__ void dft32(float2 *a) {
     for (int k = 0; k < 32; ++k) a[k] = o[k];
 }
 
+// 6 = 2 x 3: n = 2 n1 + n2 (3-point transforms over n1), twiddle w6^(n2 k1),
+// 2-point transforms over n2; X[k1 + 3 k2] lands in a[k1 + 3 k2].
+template <int DIR, bool PK> __device__ __forceinline__ void dft6(float2 *a) {
+    float2 y0[3] = {a[0], a[2], a[4]}, y1[3] = {a[1], a[3], a[5]};
+    dft3<DIR, PK>(y0[0], y0[1], y0[2]);
+    dft3<DIR, PK>(y1[0], y1[1], y1[2]);
+    const float h = 0.5f, s3 = 0.86602540378443864676f;
+    // w6^1 = (1/2, DIR s3), w6^2 = (-1/2, DIR s3)
+    y1[1] = c_mul(y1[1], make_float2(h, DIR * s3));
+    y1[2] = c_mul(y1[2], make_float2(-h, DIR * s3));
+#pragma unroll
+    for (int k1 = 0; k1 < 3; ++k1) {
+        a[k1] = c_add<PK>(y0[k1], y1[k1]);
+        a[k1 + 3] = c_sub<PK>(y0[k1], y1[k1]);
+    }
+}
+
+// 12 = 4 x 3: n = 3 n1 + n2 (4-point transforms over n1 for each n2), twiddle
+// w12^(n2 k1), 3-point transforms over n2; X[k1 + 4 k2] lands in a[k1 + 4 k2].
+template <int DIR, bool PK> __device__ __forceinline__ void dft12(float2 *a) {
+    float2 y[3][4];
+#pragma unroll
+    for (int n2 = 0; n2 < 3; ++n2) {
+        y[n2][0] = a[n2];
+        y[n2][1] = a[3 + n2];
+        y[n2][2] = a[6 + n2];
+        y[n2][3] = a[9 + n2];
+        dft4<DIR, PK>(y[n2][0], y[n2][1], y[n2][2], y[n2][3]);
+    }
+    // w12^m for m = n2 k1: 1, 2, 3 (n2 = 1) and 2, 4, 6 (n2 = 2)
+    const float c1 = 0.86602540378443864676f, h = 0.5f;
+    y[1][1] = c_mul(y[1][1], make_float2(c1, DIR * h));          // w12^1
+    y[1][2] = c_mul(y[1][2], make_float2(h, DIR * c1));          // w12^2
+    y[1][3] = c_muli<DIR>(y[1][3]);                              // w12^3 = DIR i
+    y[2][1] = c_mul(y[2][1], make_float2(h, DIR * c1));          // w12^2
+    y[2][2] = c_mul(y[2][2], make_float2(-h, DIR * c1));         // w12^4
+    y[2][3] = make_float2(-y[2][3].x, -y[2][3].y);               // w12^6 = -1
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1) {
+        dft3<DIR, PK>(y[0][k1], y[1][k1], y[2][k1]);
+        a[k1] = y[0][k1];
+        a[k1 + 4] = y[1][k1];
+        a[k1 + 8] = y[2][k1];
+    }
+}
+
 template <int R, int DIR, bool PK> __device__ __forceinline__ void dft(float2 *a) {
     if constexpr (R == 2) dft2<DIR, PK>(a[0], a[1]);
     else if constexpr (R == 3) dft3<DIR, PK>(a[0], a[1], a[2]);
     else if constexpr (R == 4) dft4<DIR, PK>(a[0], a[1], a[2], a[3]);
+    else if constexpr (R == 6) dft6<DIR, PK>(a);
+    else if constexpr (R == 12) dft12<DIR, PK>(a);
     else if constexpr (R == 8) dft8<DIR, PK>(a);
     else if constexpr (R == 16) dft16<DIR, PK>(a);
     else if constexpr (R == 32) dft32<DIR, PK>(a);
@@ -608,13 +656,31 @@ __device__ __forceinline__ void fft_line_tab(float2 (&v)[P::E], int t, const Row
     }
 }
 
-// Plan with one warp per line (same radices as Plan<N>).
+// Plan with one warp per line (same radices as Plan<N>).  OWN_TW: the kernel
+// builds its twiddle tables (radices differ from Plan<N>'s host tables).
 template <int N_> struct WarpPlan {
     using B = Plan<N_>;
     static constexpr int N = N_, T = 32, E = N_ / 32, NSTAGE = B::NSTAGE;
     static constexpr int row_swz = B::row_swz, row_sh = B::row_sh, col_c = B::col_c, col_ps = B::col_ps;
-    static constexpr bool PK = true, PKMUL = false;
+    static constexpr bool PK = true, PKMUL = false, OWN_TW = false;
     static constexpr int radix(int s) { return B::radix(s); }
+};
+// The mixed sides one warp per line with fewer stages than Plan<N>, the radix
+// 6 / 12 stage last so the spans before it are powers of two, and an exchange
+// swizzle i ^ ((i >> sh) & 15) under which every exchange is conflict-free (a
+// CPU bank model of the half-warp wavefronts checked each one): 384 = 4 x 4 x
+// 4 x 6 (12 elements per thread), 768 = 8 x 8 x 12 (24 elements per thread).
+template <> struct WarpPlan<384> {
+    static constexpr int N = 384, T = 32, E = 12, NSTAGE = 4;
+    static constexpr int row_swz = 1, row_sh = 2, col_c = 4, col_ps = 30;
+    static constexpr bool PK = true, PKMUL = false, OWN_TW = true;
+    static constexpr int radix(int s) { return s < 3 ? 4 : 6; }
+};
+template <> struct WarpPlan<768> {
+    static constexpr int N = 768, T = 32, E = 24, NSTAGE = 3;
+    static constexpr int row_swz = 1, row_sh = 3, col_c = 4, col_ps = 30;
+    static constexpr bool PK = true, PKMUL = false, OWN_TW = true;
+    static constexpr int radix(int s) { return s < 2 ? 8 : 12; }
 };
 
 }  // namespace msl

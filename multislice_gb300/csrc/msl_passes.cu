@@ -713,10 +713,13 @@ template <> __device__ __forceinline__ RowXorLin<WarpPlan<512>> make_row_addr(fl
 template <> __device__ __forceinline__ RowXorAddr<WarpPlan<384>> make_row_addr(float2 *buf) {
     return RowXorAddr<WarpPlan<384>>{buf};
 }
+template <> __device__ __forceinline__ RowXorAddr<WarpPlan<768>> make_row_addr(float2 *buf) {
+    return RowXorAddr<WarpPlan<768>>{buf};
+}
 
 template <int N> struct RowWarpCfg {
     using P = WarpPlan<N>;
-    static constexpr int W = 8, THREADS = 32 * W, NBUF = N == 512 ? 2 : 3;
+    static constexpr int W = 8, THREADS = 32 * W, NBUF = (N == 512 || N == 768) ? 2 : 3;
     static constexpr int MINB = N == 512 ? 3 : P::E <= 8 ? 3 : 2;
     static constexpr size_t LINE = sizeof(float2) * N;
     // power-of-two sides address their exchanges xor-linearly (RowXorLin), which
@@ -740,7 +743,19 @@ __global__ void __launch_bounds__(RowWarpCfg<N>::THREADS, RowWarpCfg<N>::MINB) r
     float2 *ring = reinterpret_cast<float2 *>(base) + (size_t)warp * NBUF * N;
     float2 *tw = reinterpret_cast<float2 *>(base + Cfg::OFF_TW);
     uint64_t *bar = reinterpret_cast<uint64_t *>(base + Cfg::OFF_BAR) + warp * NBUF;
-    for (int i = threadIdx.x; i < TW; i += Cfg::THREADS) tw[i] = a.tw[i];
+    if constexpr (P::OWN_TW) {  // stage s >= 1: [r][k] = exp(2 pi i r k / (NS R)), NS = span before s
+#pragma unroll
+        for (int st = 1; st < P::NSTAGE; ++st) {
+            const int R = P::radix(st), NS = plan_span<P>(st), off = plan_tw_offset<P>(st);
+            for (int i = threadIdx.x; i < R * NS; i += Cfg::THREADS) {
+                float sn, cn;
+                sincospif((float)(2 * (i / NS) * (i % NS)) / (float)(NS * R), &sn, &cn);
+                tw[off + i] = make_float2(cn, sn);
+            }
+        }
+    } else {
+        for (int i = threadIdx.x; i < TW; i += Cfg::THREADS) tw[i] = a.tw[i];
+    }
     if (lane == 0) {
         for (int s = 0; s < NBUF; ++s) mbar_init(&bar[s], 1);
         mbar_fence_init();
@@ -1300,7 +1315,7 @@ template <int N> static cudaError_t row_warp_launch(const RowArgs &a, cudaStream
 
 // Warp-owned lines for the sides whose plan fits 32 threads per line.
 static bool row_warp_eligible(int ny, const RowArgs &a) {
-    if (ny != 256 && ny != 384 && ny != 512 && ny != 1024) return false;
+    if (ny != 256 && ny != 384 && ny != 512 && ny != 768 && ny != 1024) return false;
     if (a.flags & ROW_GENT) return false;
     if (((uintptr_t)a.out & 15u) || ((a.flags & ROW_LOAD) && ((uintptr_t)a.in & 15u))) return false;
     return true;
@@ -1377,6 +1392,7 @@ cudaError_t launch_row_pass(int ny, const RowArgs &a, cudaStream_t s, int nsm, i
                     return row_two_launch<HalfWarpPlan256>(a, s, nsm);
                 return row_warp_launch<256>(a, s, nsm);
             case 384: return row_warp_launch<384>(a, s, nsm);
+            case 768: return row_warp_launch<768>(a, s, nsm);
             case 512:
                 if (a.nlines % 2 == 0 && !(((uintptr_t)a.out | (uintptr_t)a.in) & 15u))
                     return row_two_launch<HalfWarpPlan512>(a, s, nsm);
