@@ -56,17 +56,33 @@ template <int N_, int T_, int C_, int PS_, int MINB_, int NBUF_ = 3> struct ColP
     static constexpr int N = N_, T = T_, E = N_ / T_, NSTAGE = B::NSTAGE, MINB = MINB_, NBUF = NBUF_;
     static constexpr int row_swz = B::row_swz, row_sh = B::row_sh;
     static constexpr int col_c = C_, col_ps = PS_;
-    static constexpr bool PK = true, PKMUL = false;
+    static constexpr bool PK = true, PKMUL = false, OWN_TW = false;
     static constexpr int radix(int s) { return B::radix(s); }
+};
+// Column plans of the mixed sides with their own radices (the kernel builds the
+// twiddle tables, OWN_TW): 32 threads per column, 8 columns per tile, the
+// radix 6 / 12 stage last, exchange swizzle g(i) = i ^ ((i >> ps) & 1) that a
+// CPU bank model found conflict-free for every exchange and the tile access.
+struct ColPlanMixed384 {
+    static constexpr int N = 384, T = 32, E = 12, NSTAGE = 4, MINB = 3, NBUF = 2;
+    static constexpr int row_swz = 1, row_sh = 2, col_c = 8, col_ps = 2;
+    static constexpr bool PK = true, PKMUL = false, OWN_TW = true;
+    static constexpr int radix(int s) { return s < 3 ? 4 : 6; }
+};
+struct ColPlanMixed768 {
+    static constexpr int N = 768, T = 32, E = 24, NSTAGE = 3, MINB = 2, NBUF = 2;
+    static constexpr int row_swz = 1, row_sh = 3, col_c = 8, col_ps = 3;
+    static constexpr bool PK = true, PKMUL = false, OWN_TW = true;
+    static constexpr int radix(int s) { return s < 2 ? 8 : 12; }
 };
 // Tile shapes chosen by a shared-memory bank model and by timing the 512 case.
 template <int N> struct ColPlan;
 template <> struct ColPlan<64> : ColPlanT<64, 8, 16, 30, 4> {};
 template <> struct ColPlan<128> : ColPlanT<128, 16, 16, 30, 2> {};
 template <> struct ColPlan<256> : ColPlanT<256, 32, 8, 3, 2> {};
-template <> struct ColPlan<384> : ColPlanT<384, 32, 8, 30, 2> {};
+template <> struct ColPlan<384> : ColPlanMixed384 {};
 template <> struct ColPlan<512> : ColPlanT<512, 32, 4, 3, 4> {};
-template <> struct ColPlan<768> : ColPlanT<768, 64, 4, 30, 2> {};
+template <> struct ColPlan<768> : ColPlanMixed768 {};
 template <> struct ColPlan<1024> : ColPlanT<1024, 64, 8, 4, 1> {};
 template <> struct ColPlan<2048> : ColPlanT<2048, 128, 4, 4, 1> {};
 

@@ -273,7 +273,19 @@ __global__ void __launch_bounds__(ColTmaCfg<PL>::THREADS, MINB)
     const bool load = (a.flags & COL_LOAD) != 0, store = (a.flags & COL_STORE) != 0;
     const int tpi = a.ny / C, ntiles = a.batch * tpi;
     const int nmine = (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
-    for (int i = tid; i < TW; i += Cfg::THREADS) tw[i] = a.tw[i];
+    if constexpr (P::OWN_TW) {  // stage s >= 1: [r][k] = exp(2 pi i r k / (NS R)), NS = span before s
+#pragma unroll
+        for (int st = 1; st < P::NSTAGE; ++st) {
+            const int R = P::radix(st), NS = plan_span<P>(st), off = plan_tw_offset<P>(st);
+            for (int i = tid; i < R * NS; i += Cfg::THREADS) {
+                float sn, cn;
+                sincospif((float)(2 * (i / NS) * (i % NS)) / (float)(NS * R), &sn, &cn);
+                tw[off + i] = make_float2(cn, sn);
+            }
+        }
+    } else {
+        for (int i = tid; i < TW; i += Cfg::THREADS) tw[i] = a.tw[i];
+    }
     if (tid == 0) {
         for (int s = 0; s < NBUF; ++s) mbar_init(&bar[s], 1);
         mbar_fence_init();
