@@ -491,17 +491,23 @@ __device__ __forceinline__ void fft_exchange(float2 (&v)[P::E], int t, const Add
 // i = (j / NS) NS R + j % NS + r NS, i.e. T-part (t / NS) NS R + t % NS and
 // K-part T R q + NS r when NS <= T; T-part t and K-part
 // (q / (NS/T)) NS R + T (q % (NS/T)) + NS r when NS > T.  Read index t + T e.
-template <class P, int S>
-__device__ __forceinline__ void fft_exchange_xl(float2 (&v)[P::E], int t, const RowXorLin<P> &ad) {
+// sync() orders the line's threads: the warp (the default) or, for lines of 64
+// threads, the warp pair.
+struct WarpSync {
+    __device__ __forceinline__ void operator()() const { __syncwarp(); }
+};
+template <class P, int S, class Sync = WarpSync>
+__device__ __forceinline__ void fft_exchange_xl(float2 (&v)[P::E], int t, const RowXorLin<P> &ad,
+                                                const Sync &sync = Sync()) {
     constexpr int R = P::radix(S), NS = plan_span<P>(S), E = P::E, Q = E / R, T = P::T;
-    static_assert((T == 32 || T == 16) && (NS & (NS - 1)) == 0 && (R & (R - 1)) == 0 &&
+    static_assert((T == 64 || T == 32 || T == 16) && (NS & (NS - 1)) == 0 && (R & (R - 1)) == 0 &&
                       (P::N & (P::N - 1)) == 0,
-                  "xor-linear exchange needs warp- or half-warp-owned lines and power-of-two radices");
+                  "xor-linear exchange needs warp-owned (or pair-owned) lines and power-of-two radices");
     using F = RowXorLin<P>;
     const int tw_part = NS <= T ? (t / NS) * NS * R + t % NS : t;
     const uint32_t wb = ad.base + 8u * (uint32_t)F::f(tw_part);
     const uint32_t rb = ad.base + 8u * (uint32_t)F::f(t);
-    __syncwarp();  // previous readers are done
+    sync();  // previous readers are done
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
 #pragma unroll
@@ -510,7 +516,7 @@ __device__ __forceinline__ void fft_exchange_xl(float2 (&v)[P::E], int t, const 
             sts_f2(wb ^ (8u * (uint32_t)F::f(K)), v[q + r * Q]);
         }
     }
-    __syncwarp();
+    sync();
 #pragma unroll
     for (int e = 0; e < E; ++e) v[e] = lds_f2(rb ^ (8u * (uint32_t)F::f(T * e)));
 }
@@ -607,6 +613,64 @@ struct WarpPairColPlan1024 : WarpPlan1024x2 {
     static constexpr bool PKMUL = true, CW = false;
 };
 
+
+// Stages that form twiddle powers in registers from a compact table of bases
+// w^k = exp(2 pi i k / (NS R)), k < NS, stage s at offset sum_{1 <= i < s} NS_i.
+template <class P> __host__ __device__ constexpr int plan_cwb_offset(int s) {
+    int off = 0;
+    for (int i = 1; i < s; ++i) off += plan_span<P>(i);
+    return off;
+}
+template <class P> __host__ __device__ constexpr int plan_cwb_size() { return plan_cwb_offset<P>(P::NSTAGE); }
+
+template <class P, int S, int DIR>
+__device__ __forceinline__ void fft_stage_cwb(float2 (&v)[P::E], int t, const float2 *__restrict__ twb) {
+    constexpr int R = P::radix(S), NS = plan_span<P>(S), E = P::E, Q = E / R, T = P::T;
+    constexpr bool SHARED_K = NS > 1 && T % NS == 0;
+    float2 w[R];
+    auto powers = [&](int k) {
+        w[1] = twb[plan_cwb_offset<P>(S) + k];
+        if constexpr (DIR < 0) w[1].y = -w[1].y;
+#pragma unroll
+        for (int r = 2; r < R; ++r) w[r] = c_mul(w[r / 2], w[r - r / 2]);
+    };
+    if constexpr (SHARED_K) powers(t % NS);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        float2 a[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) a[r] = v[q + r * Q];
+        if constexpr (NS > 1) {
+            if constexpr (!SHARED_K) powers((t + T * q) % NS);
+#pragma unroll
+            for (int r = 1; r < R; ++r) a[r] = c_mul(a[r], w[r]);
+        }
+        dft<R, DIR, P::PK>(a);
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[q + r * Q] = a[r];
+    }
+}
+
+// Three-stage plan for 2048-point lines owned by a warp pair (64 threads x 32
+// elements): radix 16, 16, 8 with compact register twiddle powers, exchanges
+// synchronised over the pair; the swizzle i ^ ((i >> 4) & 15) keeps both
+// exchanges on 16 distinct bank pairs per half-warp (CPU bank model).
+struct WarpPairPlan2048 {
+    static constexpr int N = 2048, T = 64, E = 32, NSTAGE = 3;
+    static constexpr int row_swz = 1, row_sh = 4, col_c = 4, col_ps = 30;
+    static constexpr bool PK = true, PKMUL = false, CW = true;
+    static constexpr int radix(int s) { return s < 2 ? 16 : 8; }
+};
+
+template <class P, int DIR, int S = 0, class Sync>
+__device__ __forceinline__ void fft_line_cwb(float2 (&v)[P::E], int t, const RowXorLin<P> &ad,
+                                             const float2 *__restrict__ twb, const Sync &sync) {
+    fft_stage_cwb<P, S, DIR>(v, t, twb);
+    if constexpr (S + 1 < P::NSTAGE) {
+        fft_exchange_xl<P, S>(v, t, ad, sync);
+        fft_line_cwb<P, DIR, S + 1>(v, t, ad, twb, sync);
+    }
+}
 
 // Column tiles of C columns x N rows laid out by a TMA swizzle, and the exchange
 // that reuses each column's own slots.

@@ -864,13 +864,13 @@ __global__ void __launch_bounds__(RowWarpCfg<N>::THREADS, RowWarpCfg<N>::MINB) r
 }
 
 // ---------------------------------------------- half-warp row pass, 512
-// Row pass for 512-point lines in the two-stage layout (HalfWarpPlan512): each
-// warp transforms two consecutive lines at a time, one per half-warp, with a
-// radix-16 and a radix-32 stage and a single exchange per transform (the
-// three-stage warp layout needs two).  Lines arrive in pairs (8 KB) by 1D bulk
-// copy into a private two-slot ring per warp; the next pair is requested once
-// the previous pair's store has read its slot.  The stage-1 twiddle table is
-// formed in shared memory at start-up.
+// Row pass in the two-stage layouts (HalfWarpPlan256 / 512: each warp
+// transforms two consecutive lines at a time, one per half-warp; WarpPlan1024x2:
+// one line per warp): two register stages and a single exchange per transform
+// (the three-stage warp layout needs two).  Lines arrive in units of one or two
+// by 1D bulk copy into a private two-slot ring per warp; the next unit is
+// requested once the previous unit's store has read its slot.  The stage-1
+// twiddle table is formed in shared memory at start-up.
 template <class P_> struct RowTwoCfg {
     using P = P_;
     // CTAs per SM: 3 at 32 elements per thread (registers), 5 at 16
@@ -1004,6 +1004,156 @@ template <class P> static cudaError_t row_two_launch(const RowArgs &a, cudaStrea
     int grid = nsm * per_sm < nwarps ? nsm * per_sm : nwarps;
     if (grid < 1) grid = 1;
     row_two_kernel<P><<<grid, Cfg::THREADS, Cfg::SMEM, s>>>(a);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------ row pass, warp-pair lines, 2048
+// Lines of 2048 points held by a warp pair (64 threads x 32 elements) in three
+// register stages (WarpPairPlan2048); the two exchanges synchronise the pair on
+// a named barrier.  Each pair streams its lines through a private two-slot ring
+// of 16 KB-aligned line buffers (xor-linear exchange addresses) filled and
+// drained by 1D bulk copies; its first lane issues the copies.  Three pairs per
+// CTA, two CTAs per SM.  A wait that times out is voted over the pair, so both
+// warps leave together.
+struct RowPairCfg {
+    using P = WarpPairPlan2048;
+    static constexpr int N = P::N, W = 6, PAIRS = W / 2, THREADS = 32 * W, NBUF = 2, MINB = 2;
+    static constexpr uint32_t LINE = sizeof(float2) * N;  // 16 KB, also the line alignment
+    static constexpr int TW = plan_cwb_size<P>();
+    static constexpr size_t OFF_BAR = ((sizeof(float2) * TW + 15) / 16) * 16;
+    static constexpr size_t HEADER = OFF_BAR + sizeof(uint64_t) * PAIRS * NBUF;
+    static constexpr size_t RING = (size_t)PAIRS * NBUF * LINE;
+    static constexpr size_t SMEM = LINE + RING;  // the header, then the ring from the next line boundary
+    static_assert(HEADER < LINE && P::T == 64, "warp-pair lines");
+};
+
+__global__ void __launch_bounds__(RowPairCfg::THREADS, RowPairCfg::MINB) row_pair_kernel(RowArgs a) {
+    using Cfg = RowPairCfg;
+    using P = Cfg::P;
+    constexpr int N = Cfg::N, E = P::E, T = P::T, NBUF = Cfg::NBUF, PAIRS = Cfg::PAIRS;
+    constexpr uint32_t LINE = Cfg::LINE;
+    extern __shared__ unsigned char smraw[];
+    const uint32_t sbase = smem_u32(smraw);
+    const uint32_t ring0 = (sbase + (uint32_t)Cfg::HEADER + LINE - 1u) & ~(LINE - 1u);
+    if (ring0 + (uint32_t)Cfg::RING > sbase + (uint32_t)Cfg::SMEM) {  // uniform over the CTA
+        if (threadIdx.x == 0 && a.err) atomicExch(a.err, 2);         // layout error, not a timeout
+        return;
+    }
+    float2 *tw = reinterpret_cast<float2 *>(smraw);
+    uint64_t *barall = reinterpret_cast<uint64_t *>(smraw + Cfg::OFF_BAR);
+#pragma unroll
+    for (int st = 1; st < P::NSTAGE; ++st) {  // bases exp(2 pi i k / (NS R)), k < NS
+        const int R = P::radix(st), NS = plan_span<P>(st), off = plan_cwb_offset<P>(st);
+        for (int i = threadIdx.x; i < NS; i += Cfg::THREADS) {
+            float sn, cn;
+            sincospif((float)(2 * i) / (float)(NS * R), &sn, &cn);
+            tw[off + i] = make_float2(cn, sn);
+        }
+    }
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < PAIRS * NBUF; ++i) mbar_init(&barall[i], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();  // the only CTA-wide barrier
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, pr = warp >> 1;
+    const int t = 32 * (warp & 1) + lane;
+    const bool leader = t == 0;
+    const uint32_t barid = 1u + (uint32_t)pr;
+    auto pairsync = [&]() { bar_group(barid, 64); };
+    uint64_t *bar = barall + pr * NBUF;
+    const uint32_t ring = ring0 + (uint32_t)(pr * NBUF) * LINE;
+    const bool load = (a.flags & ROW_LOAD) != 0, store = !(a.flags & ROW_NOSTORE);
+    const int G = gridDim.x * PAIRS, gp = blockIdx.x * PAIRS + pr;
+    const int nmine = gp < a.nlines ? (a.nlines - gp + G - 1) / G : 0;
+    int issued = 0;
+    auto issue = [&](int k) {  // the pair's first thread only
+        const int line = gp + k * G, s = k % NBUF;
+        fence_proxy_async();
+        mbar_arrive_expect_tx(&bar[s], LINE);
+        bulk_load(smraw + (ring + (uint32_t)s * LINE - sbase), a.in + (size_t)line * N, LINE, &bar[s]);
+        issued = k + 1;
+    };
+    if (load && leader && nmine > 0) issue(0);
+    int k = 0;
+    bool ok = true;
+    for (; k < nmine; ++k) {
+        const int line = gp + k * G, s = k % NBUF;
+        float2 *buf = reinterpret_cast<float2 *>(smraw + (ring + (uint32_t)s * LINE - sbase));
+        const RowXorLin<P> ad{ring + (uint32_t)s * LINE};
+        const float2 *trow = (a.flags & ROW_TRANS)
+                                 ? (a.trans_b ? a.trans_b[line / a.nx] : a.trans) + (size_t)(line % a.nx) * N
+                                 : nullptr;
+        if (!load && store && leader) tma_wait_read<NBUF - 1>();  // the store of line k-2 left the slot
+        if (load && leader && k + 1 < nmine) {
+            if (store) tma_wait_read<0>();  // the store of line k-1 has read the other slot
+            issue(k + 1);
+        }
+        float2 v[E];
+        if (load) {
+            const bool got = mbar_wait_bounded(&bar[s], (uint32_t)((k / NBUF) & 1), kWaitLimit);
+            if (bar_group_or(barid, 64, !got)) {
+                ok = false;
+                break;
+            }
+#pragma unroll
+            for (int e = 0; e < E; ++e) v[e] = buf[t + T * e];
+        } else {
+#pragma unroll
+            for (int e = 0; e < E; ++e) v[e] = make_float2(1.f, 0.f);
+        }
+        if (a.flags & ROW_INV) fft_line_cwb<P, -1>(v, t, ad, tw, pairsync);
+        if (a.flags & ROW_TRANS) {
+#pragma unroll
+            for (int e = 0; e < E; ++e) v[e] = c_mul(v[e], __ldg(trow + t + T * e));
+        }
+        if (a.flags & ROW_FWD) fft_line_cwb<P, +1>(v, t, ad, tw, pairsync);
+        if (a.scale != 1.0f) {
+#pragma unroll
+            for (int e = 0; e < E; ++e) v[e] = c_scale(v[e], a.scale);
+        }
+        if (a.flags & ROW_ACCUM) {
+            double *acc = a.accum + (size_t)line * N;
+#pragma unroll
+            for (int e = 0; e < E; ++e)
+                acc[t + T * e] += a.accum_w * ((double)v[e].x * v[e].x + (double)v[e].y * v[e].y);
+        }
+        pairsync();  // both warps are done reading the slot (and, without a load, the old store left it)
+        if (store) {
+#pragma unroll
+            for (int e = 0; e < E; ++e) buf[t + T * e] = v[e];
+            fence_proxy_async();
+            pairsync();
+            if (leader) {
+                bulk_store(a.out + (size_t)line * N, buf, LINE);
+                tma_commit();
+            }
+        }
+    }
+    if (leader) {
+        if (store) tma_wait_all();
+        if (!ok) {
+            if (a.err) atomicExch(a.err, 1);
+            for (int j = k; j < issued; ++j)
+                mbar_wait_bounded(&bar[j % NBUF], (uint32_t)((j / NBUF) & 1), kWaitLimit);
+        }
+    }
+}
+
+static cudaError_t row_pair_launch(const RowArgs &a, cudaStream_t s, int nsm) {
+    using Cfg = RowPairCfg;
+    static int per_sm = 0;
+    if (!per_sm) {
+        cudaError_t e = cudaFuncSetAttribute(row_pair_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)Cfg::SMEM);
+        if (e != cudaSuccess) return e;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, row_pair_kernel, Cfg::THREADS, Cfg::SMEM);
+        if (e != cudaSuccess) return e;
+        if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    }
+    const int ncta = (a.nlines + Cfg::PAIRS - 1) / Cfg::PAIRS;
+    int grid = nsm * per_sm < ncta ? nsm * per_sm : ncta;
+    if (grid < 1) grid = 1;
+    row_pair_kernel<<<grid, Cfg::THREADS, Cfg::SMEM, s>>>(a);
     return cudaGetLastError();
 }
 
@@ -1327,7 +1477,7 @@ template <int N> static cudaError_t row_warp_launch(const RowArgs &a, cudaStream
 
 // Warp-owned lines for the sides whose plan fits 32 threads per line.
 static bool row_warp_eligible(int ny, const RowArgs &a) {
-    if (ny != 256 && ny != 384 && ny != 512 && ny != 768 && ny != 1024) return false;
+    if (ny != 256 && ny != 384 && ny != 512 && ny != 768 && ny != 1024 && ny != 2048) return false;
     if (a.flags & ROW_GENT) return false;
     if (((uintptr_t)a.out & 15u) || ((a.flags & ROW_LOAD) && ((uintptr_t)a.in & 15u))) return false;
     return true;
@@ -1410,6 +1560,7 @@ cudaError_t launch_row_pass(int ny, const RowArgs &a, cudaStream_t s, int nsm, i
                     return row_two_launch<HalfWarpPlan512>(a, s, nsm);
                 return row_warp_launch<512>(a, s, nsm);
             case 1024: return row_two_launch<WarpPlan1024x2>(a, s, nsm);
+            case 2048: return row_pair_launch(a, s, nsm);
             default: break;
         }
     }
