@@ -1,8 +1,8 @@
-"""The slice loop's two-stage passes at nx = 256, 512 and 1024 (columns in
-swizzled TMA tiles, independent thread groups per CTA; at 1024 a column is
-shared by a warp pair; rows of 256 and 512 two per warp): non-square grids,
-batches that leave groups without tiles, several detectors and checkpoints,
-against the FP64 oracle."""
+"""The slice loop's passes on every kernel family: two-stage columns at 256,
+512 and 1024 (swizzled TMA tiles, independent thread groups per CTA; at 1024 a
+column is shared by a warp pair), mixed-radix 384 / 768 rows and columns, the
+2048 warp-pair rows; non-square grids, batches that leave groups without
+tiles, several detectors and checkpoints, against the FP64 oracle."""
 import numpy as np
 import pytest
 
@@ -22,7 +22,8 @@ def _layers(rng, nt, nx, ny, ax, by, kev):
 
 @pytest.mark.parametrize("nx,ny,batch", [(256, 64, 1), (256, 384, 3), (256, 256, 7),
                                          (512, 64, 1), (512, 384, 3), (512, 1024, 2), (512, 512, 5),
-                                         (1024, 64, 1), (1024, 256, 3), (1024, 1024, 2)])
+                                         (1024, 64, 1), (1024, 256, 3), (1024, 1024, 2),
+                                         (384, 768, 2), (768, 384, 3), (768, 2048, 1), (2048, 768, 1)])
 def test_ctem_two_stage_columns_match_oracle(ctx, nx, ny, batch):
     rng = np.random.default_rng(nx + ny + batch)
     ax, by, kev = 30.0, 30.0 * ny / nx, 200.0
@@ -37,7 +38,7 @@ def test_ctem_two_stage_columns_match_oracle(ctx, nx, ny, batch):
     assert O.rel_l2(got, ref) < 2e-5
 
 
-@pytest.mark.parametrize("nx,ny", [(256, 256), (512, 384), (1024, 256)])
+@pytest.mark.parametrize("nx,ny", [(256, 256), (512, 384), (1024, 256), (384, 768), (768, 384), (2048, 64)])
 def test_stem_two_stage_columns_detectors_and_checkpoints(ctx, nx, ny):
     rng = np.random.default_rng(11)
     ax, kev = 31.0 * nx / 512, 200.0  # 0.06 A pixels: every detector inside the band limit
