@@ -257,7 +257,7 @@ def run_ours(args):
 
 
 # ------------------------------------------------------------- CPU baseline
-def cpu_baseline(cfg, nprobe, spawn_pool=False, check=None, check_fp64=4):
+def cpu_baseline(cfg, nprobe, check=None, check_fp64=4):
     """Oracle port of the reference CPU loop on a bounded probe sample.  With
     `check` (the GPU's detector sums of the same raster) it also reports their
     relative L2 error per detector against this run and against an FP64 run of
