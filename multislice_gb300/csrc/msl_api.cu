@@ -360,7 +360,7 @@ int err_reset(msl_ctx *c) {
 int err_check(msl_ctx *c) {
     int h = 0;
     CUDA_TRY(c, cudaMemcpy(&h, c->dflag, sizeof(int), cudaMemcpyDeviceToHost));
-    if (h == 2) return fail(c, MSL_E_CUDA, "the 512 column pass found its tile slots outside its shared memory");
+    if (h == 2) return fail(c, MSL_E_CUDA, "a pass found its aligned tile or line slots outside its shared memory");
     if (h) return fail(c, MSL_E_CUDA, "a pass's bounded wait for its bulk / TMA copy timed out");
     return MSL_OK;
 }
