@@ -10,13 +10,15 @@
 // with FPARAMS coefficients, K0/I0 by the Abramowitz & Stegun 9.8.1/9.8.5/9.8.6
 // polynomials the reference uses (slicelib.cpp:168-235).
 //
-// GB300 design: one CTA per 8 x 32 pixel tile of one slice.  The slice's atoms
-// stream through in chunks of 256; each chunk is culled against the tile's
+// GB300 design: one CTA per 32 x 32 pixel tile of one slice, four pixels per
+// thread (independent accumulators for latency hiding).  The slice's atoms
+// stream through in chunks of 128; each chunk is culled against the tile's
 // periodic bounding box and compacted in atom order (so the float sum order is
-// fixed), then the per-atom x and y offsets of the tile's 8 columns and 32 rows
+// fixed), then the per-atom x and y offsets of the tile's 32 columns and 32 rows
 // are formed once in FP64 (so an atom sitting exactly on a pixel gives r = 0,
 // clamped to 1e-10 A as the reference does, never a float rounding residue)
-// and the pair loop runs in FP32 on those offsets.
+// and the pair loop runs in FP32 on those offsets.  Every pixel sums its atoms
+// in atom order, whatever the tile shape.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
@@ -26,7 +28,7 @@
 namespace msl {
 
 namespace {
-constexpr int TX = 8, TY = 32, THREADS = TX * TY, CHUNK = 256;
+constexpr int TX = 32, TY = 32, THREADS = 256, PX = TX * TY / THREADS, CHUNK = 128;
 
 __device__ __forceinline__ float poly(const float *c, int n, float t) {
     float s = c[n - 1];
@@ -59,7 +61,7 @@ __global__ void __launch_bounds__(THREADS) potential_kernel(PotArgs a) {
     __shared__ float sdy[CHUNK][TY];
     __shared__ int wcount[THREADS / 32];
     const int tid = threadIdx.x;
-    const int ty = tid % TY, tx = tid / TY;
+    const int ty = tid % TY, txg = tid / TY;  // pixels (txg + 8 j, ty), j < PX
     const int lane = tid & 31, warp = tid >> 5;
     const int iy0 = blockIdx.x * TY, ix0 = blockIdx.y * TX, s = blockIdx.z;
 
@@ -68,14 +70,16 @@ __global__ void __launch_bounds__(THREADS) potential_kernel(PotArgs a) {
     const double yc = (iy0 + 0.5 * (TY - 1)) * a.dyp, hy = 0.5 * (TY - 1) * a.dyp;
     const double rad = sqrt((double)a.rad2) * (1.0 + 1e-6) + 1e-6;
     const int a0 = a.off[s], a1 = a.off[s + 1];
-    float acc = 0.f;
+    float acc[PX];
+#pragma unroll
+    for (int j = 0; j < PX; ++j) acc[j] = 0.f;
 
     for (int c0 = a0; c0 < a1; c0 += CHUNK) {
         const int ai = c0 + tid;
         bool keep = false;
         double xa = 0.0, ya = 0.0;
         int z = 0;
-        if (ai < a1) {
+        if (tid < CHUNK && ai < a1) {
             xa = a.x[ai];
             ya = a.y[ai];
             z = a.Z[ai];
@@ -118,23 +122,31 @@ __global__ void __launch_bounds__(THREADS) potential_kernel(PotArgs a) {
         }
         __syncthreads();
         for (int k = 0; k < total; ++k) {
-            const float dx = sdx[k][tx], dy = sdy[k][ty];
-            const float r2 = dx * dx + dy * dy;
-            if (r2 < a.rad2) {
-                const float r = fmaxf(sqrtf(r2), 1.0e-10f);
-                const float *p = a.sp + sZ[k] * 12;
-                float v = __ldg(p + 0) * bessk0f(__ldg(p + 1) * r) +
-                          __ldg(p + 2) * bessk0f(__ldg(p + 3) * r) +
-                          __ldg(p + 4) * bessk0f(__ldg(p + 5) * r);
-                const float rr = r * r;
-                v += __ldg(p + 6) * expf(-__ldg(p + 7) * rr) + __ldg(p + 8) * expf(-__ldg(p + 9) * rr) +
-                     __ldg(p + 10) * expf(-__ldg(p + 11) * rr);
-                acc += v;
+            const float dy = sdy[k][ty];
+            const float *p = a.sp + sZ[k] * 12;
+#pragma unroll
+            for (int j = 0; j < PX; ++j) {
+                const float dx = sdx[k][txg + 8 * j];
+                const float r2 = dx * dx + dy * dy;
+                if (r2 < a.rad2) {
+                    const float r = fmaxf(sqrtf(r2), 1.0e-10f);
+                    float v = __ldg(p + 0) * bessk0f(__ldg(p + 1) * r) +
+                              __ldg(p + 2) * bessk0f(__ldg(p + 3) * r) +
+                              __ldg(p + 4) * bessk0f(__ldg(p + 5) * r);
+                    const float rr = r * r;
+                    v += __ldg(p + 6) * expf(-__ldg(p + 7) * rr) + __ldg(p + 8) * expf(-__ldg(p + 9) * rr) +
+                         __ldg(p + 10) * expf(-__ldg(p + 11) * rr);
+                    acc[j] += v;
+                }
             }
         }
     }
-    const int ix = ix0 + tx, iy = iy0 + ty;
-    if (ix < a.nx && iy < a.ny) a.v[((size_t)s * a.nx + ix) * a.ny + iy] = acc;
+    const int iy = iy0 + ty;
+#pragma unroll
+    for (int j = 0; j < PX; ++j) {
+        const int ix = ix0 + txg + 8 * j;
+        if (ix < a.nx && iy < a.ny) a.v[((size_t)s * a.nx + ix) * a.ny + iy] = acc[j];
+    }
 }
 
 cudaError_t launch_potential(const PotArgs &a, cudaStream_t s, int64_t *launches) {
