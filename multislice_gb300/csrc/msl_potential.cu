@@ -28,6 +28,8 @@
 namespace msl {
 
 namespace {
+// tile and chunk shape picked by timing 16 / 32 / 64-pixel-wide tiles and
+// 32 / 64 / 128-atom chunks on the Au 2048^2 potentials
 constexpr int TX = 32, TY = 32, THREADS = 256, PX = TX * TY / THREADS, CHUNK = 128;
 
 __device__ __forceinline__ float poly(const float *c, int n, float t) {
