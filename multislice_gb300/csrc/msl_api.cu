@@ -381,10 +381,12 @@ int check_layers(msl_ctx *c, int ntrans, const double *dz, const int *layer_seq,
 // Slice loop plus objective-lens imaging on device buffers (mulslice.cpp:539-676
 // with one illumination angle).  w: [batch][nx][ny] entrance waves (ignored when
 // plane) and, on return, exit waves when want_exit; img_d / exit_d: FP64
-// accumulators (exit_d may be null).
+// accumulators (exit_d may be null); ttab: optional per-image transmission
+// rows, [slice step][image] device pointers (td unused then).
 int ctem_core(msl_ctx *c, const msl_grid *g, const msl_optics *o, const float2 *td, int ntrans,
               const double *dz, const int *seq, int nslice, const msl_lens *lens, float2 *w,
-              int batch, bool plane, double weight, double *img_d, double *exit_d, bool want_exit) {
+              int batch, bool plane, double weight, double *img_d, double *exit_d, bool want_exit,
+              const float2 *const *ttab) {
     int rc;
     const int nx = g->nx, ny = g->ny;
     const size_t n2 = (size_t)nx * ny;
@@ -397,7 +399,9 @@ int ctem_core(msl_ctx *c, const msl_grid *g, const msl_optics *o, const float2 *
         int rf = msl::ROW_TRANS | msl::ROW_FWD;
         if (s > 0) rf |= msl::ROW_LOAD | msl::ROW_INV;
         else if (!plane) rf |= msl::ROW_LOAD;
-        RowArgs r = row_args(g, twr, td + (size_t)l * n2, w, batch, rf, c->dflag);
+        // ttab: every image its own transmission, [slice step][image] row pointers
+        RowArgs r = row_args(g, twr, ttab ? nullptr : td + (size_t)l * n2, w, batch, rf, c->dflag);
+        if (ttab) r.trans_b = ttab + (size_t)s * batch;
         LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_row_pass(ny, r, c->stream, c->nsm, &c->launches); }));
         // the last slice keeps the spectrum: W = Psi(k) / (nx ny) after the propagator
         int cf = msl::COL_LOAD | msl::COL_FWD | msl::COL_PROP | msl::COL_STORE;
@@ -628,7 +632,7 @@ int msl_ctem_image(msl_ctx *c, const msl_grid *g, const msl_optics *o, const flo
     if (exit_intensity && !edev)
         CUDA_TRY(c, cudaMemcpyAsync(exit_d, exit_intensity, ibytes, cudaMemcpyHostToDevice, c->stream));
     if ((rc = ctem_core(c, g, o, td, ntrans, dz, layer_seq, nslice, lens, w, batch, plane_wave != 0, weight,
-                        img_d, exit_d, psi != nullptr)))
+                        img_d, exit_d, psi != nullptr, nullptr)))
         return rc;
     if (psi && !pdev) CUDA_TRY(c, cudaMemcpyAsync(psi, w, wbytes, cudaMemcpyDeviceToHost, c->stream));
     if (!idev) CUDA_TRY(c, cudaMemcpyAsync(image, img_d, ibytes, cudaMemcpyDeviceToHost, c->stream));
@@ -654,16 +658,28 @@ int msl_frozen_phonon(msl_ctx *c, const msl_atoms *at, const double *fparams, co
     CUDA_TRY(c, cudaSetDevice(c->device));
     const int nx = g->nx, ny = g->ny, na = at->natom;
     const size_t n2 = (size_t)nx * ny;
-    // device buffers: potential, transmission, wave, accumulators
-    DevBuf vbuf, tbuf;
-    vbuf.mb = tbuf.mb = &c->mem;
+    // device buffers: potential (one configuration), transmissions of a batch of
+    // configurations, their waves, accumulators.  The configurations of a batch
+    // run through one slice loop, each with its own transmission functions
+    // (per-image row pointers), and are imaged and accumulated in order, so the
+    // sums equal the one-configuration-at-a-time loop bit for bit.
+    const size_t slab = sizeof(float2) * n2 * nslice;  // one configuration's transmissions
+    size_t budget = (size_t)16 << 30;
+    if (c->mem.limit && c->mem.limit / 2 < budget) budget = c->mem.limit / 2;
+    const int B = (int)std::max<size_t>(1, std::min<size_t>((size_t)nconfig, budget / (slab + sizeof(float2) * n2)));
+    DevBuf vbuf, tbuf, pbuf;
+    vbuf.mb = tbuf.mb = pbuf.mb = &c->mem;
     CUDA_TRY(c, vbuf.ensure(sizeof(float) * n2 * nslice));
-    CUDA_TRY(c, tbuf.ensure(sizeof(float2) * n2 * nslice));
+    CUDA_TRY(c, tbuf.ensure(slab * B));
+    CUDA_TRY(c, pbuf.ensure(sizeof(float2 *) * (size_t)nslice * B));
     CUDA_TRY(c, c->acc.ensure(2 * sizeof(double) * n2));
     double *img_d = (double *)c->acc.p, *exit_d = img_d + n2;
     CUDA_TRY(c, cudaMemsetAsync(img_d, 0, 2 * sizeof(double) * n2, c->stream));
-    CUDA_TRY(c, c->wave.ensure(sizeof(float2) * n2));
+    CUDA_TRY(c, c->wave.ensure(sizeof(float2) * n2 * B));
     float2 *w = (float2 *)c->wave.p;
+    float2 *tall = (float2 *)tbuf.p;
+    const float2 **ptab = (const float2 **)pbuf.p;
+    std::vector<const float2 *> hptab((size_t)nslice * B);
     std::vector<double> x(na), y(na), z(na), d(3 * (size_t)na);
     std::vector<double> dz(nslice, at->cz / nslice);
     std::vector<int> seq(nslice);
@@ -673,20 +689,31 @@ int msl_frozen_phonon(msl_ctx *c, const msl_atoms *at, const double *fparams, co
     jat.y = y.data();
     jat.z = z.data();
     int out = MSL_OK;
-    for (int cfg = 0; cfg < nconfig && out == MSL_OK; ++cfg) {
-        msl_phonon_displacements(seed, cfg, na, sigma, d.data());
-        for (int i = 0; i < na; ++i) {
-            x[i] = at->x[i] + d[3 * i];
-            y[i] = at->y[i] + d[3 * i + 1];
-            z[i] = at->z[i] + d[3 * i + 2];
+    for (int cfg0 = 0; cfg0 < nconfig && out == MSL_OK; cfg0 += B) {
+        const int nb = std::min(B, nconfig - cfg0);
+        for (int b = 0; b < nb && out == MSL_OK; ++b) {
+            msl_phonon_displacements(seed, cfg0 + b, na, sigma, d.data());
+            for (int i = 0; i < na; ++i) {
+                x[i] = at->x[i] + d[3 * i];
+                y[i] = at->y[i] + d[3 * i + 1];
+                z[i] = at->z[i] + d[3 * i + 2];
+            }
+            float *tb = (float *)(tall + n2 * nslice * b);
+            if ((out = msl_potential_build(c, &jat, fparams, g, nslice, radius, (float *)vbuf.p))) break;
+            if ((out = msl_transmission_build(c, g, o, (const float *)vbuf.p, nslice, tb))) break;
+            for (int s = 0; s < nslice; ++s) hptab[(size_t)s * nb + b] = tall + n2 * nslice * b + n2 * s;
         }
-        if ((out = msl_potential_build(c, &jat, fparams, g, nslice, radius, (float *)vbuf.p))) break;
-        if ((out = msl_transmission_build(c, g, o, (const float *)vbuf.p, nslice, (float *)tbuf.p))) break;
-        if ((out = err_reset(c))) break;
-        if ((out = ctem_core(c, g, o, (const float2 *)tbuf.p, nslice, dz.data(), seq.data(), nslice, lens,
-                             w, 1, true, 1.0 / nconfig, img_d, exit_intensity ? exit_d : nullptr, false)))
+        if (out != MSL_OK) break;
+        if (cudaMemcpyAsync(ptab, hptab.data(), sizeof(float2 *) * (size_t)nslice * nb, cudaMemcpyHostToDevice,
+                            c->stream) != cudaSuccess) {
+            out = fail(c, MSL_E_CUDA, "frozen phonon: transmission table upload failed");
             break;
-        cudaError_t e = cudaStreamSynchronize(c->stream);
+        }
+        if ((out = err_reset(c))) break;
+        if ((out = ctem_core(c, g, o, tall, nslice, dz.data(), seq.data(), nslice, lens, w, nb, true,
+                             1.0 / nconfig, img_d, exit_intensity ? exit_d : nullptr, false, ptab)))
+            break;
+        cudaError_t e = cudaStreamSynchronize(c->stream);  // also: hptab is free for the next batch
         if (e != cudaSuccess) {
             out = fail(c, MSL_E_CUDA, std::string("frozen phonon: ") + cudaGetErrorString(e));
             break;
@@ -708,6 +735,7 @@ int msl_frozen_phonon(msl_ctx *c, const msl_atoms *at, const double *fparams, co
     cudaStreamSynchronize(c->stream);
     vbuf.release();
     tbuf.release();
+    pbuf.release();
     return out;
 }
 
@@ -953,7 +981,7 @@ int msl_ctem_partial_coherence(msl_ctx *c, const msl_grid *g, const msl_optics *
     double *img_d = idev ? image : (double *)c->acc.p;
     CUDA_TRY(c, cudaMemsetAsync(img_d, 0, sizeof(double) * n2, c->stream));
     if ((rc = ctem_core(c, g, o, td, ntrans, dz, layer_seq, nslice, lens, w, na, false, 1.0 / na, img_d,
-                        nullptr, false)))
+                        nullptr, false, nullptr)))
         return rc;
     if (!idev) CUDA_TRY(c, cudaMemcpyAsync(image, img_d, sizeof(double) * n2, cudaMemcpyDeviceToHost, c->stream));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
