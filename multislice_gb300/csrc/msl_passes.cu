@@ -392,7 +392,7 @@ __global__ void __launch_bounds__(ColTmaCfg<PL>::THREADS, MINB)
 struct ColHalfL512 {  // 512: 8 columns, a warp per column pair
     using P = HalfWarpColPlan512;
     using Lin = ColLin64;
-    static constexpr int N = 512, C = 8, G = 3;
+    static constexpr int N = 512, C = 8, G = 3, WPG = 4;
     static constexpr bool PAIR = false;
     static constexpr CUtensorMapSwizzle SWZ = CU_TENSOR_MAP_SWIZZLE_64B;
     __device__ static int col(int wg, int lane) { return 2 * wg + (lane & 1); }
@@ -401,7 +401,7 @@ struct ColHalfL512 {  // 512: 8 columns, a warp per column pair
 struct ColHalfL256 {  // 256: 8 columns, a warp per column pair, four groups per CTA
     using P = HalfWarpColPlan256;
     using Lin = ColLin64;
-    static constexpr int N = 256, C = 8, G = 4;
+    static constexpr int N = 256, C = 8, G = 4, WPG = 4;
     static constexpr bool PAIR = false;
     static constexpr CUtensorMapSwizzle SWZ = CU_TENSOR_MAP_SWIZZLE_64B;
     __device__ static int col(int wg, int lane) { return 2 * wg + (lane & 1); }
@@ -410,7 +410,7 @@ struct ColHalfL256 {  // 256: 8 columns, a warp per column pair, four groups per
 struct ColPairL1024 {  // 1024: 4 columns, a warp pair per column pair
     using P = WarpPairColPlan1024;
     using Lin = ColLin32;
-    static constexpr int N = 1024, C = 4, G = 3;
+    static constexpr int N = 1024, C = 4, G = 3, WPG = 4;
     static constexpr bool PAIR = true;
     static constexpr CUtensorMapSwizzle SWZ = CU_TENSOR_MAP_SWIZZLE_32B;
     __device__ static int col(int wg, int lane) { return 2 * (wg >> 1) + (lane & 1); }
@@ -419,18 +419,20 @@ struct ColPairL1024 {  // 1024: 4 columns, a warp pair per column pair
 
 template <class L> struct ColHalfCfg {
     using P = typename L::P;
-    static constexpr int N = L::N, C = L::C, G = L::G, GT = 128, THREADS = GT * G, NBUF = 2, BOXR = 256;
+    static constexpr int N = L::N, C = L::C, G = L::G, GT = 32 * L::WPG, THREADS = GT * G, NBUF = 2, BOXR = 256;
     static constexpr uint32_t SLOT = sizeof(float2) * N * C;  // 16 or 32 KB, also the slot alignment
     static constexpr int TW = P::radix(1) * P::radix(0);      // stage 1 table [r][k]
     static constexpr size_t OFF_RED = sizeof(float2) * TW;
-    static constexpr size_t OFF_BAR = OFF_RED + sizeof(double) * G * 4 * kMaxDet;
+    static constexpr size_t OFF_BAR = OFF_RED + sizeof(double) * G * L::WPG * kMaxDet;
     static constexpr size_t HEADER = OFF_BAR + sizeof(uint64_t) * G * NBUF;
     // the header, then 2 G slots from the next slot boundary
     static constexpr size_t SMEM = HEADER + SLOT - 1 + (size_t)NBUF * G * SLOT + 1024 <= 227 * 1024
                                        ? HEADER + SLOT - 1 + (size_t)NBUF * G * SLOT + 1024 : 227 * 1024;
     static_assert((SLOT & (SLOT - 1)) == 0 && N % BOXR == 0 && P::NSTAGE == 2 && C % 4 == 0, "two stages");
-    static_assert(1 + G + 2 * G <= 16, "named barriers: one per group, one per warp pair");
-    static_assert(L::Lin::B(P::T) == 1024 && L::Lin::B(P::T - 1) < 1024, "natural order: row t + T e at + 1024 e");
+    static_assert(1 + G + (L::PAIR ? 2 * G : 0) <= 16, "named barriers: one per group, one per warp pair");
+    // natural order: row t + T e of a column at nb + e ROWSTEP, nb the thread's base
+    static constexpr uint32_t ROWSTEP = L::Lin::B(P::T);
+    static_assert(L::Lin::B(P::T - 1) < ROWSTEP && L::Lin::B(3 * P::T) == 3 * ROWSTEP, "natural-order stride");
     static_assert(HEADER <= SLOT, "the header fits before the first slot");
 };
 
@@ -474,7 +476,7 @@ __global__ void __launch_bounds__(ColHalfCfg<L>::THREADS, 1)
     };
     const uint32_t barid = 1u + (uint32_t)g;
     uint64_t *bar = barall + g * NBUF;
-    double *red = redall + g * 4 * kMaxDet;
+    double *red = redall + g * L::WPG * kMaxDet;
     const uint32_t gslot = slot0 + (uint32_t)(g * NBUF) * SLOT;
     const bool store = (a.flags & COL_STORE) != 0;
     const int tpi = a.ny / C, ntiles = a.batch * tpi;
@@ -507,10 +509,10 @@ __global__ void __launch_bounds__(ColHalfCfg<L>::THREADS, 1)
             break;
         }
         const uint32_t cb = (gslot + (uint32_t)s * SLOT) ^ (8u * (uint32_t)c);
-        const uint32_t nb = cb ^ Lin::B((uint32_t)t);  // row t + T e at nb + 1024 e
+        const uint32_t nb = cb ^ Lin::B((uint32_t)t);  // row t + T e at nb + ROWSTEP e
         float2 v[E];
 #pragma unroll
-        for (int e = 0; e < E; ++e) v[e] = lds_f2(nb + 1024u * (uint32_t)e);
+        for (int e = 0; e < E; ++e) v[e] = lds_f2(nb + Cfg::ROWSTEP * (uint32_t)e);
         fft_stage<P, 0, +1>(v, t, tw);
         fft_exchange_ch<P, 0, Lin>(v, t, cb, colsync);
         fft_stage<P, 1, +1>(v, t, tw);
@@ -540,7 +542,7 @@ __global__ void __launch_bounds__(ColHalfCfg<L>::THREADS, 1)
                 }
             }
             bar_group(barid, GT);
-            constexpr int NBLK = C / 4, WPB = 4 / NBLK;  // 4-column blocks per tile, warps per block
+            constexpr int NBLK = C / 4, WPB = L::WPG / NBLK;  // 4-column blocks per tile, warps per block
             if (gt < NBLK * a.ndet) {                   // warps WPB hq .. WPB hq + WPB - 1 hold block hq
                 const int hq = gt / a.ndet, d = gt % a.ndet;
                 double sum = 0.0;
@@ -557,7 +559,7 @@ __global__ void __launch_bounds__(ColHalfCfg<L>::THREADS, 1)
         if (store) {
             colsync();  // every thread of the columns is done reading them
 #pragma unroll
-            for (int e = 0; e < E; ++e) sts_f2(nb + 1024u * (uint32_t)e, v[e]);
+            for (int e = 0; e < E; ++e) sts_f2(nb + Cfg::ROWSTEP * (uint32_t)e, v[e]);
             fence_proxy_async();
             bar_group(barid, GT);
             if (gt == 0) {
