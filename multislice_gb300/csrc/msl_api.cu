@@ -1235,9 +1235,14 @@ int msl_transmission_build(msl_ctx *c, const msl_grid *g, const msl_optics *o, c
     if ((rc = build_slice_tables(c, g, o, 1, nullptr, st))) return rc;
     float2 *twr = twiddles(c, ny), *twc = twiddles(c, nx);
     if (!twr || !twc) return fail(c, MSL_E_NOMEM, "twiddle table allocation failed");
-    RowArgs r = row_args(g, twr, nullptr, td, nlayer, msl::ROW_GENT | msl::ROW_FWD, c->dflag);
-    r.vpot = vd;
-    r.phase_scale = msl_sigma(o->kev) / 1000.0;  // rad per V*A
+    // t = exp(i sigma V) elementwise, then the band limit: forward transform,
+    // 2/3 mask, inverse transform (mulslice.cpp:414-421, :515-522)
+    const double phase_scale = msl_sigma(o->kev) / 1000.0;  // rad per V*A
+    LAUNCH_TRY(c, timed(c, MSL_PROF_OTHER, [&] {
+                   return msl::launch_transmission_phase(vd, phase_scale, n2 * nlayer, td, c->nsm, c->stream,
+                                                         &c->launches);
+               }));
+    RowArgs r = row_args(g, twr, nullptr, td, nlayer, msl::ROW_LOAD | msl::ROW_FWD, c->dflag);
     LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_row_pass(ny, r, c->stream, c->nsm, &c->launches); }));
     ColArgs ca = col_args(g, st, twc, 0, td, nlayer, msl::COL_LOAD | msl::COL_FWD | msl::COL_PROP | msl::COL_INV | msl::COL_STORE, c->dflag);
     LAUNCH_TRY(c, timed(c, MSL_PROF_COL, [&] { return msl::launch_col_pass(nx, ca, c->stream, c->nsm, &c->launches); }));

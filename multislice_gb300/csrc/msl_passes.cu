@@ -1250,6 +1250,32 @@ __global__ void tilt_wave_kernel(int nx, int ny, const float *xpos, const float 
 
 // Self-test of the bounded waits: an mbarrier that nothing ever arrives on is
 // polled `polls` times; the wait gives up, the kernel raises *err and returns.
+// Transmission function t = exp(i sigma V) of every pixel (mulslice.cpp:414-421).
+// The phase carries FP64-grade accuracy in float-float arithmetic (FP64
+// instructions run at a small fraction of the FP32 rate on this GPU and bound
+// an FP64 version of this elementwise kernel): sigma = s_hi + s_lo, the product
+// s_hi V kept exactly as p + e (fma), then a Cody-Waite reduction by 2 pi split
+// into three floats (C1 = 6.28125 has 8 significant bits, so k C1 is exact for
+// |k| < 2^16), the low parts added last.  The reduced phase in [-pi, pi] then
+// goes to the single-precision sincos.  Elementwise, so the band-limiting
+// transforms that follow run on the fast row / column kernels.
+__global__ void transmission_phase_kernel(const float *__restrict__ v, float s_hi, float s_lo, size_t n,
+                                          float2 *__restrict__ t) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const float x = v[i];
+        const float p = s_hi * x;
+        const float e = fmaf(s_hi, x, -p) + s_lo * x;  // sigma x = p + e to about 48 bits
+        const float k = rintf(p * 0.15915494309189535f);
+        float r = fmaf(-k, 6.28125f, p);
+        r = fmaf(-k, 1.9353071693331003e-3f, r);
+        r += e;
+        r = fmaf(-k, 1.0253131677018246e-11f, r);
+        float sn, cn;
+        sincosf(r, &sn, &cn);
+        t[i] = make_float2(cn, sn);
+    }
+}
+
 __global__ void wait_timeout_kernel(int *err, uint32_t polls) {
     __shared__ uint64_t bar;
     if (threadIdx.x == 0) {
@@ -1648,6 +1674,18 @@ cudaError_t launch_tilt_waves(int nx, int ny, int nb, const float *xpos, const f
     ++*launches;
     dim3 grid((ny + 255) / 256, nx, nb);
     tilt_wave_kernel<<<grid, 256, 0, s>>>(nx, ny, xpos, ypos, q, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_transmission_phase(const float *v, double scale, size_t n, float2 *t, int nsm, cudaStream_t s,
+                                      int64_t *launches) {
+    ++*launches;
+    const float s_hi = (float)scale, s_lo = (float)(scale - (double)s_hi);
+    size_t blocks = (n + 255) / 256;
+    const size_t cap = (size_t)nsm * 16;
+    if (blocks > cap) blocks = cap;
+    if (blocks < 1) blocks = 1;
+    transmission_phase_kernel<<<(unsigned)blocks, 256, 0, s>>>(v, s_hi, s_lo, n, t);
     return cudaGetLastError();
 }
 
