@@ -1165,17 +1165,22 @@ int msl_potential_build(msl_ctx *c, const msl_atoms *at, const double *fparams, 
             sp[z * 12 + 7 + 2 * i] = (float)(PIK * PIK / d);
         }
     }
-    // one upload: off | x | y | Z | sp
+    // one upload: off | x | y | Z | sp | xf | yf
+    std::vector<float> xf(xs.begin(), xs.end()), yf(ys.begin(), ys.end());
     const size_t o_off = 0, o_x = ((sizeof(int) * (nslice + 1) + 15) / 16) * 16;
     const size_t o_y = o_x + sizeof(double) * xs.size(), o_z = o_y + sizeof(double) * ys.size();
     const size_t o_sp = ((o_z + sizeof(int) * zs.size() + 15) / 16) * 16;
-    const size_t total = o_sp + sizeof(float) * sp.size();
+    const size_t o_xf = ((o_sp + sizeof(float) * sp.size() + 15) / 16) * 16;
+    const size_t o_yf = ((o_xf + sizeof(float) * xf.size() + 15) / 16) * 16;
+    const size_t total = o_yf + sizeof(float) * yf.size();
     std::vector<unsigned char> h(total, 0);
     memcpy(h.data() + o_off, count.data(), sizeof(int) * (nslice + 1));
     memcpy(h.data() + o_x, xs.data(), sizeof(double) * xs.size());
     memcpy(h.data() + o_y, ys.data(), sizeof(double) * ys.size());
     memcpy(h.data() + o_z, zs.data(), sizeof(int) * zs.size());
     memcpy(h.data() + o_sp, sp.data(), sizeof(float) * sp.size());
+    memcpy(h.data() + o_xf, xf.data(), sizeof(float) * xf.size());
+    memcpy(h.data() + o_yf, yf.data(), sizeof(float) * yf.size());
     rc = upload(c, c->atoms, h.data(), total);
     if (rc) return rc;
     unsigned char *d = (unsigned char *)c->atoms.p;
@@ -1191,6 +1196,8 @@ int msl_potential_build(msl_ctx *c, const msl_atoms *at, const double *fparams, 
     msl::PotArgs a;
     a.x = (const double *)(d + o_x);
     a.y = (const double *)(d + o_y);
+    a.xf = (const float *)(d + o_xf);
+    a.yf = (const float *)(d + o_yf);
     a.Z = (const int *)(d + o_z);
     a.off = (const int *)(d + o_off);
     a.nslice = nslice;

@@ -74,6 +74,7 @@ struct ColArgs {
 
 struct PotArgs {
     const double *x, *y;      // wrapped into [0, ax), [0, by)
+    const float *xf, *yf;     // the same, rounded to float (for the conservative tile culling)
     const int *Z;
     const int *off;           // [nslice + 1] atom ranges per slice
     int nslice, nx, ny;

@@ -13,7 +13,9 @@
 // GB300 design: one CTA per 32 x 32 pixel tile of one slice, four pixels per
 // thread (independent accumulators for latency hiding).  The slice's atoms
 // stream through in chunks of 128; each chunk is culled against the tile's
-// periodic bounding box and compacted in atom order (so the float sum order is
+// periodic bounding box (in float, from float copies of the coordinates, with a
+// margin that keeps every atom the FP64 test would: culling only has to be
+// conservative) and compacted in atom order (so the float sum order is
 // fixed), then the per-atom x and y offsets of the tile's 32 columns and 32 rows
 // are formed once in FP64 (so an atom sitting exactly on a pixel gives r = 0,
 // clamped to 1e-10 A as the reference does, never a float rounding residue)
@@ -67,10 +69,13 @@ __global__ void __launch_bounds__(THREADS) potential_kernel(PotArgs a) {
     const int lane = tid & 31, warp = tid >> 5;
     const int iy0 = blockIdx.x * TY, ix0 = blockIdx.y * TX, s = blockIdx.z;
 
-    // tile bounding box (pixel positions) for culling
-    const double xc = (ix0 + 0.5 * (TX - 1)) * a.dxp, hx = 0.5 * (TX - 1) * a.dxp;
-    const double yc = (iy0 + 0.5 * (TY - 1)) * a.dyp, hy = 0.5 * (TY - 1) * a.dyp;
-    const double rad = sqrt((double)a.rad2) * (1.0 + 1e-6) + 1e-6;
+    // tile bounding box (pixel positions) for the culling, in float with a margin
+    // that covers the float rounding of the coordinates (the culling only has to
+    // keep every atom that can reach the tile; the pair loop tests r < radius)
+    const float xc = (float)((ix0 + 0.5 * (TX - 1)) * a.dxp), hx = (float)(0.5 * (TX - 1) * a.dxp);
+    const float yc = (float)((iy0 + 0.5 * (TY - 1)) * a.dyp), hy = (float)(0.5 * (TY - 1) * a.dyp);
+    const float axf = (float)a.ax, byf = (float)a.by;
+    const float rad = sqrtf(a.rad2) * (1.0f + 1e-5f) + 1e-3f;
     const int a0 = a.off[s], a1 = a.off[s + 1];
     float acc[PX];
 #pragma unroll
@@ -82,14 +87,16 @@ __global__ void __launch_bounds__(THREADS) potential_kernel(PotArgs a) {
         double xa = 0.0, ya = 0.0;
         int z = 0;
         if (tid < CHUNK && ai < a1) {
-            xa = a.x[ai];
-            ya = a.y[ai];
-            z = a.Z[ai];
-            double dx = fabs(xa - xc);
-            dx = fmin(dx, a.ax - dx);
-            double dy = fabs(ya - yc);
-            dy = fmin(dy, a.by - dy);
+            float dx = fabsf(a.xf[ai] - xc);
+            dx = fminf(dx, axf - dx);
+            float dy = fabsf(a.yf[ai] - yc);
+            dy = fminf(dy, byf - dy);
             keep = (dx - hx < rad) && (dy - hy < rad);
+            if (keep) {
+                xa = a.x[ai];
+                ya = a.y[ai];
+                z = a.Z[ai];
+            }
         }
         // order-preserving compaction of the kept atoms
         const unsigned ball = __ballot_sync(0xffffffffu, keep);
