@@ -252,7 +252,10 @@ int msl_phonon_displacements(uint64_t seed, int config, int natom, double sigma,
  * (msl_phonon_displacements), build the potential and transmission functions
  * of nslice equal slices, run a plane wave through them and image it; image and
  * exit_intensity (either may be NULL) receive the averages over configurations,
- * double [nx][ny] (overwritten). */
+ * double [nx][ny] (overwritten).  Configurations run in batches through one
+ * slice loop, as many as 16 GiB of transmission functions hold (half the
+ * context's memory limit when one is set); the averages do not depend on the
+ * batch size. */
 int msl_frozen_phonon(msl_ctx *ctx, const msl_atoms *atoms, const double *fparams,
                       const msl_grid *grid, int nslice, double radius, const msl_optics *optics,
                       const msl_lens *lens, int nconfig, double sigma, uint64_t seed,
