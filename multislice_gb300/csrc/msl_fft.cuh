@@ -60,14 +60,15 @@ template <int N_, int T_, int C_, int PS_, int MINB_, int NBUF_ = 3> struct ColP
     static constexpr int radix(int s) { return B::radix(s); }
 };
 // Column plans of the mixed sides with their own radices (the kernel builds the
-// twiddle tables, OWN_TW): 32 threads per column, 8 columns per tile, the
-// radix 6 / 12 stage last, exchange swizzle g(i) = i ^ ((i >> ps) & 1) that a
-// CPU bank model found conflict-free for every exchange and the tile access.
-struct ColPlanMixed384 {
-    static constexpr int N = 384, T = 32, E = 12, NSTAGE = 4, MINB = 3, NBUF = 2;
-    static constexpr int row_swz = 1, row_sh = 2, col_c = 8, col_ps = 2;
+// twiddle tables, OWN_TW): 16 (384) or 32 (768) threads per column, 8 columns
+// per tile, the radix 6 / 12 stage last, exchange swizzle g(i) = i ^ ((i >> ps)
+// & 1) that a CPU bank model found conflict-free for every exchange and the
+// tile access.
+struct ColPlanMixed384 {  // 16 threads per column, radix 8 x 8 x 6
+    static constexpr int N = 384, T = 16, E = 24, NSTAGE = 3, MINB = 4, NBUF = 2;
+    static constexpr int row_swz = 1, row_sh = 2, col_c = 8, col_ps = 3;
     static constexpr bool PK = true, PKMUL = false, OWN_TW = true;
-    static constexpr int radix(int s) { return s < 3 ? 4 : 6; }
+    static constexpr int radix(int s) { return s < 2 ? 8 : 6; }
 };
 struct ColPlanMixed768 {
     static constexpr int N = 768, T = 32, E = 24, NSTAGE = 3, MINB = 2, NBUF = 2;
