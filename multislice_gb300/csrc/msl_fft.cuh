@@ -473,7 +473,7 @@ __device__ __forceinline__ void fft_stage_cw(float2 (&v)[P::E], int t, const flo
 template <class P, int S, bool WARP = false, class Addr>
 __device__ __forceinline__ void fft_exchange(float2 (&v)[P::E], int t, const Addr &ad) {
     constexpr int R = P::radix(S), NS = plan_span<P>(S), E = P::E, Q = E / R, T = P::T;
-    static_assert(!WARP || T == 32, "warp-owned lines need 32 threads per line");
+    static_assert(!WARP || T == 32 || T == 16, "warp-owned lines: 32 threads per line, or two half-warp lines");
     if constexpr (WARP) __syncwarp(); else __syncthreads();  // previous readers are done
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
@@ -749,13 +749,14 @@ template <int N_> struct WarpPlan {
 // The mixed sides one warp per line with fewer stages than Plan<N>, the radix
 // 6 / 12 stage last so the spans before it are powers of two, and an exchange
 // swizzle i ^ ((i >> sh) & 15) under which every exchange is conflict-free (a
-// CPU bank model of the half-warp wavefronts checked each one): 384 = 4 x 4 x
-// 4 x 6 (12 elements per thread), 768 = 8 x 8 x 12 (24 elements per thread).
-template <> struct WarpPlan<384> {
-    static constexpr int N = 384, T = 32, E = 12, NSTAGE = 4;
-    static constexpr int row_swz = 1, row_sh = 2, col_c = 4, col_ps = 30;
+// CPU bank model of the half-warp wavefronts checked each one): 384 = 8 x 8 x 6
+// on half-warp lines (16 threads x 24 elements, two lines per warp), 768 = 8 x 8
+// x 12 on warp lines (32 threads x 24 elements).
+template <> struct WarpPlan<384> {  // half-warp lines (two per warp)
+    static constexpr int N = 384, T = 16, E = 24, NSTAGE = 3;
+    static constexpr int row_swz = 1, row_sh = 3, col_c = 4, col_ps = 30;
     static constexpr bool PK = true, PKMUL = false, OWN_TW = true;
-    static constexpr int radix(int s) { return s < 3 ? 4 : 6; }
+    static constexpr int radix(int s) { return s < 2 ? 8 : 6; }
 };
 template <> struct WarpPlan<768> {
     static constexpr int N = 768, T = 32, E = 24, NSTAGE = 3;

@@ -733,28 +733,30 @@ template <> __device__ __forceinline__ RowXorAddr<WarpPlan<768>> make_row_addr(f
 
 template <int N> struct RowWarpCfg {
     using P = WarpPlan<N>;
-    static constexpr int W = 8, THREADS = 32 * W, NBUF = (N == 512 || N == 768) ? 2 : 3;
+    static constexpr int LPW = 32 / P::T;  // lines per warp: 1, or 2 for half-warp lines
+    static constexpr int W = 8, THREADS = 32 * W, NBUF = (N == 512 || N == 768 || LPW > 1) ? 2 : 3;
     static constexpr int MINB = N == 512 ? 3 : P::E <= 8 ? 3 : 2;
-    static constexpr size_t LINE = sizeof(float2) * N;
+    static constexpr size_t LINE = sizeof(float2) * N, UNIT = LPW * LINE;
     // power-of-two sides address their exchanges xor-linearly (RowXorLin), which
     // needs every line buffer aligned to its size
     static constexpr bool XL = (N & (N - 1)) == 0;
     static constexpr uint32_t ALIGN = XL ? (uint32_t)LINE : 128u;
-    static constexpr size_t OFF_TW = (size_t)W * NBUF * LINE;
+    static constexpr size_t OFF_TW = (size_t)W * NBUF * UNIT;
     static constexpr size_t OFF_BAR = OFF_TW + ((sizeof(float2) * plan_tw_size<P>() + 15) / 16) * 16;
     static constexpr size_t SMEM = OFF_BAR + sizeof(uint64_t) * W * NBUF + ALIGN;
+    static_assert(P::T == 32 || P::T == 16, "warp- or half-warp-owned lines");
 };
 
 template <int N>
 __global__ void __launch_bounds__(RowWarpCfg<N>::THREADS, RowWarpCfg<N>::MINB) row_warp_kernel(RowArgs a) {
     using Cfg = RowWarpCfg<N>;
     using P = WarpPlan<N>;
-    constexpr int E = P::E, NBUF = Cfg::NBUF, W = Cfg::W, TW = plan_tw_size<P>();
+    constexpr int E = P::E, T = P::T, LPW = Cfg::LPW, NBUF = Cfg::NBUF, W = Cfg::W, TW = plan_tw_size<P>();
     constexpr uint32_t AL = Cfg::ALIGN;
     extern __shared__ unsigned char smraw[];
     unsigned char *base = smraw + ((AL - (smem_u32(smraw) & (AL - 1u))) & (AL - 1u));
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    float2 *ring = reinterpret_cast<float2 *>(base) + (size_t)warp * NBUF * N;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, h = lane / T, t = lane % T;
+    float2 *ring = reinterpret_cast<float2 *>(base) + (size_t)warp * NBUF * LPW * N;
     float2 *tw = reinterpret_cast<float2 *>(base + Cfg::OFF_TW);
     uint64_t *bar = reinterpret_cast<uint64_t *>(base + Cfg::OFF_BAR) + warp * NBUF;
     if constexpr (P::OWN_TW) {  // stage s >= 1: [r][k] = exp(2 pi i r k / (NS R)), NS = span before s
@@ -776,14 +778,15 @@ __global__ void __launch_bounds__(RowWarpCfg<N>::THREADS, RowWarpCfg<N>::MINB) r
     }
     __syncthreads();  // the only CTA barrier: tables and barriers are ready
     const bool load = (a.flags & ROW_LOAD) != 0, store = !(a.flags & ROW_NOSTORE);
+    const int nunits = a.nlines / LPW;  // units of LPW consecutive lines, one per warp at a time
     const int G = gridDim.x * W, gw = blockIdx.x * W + warp;
-    const int nmine = gw < a.nlines ? (a.nlines - gw + G - 1) / G : 0;
+    const int nmine = gw < nunits ? (nunits - gw + G - 1) / G : 0;
     int issued = 0;
     auto issue = [&](int k) {  // lane 0 only
-        const int line = gw + k * G, s = k % NBUF;
+        const int unit = gw + k * G, s = k % NBUF;
         fence_proxy_async();
-        mbar_arrive_expect_tx(&bar[s], (uint32_t)Cfg::LINE);
-        bulk_load(ring + (size_t)s * N, a.in + (size_t)line * N, (uint32_t)Cfg::LINE, &bar[s]);
+        mbar_arrive_expect_tx(&bar[s], (uint32_t)Cfg::UNIT);
+        bulk_load(ring + (size_t)s * LPW * N, a.in + (size_t)unit * LPW * N, (uint32_t)Cfg::UNIT, &bar[s]);
         issued = k + 1;
     };
     if (load && lane == 0)
@@ -791,8 +794,9 @@ __global__ void __launch_bounds__(RowWarpCfg<N>::THREADS, RowWarpCfg<N>::MINB) r
     int k = 0;
     bool ok = true;
     for (; k < nmine; ++k) {
-        const int line = gw + k * G, s = k % NBUF;
-        float2 *buf = ring + (size_t)s * N;
+        const int unit = gw + k * G, s = k % NBUF, line = LPW * unit + h;
+        float2 *slot = ring + (size_t)s * LPW * N;
+        float2 *buf = slot + (size_t)h * N;
         using Addr = typename std::conditional<Cfg::XL, RowXorLin<P>, RowXorAddr<P>>::type;
         Addr ad = make_row_addr<Addr>(buf);
         const float2 *trow = (a.flags & ROW_TRANS)
@@ -815,17 +819,17 @@ __global__ void __launch_bounds__(RowWarpCfg<N>::THREADS, RowWarpCfg<N>::MINB) r
                 break;
             }
 #pragma unroll
-            for (int e = 0; e < E; ++e) v[e] = buf[lane + 32 * e];
+            for (int e = 0; e < E; ++e) v[e] = buf[t + T * e];
         } else {
 #pragma unroll
             for (int e = 0; e < E; ++e) v[e] = make_float2(1.f, 0.f);
         }
-        if (a.flags & ROW_INV) fft_line<P, -1, 0, true>(v, lane, ad, tw);
+        if (a.flags & ROW_INV) fft_line<P, -1, 0, true>(v, t, ad, tw);
         if (a.flags & ROW_TRANS) {
 #pragma unroll
-            for (int e = 0; e < E; ++e) v[e] = c_mul(v[e], __ldg(trow + lane + 32 * e));
+            for (int e = 0; e < E; ++e) v[e] = c_mul(v[e], __ldg(trow + t + T * e));
         }
-        if (a.flags & ROW_FWD) fft_line<P, +1, 0, true>(v, lane, ad, tw);
+        if (a.flags & ROW_FWD) fft_line<P, +1, 0, true>(v, t, ad, tw);
         if (a.scale != 1.0f) {
 #pragma unroll
             for (int e = 0; e < E; ++e) v[e] = c_scale(v[e], a.scale);
@@ -834,16 +838,16 @@ __global__ void __launch_bounds__(RowWarpCfg<N>::THREADS, RowWarpCfg<N>::MINB) r
             double *acc = a.accum + (size_t)line * N;
 #pragma unroll
             for (int e = 0; e < E; ++e)
-                acc[lane + 32 * e] += a.accum_w * ((double)v[e].x * v[e].x + (double)v[e].y * v[e].y);
+                acc[t + T * e] += a.accum_w * ((double)v[e].x * v[e].x + (double)v[e].y * v[e].y);
         }
         if (store) {
-            __syncwarp();  // every lane is done reading buf
+            __syncwarp();  // every lane is done reading the slot
 #pragma unroll
-            for (int e = 0; e < E; ++e) buf[lane + 32 * e] = v[e];
+            for (int e = 0; e < E; ++e) buf[t + T * e] = v[e];
             fence_proxy_async();
             __syncwarp();
             if (lane == 0) {
-                bulk_store(a.out + (size_t)line * N, buf, (uint32_t)Cfg::LINE);
+                bulk_store(a.out + (size_t)unit * LPW * N, slot, (uint32_t)Cfg::UNIT);
                 tma_commit();
             }
         }
@@ -1496,7 +1500,7 @@ template <int N> static cudaError_t row_warp_launch(const RowArgs &a, cudaStream
         if (e != cudaSuccess) return e;
         if (per_sm < 1) per_sm = 1;
     }
-    const int nwarps = (a.nlines + Cfg::W - 1) / Cfg::W;
+    const int nwarps = (a.nlines / Cfg::LPW + Cfg::W - 1) / Cfg::W;
     int grid = nsm * per_sm < nwarps ? nsm * per_sm : nwarps;
     if (grid < 1) grid = 1;
     row_warp_kernel<N><<<grid, Cfg::THREADS, Cfg::SMEM, s>>>(a);
@@ -1581,7 +1585,9 @@ cudaError_t launch_row_pass(int ny, const RowArgs &a, cudaStream_t s, int nsm, i
                 if (a.nlines % 2 == 0 && !(((uintptr_t)a.out | (uintptr_t)a.in) & 15u))
                     return row_two_launch<HalfWarpPlan256>(a, s, nsm);
                 return row_warp_launch<256>(a, s, nsm);
-            case 384: return row_warp_launch<384>(a, s, nsm);
+            case 384:  // half-warp lines: in pairs
+                if (a.nlines % 2 == 0) return row_warp_launch<384>(a, s, nsm);
+                break;
             case 768: return row_warp_launch<768>(a, s, nsm);
             case 512:
                 if (a.nlines % 2 == 0 && !(((uintptr_t)a.out | (uintptr_t)a.in) & 15u))
