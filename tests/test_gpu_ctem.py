@@ -61,6 +61,29 @@ def test_frozen_phonon_vs_oracle(ctx, fparams):
     assert O.rel_l2(img, ref_img) < 2e-5
 
 
+def test_frozen_phonon_batch_size_does_not_change_the_average():
+    """Configurations run in batches through one slice loop; a memory cap that
+    leaves room for one configuration per batch gives bit-identical averages."""
+    from multislice_gb300 import Context
+    spec = S.fcc_au(2, 2, 4)
+    args = (spec, 128, 128, 8, 3.0, 300.0, CS, DF, 2.0)
+    with Context(0) as c:
+        l0 = c.launches
+        img_b, exi_b = c.frozen_phonon(*args, nconfig=5, sigma=0.085, seed=11)
+        batched = c.launches - l0
+    with Context(0) as c:
+        # transmissions of one configuration: 1 MiB; a 4 MiB cap leaves a 2 MiB
+        # batch budget, so one configuration per batch
+        c.set_memory_limit(4 << 20)
+        l0 = c.launches
+        img_1, exi_1 = c.frozen_phonon(*args, nconfig=5, sigma=0.085, seed=11)
+        single = c.launches - l0
+        assert c.memory_in_use() <= 4 << 20
+    assert single > batched   # five slice loops instead of one
+    assert np.array_equal(img_b, img_1)
+    assert np.array_equal(exi_b, exi_1)
+
+
 def test_frozen_phonon_zero_sigma_equals_static_image(ctx):
     spec = S.fcc_au(2, 2, 4)
     img, exi = ctx.frozen_phonon(spec, 128, 128, 8, 3.0, 300.0, CS, DF, 2.0, nconfig=2, sigma=0.0, seed=1)
