@@ -374,21 +374,22 @@ __global__ void __launch_bounds__(ColTmaCfg<PL>::THREADS, MINB)
 }
 
 
-// ------------------------------- column pass, two-stage columns, 512 / 1024
-// The slice loop's column transform pair at N = 512 and 1024 built like the
-// two-stage row pass: each column is one line of T threads x 32 elements
-// (radix 16 x 32 at 512, 32 x 32 at 1024), one exchange per transform.  Tiles
-// of C columns x N rows (32 KB) arrive by TMA with a swizzle (ColLin64,
-// ColLin32) under which the natural-order reads and writes of the tile are
-// conflict-free; the exchange reuses each column's own slots in a permuted
-// order, conflict-free too.  At 512 a warp owns two columns (16 lanes each,
-// alternating) and its exchanges need only the warp; at 1024 a warp pair owns
-// two columns (16 lanes of each warp per column) and syncs on a named barrier
-// of 64 threads.  One CTA per SM runs G groups of 4 warps; each group streams
-// its own tiles through a two-slot ring of 32 KB-aligned slots (every exchange
-// address is a per-thread base xor a constant).  Group barriers per tile: the
-// arrival vote and the one before the TMA store (two more at detector
-// checkpoints).  Detector partial sums are written per 4 columns.
+// ------------------------- column pass, two-stage columns, 256 / 512 / 1024
+// The slice loop's column passes at N = 256, 512 and 1024 built like the
+// two-stage row pass: each column is one line of T threads x E elements
+// (radix 16 x 16 at 256, 16 x 32 at 512, 32 x 32 at 1024), one exchange per
+// transform.  Tiles of C columns x N rows (16 KB at 256, else 32 KB) arrive by
+// TMA with a swizzle (ColLin64, ColLin32) under which the natural-order reads
+// and writes of the tile are conflict-free; the exchange reuses each column's
+// own slots in a permuted order, conflict-free too.  At 256 and 512 a warp owns
+// two columns (16 lanes each, alternating) and its exchanges need only the
+// warp; at 1024 a warp pair owns two columns (16 lanes of each warp per column)
+// and syncs on a named barrier of 64 threads.  One CTA per SM runs G groups of
+// 4 warps; each group streams its own tiles through a two-slot ring of
+// slot-aligned buffers (every exchange address is a per-thread base xor a
+// constant).  Group barriers per tile: the arrival vote and the one before the
+// TMA store (two more at detector checkpoints).  Detector partial sums are
+// written per 4 columns.
 struct ColHalfL512 {  // 512: 8 columns, a warp per column pair
     using P = HalfWarpColPlan512;
     using Lin = ColLin64;
@@ -710,9 +711,10 @@ __global__ void __launch_bounds__(RowTmaCfg<N, TH>::THREADS, MINB)
 }
 
 
-// ------------------------------------------------ warp-per-line row pass
-// Persistent kernel in which every warp owns whole lines: it streams its lines
-// through its own three-line ring in shared memory with 1D bulk copies
+// ---------------------- warp-per-line row pass (half-warp lines at 384)
+// Persistent kernel in which every warp owns whole lines (one, or two
+// half-warp lines when the plan has 16 threads per line): it streams them
+// through its own two- or three-slot ring in shared memory with 1D bulk copies
 // (cp.async.bulk) and its own mbarriers, and the line transforms exchange
 // through that ring with warp-level synchronisation only.  No CTA-wide barrier
 // runs after the prologue, so a warp waiting on its exchange or its next line
@@ -869,7 +871,7 @@ __global__ void __launch_bounds__(RowWarpCfg<N>::THREADS, RowWarpCfg<N>::MINB) r
     }
 }
 
-// ---------------------------------------------- half-warp row pass, 512
+// ------------------------------------- two-stage row pass, 256 / 512 / 1024
 // Row pass in the two-stage layouts (HalfWarpPlan256 / 512: each warp
 // transforms two consecutive lines at a time, one per half-warp; WarpPlan1024x2:
 // one line per warp): two register stages and a single exchange per transform
