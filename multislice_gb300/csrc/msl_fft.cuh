@@ -580,7 +580,8 @@ __device__ __forceinline__ void fft_line(float2 (&v)[P::E], int t, const Addr &a
 struct HalfWarpPlan512 {
     static constexpr int N = 512, T = 16, E = 32, NSTAGE = 2;
     static constexpr int row_swz = 1, row_sh = 4, col_c = 4, col_ps = 30;
-    static constexpr bool PK = true, PKMUL = false, CW = false;
+    static constexpr bool PK = true, PKMUL = false, CW = false, GTW = false;
+    static constexpr int GTW_OFF = 0;
     static constexpr int radix(int s) { return s == 0 ? 16 : 32; }
 };
 // Two-stage plan for 256-point lines, 16 threads x 16 elements (two lines per
@@ -588,19 +589,23 @@ struct HalfWarpPlan512 {
 struct HalfWarpPlan256 {
     static constexpr int N = 256, T = 16, E = 16, NSTAGE = 2;
     static constexpr int row_swz = 1, row_sh = 4, col_c = 4, col_ps = 30;
-    static constexpr bool PK = true, PKMUL = false, CW = false;
+    static constexpr bool PK = true, PKMUL = false, CW = false, GTW = false;
+    static constexpr int GTW_OFF = 0;
     static constexpr int radix(int) { return 16; }
 };
 // Two-stage plan for 1024-point lines, one warp per line (32 threads x 32
 // elements): radix 32 then radix 32, a single exchange per transform.  The
 // exchange swizzle i ^ ((i >> 5) & 15) keeps both of its access patterns
 // (32 t + r and t + 32 e) on 16 distinct bank pairs per half-warp.
-// Its stage-1 twiddles are formed in registers from w^k (CW, fft_stage_cw), so
-// the kernel's table is two rows of 32 instead of 32 x 32 entries.
+// Its 32 x 32 stage-1 table (8 KB) would cost the row kernel a CTA per SM in
+// shared memory: it is read through L1 from the host-built twiddle buffer of
+// side 1024 (GTW, after Plan<1024>'s tables).  Measured 70 % of HBM against
+// 67 % with the powers w^r formed in registers from w^k (CW).
 struct WarpPlan1024x2 {
     static constexpr int N = 1024, T = 32, E = 32, NSTAGE = 2;
     static constexpr int row_swz = 1, row_sh = 5, col_c = 4, col_ps = 30;
-    static constexpr bool PK = true, PKMUL = false, CW = true;
+    static constexpr bool PK = true, PKMUL = false, CW = false, GTW = true;
+    static constexpr int GTW_OFF = plan_tw_size<Plan<1024>>();
     static constexpr int radix(int) { return 32; }
 };
 // The same plans for the column passes: table twiddles with packed products.

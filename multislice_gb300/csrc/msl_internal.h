@@ -85,6 +85,11 @@ struct PotArgs {
 };
 
 bool plan_supported(int n);
+// Entries the twiddle buffer of side n needs (0: the plan's own tables only) and
+// the tables appended for the two-stage row kernels, written into `tables`
+// (which holds at least that many entries).
+int row_two_twiddles_size(int n);
+void append_row_two_twiddles(int n, float2 *tables);
 // Columns per detector-partial tile of the slice loop's column pass for this
 // call's buffers: 4 for the two-stage kernels (512, 1024), the TMA-fed
 // kernel's tile width where the wave buffer allows TMA, else the register-only

@@ -46,7 +46,7 @@ namespace {
 
 constexpr int kMaxSide = MSL_NOALLOC_MAX_SIDE;
 constexpr int kMaxLayers = MSL_NOALLOC_MAX_LAYERS;
-constexpr int kMaxTw = 2304;  // largest per-plan twiddle table (side 2048), float2 entries
+constexpr int kMaxTw = 2304;  // largest per-side twiddle buffer (side 2048), float2 entries
 constexpr size_t kOffTwRow = 0;
 constexpr size_t kOffTwCol = kOffTwRow + sizeof(float2) * kMaxTw;
 constexpr size_t kOffKx2 = kOffTwCol + sizeof(float2) * kMaxTw;
@@ -54,6 +54,7 @@ constexpr size_t kOffKy2 = kOffKx2 + sizeof(float) * kMaxSide;
 constexpr size_t kOffProp = kOffKy2 + sizeof(float) * kMaxSide;
 constexpr size_t kScratchBytes = kOffProp + sizeof(float2) * (size_t)kMaxLayers * 2 * kMaxSide;
 static_assert(kScratchBytes == MSL_NOALLOC_SCRATCH_BYTES, "scratch size must match msl.h");
+static_assert(msl::WarpPlan1024x2::GTW_OFF + 32 * 32 <= kMaxTw, "the 1024 buffer holds the two-stage row table");
 static_assert(kOffTwCol % 256 == 0 && kOffKx2 % 256 == 0 && kOffProp % 256 == 0, "alignment");
 
 std::mutex g_mu;
@@ -81,7 +82,10 @@ bool twiddles_for_side(int n, float2 *out) {
         case 384: twiddles_into<384>(out); return true;
         case 512: twiddles_into<512>(out); return true;
         case 768: twiddles_into<768>(out); return true;
-        case 1024: twiddles_into<1024>(out); return true;
+        case 1024:
+            twiddles_into<1024>(out);
+            msl::append_row_two_twiddles(1024, out);  // the two-stage row kernel's table
+            return true;
         case 2048: twiddles_into<2048>(out); return true;
         default: return false;
     }

@@ -461,6 +461,7 @@ __global__ void __launch_bounds__(ColHalfCfg<L>::THREADS, 1)
         sincospif((float)(2 * (i / R0) * (i % R0)) / (float)N, &sn, &cn);  // exp(2 pi i r k / N), [r][k]
         tw[i] = make_float2(cn, sn);
     }
+    const float2 *twp = P::GTW ? a.tw + P::GTW_OFF : tw;
     if (threadIdx.x == 0) {
         for (int s = 0; s < G * NBUF; ++s) mbar_init(&barall[s], 1);
         mbar_fence_init();
@@ -887,9 +888,10 @@ template <class P_> struct RowTwoCfg {
     static constexpr int R0 = P::radix(0), R1 = P::radix(1);
     static constexpr size_t LINE = sizeof(float2) * N, SLOT = LPW * LINE;
     static constexpr uint32_t ALIGN = (uint32_t)LINE;  // each line's exchange space is line-aligned
-    // stage 1 table [r][k], k < R0: every r < R1, or rows 0 and 1 when the
-    // plan forms the powers w^r in registers (CW)
-    static constexpr int TW = (P::CW ? 2 : R1) * R0;
+    // stage 1 table [r][k], k < R0, in shared memory: every r < R1, or rows 0
+    // and 1 when the plan forms the powers w^r in registers (CW), or none when
+    // the plan reads the table from the host-built twiddle buffer (GTW)
+    static constexpr int TW = P::GTW ? 0 : (P::CW ? 2 : R1) * R0;
     static_assert(P::NSTAGE == 2 && R0 * R1 == N && (P::T == 16 || P::T == 32), "two-stage warp-owned lines");
     static constexpr size_t OFF_TW = (size_t)W * NBUF * SLOT;
     static constexpr size_t OFF_BAR = OFF_TW + sizeof(float2) * TW;
@@ -912,6 +914,7 @@ __global__ void __launch_bounds__(RowTwoCfg<P>::THREADS, RowTwoCfg<P>::MINB) row
         sincospif((float)(2 * (i / R0) * (i % R0)) / (float)N, &sn, &cn);  // exp(2 pi i r k / N), [r][k]
         tw[i] = make_float2(cn, sn);
     }
+    const float2 *twp = P::GTW ? a.tw + P::GTW_OFF : tw;
     if (lane == 0) {
         for (int s = 0; s < NBUF; ++s) mbar_init(&bar[s], 1);
         mbar_fence_init();
@@ -958,12 +961,12 @@ __global__ void __launch_bounds__(RowTwoCfg<P>::THREADS, RowTwoCfg<P>::MINB) row
 #pragma unroll
             for (int e = 0; e < E; ++e) v[e] = make_float2(1.f, 0.f);
         }
-        if (a.flags & ROW_INV) fft_line_tab<P, -1>(v, t, ad, tw);
+        if (a.flags & ROW_INV) fft_line_tab<P, -1>(v, t, ad, twp);
         if (a.flags & ROW_TRANS) {
 #pragma unroll
             for (int e = 0; e < E; ++e) v[e] = c_mul(v[e], __ldg(trow + t + T * e));
         }
-        if (a.flags & ROW_FWD) fft_line_tab<P, +1>(v, t, ad, tw);
+        if (a.flags & ROW_FWD) fft_line_tab<P, +1>(v, t, ad, twp);
         if (a.scale != 1.0f) {
 #pragma unroll
             for (int e = 0; e < E; ++e) v[e] = c_scale(v[e], a.scale);
@@ -1577,6 +1580,27 @@ void plan_twiddles(int n, std::vector<float2> &out) {
 #undef X
         default: out.clear();
     }
+    const int extra = row_two_twiddles_size(n);
+    if (extra > (int)out.size()) {
+        out.resize(extra);
+        append_row_two_twiddles(n, out.data());
+    }
+}
+
+int row_two_twiddles_size(int n) {
+    return n == WarpPlan1024x2::N && WarpPlan1024x2::GTW ? WarpPlan1024x2::GTW_OFF + 32 * 32 : 0;
+}
+
+void append_row_two_twiddles(int n, float2 *tables) {
+    if (!row_two_twiddles_size(n)) return;
+    // the two-stage 1024 row plan's stage-1 table [r][k] = exp(2 pi i r k / 1024),
+    // r, k < 32, after Plan<1024>'s own tables (read through L1 by the row kernel)
+    using P = WarpPlan1024x2;
+    for (int r = 0; r < 32; ++r)
+        for (int k = 0; k < 32; ++k) {
+            const double ph = 2.0 * 3.14159265358979323846 * (double)((r * k) % 1024) / 1024.0;
+            tables[(size_t)P::GTW_OFF + r * 32 + k] = make_float2((float)cos(ph), (float)sin(ph));
+        }
 }
 
 cudaError_t launch_row_pass(int ny, const RowArgs &a, cudaStream_t s, int nsm, int64_t *launches) {
