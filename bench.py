@@ -370,6 +370,34 @@ def run_sides(args):
             torch.cuda.empty_cache()
 
 
+def run_frozen_phonon(args):
+    """The Au 2048^2 frozen-phonon image (fcc Au 16x16x40 cells, 80 slices, 32
+    configurations, 300 kV, Cs 1.2 mm, defocus -60 nm, 25 mrad objective
+    aperture): wall time of one msl_frozen_phonon call after a warm-up call, and
+    the device time per kind (row / column passes, potentials, other)."""
+    import ctypes
+
+    from multislice_gb300 import Context, specimen as S
+
+    spec = S.fcc_au()
+    kev = 300.0
+    k_obj = float(S.mrad_to_k(25.0, kev))
+    with Context(0) as c:
+        c.frozen_phonon(spec, 2048, 2048, 80, 3.0, kev, 1.2e7, -600.0, k_obj, nconfig=2, sigma=0.085, seed=1)
+        c._lib.msl_profile_enable(c._h, 1)
+        t0 = time.perf_counter()
+        c.frozen_phonon(spec, 2048, 2048, 80, 3.0, kev, 1.2e7, -600.0, k_obj, nconfig=32, sigma=0.085, seed=2026)
+        wall = time.perf_counter() - t0
+        line = {"workload": "Au fcc 16x16x40, 2048^2, 80 slices, 32 frozen-phonon configurations, 300 kV",
+                "wall_ms": 1e3 * wall}
+        for k, name in enumerate(("row", "col", "potential", "other")):
+            n, ms = ctypes.c_int64(), ctypes.c_double()
+            c._lib.msl_profile_read(c._h, k, ctypes.byref(n), ctypes.byref(ms))
+            line[name] = {"launches": n.value, "ms": ms.value}
+        c._lib.msl_profile_enable(c._h, 0)
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -384,9 +412,13 @@ def main():
     ap.add_argument("--batch", type=int, default=0, help="probes per launch (0: library default)")
     ap.add_argument("--sides", action="store_true",
                     help="per-pass bandwidth of the slice loop at every side instead of the scan")
+    ap.add_argument("--frozen-phonon", action="store_true",
+                    help="time the Au 2048^2, 32-configuration frozen-phonon image instead of the scan")
     args = ap.parse_args()
     if args.sides:
         run_sides(args)
+    elif args.frozen_phonon:
+        run_frozen_phonon(args)
     elif args.impl == "reference":
         run_reference(args)
     else:
