@@ -257,7 +257,23 @@ def run_ours(args):
 
 
 # ------------------------------------------------------------- CPU baseline
-def cpu_baseline(cfg, nprobe, check=None, check_fp64=4):
+def cpu_prepare(cfg):
+    """Inputs of the CPU leg (not timed): the oracle's potential, transmission
+    functions, propagator, band limit and detector masks of the workload."""
+    from oracle import msl_oracle as O
+    spec = cfg["spec"]
+    nx = ny = 512
+    fp = np.load(os.path.join(ROOT, "multislice_gb300", "data", "fparams.npy"))
+    V = O.potential(spec.x, spec.y, spec.z, spec.Z, fp, spec.ax, spec.by, spec.cz, nx, ny,
+                    NSLICE, cfg["radius"])
+    return {"V": V, "T": O.transmission(V, 200.0, spec.ax, spec.by, np.complex64),
+            "props": [O.propagator_tables(nx, ny, spec.ax, spec.by, 200.0, spec.cz / NSLICE,
+                                          precision="f32")] * NSLICE,
+            "mask": O.band_mask(nx, ny, spec.ax, spec.by),
+            "dm": O.detector_masks(nx, ny, spec.ax, spec.by, cfg["det_k"])}
+
+
+def cpu_baseline(cfg, nprobe, check=None, check_fp64=4, prep=None):
     """Oracle port of the reference CPU loop on a bounded probe sample.  With
     `check` (the GPU's detector sums of the same raster) it also reports their
     relative L2 error per detector against this run and against an FP64 run of
@@ -266,14 +282,9 @@ def cpu_baseline(cfg, nprobe, check=None, check_fp64=4):
     spec = cfg["spec"]
     nx = ny = 512
     workers = os.cpu_count() or 1
-    fp = np.load(os.path.join(ROOT, "multislice_gb300", "data", "fparams.npy"))
-    # inputs (not timed): transmission functions from the oracle's potential
-    V = O.potential(spec.x, spec.y, spec.z, spec.Z, fp, spec.ax, spec.by, spec.cz, nx, ny,
-                    NSLICE, cfg["radius"])
-    T = O.transmission(V, 200.0, spec.ax, spec.by, np.complex64)
-    props = [O.propagator_tables(nx, ny, spec.ax, spec.by, 200.0, spec.cz / NSLICE, precision="f32")] * NSLICE
-    mask = O.band_mask(nx, ny, spec.ax, spec.by)
-    dm = O.detector_masks(nx, ny, spec.ax, spec.by, cfg["det_k"])
+    if prep is None:
+        prep = cpu_prepare(cfg)
+    T, props, mask, dm = prep["T"], prep["props"], prep["mask"], prep["dm"]
     xy = cfg["probe_xy"][:nprobe]
     t0 = time.perf_counter()
     P = O.probe(nx, ny, spec.ax, spec.by, 200.0, 0.0, cfg["k_ap"], 0.0, 0.0, xy, np.complex64)
@@ -287,7 +298,7 @@ def cpu_baseline(cfg, nprobe, check=None, check_fp64=4):
         # against this FP32 CPU run and against an FP64 run of the first few
         got = np.asarray(check)
         nf = min(check_fp64, nprobe)
-        T64 = O.transmission(V, 200.0, spec.ax, spec.by, np.complex128)
+        T64 = O.transmission(prep["V"], 200.0, spec.ax, spec.by, np.complex128)
         props64 = [O.propagator_tables(nx, ny, spec.ax, spec.by, 200.0, spec.cz / NSLICE, precision="f64")] * NSLICE
         P64 = O.probe(nx, ny, spec.ax, spec.by, 200.0, 0.0, cfg["k_ap"], 0.0, 0.0, xy[:nf], np.complex128)
         det64 = O.stem(T64, props64, np.arange(NSLICE), mask, P64, dm, [NSLICE - 1], workers=workers)
@@ -305,11 +316,11 @@ def run_reference(args):
     if rank != 0:
         return
     cfg = workload()
+    prep = cpu_prepare(cfg)  # the workload's inputs, built once outside the timed steps
     res = None
     times = []
     for i in range(args.warmup + args.steps):
-        t0 = time.perf_counter()
-        res = cpu_baseline(cfg, args.cpu_probes)
+        res = cpu_baseline(cfg, args.cpu_probes, prep=prep)
         if i >= args.warmup:
             times.append(res["value"])
     value = float(np.median(times))

@@ -416,10 +416,13 @@ void CreatePots_rs_DT_DW(uint32_t Ntypes, uint32_t Npoints, double dds, int32_t 
  * current; make that first call before any stream capture.  All calls share
  * the array: calls that overlap on the GPU (several host threads, several
  * streams of one device) race on it.  Errors are reported by the return code
- * only (there is no context to hold a message). */
+ * only (there is no context to hold a message); a pass kernel that gives up a
+ * bounded wait or finds its shared-memory layout wrong raises an error word
+ * kept in the same array (cleared by every call), and the call then returns
+ * MSL_E_CUDA. */
 #define MSL_NOALLOC_MAX_SIDE 2048
 #define MSL_NOALLOC_MAX_LAYERS 64
-#define MSL_NOALLOC_SCRATCH_BYTES 2150400
+#define MSL_NOALLOC_SCRATCH_BYTES 2150656
 int msl_multislice_noalloc(const msl_grid *grid, const msl_optics *optics, const float *trans,
                            int ntrans, const double *dz, const int *layer_seq, int nslice,
                            float *psi, int batch, int plane_wave, void *stream);

@@ -19,6 +19,63 @@
 using msl::ColArgs;
 using msl::RowArgs;
 
+namespace msl {
+
+// Spatial frequencies in float exactly as freqn() (slicelib.cpp:433-463).
+void freqn_f32(int n, double a, float *k, float *k2) {
+    const int imid = (int)(n / 2.0 + 0.5);
+    for (int i = 0; i < n; ++i) {
+        const float num = (float)(i > imid ? i - n : i);
+        k[i] = num / (float)a;
+        k2[i] = k[i] * k[i];
+    }
+}
+
+// Squared band limit in float as mulslice.cpp:481-489.
+float k2max_f32(int nx, int ny, double ax, double by, double bw) {
+    float k = (float)nx / (2.0F * (float)ax);
+    float t = (float)ny / (2.0F * (float)by);
+    if (t < k) k = t;
+    k = (float)bw * k;
+    return k * k;
+}
+
+// Propagator tables of one slice thickness (mulslice.cpp:494-513): px, py with
+// py already carrying the ifft scale 1/(nx ny).
+void prop_tables(int nx, int ny, const msl_optics *o, double dz, const float *kx, const float *kx2,
+                 const float *ky, const float *ky2, float2 *px, float2 *py) {
+    const float scale = 1.0f / ((float)nx * (float)ny);
+    const double lam = msl_wavelength(o->kev);
+    if (o->f32_prop_args) {
+        const float wl = (float)lam;
+        const float sc = (float)(4.0 * atan(1.0)) * (float)dz;
+        const float tctx = (float)(2.0 * tan(o->tilt_x)), tcty = (float)(2.0 * tan(o->tilt_y));
+        for (int i = 0; i < nx; ++i) {
+            const double t = sc * (kx2[i] * wl - kx[i] * tctx);
+            px[i] = make_float2((float)cos(t), (float)-sin(t));
+        }
+        for (int i = 0; i < ny; ++i) {
+            const double t = sc * (ky2[i] * wl - ky[i] * tcty);
+            py[i] = make_float2((float)cos(t) * scale, (float)-sin(t) * scale);
+        }
+        return;
+    }
+    const double pi = 3.14159265358979323846;
+    const double ttx = 2.0 * tan(o->tilt_x), tty = 2.0 * tan(o->tilt_y);
+    for (int i = 0; i < nx; ++i) {
+        const double k = kx[i];
+        const double t = pi * dz * (k * k * lam - k * ttx);
+        px[i] = make_float2((float)cos(t), (float)-sin(t));
+    }
+    for (int i = 0; i < ny; ++i) {
+        const double k = ky[i];
+        const double t = pi * dz * (k * k * lam - k * tty);
+        py[i] = make_float2((float)cos(t) * scale, (float)-sin(t) * scale);
+    }
+}
+
+}  // namespace msl
+
 namespace {
 
 const char kVersion[] = "msl 0.1 (sm_103a)";
@@ -171,61 +228,17 @@ int check_optics(msl_ctx *c, const msl_optics *o) {
     return MSL_OK;
 }
 
-// Spatial frequencies in float exactly as freqn() (slicelib.cpp:433-463).
 void freqn_f32(int n, double a, std::vector<float> &k, std::vector<float> &k2) {
     k.resize(n);
     k2.resize(n);
-    const int imid = (int)(n / 2.0 + 0.5);
-    for (int i = 0; i < n; ++i) {
-        const float num = (float)(i > imid ? i - n : i);
-        k[i] = num / (float)a;
-        k2[i] = k[i] * k[i];
-    }
+    msl::freqn_f32(n, a, k.data(), k2.data());
 }
-
-// Squared band limit in float as mulslice.cpp:481-489.
-float k2max_f32(int nx, int ny, double ax, double by, double bw) {
-    float k = (float)nx / (2.0F * (float)ax);
-    float t = (float)ny / (2.0F * (float)by);
-    if (t < k) k = t;
-    k = (float)bw * k;
-    return k * k;
-}
-
-// Propagator tables of one slice thickness (mulslice.cpp:494-513): px, py with
-// py already carrying the ifft scale 1/(nx ny).
+using msl::k2max_f32;
 void prop_tables(int nx, int ny, double ax, double by, const msl_optics *o, double dz,
                  const std::vector<float> &kx, const std::vector<float> &kx2,
                  const std::vector<float> &ky, const std::vector<float> &ky2, float2 *px,
                  float2 *py) {
-    const float scale = 1.0f / ((float)nx * (float)ny);
-    const double lam = msl_wavelength(o->kev);
-    if (o->f32_prop_args) {
-        const float wl = (float)lam;
-        const float sc = (float)(4.0 * atan(1.0)) * (float)dz;
-        const float tctx = (float)(2.0 * tan(o->tilt_x)), tcty = (float)(2.0 * tan(o->tilt_y));
-        for (int i = 0; i < nx; ++i) {
-            const double t = sc * (kx2[i] * wl - kx[i] * tctx);
-            px[i] = make_float2((float)cos(t), (float)-sin(t));
-        }
-        for (int i = 0; i < ny; ++i) {
-            const double t = sc * (ky2[i] * wl - ky[i] * tcty);
-            py[i] = make_float2((float)cos(t) * scale, (float)-sin(t) * scale);
-        }
-        return;
-    }
-    const double pi = 3.14159265358979323846;
-    const double ttx = 2.0 * tan(o->tilt_x), tty = 2.0 * tan(o->tilt_y);
-    for (int i = 0; i < nx; ++i) {
-        const double k = kx[i];
-        const double t = pi * dz * (k * k * lam - k * ttx);
-        px[i] = make_float2((float)cos(t), (float)-sin(t));
-    }
-    for (int i = 0; i < ny; ++i) {
-        const double k = ky[i];
-        const double t = pi * dz * (k * k * lam - k * tty);
-        py[i] = make_float2((float)cos(t) * scale, (float)-sin(t) * scale);
-    }
+    msl::prop_tables(nx, ny, o, dz, kx.data(), kx2.data(), ky.data(), ky2.data(), px, py);
 }
 
 float2 *twiddles(msl_ctx *c, int n) {

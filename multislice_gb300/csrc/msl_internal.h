@@ -6,7 +6,12 @@
 
 #include <vector>
 
+#include "../../include/msl.h"
+
 namespace msl {
+
+// Every grid side the line transforms are built for.
+#define MSL_FOR_EACH_SIDE(X) X(64) X(128) X(256) X(384) X(512) X(768) X(1024) X(2048)
 
 // Row pass: contiguous lines of length ny (one line = one ix of one image).
 enum RowFlags {
@@ -98,6 +103,18 @@ int plan_col_c(int n);
 int plan_col_c_launch(int n, const ColArgs &a);
 // Per-stage twiddle tables for side n (exp(+2 pi i r k / (NS R)) at [r][k]).
 void plan_twiddles(int n, std::vector<float2> &out);
+// The same tables written into out[cap]; returns the entry count, or -1 when
+// the side is not built or cap is too small (nothing is allocated).
+int plan_twiddles_into(int n, float2 *out, int cap);
+
+// Host-side slice tables shared by every entry point (no allocation):
+// spatial frequencies in float as freqn() (slicelib.cpp:433-463), the squared
+// band limit in float (mulslice.cpp:481-489), and the propagator tables of one
+// thickness (mulslice.cpp:494-513), py carrying the ifft scale 1/(nx ny).
+void freqn_f32(int n, double a, float *k, float *k2);
+float k2max_f32(int nx, int ny, double ax, double by, double bw);
+void prop_tables(int nx, int ny, const msl_optics *o, double dz, const float *kx, const float *kx2,
+                 const float *ky, const float *ky2, float2 *px, float2 *py);
 
 // Each launcher returns cudaSuccess or the launch error; *launches is bumped.
 cudaError_t launch_row_pass(int ny, const RowArgs &a, cudaStream_t s, int nsm, int64_t *launches);

@@ -14,6 +14,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <mutex>
 #include <vector>
 
 namespace {
@@ -108,10 +109,13 @@ __host__ __device__ inline double dt_rs2(const double (*tab)[8], int z, double r
     return sf * 4 * M_PI;
 }
 
+// Once per device (constant memory is per device), under a lock.
 bool dt_upload() {
+    static std::mutex mu;
     static bool done[64] = {};
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return false;
+    std::lock_guard<std::mutex> lock(mu);
     if (done[dev]) return true;
     if (cudaMemcpyToSymbol(c_dt, h_dt, sizeof(h_dt)) != cudaSuccess) return false;
     done[dev] = true;

@@ -16,15 +16,15 @@
 // cudaFree or other allocating routine is called, and no context is needed.
 //
 // Limits: nx, ny <= 2048 (every supported side) and at most 64 layers; the
-// array is 2,150,400 bytes and every GPU that loads the library holds it until
+// array is 2,150,656 bytes and every GPU that loads the library holds it until
 // the process exits.
 //
 // Sharing: every call uses the same array and leaves its tables in it.  The
-// tables are rewritten in full at the start of each call (nothing is expected
-// to start at zero), on the caller's stream, and the call waits for its stream
-// before returning; calls that overlap on the GPU -- from different host
-// threads on different streams of one device -- race on the array.  Host-side,
-// calls are serialised by a mutex.
+// tables are rewritten in full at the start of each call, on the caller's
+// stream, together with the error word the pass kernels raise (cleared to
+// zero), and the call waits for its stream before returning; calls that
+// overlap on the GPU -- from different host threads on different streams of
+// one device -- race on the array.  Host-side, calls are serialised by a mutex.
 //
 // Set-up: the first call on each device looks up the array's device address
 // with cudaGetSymbolAddress while that device is current (a host-side name of
@@ -47,49 +47,26 @@ namespace {
 constexpr int kMaxSide = MSL_NOALLOC_MAX_SIDE;
 constexpr int kMaxLayers = MSL_NOALLOC_MAX_LAYERS;
 constexpr int kMaxTw = 2304;  // largest per-side twiddle buffer (side 2048), float2 entries
-constexpr size_t kOffTwRow = 0;
+// Layout of the array: the kernels' error word, then the tables.
+constexpr size_t kOffErr = 0;
+constexpr size_t kOffTwRow = 256;
 constexpr size_t kOffTwCol = kOffTwRow + sizeof(float2) * kMaxTw;
 constexpr size_t kOffKx2 = kOffTwCol + sizeof(float2) * kMaxTw;
 constexpr size_t kOffKy2 = kOffKx2 + sizeof(float) * kMaxSide;
 constexpr size_t kOffProp = kOffKy2 + sizeof(float) * kMaxSide;
 constexpr size_t kScratchBytes = kOffProp + sizeof(float2) * (size_t)kMaxLayers * 2 * kMaxSide;
 static_assert(kScratchBytes == MSL_NOALLOC_SCRATCH_BYTES, "scratch size must match msl.h");
+// every side's twiddle buffer (with the two-stage 1024 row table appended) fits its slot
+#define X(N) static_assert(msl::plan_tw_size<msl::Plan<N>>() <= kMaxTw, "twiddle slot too small for side " #N);
+MSL_FOR_EACH_SIDE(X)
+#undef X
 static_assert(msl::WarpPlan1024x2::GTW_OFF + 32 * 32 <= kMaxTw, "the 1024 buffer holds the two-stage row table");
 static_assert(kOffTwCol % 256 == 0 && kOffKx2 % 256 == 0 && kOffProp % 256 == 0, "alignment");
 
 std::mutex g_mu;
 unsigned char *g_dev_ptr[256] = {};                                  // per device ordinal
 alignas(256) unsigned char g_host_stage[kScratchBytes];              // host copy of the tables
-
-template <int N> void twiddles_into(float2 *out) {
-    using P = msl::Plan<N>;
-    for (int s = 1; s < P::NSTAGE; ++s) {
-        const int R = P::radix(s), NS = msl::plan_span<P>(s), off = msl::plan_tw_offset<P>(s);
-        for (int r = 0; r < R; ++r)
-            for (int k = 0; k < NS; ++k) {
-                const long m = ((long)r * k) % ((long)NS * R);
-                const double ang = 2.0 * 3.14159265358979323846 * (double)m / (double)(NS * R);
-                out[off + r * NS + k] = make_float2((float)cos(ang), (float)sin(ang));
-            }
-    }
-}
-
-bool twiddles_for_side(int n, float2 *out) {
-    switch (n) {
-        case 64: twiddles_into<64>(out); return true;
-        case 128: twiddles_into<128>(out); return true;
-        case 256: twiddles_into<256>(out); return true;
-        case 384: twiddles_into<384>(out); return true;
-        case 512: twiddles_into<512>(out); return true;
-        case 768: twiddles_into<768>(out); return true;
-        case 1024:
-            twiddles_into<1024>(out);
-            msl::append_row_two_twiddles(1024, out);  // the two-stage row kernel's table
-            return true;
-        case 2048: twiddles_into<2048>(out); return true;
-        default: return false;
-    }
-}
+float g_kx[kMaxSide], g_ky[kMaxSide];                                 // float frequencies (host)
 
 bool is_dev(const void *p, int dev) {
     cudaPointerAttributes at;
@@ -143,61 +120,32 @@ extern "C" int msl_multislice_noalloc(const msl_grid *g, const msl_optics *o, co
     int nsm = 1;
     if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return MSL_E_CUDA;
 
-    // ---- tables, built on the host exactly as msl_multislice builds them
+    // ---- tables, built on the host by the same helpers msl_multislice uses
     float2 *h_twr = (float2 *)(g_host_stage + kOffTwRow), *h_twc = (float2 *)(g_host_stage + kOffTwCol);
     float *h_kx2 = (float *)(g_host_stage + kOffKx2), *h_ky2 = (float *)(g_host_stage + kOffKy2);
     float2 *h_prop = (float2 *)(g_host_stage + kOffProp);
-    if (!twiddles_for_side(ny, h_twr) || !twiddles_for_side(nx, h_twc)) return MSL_E_UNSUPPORTED;
-    static float kx[kMaxSide], ky[kMaxSide];
-    // spatial frequencies in float as freqn() (slicelib.cpp:433-463)
-    const int imx = (int)(nx / 2.0 + 0.5), imy = (int)(ny / 2.0 + 0.5);
-    for (int i = 0; i < nx; ++i) {
-        kx[i] = (float)(i > imx ? i - nx : i) / (float)g->ax;
-        h_kx2[i] = kx[i] * kx[i];
-    }
-    for (int i = 0; i < ny; ++i) {
-        ky[i] = (float)(i > imy ? i - ny : i) / (float)g->by;
-        h_ky2[i] = ky[i] * ky[i];
-    }
-    // band limit in float (mulslice.cpp:481-489)
-    float k2max = (float)nx / (2.0F * (float)g->ax);
-    const float tk = (float)ny / (2.0F * (float)g->by);
-    if (tk < k2max) k2max = tk;
-    k2max = (float)o->bandlimit * k2max;
-    k2max = k2max * k2max;
-    // propagator tables per layer (mulslice.cpp:494-513), py carrying 1/(nx ny)
-    const float scale = 1.0f / ((float)nx * (float)ny);
-    const double lam = msl_wavelength(o->kev);
+    *(int *)(g_host_stage + kOffErr) = 0;  // the error word starts every call at zero
+    if (msl::plan_twiddles_into(ny, h_twr, kMaxTw) < 0 || msl::plan_twiddles_into(nx, h_twc, kMaxTw) < 0)
+        return MSL_E_UNSUPPORTED;
+    msl::freqn_f32(nx, g->ax, g_kx, h_kx2);
+    msl::freqn_f32(ny, g->by, g_ky, h_ky2);
+    const float k2max = msl::k2max_f32(nx, ny, g->ax, g->by, o->bandlimit);
     for (int l = 0; l < ntrans; ++l) {
         float2 *px = h_prop + (size_t)l * (nx + ny), *py = px + nx;
-        if (o->f32_prop_args) {
-            const float wl = (float)lam, sc = (float)(4.0 * atan(1.0)) * (float)dz[l];
-            const float tx = (float)(2.0 * tan(o->tilt_x)), ty = (float)(2.0 * tan(o->tilt_y));
-            for (int i = 0; i < nx; ++i) {
-                const double t = sc * (h_kx2[i] * wl - kx[i] * tx);
-                px[i] = make_float2((float)cos(t), (float)-sin(t));
-            }
-            for (int i = 0; i < ny; ++i) {
-                const double t = sc * (h_ky2[i] * wl - ky[i] * ty);
-                py[i] = make_float2((float)cos(t) * scale, (float)-sin(t) * scale);
-            }
-        } else {
-            const double pi = 3.14159265358979323846;
-            const double ttx = 2.0 * tan(o->tilt_x), tty = 2.0 * tan(o->tilt_y);
-            for (int i = 0; i < nx; ++i) {
-                const double k = kx[i], t = pi * dz[l] * (k * k * lam - k * ttx);
-                px[i] = make_float2((float)cos(t), (float)-sin(t));
-            }
-            for (int i = 0; i < ny; ++i) {
-                const double k = ky[i], t = pi * dz[l] * (k * k * lam - k * tty);
-                py[i] = make_float2((float)cos(t) * scale, (float)-sin(t) * scale);
-            }
-        }
+        msl::prop_tables(nx, ny, o, dz[l], g_kx, h_kx2, g_ky, h_ky2, px, py);
     }
     // ---- into the device array (every region this call reads is rewritten)
     const size_t prop_bytes = sizeof(float2) * (size_t)ntrans * (nx + ny);
     if (cudaMemcpyAsync(d, g_host_stage, kOffProp + prop_bytes, cudaMemcpyHostToDevice, st) != cudaSuccess)
         return MSL_E_CUDA;
+    int *derr = (int *)(d + kOffErr);
+    // a failure after the upload still waits for what is queued, so no kernel of
+    // this call reads the array once the lock is released
+    auto bail = [&]() {
+        cudaStreamSynchronize(st);
+        cudaGetLastError();
+        return MSL_E_CUDA;
+    };
 
     // ---- the slice loop of msl_multislice
     const float2 *twr = (const float2 *)(d + kOffTwRow), *twc = (const float2 *)(d + kOffTwCol);
@@ -218,6 +166,7 @@ extern "C" int msl_multislice_noalloc(const msl_grid *g, const msl_optics *o, co
         a.tw = twr;
         a.flags = flags;
         a.scale = 1.0f;
+        a.err = derr;
         return msl::launch_row_pass(ny, a, st, nsm, &launches);
     };
     auto col = [&](int layer) {
@@ -234,6 +183,7 @@ extern "C" int msl_multislice_noalloc(const msl_grid *g, const msl_optics *o, co
         a.kx2 = kx2d;
         a.ky2 = ky2d;
         a.k2max = k2max;
+        a.err = derr;
         return msl::launch_col_pass(nx, a, st, nsm, &launches);
     };
     for (int s = 0; s < nslice; ++s) {
@@ -241,10 +191,16 @@ extern "C" int msl_multislice_noalloc(const msl_grid *g, const msl_optics *o, co
         int rf = msl::ROW_TRANS | msl::ROW_FWD;
         if (s > 0) rf |= msl::ROW_LOAD | msl::ROW_INV;
         else if (!plane_wave) rf |= msl::ROW_LOAD;
-        if (row(td + (size_t)l * n2, rf) != cudaSuccess) return MSL_E_CUDA;
-        if (col(l) != cudaSuccess) return MSL_E_CUDA;
+        if (row(td + (size_t)l * n2, rf) != cudaSuccess) return bail();
+        if (col(l) != cudaSuccess) return bail();
     }
-    if (row(nullptr, msl::ROW_LOAD | msl::ROW_INV) != cudaSuccess) return MSL_E_CUDA;
+    if (row(nullptr, msl::ROW_LOAD | msl::ROW_INV) != cudaSuccess) return bail();
+    // the error word: 1 = a pass's bounded wait gave up, 2 = a pass found its
+    // aligned slots outside its shared memory; either leaves the wave partly
+    // transformed.  A pageable copy into a host int allocates nothing.
+    int herr = 0;
+    if (cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess) return bail();
     if (cudaStreamSynchronize(st) != cudaSuccess) return MSL_E_CUDA;
+    if (herr) return MSL_E_CUDA;
     return MSL_OK;
 }

@@ -14,6 +14,7 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <mutex>
 #include <vector>
 
 #include "msl_fft.cuh"
@@ -23,6 +24,38 @@
 namespace msl {
 
 constexpr int kMaxDet = 8;
+
+// Launch set-up of one kernel, kept per device: cudaFuncSetAttribute acts on
+// the current device only, so the dynamic shared-memory limit is raised and
+// the occupancy computed once for every device that launches the kernel, and
+// a mutex makes first launches from several host threads safe.
+constexpr int kMaxDevices = 64;
+struct KernelSetup {
+    std::mutex mu;
+    int per_sm[kMaxDevices] = {};
+    // *out = resident CTAs per SM (at least 1; need_one: fail instead when none fit)
+    template <class K> cudaError_t get(K kern, int threads, size_t smem, bool need_one, int *out) {
+        int dev = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e != cudaSuccess) return e;
+        if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+        std::lock_guard<std::mutex> lock(mu);
+        if (!per_sm[dev]) {
+            e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return e;
+            int b = 0;
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, threads, smem);
+            if (e != cudaSuccess) return e;
+            if (b < 1) {
+                if (need_one) return cudaErrorInvalidConfiguration;
+                b = 1;
+            }
+            per_sm[dev] = b;
+        }
+        *out = per_sm[dev];
+        return cudaSuccess;
+    }
+};
 
 template <int N> struct RowCfg {
     using P = Plan<N>;
@@ -1002,14 +1035,11 @@ __global__ void __launch_bounds__(RowTwoCfg<P>::THREADS, RowTwoCfg<P>::MINB) row
 
 template <class P> static cudaError_t row_two_launch(const RowArgs &a, cudaStream_t s, int nsm) {
     using Cfg = RowTwoCfg<P>;
-    static int per_sm = 0;
-    if (!per_sm) {
-        cudaError_t e = cudaFuncSetAttribute(row_two_kernel<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)Cfg::SMEM);
+    static KernelSetup ks;
+    int per_sm = 0;
+    {
+        cudaError_t e = ks.get(row_two_kernel<P>, Cfg::THREADS, Cfg::SMEM, false, &per_sm);
         if (e != cudaSuccess) return e;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, row_two_kernel<P>, Cfg::THREADS, Cfg::SMEM);
-        if (e != cudaSuccess) return e;
-        if (per_sm < 1) per_sm = 1;
     }
     const int nwarps = (a.nlines / Cfg::LPW + Cfg::W - 1) / Cfg::W;
     int grid = nsm * per_sm < nwarps ? nsm * per_sm : nwarps;
@@ -1152,14 +1182,11 @@ __global__ void __launch_bounds__(RowPairCfg::THREADS, RowPairCfg::MINB) row_pai
 
 static cudaError_t row_pair_launch(const RowArgs &a, cudaStream_t s, int nsm) {
     using Cfg = RowPairCfg;
-    static int per_sm = 0;
-    if (!per_sm) {
-        cudaError_t e = cudaFuncSetAttribute(row_pair_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)Cfg::SMEM);
+    static KernelSetup ks;
+    int per_sm = 0;
+    {
+        cudaError_t e = ks.get(row_pair_kernel, Cfg::THREADS, Cfg::SMEM, true, &per_sm);
         if (e != cudaSuccess) return e;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, row_pair_kernel, Cfg::THREADS, Cfg::SMEM);
-        if (e != cudaSuccess) return e;
-        if (per_sm < 1) return cudaErrorInvalidConfiguration;
     }
     const int ncta = (a.nlines + Cfg::PAIRS - 1) / Cfg::PAIRS;
     int grid = nsm * per_sm < ncta ? nsm * per_sm : ncta;
@@ -1257,8 +1284,6 @@ __global__ void tilt_wave_kernel(int nx, int ny, const float *xpos, const float 
     out[((size_t)b * nx + ix) * ny + iy] = make_float2((float)cn, (float)sn);
 }
 
-// Self-test of the bounded waits: an mbarrier that nothing ever arrives on is
-// polled `polls` times; the wait gives up, the kernel raises *err and returns.
 // Transmission function t = exp(i sigma V) of every pixel (mulslice.cpp:414-421).
 // The phase carries FP64-grade accuracy in float-float arithmetic (FP64
 // instructions run at a small fraction of the FP32 rate on this GPU and bound
@@ -1285,6 +1310,8 @@ __global__ void transmission_phase_kernel(const float *__restrict__ v, float s_h
     }
 }
 
+// Self-test of the bounded waits: an mbarrier that nothing ever arrives on is
+// polled `polls` times; the wait gives up, the kernel raises *err and returns.
 __global__ void wait_timeout_kernel(int *err, uint32_t polls) {
     __shared__ uint64_t bar;
     if (threadIdx.x == 0) {
@@ -1308,15 +1335,11 @@ __global__ void detector_finalize_kernel(int nb, int ntile, int ndet, const doub
 
 // ----------------------------------------------------------------- dispatch
 template <int N> static cudaError_t row_launch(const RowArgs &a, cudaStream_t s, int nsm) {
-    static int blocks_per_sm = -1;
-    if (blocks_per_sm < 0) {
-        cudaError_t e = cudaFuncSetAttribute(row_pass_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)RowCfg<N>::SMEM);
+    static KernelSetup ks;
+    int blocks_per_sm = 0;
+    {
+        cudaError_t e = ks.get(row_pass_kernel<N>, RowCfg<N>::THREADS, RowCfg<N>::SMEM, false, &blocks_per_sm);
         if (e != cudaSuccess) return e;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, row_pass_kernel<N>,
-                                                          RowCfg<N>::THREADS, RowCfg<N>::SMEM);
-        if (e != cudaSuccess) return e;
-        if (blocks_per_sm < 1) blocks_per_sm = 1;
     }
     const int ngroups = (a.nlines + RowCfg<N>::LPB - 1) / RowCfg<N>::LPB;
     int grid = nsm * blocks_per_sm;
@@ -1328,15 +1351,11 @@ template <int N> static cudaError_t row_launch(const RowArgs &a, cudaStream_t s,
 }
 
 template <int N> static cudaError_t col_launch(const ColArgs &a, cudaStream_t s, int nsm) {
-    static int blocks_per_sm = -1;
-    if (blocks_per_sm < 0) {
-        cudaError_t e = cudaFuncSetAttribute(col_pass_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)ColCfg<N>::SMEM);
+    static KernelSetup ks;
+    int blocks_per_sm = 0;
+    {
+        cudaError_t e = ks.get(col_pass_kernel<N>, ColCfg<N>::THREADS, ColCfg<N>::SMEM, false, &blocks_per_sm);
         if (e != cudaSuccess) return e;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, col_pass_kernel<N>,
-                                                          ColCfg<N>::THREADS, ColCfg<N>::SMEM);
-        if (e != cudaSuccess) return e;
-        if (blocks_per_sm < 1) blocks_per_sm = 1;
     }
     const int ntiles = a.batch * (a.ny / ColCfg<N>::C);
     int grid = nsm * blocks_per_sm;
@@ -1352,20 +1371,20 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t
                                   const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
+static EncodeTiledFn lookup_encode_fn() {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+        return (EncodeTiledFn)p;
+    cudaGetLastError();
+    return nullptr;
+}
+
+// The driver entry point is process-wide; the static's initialisation is thread-safe.
 static EncodeTiledFn encode_fn() {
-    static EncodeTiledFn fn = nullptr;
-    static bool tried = false;
-    if (!tried) {
-        tried = true;
-        void *p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-                cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = (EncodeTiledFn)p;
-        else
-            cudaGetLastError();
-    }
+    static const EncodeTiledFn fn = lookup_encode_fn();
     return fn;
 }
 
@@ -1381,15 +1400,11 @@ static bool tma_eligible(const ColArgs &a) {
 template <class PL, int MINB> static cudaError_t col_tma_launch_v(const ColArgs &a, cudaStream_t s, int nsm) {
     using Cfg = ColTmaCfg<PL>;
     constexpr int N = PL::N;
-    static int per_sm = 0;
-    if (!per_sm) {
-        cudaError_t e = cudaFuncSetAttribute(col_tma_kernel<PL, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)Cfg::SMEM);
+    static KernelSetup ks;
+    int per_sm = 0;
+    {
+        cudaError_t e = ks.get(col_tma_kernel<PL, MINB>, Cfg::THREADS, Cfg::SMEM, false, &per_sm);
         if (e != cudaSuccess) return e;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, col_tma_kernel<PL, MINB>, Cfg::THREADS,
-                                                          Cfg::SMEM);
-        if (e != cudaSuccess) return e;
-        if (per_sm < 1) per_sm = 1;
     }
     CUtensorMap map;
     const cuuint64_t gdim[2] = {(cuuint64_t)a.ny, (cuuint64_t)a.batch * N};
@@ -1409,14 +1424,11 @@ template <class PL, int MINB> static cudaError_t col_tma_launch_v(const ColArgs 
 
 template <class L> static cudaError_t col_half_launch(const ColArgs &a, cudaStream_t s, int nsm) {
     using Cfg = ColHalfCfg<L>;
-    static int per_sm = 0;
-    if (!per_sm) {
-        cudaError_t e = cudaFuncSetAttribute(col_half_kernel<L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)Cfg::SMEM);
+    static KernelSetup ks;
+    int per_sm = 0;
+    {
+        cudaError_t e = ks.get(col_half_kernel<L>, Cfg::THREADS, Cfg::SMEM, true, &per_sm);
         if (e != cudaSuccess) return e;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, col_half_kernel<L>, Cfg::THREADS, Cfg::SMEM);
-        if (e != cudaSuccess) return e;
-        if (per_sm < 1) return cudaErrorInvalidConfiguration;
     }
     CUtensorMap map;
     const cuuint64_t gdim[2] = {(cuuint64_t)a.ny, (cuuint64_t)a.batch * Cfg::N};
@@ -1459,15 +1471,11 @@ static bool row_tma_eligible(const RowArgs &a) {
 template <int N, int TH, int MINB>
 static cudaError_t row_tma_launch_v(const RowArgs &a, cudaStream_t s, int nsm) {
     using Cfg = RowTmaCfg<N, TH>;
-    static int per_sm = 0;
-    if (!per_sm) {
-        cudaError_t e = cudaFuncSetAttribute(row_tma_kernel<N, TH, MINB>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::SMEM);
+    static KernelSetup ks;
+    int per_sm = 0;
+    {
+        cudaError_t e = ks.get(row_tma_kernel<N, TH, MINB>, Cfg::THREADS, Cfg::SMEM, false, &per_sm);
         if (e != cudaSuccess) return e;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, row_tma_kernel<N, TH, MINB>, Cfg::THREADS,
-                                                          Cfg::SMEM);
-        if (e != cudaSuccess) return e;
-        if (per_sm < 1) per_sm = 1;
     }
     if (a.nlines % Cfg::L) return cudaErrorInvalidValue;
     CUtensorMap map;
@@ -1496,14 +1504,11 @@ template <int N> static cudaError_t row_tma_launch(const RowArgs &a, cudaStream_
 
 template <int N> static cudaError_t row_warp_launch(const RowArgs &a, cudaStream_t s, int nsm) {
     using Cfg = RowWarpCfg<N>;
-    static int per_sm = 0;
-    if (!per_sm) {
-        cudaError_t e = cudaFuncSetAttribute(row_warp_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)Cfg::SMEM);
+    static KernelSetup ks;
+    int per_sm = 0;
+    {
+        cudaError_t e = ks.get(row_warp_kernel<N>, Cfg::THREADS, Cfg::SMEM, false, &per_sm);
         if (e != cudaSuccess) return e;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, row_warp_kernel<N>, Cfg::THREADS, Cfg::SMEM);
-        if (e != cudaSuccess) return e;
-        if (per_sm < 1) per_sm = 1;
     }
     const int nwarps = (a.nlines / Cfg::LPW + Cfg::W - 1) / Cfg::W;
     int grid = nsm * per_sm < nwarps ? nsm * per_sm : nwarps;
@@ -1519,8 +1524,6 @@ static bool row_warp_eligible(int ny, const RowArgs &a) {
     if (((uintptr_t)a.out & 15u) || ((a.flags & ROW_LOAD) && ((uintptr_t)a.in & 15u))) return false;
     return true;
 }
-
-#define MSL_FOR_EACH_SIDE(X) X(64) X(128) X(256) X(384) X(512) X(768) X(1024) X(2048)
 
 bool plan_supported(int n) {
     switch (n) {
@@ -1558,9 +1561,8 @@ int plan_col_c_launch(int n, const ColArgs &a) {
     return plan_col_c(n);
 }
 
-template <int N> static void twiddles_for(std::vector<float2> &out) {
+template <int N> static void twiddles_fill(float2 *out) {
     using P = Plan<N>;
-    out.assign(plan_tw_size<P>() > 0 ? plan_tw_size<P>() : 1, make_float2(0.f, 0.f));
     for (int s = 1; s < P::NSTAGE; ++s) {
         const int R = P::radix(s), NS = plan_span<P>(s), off = plan_tw_offset<P>(s);
         for (int r = 0; r < R; ++r)
@@ -1571,6 +1573,11 @@ template <int N> static void twiddles_for(std::vector<float2> &out) {
                 out[off + r * NS + k] = make_float2((float)cos(ang), (float)sin(ang));
             }
     }
+}
+
+template <int N> static void twiddles_for(std::vector<float2> &out) {
+    out.assign(plan_tw_size<Plan<N>>() > 0 ? plan_tw_size<Plan<N>>() : 1, make_float2(0.f, 0.f));
+    twiddles_fill<N>(out.data());
 }
 
 void plan_twiddles(int n, std::vector<float2> &out) {
@@ -1585,6 +1592,27 @@ void plan_twiddles(int n, std::vector<float2> &out) {
         out.resize(extra);
         append_row_two_twiddles(n, out.data());
     }
+}
+
+int plan_twiddles_into(int n, float2 *out, int cap) {
+    int size = 0;
+    switch (n) {
+#define X(N) case N: size = plan_tw_size<Plan<N>>() > 0 ? plan_tw_size<Plan<N>>() : 1; break;
+        MSL_FOR_EACH_SIDE(X)
+#undef X
+        default: return -1;
+    }
+    if (row_two_twiddles_size(n) > size) size = row_two_twiddles_size(n);
+    if (size > cap) return -1;
+    for (int i = 0; i < size; ++i) out[i] = make_float2(0.f, 0.f);
+    switch (n) {
+#define X(N) case N: twiddles_fill<N>(out); break;
+        MSL_FOR_EACH_SIDE(X)
+#undef X
+        default: return -1;
+    }
+    append_row_two_twiddles(n, out);
+    return size;
 }
 
 int row_two_twiddles_size(int n) {

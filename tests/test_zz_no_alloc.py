@@ -82,6 +82,34 @@ def test_noalloc_matches_allocating_entry_point_twice(golden):
         assert O.rel_l2(_to_host(psi2), ref2) < 1e-6
 
 
+@pytest.mark.parametrize("n", [1024, 2048])
+def test_noalloc_large_sides_twice(n):
+    """1024 carries the two-stage row kernel's appended twiddle table and 2048
+    fills the array's twiddle slot exactly; two calls in a row, different inputs."""
+    import torch
+
+    from multislice_gb300 import Context
+
+    lib = _abi.load()
+    torch.cuda.set_device(0)
+    rng = np.random.default_rng(n)
+    with Context(0) as ctx:
+        for call in range(2):
+            nt = 2 + call
+            t = np.exp(1j * 0.2 * rng.standard_normal((nt, n, n))).astype(np.complex64)
+            psi = (rng.standard_normal((1, n, n)) + 1j * rng.standard_normal((1, n, n))).astype(np.complex64)
+            dzs = [1.0 + 0.5 * l for l in range(nt)]
+            seq = list(range(nt)) + [0]
+            ax = 0.1 * n + call
+            t_d = _to_dev(torch, t)
+            psi_d = _to_dev(torch, psi)
+            rc = _noalloc(lib, t_d, dzs, seq, ax, ax + 1.0, 200.0, psi_d, 1, 0)
+            assert rc == _abi.MSL_OK
+            ref = ctx.multislice(t, dzs, seq, ax, ax + 1.0, 200.0, psi=psi.copy())
+            assert O.rel_l2(_to_host(psi_d), ref) < 1e-6
+            del t_d, psi_d
+
+
 def test_noalloc_refuses_requests_beyond_its_limits():
     import torch
 
