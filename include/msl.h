@@ -261,6 +261,26 @@ int msl_frozen_phonon(msl_ctx *ctx, const msl_atoms *atoms, const double *fparam
                       const msl_lens *lens, int nconfig, double sigma, uint64_t seed,
                       double *image, double *exit_intensity);
 
+/* Frozen-phonon STEM (the thermal-vibration loop wrapped around every probe
+ * position: MSProjectUseOnce.cs:235-273, jitter MSUseOnceCalculator.cs:179-199
+ * with MusliRandom.Vobble, MusliRandom.cs:43-55).  For each of nconfig
+ * configurations the atoms are displaced (msl_phonon_displacements with seed
+ * and sigma), the potential and transmission functions of nslice equal slices
+ * are built, and every probe of probe_xy runs the slice loop with detection at
+ * the checkpoints as msl_stem_scan does.  det_out[nprobe][ncheck][ndet]
+ * receives the detector sums added over the configurations, as the reference
+ * adds each configuration into its STEM image (MSProject.cs:836-837; divide
+ * by nconfig for the average).  Configurations x probes run together as one
+ * batch of waves through one slice loop, each wave reading its own
+ * configuration's transmission rows; each probe's sums are added in
+ * configuration order in FP64, so the result does not depend on the batch
+ * sizes (msl_set_probe_batch, memory cap). */
+int msl_stem_scan_phonon(msl_ctx *ctx, const msl_atoms *atoms, const double *fparams,
+                         const msl_grid *grid, int nslice, double radius, const msl_optics *optics,
+                         const msl_probe *probe, const double *probe_xy, int nprobe,
+                         const msl_detectors *det, const int *checkpoints, int ncheck, int nconfig,
+                         double sigma, uint64_t seed, double *det_out);
+
 /* ------------------------------------------------------- uneven batches */
 
 #define MSL_PLANE_WAVE 0

@@ -24,7 +24,7 @@ EXPORTS = (
     "msl_set_probe_batch", "msl_profile_enable", "msl_profile_read", "msl_multislice_noalloc",
     "msl_ctem_image", "msl_phonon_displacements", "msl_frozen_phonon", "msl_coo_parse",
     "msl_run_jobs", "msl_ctem_partial_coherence", "msl_check_wait_timeout", "msl_set_memory_limit",
-    "msl_memory_in_use",
+    "msl_memory_in_use", "msl_stem_scan_phonon",
 )
 PLANE_WAVE, PROBE = 0, 1
 # Muslib-shaped exports (reference names, no msl_ prefix)
@@ -132,6 +132,10 @@ def load(path=LIB_PATH):
         "msl_frozen_phonon": (c_int, [P, POINTER(Atoms), P, POINTER(Grid), c_int, c_double,
                                       POINTER(Optics), POINTER(Lens), c_int, c_double,
                                       ctypes.c_uint64, P, P]),
+        "msl_stem_scan_phonon": (c_int, [P, POINTER(Atoms), P, POINTER(Grid), c_int, c_double,
+                                         POINTER(Optics), POINTER(Probe), P, c_int,
+                                         POINTER(Detectors), P, c_int, c_int, c_double,
+                                         ctypes.c_uint64, P]),
     }
     U = ctypes.c_uint32
     for kind, src, coord, wrap in _RS_FORMS:

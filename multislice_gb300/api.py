@@ -270,6 +270,38 @@ class Context:
                                                 None if ex is None else _ptr(ex, np.float64)))
         return img, ex
 
+    def stem_scan_phonon(self, spec, nx, ny, nslice, radius, kev, k_ap, probe_xy, det_k,
+                         nconfig, sigma, seed, checkpoints=None, df=0.0, cs=0.0, k_ap_in=0.0,
+                         fparams=None, bandlimit=2.0 / 3.0, out=None):
+        """Frozen-phonon STEM: detector sums added over nconfig configurations,
+        float64 [nprobe, ncheck, ndet] (msl_stem_scan_phonon)."""
+        fp = np.ascontiguousarray(fparams_table() if fparams is None else fparams, np.float64)
+        x = np.ascontiguousarray(spec.x, np.float64)
+        y = np.ascontiguousarray(spec.y, np.float64)
+        z = np.ascontiguousarray(spec.z, np.float64)
+        Z = np.ascontiguousarray(spec.Z, np.int32)
+        at = Atoms(len(x), x.ctypes.data, y.ctypes.data, z.ctypes.data, Z.ctypes.data, float(spec.cz))
+        g = Grid(int(nx), int(ny), float(spec.ax), float(spec.by))
+        o = self._optics(kev, bandlimit)
+        if checkpoints is None:
+            checkpoints = [nslice - 1]
+        cps = np.ascontiguousarray(checkpoints, np.int32)
+        xy = np.ascontiguousarray(probe_xy, np.float64).reshape(-1, 2)
+        det = np.asarray(det_k, np.float64).reshape(-1, 2)
+        kin = np.ascontiguousarray(det[:, 0])
+        kout = np.ascontiguousarray(det[:, 1])
+        dets = Detectors(len(det), kin.ctypes.data, kout.ctypes.data)
+        pr = Probe(float(k_ap_in), float(k_ap), float(df), float(cs))
+        if out is None:
+            out = np.empty((len(xy), len(cps), len(det)), np.float64)
+        self._check(self._lib.msl_stem_scan_phonon(self._h, ctypes.byref(at), _ptr(fp, np.float64),
+                                                   ctypes.byref(g), int(nslice), float(radius),
+                                                   ctypes.byref(o), ctypes.byref(pr), _ptr(xy, np.float64),
+                                                   len(xy), ctypes.byref(dets), _ptr(cps, np.int32),
+                                                   len(cps), int(nconfig), float(sigma), int(seed),
+                                                   _ptr(out, np.float64)))
+        return out
+
     # ---------------------------------------------------------- uneven jobs
     def run_jobs(self, jobs, bandlimit=2.0 / 3.0):
         """Run many independent slice loops at once (msl_run_jobs).

@@ -1505,4 +1505,185 @@ int msl_stem_scan(msl_ctx *c, const msl_grid *g, const msl_optics *o, const floa
     return MSL_OK;
 }
 
+int msl_stem_scan_phonon(msl_ctx *c, const msl_atoms *at, const double *fparams, const msl_grid *g,
+                         int nslice, double radius, const msl_optics *o, const msl_probe *pr,
+                         const double *probe_xy, int nprobe, const msl_detectors *det,
+                         const int *checkpoints, int ncheck, int nconfig, double sigma, uint64_t seed,
+                         double *det_out) {
+    if (!c) return MSL_E_ARG;
+    int rc = check_grid(c, g);
+    if (rc) return rc;
+    if ((rc = check_optics(c, o))) return rc;
+    if (!at || !fparams || !pr || !probe_xy || !det || !checkpoints || !det_out)
+        return fail(c, MSL_E_ARG, "null argument");
+    if (nconfig < 1 || !(sigma >= 0) || !is_fin(sigma) || nslice < 1 || nprobe < 1)
+        return fail(c, MSL_E_ARG, "nconfig >= 1, sigma >= 0, nslice >= 1 and nprobe >= 1 are required");
+    if (!(at->cz > 0) || !is_fin(at->cz)) return fail(c, MSL_E_ARG, "thickness cz must be positive");
+    if (det->ndet < 1 || det->ndet > MSL_MAX_DETECTORS || !det->k_in || !det->k_out)
+        return fail(c, MSL_E_ARG, "1..8 detectors with k_in/k_out arrays are required");
+    for (int d = 0; d < det->ndet; ++d)
+        if (!(det->k_in[d] >= 0) || !(det->k_out[d] >= det->k_in[d]) || !is_fin(det->k_out[d]))
+            return fail(c, MSL_E_ARG, "detector bounds must satisfy 0 <= k_in <= k_out");
+    if (!(pr->k_in >= 0) || !(pr->k_out > pr->k_in) || !is_fin(pr->k_out) || !is_fin(pr->df) ||
+        !is_fin(pr->cs))
+        return fail(c, MSL_E_ARG, "probe aperture must satisfy 0 <= k_in < k_out; df, cs finite");
+    if (ncheck < 1) return fail(c, MSL_E_ARG, "ncheck must be >= 1");
+    for (int i = 0; i < ncheck; ++i)
+        if (checkpoints[i] < 0 || checkpoints[i] >= nslice || (i > 0 && checkpoints[i] <= checkpoints[i - 1]))
+            return fail(c, MSL_E_ARG, "checkpoints must be ascending slice indices in [0, nslice)");
+    for (int p = 0; p < 2 * nprobe; ++p)
+        if (!is_fin(probe_xy[p])) return fail(c, MSL_E_ARG, "probe positions must be finite");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    const int nx = g->nx, ny = g->ny, ndet = det->ndet, na = at->natom;
+    const size_t n2 = (size_t)nx * ny;
+
+    // configurations per batch: as many transmission stacks as 16 GiB hold (half
+    // the context's cap when one is set); probes per launch then share the wave
+    // budget (8 GiB, or a quarter of the cap) with them: images = configs x probes
+    const size_t slab = sizeof(float2) * n2 * nslice;
+    size_t tbudget = (size_t)16 << 30, wbudget = (size_t)8 << 30;
+    if (c->mem.limit && c->mem.limit / 2 < tbudget) tbudget = c->mem.limit / 2;
+    if (c->mem.limit && c->mem.limit / 4 < wbudget) wbudget = c->mem.limit / 4;
+    const int BC = (int)std::max<size_t>(1, std::min<size_t>((size_t)nconfig, tbudget / slab));
+    int BP = c->probe_batch > 0 ? c->probe_batch
+                                : (int)std::max<size_t>(1, wbudget / (sizeof(float2) * n2 * BC));
+    if (BP > nprobe) BP = nprobe;
+    const int BI = BC * BP;  // images per launch at most
+    DevBuf vbuf, tbuf, pbuf;
+    vbuf.mb = tbuf.mb = pbuf.mb = &c->mem;
+    CUDA_TRY(c, vbuf.ensure(sizeof(float) * n2 * nslice));
+    CUDA_TRY(c, tbuf.ensure(slab * BC));
+    CUDA_TRY(c, pbuf.ensure(sizeof(float2 *) * (size_t)nslice * BI));
+
+    std::vector<double> dz(nslice, at->cz / nslice);
+    CUDA_TRY(c, c->wave.ensure(sizeof(float2) * n2 * BI));
+    CUDA_TRY(c, c->exy.ensure(sizeof(float2) * (size_t)BI * (nx + ny) + sizeof(double) * 2 * BI));
+    const size_t obytes = sizeof(double) * (size_t)nprobe * ncheck * ndet;
+    const bool odev = on_device(det_out);
+    double *od;
+    if (odev) {
+        od = det_out;
+    } else {
+        CUDA_TRY(c, c->detout.ensure(obytes));
+        od = (double *)c->detout.p;
+    }
+    CUDA_TRY(c, cudaMemsetAsync(od, 0, obytes, c->stream));  // sums over configurations start at 0
+    float2 *w = (float2 *)c->wave.p;
+    float2 *ex = (float2 *)c->exy.p, *ey = ex + (size_t)BI * nx;
+    double *fxy = (double *)(ey + (size_t)BI * ny);
+    float2 *tall = (float2 *)tbuf.p;
+    const float2 **ptab = (const float2 **)pbuf.p;
+    const int last = checkpoints[ncheck - 1];
+    const double dscale = (double)n2 * (double)n2;
+    std::vector<const float2 *> hptab((size_t)nslice * BI);
+    std::vector<double> hf(2 * (size_t)BI);
+    std::vector<double> x(na), y(na), z(na), dd(3 * (size_t)na);
+    msl_atoms jat = *at;
+    jat.x = x.data();
+    jat.y = y.data();
+    jat.z = z.data();
+    if ((rc = err_reset(c))) return rc;
+    for (int c0 = 0; c0 < nconfig; c0 += BC) {
+        const int nc = std::min(BC, nconfig - c0);
+        // this batch's configurations: displaced atoms -> potential -> transmission stack
+        for (int j = 0; j < nc; ++j) {
+            msl_phonon_displacements(seed, c0 + j, na, sigma, dd.data());
+            for (int i = 0; i < na; ++i) {
+                x[i] = at->x[i] + dd[3 * i];
+                y[i] = at->y[i] + dd[3 * i + 1];
+                z[i] = at->z[i] + dd[3 * i + 2];
+            }
+            if ((rc = msl_potential_build(c, &jat, fparams, g, nslice, radius, (float *)vbuf.p))) return rc;
+            if ((rc = msl_transmission_build(c, g, o, (const float *)vbuf.p, nslice,
+                                             (float *)(tall + slab / sizeof(float2) * j))))
+                return rc;
+        }
+        if ((rc = err_reset(c))) return rc;  // the builders above check and clear the flag themselves
+        // the builders above reuse the context's table buffers, so this batch's
+        // slice tables, probe and detector tables are built after them
+        SliceTables st;
+        if ((rc = build_slice_tables(c, g, o, 1, dz.data(), st))) return rc;
+        float2 *twr = twiddles(c, ny), *twc = twiddles(c, nx);
+        if (!twr || !twc) return fail(c, MSL_E_NOMEM, "twiddle table allocation failed");
+        std::vector<double> hk(nx + ny + 2 * ndet);
+        for (int i = 0; i < nx; ++i) hk[i] = (double)(i < nx / 2 ? i : i - nx) / g->ax;
+        for (int i = 0; i < ny; ++i) hk[nx + i] = (double)(i < ny / 2 ? i : i - ny) / g->by;
+        for (int d = 0; d < ndet; ++d) {
+            hk[nx + ny + d] = det->k_in[d] * det->k_in[d];
+            hk[nx + ny + ndet + d] = det->k_out[d] * det->k_out[d];
+        }
+        if ((rc = upload(c, c->fxy, hk.data(), sizeof(double) * hk.size()))) return rc;
+        const double *kxd = (const double *)c->fxy.p, *kyd = kxd + nx;
+        CUDA_TRY(c, c->apchi.ensure(sizeof(float2) * n2 + n2));
+        float2 *apchi = (float2 *)c->apchi.p;
+        uint8_t *mask = (uint8_t *)(apchi + n2);
+        const double lam = msl_wavelength(o->kev);
+        LAUNCH_TRY(c, timed(c, MSL_PROF_OTHER, [&] { return msl::launch_probe_table(nx, ny, kxd, kyd, pr->k_in * pr->k_in, pr->k_out * pr->k_out,
+                                              lam, pr->df, pr->cs, 1.0 / ((double)nx * ny), apchi,
+                                              c->stream, &c->launches); }));
+        LAUNCH_TRY(c, timed(c, MSL_PROF_OTHER, [&] { return msl::launch_detector_mask(nx, ny, kxd, kyd, ndet, kyd + ny, kyd + ny + ndet, mask,
+                                                c->stream, &c->launches); }));
+        int ntile;
+        {
+            ColArgs probe_cfg = col_args(g, st, twc, 0, w, 1, msl::COL_LOAD | msl::COL_STORE, c->dflag);
+            ntile = ny / msl::plan_col_c_launch(nx, probe_cfg);
+        }
+        CUDA_TRY(c, c->partial.ensure(sizeof(double) * (size_t)ncheck * BI * ntile * ndet));
+        double *partial = (double *)c->partial.p;
+        for (int p0 = 0; p0 < nprobe; p0 += BP) {
+            const int np_ = std::min(BP, nprobe - p0), nb = nc * np_;
+            // image b = j * np_ + p: configuration c0 + j, probe p0 + p
+            for (int j = 0; j < nc; ++j)
+                for (int p = 0; p < np_; ++p) {
+                    const int b = j * np_ + p;
+                    hf[2 * b] = probe_xy[2 * (p0 + p)] / g->ax;
+                    hf[2 * b + 1] = probe_xy[2 * (p0 + p) + 1] / g->by;
+                    for (int s = 0; s < nslice; ++s)
+                        hptab[(size_t)s * nb + b] = tall + slab / sizeof(float2) * j + n2 * s;
+                }
+            // the stream is idle here (synchronized after the previous block), so the
+            // host tables can be reused
+            CUDA_TRY(c, cudaMemcpyAsync(fxy, hf.data(), sizeof(double) * 2 * nb, cudaMemcpyHostToDevice, c->stream));
+            CUDA_TRY(c, cudaMemcpyAsync(ptab, hptab.data(), sizeof(float2 *) * (size_t)nslice * nb,
+                                        cudaMemcpyHostToDevice, c->stream));
+            LAUNCH_TRY(c, timed(c, MSL_PROF_OTHER, [&] { return msl::launch_probe_shifts(nx, ny, nb, fxy, ex, ey, c->stream, &c->launches); }));
+            ColArgs pa = col_args(g, st, twc, 0, w, nb, msl::COL_PROBE | msl::COL_INV | msl::COL_STORE, c->dflag);
+            pa.apchi = apchi;
+            pa.ex = ex;
+            pa.ey = ey;
+            LAUNCH_TRY(c, timed(c, MSL_PROF_COL, [&] { return msl::launch_col_pass(nx, pa, c->stream, c->nsm, &c->launches); }));
+            int ic = 0;
+            for (int s = 0; s <= last; ++s) {
+                RowArgs r = row_args(g, twr, nullptr, w, nb, msl::ROW_LOAD | msl::ROW_INV | msl::ROW_TRANS | msl::ROW_FWD, c->dflag);
+                r.trans_b = ptab + (size_t)s * nb;
+                LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_row_pass(ny, r, c->stream, c->nsm, &c->launches); }));
+                const bool detect = checkpoints[ic] == s;
+                int cf = msl::COL_LOAD | msl::COL_FWD | msl::COL_PROP;
+                if (detect) cf |= msl::COL_DETECT;
+                if (s < last) cf |= msl::COL_INV | msl::COL_STORE;
+                ColArgs ca = col_args(g, st, twc, 0, w, nb, cf, c->dflag);
+                ca.detmask = mask;
+                ca.ndet = ndet;
+                ca.partial = partial + (size_t)ic * BI * ntile * ndet;
+                LAUNCH_TRY(c, timed(c, MSL_PROF_COL, [&] { return msl::launch_col_pass(nx, ca, c->stream, c->nsm, &c->launches); }));
+                if (detect) {
+                    // += each configuration's sums in configuration order: the result
+                    // does not depend on how configurations or probes were batched
+                    LAUNCH_TRY(c, timed(c, MSL_PROF_OTHER, [&] { return msl::launch_detector_accumulate(
+                                      nc, np_, ntile, ndet, ca.partial, dscale,
+                                      od + ((size_t)p0 * ncheck + ic) * ndet, ncheck * ndet, c->stream,
+                                      &c->launches); }));
+                    ++ic;
+                }
+            }
+            CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+            collect_profile(c);
+            if ((rc = err_check(c))) return rc;
+        }
+    }
+    if (!odev) CUDA_TRY(c, cudaMemcpyAsync(det_out, od, obytes, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    return MSL_OK;
+}
+
 }  // extern "C"

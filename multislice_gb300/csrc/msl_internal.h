@@ -149,6 +149,10 @@ cudaError_t launch_wait_timeout(int *err, uint32_t polls, cudaStream_t s, int64_
 // out[b * out_stride + d] = scale * sum_t partial[b][t][d]
 cudaError_t launch_transmission_phase(const float *v, double scale, size_t n, float2 *t, int nsm, cudaStream_t s,
                                       int64_t *launches);
+// out[p * out_stride + d] += scale * sum_t partial[j * np + p][t][d] for j = 0..nconf-1 in order
+cudaError_t launch_detector_accumulate(int nconf, int np, int ntile, int ndet, const double *partial,
+                                       double scale, double *out, int out_stride, cudaStream_t s,
+                                       int64_t *launches);
 cudaError_t launch_detector_finalize(int nb, int ntile, int ndet, const double *partial,
                                      double scale, double *out, int out_stride, cudaStream_t s,
                                      int64_t *launches);

@@ -1333,6 +1333,23 @@ __global__ void detector_finalize_kernel(int nb, int ntile, int ndet, const doub
     out[(size_t)b * out_stride + d] = s * scale;
 }
 
+// Frozen-phonon STEM: image j * np + p is configuration j of probe p; the
+// configurations' sums are added to the running total one after another.
+__global__ void detector_accumulate_kernel(int nconf, int np, int ntile, int ndet, const double *partial,
+                                           double scale, double *out, int out_stride) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= np * ndet) return;
+    const int p = i / ndet, d = i % ndet;
+    double v = out[(size_t)p * out_stride + d];
+    for (int j = 0; j < nconf; ++j) {
+        const double *q = partial + (size_t)(j * np + p) * ntile * ndet + d;
+        double s = 0.0;
+        for (int t = 0; t < ntile; ++t) s += q[(size_t)t * ndet];
+        v += s * scale;
+    }
+    out[(size_t)p * out_stride + d] = v;
+}
+
 // ----------------------------------------------------------------- dispatch
 template <int N> static cudaError_t row_launch(const RowArgs &a, cudaStream_t s, int nsm) {
     static KernelSetup ks;
@@ -1752,6 +1769,16 @@ cudaError_t launch_transmission_phase(const float *v, double scale, size_t n, fl
 cudaError_t launch_wait_timeout(int *err, uint32_t polls, cudaStream_t s, int64_t *launches) {
     ++*launches;
     wait_timeout_kernel<<<1, 64, 0, s>>>(err, polls);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_detector_accumulate(int nconf, int np, int ntile, int ndet, const double *partial,
+                                       double scale, double *out, int out_stride, cudaStream_t s,
+                                       int64_t *launches) {
+    ++*launches;
+    const int n = np * ndet;
+    detector_accumulate_kernel<<<(n + 127) / 128, 128, 0, s>>>(nconf, np, ntile, ndet, partial, scale, out,
+                                                               out_stride);
     return cudaGetLastError();
 }
 
