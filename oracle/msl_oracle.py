@@ -345,13 +345,20 @@ def ctf(nx, ny, ax, by, v0, cs, df, k_obj, dtype=np.complex128, astig=(0.0, 0.0,
     inside = k2 <= np.float32(kob * kob)
     q = k2.astype(np.float64)
     lam = wavelength(v0)
-    w = 0.5 * cs * lam * lam * q - df
+    phi = np.arctan2(ky.astype(np.float64)[None, :], kx.astype(np.float64)[:, None])
+    c = chi(q, phi, lam, cs, df, astig)
+    return np.where(inside, np.exp(-1j * c), 0).astype(dtype)
+
+
+def chi(k2, phi, lam, cs, df, astig=(0.0, 0.0, 0.0, 0.0)):
+    """Aberration phase of mulslice.cpp:613-619 at |k|^2 = k2 and azimuth phi:
+    pi lam k2 (cs lam^2 k2 / 2 - df + dfa2 sin(2(phi - dfa2phi))
+    + (2/3) dfa3 lam |k| sin(3(phi - dfa3phi)))."""
     dfa2, dfa2phi, dfa3, dfa3phi = astig
+    w = 0.5 * cs * lam * lam * k2 - df
     if dfa2 != 0.0 or dfa3 != 0.0:
-        phi = np.arctan2(ky.astype(np.float64)[None, :], kx.astype(np.float64)[:, None])
-        w = w + dfa2 * np.sin(2.0 * (phi - dfa2phi)) + 2.0 * dfa3 * lam * np.sqrt(q) * np.sin(3.0 * (phi - dfa3phi)) / 3.0
-    chi = np.pi * lam * q * w
-    return np.where(inside, np.exp(-1j * chi), 0).astype(dtype)
+        w = w + dfa2 * np.sin(2.0 * (phi - dfa2phi)) + 2.0 * dfa3 * lam * np.sqrt(k2) * np.sin(3.0 * (phi - dfa3phi)) / 3.0
+    return np.pi * lam * k2 * w
 
 
 def defocus_weights(df, df_spread, df_step):

@@ -320,6 +320,152 @@ int kref_stem(int nx, int ny, double ax, double by, double v0, int nlayer,
     return 0;
 }
 
+/* The reference's aberration function chi() (slicelib.cpp:258-323) as compiled
+ * from slicelib.cpp: p holds the aberration coefficients at the slicelib
+ * parameter indices (pCS, pDEFOCUS, pC12a, ...; Angstrom; kref_nparam() floats),
+ * (alx, aly) the angles in radians; returns w, chi = 2 pi w / lambda. */
+static const int kChiParams = 64;  // chi() reads indices up to pC56b = 56
+double kref_chi(const float *p, double alx, double aly, int multiMode)
+{
+    std::vector<float> q(p, p + kChiParams);
+    return chi(q.data(), alx, aly, multiMode);
+}
+int kref_nparam(void) { return kChiParams; }
+int kref_param_index(int which)
+{
+    switch (which) {
+        case 0: return pCS;
+        case 1: return pDEFOCUS;
+        case 2: return pC12a;
+        case 3: return pC12b;
+        case 4: return pC23a;
+        case 5: return pC23b;
+        default: return -1;
+    }
+}
+
+/* Partial-coherence CTEM image of mulslice.cpp:539-676 (its lpartl == 1 branch),
+ * restated with the same variable types (float images and angles, double chi,
+ * float defocus weights) and driven by the reference's cfpix fft / ifft and
+ * propagate: every illumination angle (qx, qy) = (iqx rx, iqy ry) with
+ * q2min <= q2 <= q2max starts a tilted plane wave (mulslice.cpp:583-590), runs the
+ * slice loop, and its spectrum is imaged through exp(-i chi) inside the
+ * objective aperture for defocus df0 + idf dfdelt, |idf| <= 2.5 sigmaf / dfdelt,
+ * weighted exp(-(idf dfdelt / sigmaf)^2 / 2); pix [nx][ny] is normalised by
+ * nillum * sum of weights.  cs_mm in mm, df0 / sigmaf / dfdelt / dfa2 / dfa3 in
+ * Angstrom, angles acmin / acmax / aobj in mrad as mulslice reads them
+ * (mulslice.cpp:233-283), dfa2phi / dfa3phi in degrees.  *nillum_out receives
+ * the angle count. */
+int kref_partial_coherence(int nx, int ny, double ax_d, double by_d, double v0_d, int nlayer,
+                           const double *vz, const double *cz, int nslice, const int *layer_seq,
+                           double cs_mm, double df0_d, double sigmaf_d, double dfdelt_d, double aobj_mrad,
+                           double acmin_mrad, double acmax_mrad, double dfa2_d, double dfa2phi_deg,
+                           double dfa3_d, double dfa3phi_deg, float *pix_out, int *nillum_out)
+{
+    KSetup S;
+    ksetup(S, nx, ny, ax_d, by_d, v0_d, nlayer, vz, cz, 0.0, 0.0);
+    const float pi = (float)(4.0 * atan(1.0));
+    const float ax = (float)ax_d, by = (float)by_d;
+    const float wavlen = S.wavlen;
+    // mulslice.cpp reads these as floats and converts the units (:233-283)
+    float Cs = (float)cs_mm * 1.0e7F;
+    float df0 = (float)df0_d, sigmaf = (float)sigmaf_d, dfdelt = (float)dfdelt_d;
+    float aobj = (float)aobj_mrad * 0.001F, acmin = (float)acmin_mrad * 0.001F,
+          acmax = (float)acmax_mrad * 0.001F;
+    float dfa2 = (float)dfa2_d, dfa3 = (float)dfa3_d;
+    float dfa2phi = (float)dfa2phi_deg * pi / 180.0F, dfa3phi = (float)dfa3phi_deg * pi / 180.0F;
+    float rx = 1.0F / ax, ry = 1.0F / by;
+    if (sigmaf <= 0.0F) { sigmaf = 0.0F; dfdelt = 1.0F; }   // one defocus value
+
+    cfpix wave, ctemp;
+    wave.resize(nx, ny);
+    wave.copyInit(S.trans[0]);
+    ctemp.resize(nx, ny);
+    ctemp.copyInit(S.trans[0]);
+    std::vector<float> pix((size_t)nx * ny, 0.0F);
+
+    float scale = 1.0F / (((float)nx) * ((float)ny));
+    int ndf = (int)((2.5F * sigmaf) / dfdelt);
+    int nacx = (int)((acmax / (wavlen * rx)) + 1.5F);
+    int nacy = (int)((acmax / (wavlen * ry)) + 1.5F);
+    float q2max = acmax / wavlen;
+    q2max = q2max * q2max;
+    float q2min = acmin / wavlen;
+    q2min = q2min * q2min;
+    float k2maxo = aobj / wavlen;
+    k2maxo = k2maxo * k2maxo;
+    double chi1 = pi * wavlen;
+    double chi2 = 0.5 * Cs * wavlen * wavlen;
+    long nillum = 0;
+    float sumdf = 0.0F;
+    for (int iqy = -nacy; iqy <= nacy; iqy++) {
+        float qy = iqy * ry;
+        float qy2 = qy * qy;
+        for (int iqx = -nacx; iqx <= nacx; iqx++) {
+            float qx = iqx * rx;
+            float q2 = qx * qx + qy2;
+            if ((q2 <= q2max) && (q2 >= q2min)) {
+                nillum += 1;
+                for (int ix = 0; ix < nx; ix++)
+                    for (int iy = 0; iy < ny; iy++) {
+                        double t = 2.0 * pi * (qx * S.xpos[ix] + qy * S.ypos[iy]);
+                        wave.re(ix, iy) = (float)cos(t);
+                        wave.im(ix, iy) = (float)sin(t);
+                    }
+                for (int islice = 0; islice < nslice; islice++) {
+                    int l = layer_seq[islice];
+                    wave *= S.trans[l];
+                    wave.fft();
+                    propagate(wave, S.pxr[l].data(), S.pxi[l].data(), S.pyr[l].data(), S.pyi[l].data(),
+                              S.kx2.data(), S.ky2.data(), S.k2max, nx, ny);
+                    wave.ifft();
+                }
+                wave.fft();
+                sumdf = 0.0F;
+                for (int idf = -ndf; idf <= ndf; idf++) {
+                    float df = df0 + idf * dfdelt;
+                    for (int ix = 0; ix < nx; ix++)
+                        for (int iy = 0; iy < ny; iy++) {
+                            float k2 = S.kx2[ix] + S.ky2[iy];
+                            if (k2 <= k2maxo) {
+                                double phi = atan2(S.ky[iy], S.kx[ix]);
+                                double chi = chi1 * k2 * (chi2 * k2 - df + dfa2 * sin(2.0 * (phi - dfa2phi)) +
+                                                          2.0F * dfa3 * wavlen * sqrt(k2) *
+                                                              sin(3.0 * (phi - dfa3phi)) / 3.0);
+                                float tr = (float)cos(chi);
+                                float ti = (float)-sin(chi);
+                                float wr = wave.re(ix, iy);
+                                float wi = wave.im(ix, iy);
+                                ctemp.re(ix, iy) = wr * tr - wi * ti;
+                                ctemp.im(ix, iy) = wr * ti + wi * tr;
+                            } else {
+                                ctemp.re(ix, iy) = 0.0F;
+                                ctemp.im(ix, iy) = 0.0F;
+                            }
+                        }
+                    ctemp.ifft();
+                    float pdf = 1.0F;
+                    if (sigmaf > 0.0F) {
+                        double xdf = (double)((df - df0) / sigmaf);
+                        pdf = (float)exp(-0.5F * xdf * xdf);
+                    }
+                    sumdf += pdf;
+                    for (int ix = 0; ix < nx; ix++)
+                        for (int iy = 0; iy < ny; iy++) {
+                            float x = ctemp.re(ix, iy), y = ctemp.im(ix, iy);
+                            pix[(size_t)ix * ny + iy] += pdf * (x * x + y * y);
+                        }
+                }
+            }
+        }
+    }
+    scale = 1.0F / (((float)nillum) * sumdf);
+    for (size_t i = 0; i < pix.size(); i++) pix_out[i] = pix[i] * scale;
+    if (nillum_out) *nillum_out = (int)nillum;
+    kfree(S);
+    return 0;
+}
+
 // floatTIFF round trip: the reference's own reader and writer of Kirkland's
 // TIFF files (floatTIFF.cpp:324-350, :1263-1840).  data is [ny][nx] (row iy,
 // column ix); params holds PMAX = 512 floats.

@@ -142,3 +142,40 @@ def test_partial_coherence_single_angle_equals_coherent_image(ctx, golden):
                                df_step=15.0)
     assert na == 1
     assert O.rel_l2(img, ref) < 1e-6
+
+
+# ------------------------------------------- against the compiled reference's images
+# tests/golden/ctem_partial.npz: mulslice.cpp:539-676 (partial coherence, defocus
+# spread, objective aperture, 2- and 3-fold astigmatism) driven by the reference's
+# own cfpix transforms and propagate() (tests/golden/make_ctem_golden.py).
+
+def _lens(G, ci, lam):
+    acmin, acmax, cs, df0, sigf, dfd, aobj, dfa2, dfa2p, dfa3, dfa3p = G["cases"][ci]
+    return dict(acmin=acmin * 1e-3, acmax=acmax * 1e-3, cs=cs * 1e7, df=df0, df_spread=sigf, df_step=dfd,
+                k_obj=float(np.float32(aobj * 1e-3) / np.float32(lam)),
+                astig=(dfa2, np.radians(dfa2p), dfa3, np.radians(dfa3p)))
+
+
+@pytest.mark.parametrize("ci", [0, 1, 2])
+def test_partial_coherence_vs_compiled_reference(ctx, golden, ci):
+    G = golden("ctem_partial.npz")
+    S = golden("si_small.npz")
+    ax, by, dz, kev = float(S["ax"]), float(S["by"]), float(S["dz"]), float(S["kev"])
+    L = _lens(G, ci, float(np.float32(O.wavelength(kev))))
+    img, nang = ctx.partial_coherence(S["t"], dz, S["seq"], ax, by, kev, L["cs"], L["df"], L["k_obj"],
+                                      L["acmin"], L["acmax"], df_spread=L["df_spread"], df_step=L["df_step"],
+                                      astig=L["astig"])
+    assert nang == int(G[f"pc_{ci}_nillum"])
+    assert O.rel_l2(img, G[f"pc_{ci}_pix"]) < 2e-5
+
+
+@pytest.mark.parametrize("ci", [1, 2])
+def test_ctem_image_vs_compiled_reference(ctx, golden, ci):
+    """One illumination angle: msl_ctem_image's lens with the reference's image."""
+    G = golden("ctem_partial.npz")
+    S = golden("si_small.npz")
+    ax, by, dz, kev = float(S["ax"]), float(S["by"]), float(S["dz"]), float(S["kev"])
+    L = _lens(G, ci, float(np.float32(O.wavelength(kev))))
+    img, _, _ = ctx.ctem_image(S["t"], dz, S["seq"], ax, by, kev, L["cs"], L["df"], L["k_obj"],
+                               df_spread=L["df_spread"], df_step=L["df_step"], astig=L["astig"])
+    assert O.rel_l2(img, G[f"pc_{ci}_pix"]) < 2e-5

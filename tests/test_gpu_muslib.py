@@ -209,3 +209,115 @@ def test_reciprocal_space_potential(form, gam, mult, band):
     for _ in range(rows):
         ref_p = np.float32(np.float64(ref_p) + 200.0 / M)
     assert cpro.value == ref_p
+
+
+# --------------------------------------- against the compiled reference's outputs
+# tests/golden/muslib.npz: every export of the reference's Muslib compiled
+# unchanged and run on seeded inputs (tests/golden/make_muslib_golden.py).
+
+GAMS = (np.pi / 2, 1.8)
+
+
+@pytest.mark.parametrize("name", _abi.MUSLIB_RS)
+@pytest.mark.parametrize("gi", [0, 1])
+def test_real_space_forms_vs_compiled_reference(golden, name, gi):
+    import torch  # noqa: F401
+    lib = _abi.load()
+    G = golden("muslib.npz")
+    kind, _, src, coord, _ = name.split("_")
+    pre = f"rsin_{src}_{coord}_"
+    a, b, E, atrad, N, M = G[pre + "scalars"]
+    N, M = int(N), int(M)
+    I = {k: np.ascontiguousarray(G[pre + k]) for k in ("xx", "yy", "ads", "occ", "dw", "typ", "curves")}
+    gli = np.zeros((M, N, 2))
+    if kind == "PG":
+        gli[..., 0] = 1.0
+    cpro = ctypes.c_float(0)
+    head = (a, b, GAMS[gi], E, atrad) if kind == "PG" else (a, b, GAMS[gi], atrad)
+    common = (N, M, len(I["xx"]), _p(I["xx"]), _p(I["yy"]))
+    if src == "curve":
+        tail = (_p(I["ads"]), _p(I["occ"]), _p(I["typ"]), _p(I["curves"]), I["curves"].shape[1], 0.01,
+                _p(gli), ctypes.byref(cpro))
+    elif coord == "DW":
+        tail = (_p(I["dw"]), _p(I["ads"]), _p(I["occ"]), _p(I["typ"]), _p(gli), ctypes.byref(cpro))
+    else:
+        tail = (_p(I["ads"]), _p(I["occ"]), _p(I["typ"]), _p(gli), ctypes.byref(cpro))
+    assert getattr(lib, name)(*head, *common, *tail) == 0
+    ref = G[f"rs_{name}_{gi}_gli"]
+    assert O.rel_l2(gli[..., 0] + 1j * gli[..., 1], ref[..., 0] + 1j * ref[..., 1]) < 1e-12
+    assert cpro.value == float(G[f"rs_{name}_{gi}_cpro"])
+
+
+@pytest.mark.parametrize("gi", [0, 1])
+def test_propagator_vs_compiled_reference(golden, gi):
+    import torch  # noqa: F401
+    lib = _abi.load()
+    G = golden("muslib.npz")
+    a, b, gam, dz, E, tx, ty, N, M = G[f"prop_{gi}_args"]
+    gli = np.zeros((int(M), int(N), 2))
+    cpro = ctypes.c_float(-1)
+    assert lib.CreatePropagator(a, b, gam, dz, E, tx, ty, int(N), int(M), _p(gli), ctypes.byref(cpro)) == 0
+    np.testing.assert_allclose(gli, G[f"prop_{gi}_gli"], atol=1e-12)
+    assert cpro.value == float(G[f"prop_{gi}_cpro"])
+
+
+def test_one_atom_vs_compiled_reference(golden):
+    import torch  # noqa: F401
+    lib = _abi.load()
+    G = golden("muslib.npz")
+    cur = np.ascontiguousarray(G["oneatom_curve"])
+    gli = np.zeros((40, 48, 2))
+    gli[..., 0] = 1.0
+    assert lib.PG_rs_curve_DW_cutpot_oneatom(8.0, 8.0, 1.9, 0.025, 1.0, 48, 40, 0.3, 0.7, 0.04, 0.9, _p(cur),
+                                             500, 0.01, _p(gli)) == 0
+    ref = G["oneatom_gli"]
+    assert O.rel_l2(gli[..., 0] + 1j * gli[..., 1], ref[..., 0] + 1j * ref[..., 1]) < 1e-12
+
+
+@pytest.mark.parametrize("ci", [0, 1, 2])
+@pytest.mark.parametrize("form", ["DT", "curve"])
+def test_reciprocal_space_vs_compiled_reference(golden, ci, form):
+    import torch  # noqa: F401
+    lib = _abi.load()
+    G = golden("muslib.npz")
+    gam, Nm, Mm, SL, EL = G[f"rec_{ci}_case"]
+    Nm, Mm, SL, EL = int(Nm), int(Mm), int(SL), int(EL)
+    xx, yy = np.ascontiguousarray(G["recin_xx"]), np.ascontiguousarray(G["recin_yy"])
+    ads, occ = np.ascontiguousarray(G["recin_ads"]), np.ascontiguousarray(G["recin_occ"])
+    zs, pick, dwv = G["recin_zs"], G["recin_pick"], G["recin_dwv"]
+    na = len(xx)
+    gli = np.zeros((EL - SL, 48, 2))
+    cpro = ctypes.c_float(0)
+    if form == "DT":
+        typ = np.ascontiguousarray(zs[pick], np.int32)
+        DW = np.ascontiguousarray(dwv[pick])
+        rc = lib.Potential_rec_DT_DW(11.0, 12.0, gam, Nm, Mm, 48, 64, na, SL, EL, _p(xx), _p(yy), _p(DW),
+                                     _p(ads), _p(occ), _p(typ), _p(gli), ctypes.byref(cpro))
+    else:
+        typ = np.ascontiguousarray(pick, np.int32)
+        cur = np.ascontiguousarray(G[f"rec_{ci}_curves"])
+        rc = lib.Potential_rec_curve_DW(11.0, 12.0, gam, Nm, Mm, 48, 64, na, SL, EL, _p(xx), _p(yy), _p(ads),
+                                        _p(occ), _p(typ), _p(cur), 60, 0.02, _p(gli), ctypes.byref(cpro))
+    assert rc == 0
+    ref = G[f"rec_{ci}_{form}_gli"]
+    np.testing.assert_allclose(gli, ref, atol=1e-12 * np.abs(ref).max())
+    assert cpro.value == float(G[f"rec_{ci}_{form}_cpro"])
+
+
+def test_curves_vs_compiled_reference(golden):
+    lib = _abi.load()
+    G = golden("muslib.npz")
+    zq, sq, tab = G["scat_z"], G["scat_s"], G["scat_tab"]
+    for i, z in enumerate(zq):
+        for j, s_ in enumerate(sq):
+            assert lib.scat_ampl_rs_DT_DW(int(z), float(s_), 0.4) == pytest.approx(tab[0, i, j], rel=1e-14, abs=0)
+            assert lib.scat_ampl_rs2_DT_DW(int(z), float(s_), 0.4) == pytest.approx(tab[1, i, j], rel=1e-14, abs=0)
+            assert lib.scat_ampl_rs2_DT_DW0(int(z), float(s_)) == pytest.approx(tab[2, i, j], rel=1e-14, abs=0)
+    types, dws = np.ascontiguousarray(G["pots_types"]), np.ascontiguousarray(G["pots_dw"])
+    for vol, key in ((0.0123, "pots_rec"), (None, "pots_rs")):
+        sc = np.zeros((3, 80))
+        if vol is None:
+            lib.CreatePots_rs_DT_DW(3, 80, 0.015, _p(types), _p(dws), _p(sc))
+        else:
+            lib.CreatePots_rec_DT_DW(3, 80, 0.015, _p(types), _p(dws), vol, _p(sc))
+        np.testing.assert_allclose(sc, G[key], rtol=1e-13, atol=0)

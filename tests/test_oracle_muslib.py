@@ -150,3 +150,100 @@ def test_rec_potential_curve_band_and_symmetry():
     dt = O.muslib_rec_potential(a, b, gam, 1, 1, N, M, 0, M, xx, yy, np.zeros(na), occ,
                                 np.array([8, 38])[typ], DW=np.array([0.2, 0.4])[typ])
     assert O.rel_l2(full, dt) < 1e-4      # the tabulated curve approximates the DT form
+
+
+# ------------------------------------------------- against the compiled reference
+# tests/golden/muslib.npz holds the outputs of the reference's own Muslib sources
+# compiled unchanged (tests/golden/make_muslib_golden.py); the restatement must
+# reproduce them to rounding.
+
+RS_NAMES = [f"{k}_rs_{s}_{c}_{w}" for k in ("PG", "Potential") for s in ("curve", "DT") for c in ("DW", "TV")
+            for w in ("cutpot", "periodic")]
+GAMS = (np.pi / 2, 1.8)
+
+
+def muslib_case(G, name):
+    """Inputs of one real-space form from the fixture."""
+    _, _, src, coord, _ = name.split("_")
+    pre = f"rsin_{src}_{coord}_"
+    a, b, E, atrad, N, M = G[pre + "scalars"]
+    inp = {k: G[pre + k] for k in ("xx", "yy", "ads", "occ", "dw", "typ", "curves")}
+    return float(a), float(b), float(E), float(atrad), int(N), int(M), inp
+
+
+def restated_rs(name, gam, G):
+    kind, _, src, coord, wrap = name.split("_")
+    a, b, E, atrad, N, M, I = muslib_case(G, name)
+    A, B = O.muslib_rs_sums(a, b, gam, atrad, N, M, I["xx"], I["yy"], I["ads"], I["occ"], I["typ"],
+                            curves=I["curves"] if src == "curve" else None, dds=0.01, dw=I["dw"],
+                            source="curve" if src == "curve" else f"DT_{coord}", angstrom=coord == "TV",
+                            periodic=wrap == "periodic")
+    if kind == "PG":
+        return O.muslib_pg(A, B, E)
+    return A + 1j * B
+
+
+@pytest.mark.parametrize("name", RS_NAMES)
+@pytest.mark.parametrize("gi", [0, 1])
+def test_restatement_matches_compiled_muslib_real_space(golden, name, gi):
+    G = golden("muslib.npz")
+    ref = G[f"rs_{name}_{gi}_gli"]
+    got = restated_rs(name, GAMS[gi], G)
+    r = ref[..., 0] + 1j * ref[..., 1]
+    assert np.abs(r).max() > 0.5
+    assert O.rel_l2(got, r) < 1e-12
+
+
+@pytest.mark.parametrize("gi", [0, 1])
+def test_restatement_matches_compiled_muslib_propagator(golden, gi):
+    G = golden("muslib.npz")
+    a, b, gam, dz, E, tx, ty, N, M = G[f"prop_{gi}_args"]
+    ref = G[f"prop_{gi}_gli"]
+    got = O.muslib_propagator(a, b, gam, dz, E, tx, ty, int(N), int(M))
+    np.testing.assert_allclose(got, ref[..., 0] + 1j * ref[..., 1], atol=1e-12)
+    assert float(G[f"prop_{gi}_cpro"]) == 100.0
+
+
+@pytest.mark.parametrize("ci", [0, 1, 2])
+@pytest.mark.parametrize("form", ["DT", "curve"])
+def test_restatement_matches_compiled_muslib_reciprocal(golden, ci, form):
+    G = golden("muslib.npz")
+    gam, Nm, Mm, SL, EL = G[f"rec_{ci}_case"]
+    Nm, Mm, SL, EL = int(Nm), int(Mm), int(SL), int(EL)
+    xx, yy, ads, occ = G["recin_xx"], G["recin_yy"], G["recin_ads"], G["recin_occ"]
+    zs, pick, dwv = G["recin_zs"], G["recin_pick"], G["recin_dwv"]
+    if form == "DT":
+        got = O.muslib_rec_potential(11.0, 12.0, gam, Nm, Mm, 48, 64, SL, EL, xx, yy, ads, occ, zs[pick],
+                                     DW=dwv[pick])
+    else:
+        cur = G[f"rec_{ci}_curves"]
+        np.testing.assert_allclose(O.create_pots(zs, dwv, 60, 0.02, vol=1 / (11.0 * 12.0 * np.sin(gam))), cur,
+                                   rtol=1e-13, atol=0)
+        got = O.muslib_rec_potential(11.0, 12.0, gam, Nm, Mm, 48, 64, SL, EL, xx, yy, ads, occ,
+                                     pick.astype(np.int32), curves=cur, dds=0.02)
+    ref = G[f"rec_{ci}_{form}_gli"]
+    r = ref[..., 0] + 1j * ref[..., 1]
+    assert np.abs(r).max() > 0.1
+    np.testing.assert_allclose(got, r, atol=1e-12 * np.abs(r).max())
+
+
+def test_restatement_matches_compiled_muslib_curves(golden):
+    G = golden("muslib.npz")
+    zq, sq, tab = G["scat_z"], G["scat_s"], G["scat_tab"]
+    for i, z in enumerate(zq):
+        np.testing.assert_allclose(O.dt_rs(int(z), sq, 0.4), tab[0, i], rtol=1e-14, atol=0)
+        np.testing.assert_allclose(O.dt_rs2(int(z), sq, 0.4), tab[1, i], rtol=1e-14, atol=0)
+        np.testing.assert_allclose(O.dt_rs2(int(z), sq, 0.0), tab[2, i], rtol=1e-14, atol=0)
+    types, dws = G["pots_types"], G["pots_dw"]
+    np.testing.assert_allclose(O.create_pots(types, dws, 80, 0.015, vol=0.0123), G["pots_rec"], rtol=1e-13)
+    np.testing.assert_allclose(O.create_pots(types, dws, 80, 0.015), G["pots_rs"], rtol=1e-13)
+
+
+def test_restatement_matches_compiled_muslib_one_atom(golden):
+    G = golden("muslib.npz")
+    cur = G["oneatom_curve"]
+    A, B = O.muslib_rs_sums(8.0, 8.0, 1.9, 1.0, 48, 40, np.array([0.3]), np.array([0.7]), np.array([0.04]),
+                            np.array([0.9]), np.array([0]), curves=cur[None], dds=0.01, periodic=False,
+                            whole=True)
+    ref = G["oneatom_gli"]
+    assert O.rel_l2(O.muslib_pg(A, B, 0, K=0.025), ref[..., 0] + 1j * ref[..., 1]) < 1e-12
