@@ -95,7 +95,8 @@ def test_frozen_phonon_zero_sigma_equals_static_image(ctx):
 
 def test_frozen_phonon_au_2048_full_size(ctx):
     """fcc Au 16x16x40 cells, 2048^2, 80 slices, 32 configurations, 300 kV, Cs 1.2 mm,
-    df -60 nm: configuration averaging is deterministic and physically bounded."""
+    df -60 nm: configuration averaging is deterministic, physically bounded and,
+    on every pixel, within 1e-4 of the FP64 oracle."""
     spec = S.fcc_au()
     kev = 300.0
     k_obj = float(S.mrad_to_k(25.0, kev))
@@ -107,6 +108,16 @@ def test_frozen_phonon_au_2048_full_size(ctx):
     img2, _ = ctx.frozen_phonon(spec, 2048, 2048, 80, 3.0, kev, CS, DF, k_obj, nconfig=32,
                                 sigma=0.085, seed=2026, want_exit=False)
     assert np.array_equal(img, img2)
+    # every pixel against the FP64 oracle (torch complex128 on the same GPU), same seed
+    import torch
+
+    from oracle import fp64_gpu
+    from multislice_gb300 import fparams_table
+    ref_img, ref_exi = fp64_gpu.frozen_phonon(spec, fparams_table(), 2048, 2048, 80, 3.0, kev, CS, DF, k_obj,
+                                              32, 0.085, 2026, torch.device("cuda", 0))
+    torch.cuda.empty_cache()
+    assert O.rel_l2(exi, ref_exi) < 1e-4
+    assert O.rel_l2(img, ref_img) < 1e-4
 
 
 def test_astigmatic_image_vs_oracle(ctx, golden):

@@ -166,6 +166,36 @@ def test_stem_config2_subset_vs_reference(ctx, golden):
         assert err < 5e-5, err   # what the path holds
 
 
+def test_stem_config2_full_image_vs_fp64(ctx):
+    """The whole 64x64-probe HAADF and ABF images of the SrTiO3 512^2, 100-slice
+    scan against the FP64 oracle (torch complex128 on the same GPU, potential
+    included): the 1e-3 bar of the metric on every pixel."""
+    import torch
+
+    from multislice_gb300 import fparams_table
+    from oracle import fp64_gpu
+    cfg = S.config_srtio3_stem()
+    spec = cfg["spec"]
+    v = ctx.potential(spec, 512, 512, 100, cfg["radius"])
+    t = ctx.transmission(v, spec.ax, spec.by, 200.0)
+    d = ctx.stem_scan(t, spec.cz / 100, np.arange(100), spec.ax, spec.by, 200.0, cfg["k_ap"],
+                      cfg["probe_xy"], cfg["det_k"])
+    dev = torch.device("cuda", 0)
+    V = fp64_gpu.potential(spec.x, spec.y, spec.z, spec.Z, fparams_table(), spec.ax, spec.by, spec.cz, 512, 512,
+                           100, cfg["radius"], dev)
+    T = fp64_gpu.transmission(V, 200.0, spec.ax, spec.by)
+    del V
+    P = fp64_gpu.propagator(512, 512, spec.ax, spec.by, 200.0, spec.cz / 100, dev)
+    ref = fp64_gpu.stem_scan(T, P, np.arange(100), 512, 512, spec.ax, spec.by, 200.0, cfg["k_ap"],
+                             cfg["probe_xy"], cfg["det_k"], [99], batch=256)
+    del T
+    torch.cuda.empty_cache()
+    for k in range(2):
+        err = O.rel_l2(d[:, 0, k], ref[:, 0, k])
+        assert err < 1e-3, err   # the metric's bar
+        assert err < 1e-4, err   # what the path holds
+
+
 def test_invalid_arguments_fail_before_launch(ctx):
     t = np.ones((1, 100, 100), np.complex64)
     with pytest.raises(MslError) as e:
