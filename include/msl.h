@@ -281,6 +281,45 @@ int msl_stem_scan_phonon(msl_ctx *ctx, const msl_atoms *atoms, const double *fpa
                          const msl_detectors *det, const int *checkpoints, int ncheck, int nconfig,
                          double sigma, uint64_t seed, double *det_out);
 
+/* ------------------------------------------------------ tensor cores */
+
+/* D[M][N] (FP32) = A[M][K] * B[N][K]^T with bf16 operands (raw 16-bit
+ * patterns, row-major) on the tensor cores (tcgen05.mma, accumulator in tensor
+ * memory).  M % 128 == 0, K % 64 == 0, 16 <= N <= 256 and N % 16 == 0.  No
+ * counterpart in the reference: the contraction under the learned
+ * coarse-slice closure, exported so it can be checked on its own. */
+int msl_tc_gemm_bf16(msl_ctx *ctx, const uint16_t *A, const uint16_t *B, float *D, int M, int N, int K);
+
+/* ------------------------------------------- learned coarse-slice closure */
+
+/* A small complex-valued convolutional network that corrects an exit wave
+ * computed with 4x thicker slices toward the fine-slice result (no counterpart
+ * in the reference; the reference's fine-slice loop, mulslice.cpp:706-739, is
+ * its fallback and the judge of its error).  Six complex 3x3 convolutions with
+ * periodic boundaries -- 1 -> 32 -> 32 -> 32 -> 32 -> 32 -> 1 channels, CReLU
+ * between them -- act on the wave divided by its RMS s, and the output adds
+ * s times the result to the wave.  Parameters are FP32 master copies used as
+ * bf16; the 32 -> 32 layers run on the tensor cores (forward and input
+ * gradient), the rest on the CUDA cores; training uses Adam.  Waves are
+ * complex64 [batch][h][w] (w a multiple of 128, h >= 3), host or device. */
+typedef struct msl_closure msl_closure;
+int msl_closure_create(msl_ctx *ctx, uint64_t seed, msl_closure **out);
+int msl_closure_destroy(msl_closure *net);
+/* Number of FP32 parameters: per layer, weights [9][co][ci][2] then bias [co][2]. */
+int msl_closure_param_count(void);
+int msl_closure_get_params(msl_ctx *ctx, const msl_closure *net, float *params);
+/* Replaces the parameters and resets the optimiser state. */
+int msl_closure_set_params(msl_ctx *ctx, msl_closure *net, const float *params);
+/* psi <- psi + s * net(psi / s), in place. */
+int msl_closure_apply(msl_ctx *ctx, msl_closure *net, float *psi, int batch, int h, int w);
+/* Loss L = mean over pixels of |net(coarse / s) - (fine - coarse) / s|^2 and
+ * its gradient dL/dparams (grad may be NULL). */
+int msl_closure_gradients(msl_ctx *ctx, msl_closure *net, const float *coarse, const float *fine, int batch,
+                          int h, int w, float *grad, double *loss);
+/* One Adam step (lr; beta 0.9 / 0.999) on that loss; *loss before the step. */
+int msl_closure_train_step(msl_ctx *ctx, msl_closure *net, const float *coarse, const float *fine, int batch,
+                           int h, int w, float lr, double *loss);
+
 /* ------------------------------------------------------- uneven batches */
 
 #define MSL_PLANE_WAVE 0

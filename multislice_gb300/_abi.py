@@ -24,7 +24,9 @@ EXPORTS = (
     "msl_set_probe_batch", "msl_profile_enable", "msl_profile_read", "msl_multislice_noalloc",
     "msl_ctem_image", "msl_phonon_displacements", "msl_frozen_phonon", "msl_coo_parse",
     "msl_run_jobs", "msl_ctem_partial_coherence", "msl_check_wait_timeout", "msl_set_memory_limit",
-    "msl_memory_in_use", "msl_stem_scan_phonon",
+    "msl_memory_in_use", "msl_stem_scan_phonon", "msl_tc_gemm_bf16", "msl_closure_create",
+    "msl_closure_destroy", "msl_closure_param_count", "msl_closure_get_params", "msl_closure_set_params",
+    "msl_closure_apply", "msl_closure_gradients", "msl_closure_train_step",
 )
 PLANE_WAVE, PROBE = 0, 1
 # Muslib-shaped exports (reference names, no msl_ prefix)
@@ -132,6 +134,15 @@ def load(path=LIB_PATH):
         "msl_frozen_phonon": (c_int, [P, POINTER(Atoms), P, POINTER(Grid), c_int, c_double,
                                       POINTER(Optics), POINTER(Lens), c_int, c_double,
                                       ctypes.c_uint64, P, P]),
+        "msl_tc_gemm_bf16": (c_int, [P, P, P, P, c_int, c_int, c_int]),
+        "msl_closure_create": (c_int, [P, ctypes.c_uint64, P]),
+        "msl_closure_destroy": (c_int, [P]),
+        "msl_closure_param_count": (c_int, []),
+        "msl_closure_get_params": (c_int, [P, P, P]),
+        "msl_closure_set_params": (c_int, [P, P, P]),
+        "msl_closure_apply": (c_int, [P, P, P, c_int, c_int, c_int]),
+        "msl_closure_gradients": (c_int, [P, P, P, P, c_int, c_int, c_int, P, P]),
+        "msl_closure_train_step": (c_int, [P, P, P, P, c_int, c_int, c_int, ctypes.c_float, P]),
         "msl_stem_scan_phonon": (c_int, [P, POINTER(Atoms), P, POINTER(Grid), c_int, c_double,
                                          POINTER(Optics), POINTER(Probe), P, c_int,
                                          POINTER(Detectors), P, c_int, c_int, c_double,

@@ -389,3 +389,74 @@ def wavelength(kev):
 
 def sigma(kev):
     return _abi.load().msl_sigma(float(kev))
+
+
+class Closure:
+    """The learned coarse-slice closure (msl_closure_*): a complex 3x3
+    convolutional network correcting a coarse-slice exit wave toward the
+    fine-slice one.  Waves are complex64 [batch, h, w] (numpy, or torch device
+    tensors of shape [batch, h, w, 2] float32)."""
+
+    def __init__(self, ctx, seed=0):
+        self.ctx = ctx
+        self._lib = ctx._lib
+        h = ctypes.c_void_p()
+        ctx._check(self._lib.msl_closure_create(ctx._h, int(seed), ctypes.byref(h)))
+        self._h = h
+
+    @staticmethod
+    def param_count():
+        return int(_abi.load().msl_closure_param_count())
+
+    def close(self):
+        if self._h:
+            self._lib.msl_closure_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def get_params(self):
+        p = np.empty(self.param_count(), np.float32)
+        self.ctx._check(self._lib.msl_closure_get_params(self.ctx._h, self._h, p.ctypes.data))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        assert p.size == self.param_count()
+        self.ctx._check(self._lib.msl_closure_set_params(self.ctx._h, self._h, p.ctypes.data))
+
+    @staticmethod
+    def _wave_ptr(w):
+        if hasattr(w, "data_ptr"):
+            return ctypes.c_void_p(w.data_ptr()), tuple(w.shape[:3])
+        assert w.dtype == np.complex64 and w.flags.c_contiguous
+        return ctypes.c_void_p(w.ctypes.data), w.shape
+
+    def apply(self, psi):
+        """psi <- psi + s net(psi / s), in place; returns psi."""
+        if not hasattr(psi, "data_ptr"):
+            psi = np.ascontiguousarray(psi, np.complex64)
+        ptr, (b, h, w) = self._wave_ptr(psi)
+        self.ctx._check(self._lib.msl_closure_apply(self.ctx._h, self._h, ptr, b, h, w))
+        return psi
+
+    def gradients(self, coarse, fine):
+        pc, (b, h, w) = self._wave_ptr(coarse)
+        pf, _ = self._wave_ptr(fine)
+        g = np.empty(self.param_count(), np.float32)
+        loss = ctypes.c_double()
+        self.ctx._check(self._lib.msl_closure_gradients(self.ctx._h, self._h, pc, pf, b, h, w,
+                                                        g.ctypes.data, ctypes.byref(loss)))
+        return loss.value, g
+
+    def train_step(self, coarse, fine, lr):
+        pc, (b, h, w) = self._wave_ptr(coarse)
+        pf, _ = self._wave_ptr(fine)
+        loss = ctypes.c_double()
+        self.ctx._check(self._lib.msl_closure_train_step(self.ctx._h, self._h, pc, pf, b, h, w, float(lr),
+                                                         ctypes.byref(loss)))
+        return loss.value

@@ -1505,6 +1505,184 @@ int msl_stem_scan(msl_ctx *c, const msl_grid *g, const msl_optics *o, const floa
     return MSL_OK;
 }
 
+int msl_tc_gemm_bf16(msl_ctx *c, const uint16_t *A, const uint16_t *B, float *D, int M, int N, int K) {
+    if (!c) return MSL_E_ARG;
+    if (!A || !B || !D) return fail(c, MSL_E_ARG, "null argument");
+    if (M <= 0 || M % 128 || K <= 0 || K % 64 || N < 16 || N > 256 || N % 16)
+        return fail(c, MSL_E_ARG, "M % 128 == 0, K % 64 == 0, 16 <= N <= 256, N % 16 == 0 required");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    int rc;
+    if ((rc = err_reset(c))) return rc;
+    const uint16_t *ad, *bd;
+    if ((rc = stage_in(c, A, sizeof(uint16_t) * (size_t)M * K, c->in_stage, &ad))) return rc;
+    if ((rc = stage_in(c, B, sizeof(uint16_t) * (size_t)N * K, c->trans_stage, &bd))) return rc;
+    const bool ddev = on_device(D);
+    float *dd = D;
+    if (!ddev) {
+        CUDA_TRY(c, c->tmpw.ensure(sizeof(float) * (size_t)M * N));
+        dd = (float *)c->tmpw.p;
+    }
+    LAUNCH_TRY(c, timed(c, MSL_PROF_OTHER, [&] {
+                   return msl::launch_tc_gemm(ad, bd, dd, M, N, K, c->dflag, c->stream, &c->launches);
+               }));
+    if (!ddev) CUDA_TRY(c, cudaMemcpyAsync(D, dd, sizeof(float) * (size_t)M * N, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    collect_profile(c);
+    if ((rc = err_check(c))) return rc;
+    return MSL_OK;
+}
+
+}  // extern "C"
+
+struct msl_closure {
+    int device = 0;
+    msl::ClosureNet net;
+};
+
+namespace {
+
+int closure_check(msl_ctx *c, const msl_closure *n, int batch, int h, int w) {
+    if (!c || !n) return MSL_E_ARG;
+    if (n->device != c->device) return fail(c, MSL_E_ARG, "closure and context are on different devices");
+    if (batch < 1 || h < 3 || w < 128 || w % 128)
+        return fail(c, MSL_E_ARG, "closure images need batch >= 1, height >= 3 and a width that is a multiple of 128");
+    return MSL_OK;
+}
+
+// Sum of the forward pass's per-block loss terms / pixel count (after a sync).
+int closure_loss(msl_ctx *c, msl_closure *n, size_t npix, double *loss) {
+    if (!loss) return MSL_OK;
+    std::vector<double> part(n->net.loss_blocks);
+    CUDA_TRY(c, cudaMemcpy(part.data(), n->net.loss_part, sizeof(double) * part.size(), cudaMemcpyDeviceToHost));
+    double s = 0.0;
+    for (double v : part) s += v;
+    *loss = s / (double)npix;
+    return MSL_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int msl_closure_param_count(void) { return msl::closure_param_count(); }
+
+int msl_closure_create(msl_ctx *c, uint64_t seed, msl_closure **out) {
+    if (!c || !out) return MSL_E_ARG;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    msl_closure *n = new msl_closure();
+    n->device = c->device;
+    if (n->net.alloc_params() != cudaSuccess) {
+        n->net.release();
+        delete n;
+        cudaGetLastError();
+        return fail(c, MSL_E_NOMEM, "closure parameter allocation failed");
+    }
+    std::vector<float> h;
+    msl::closure_init_params(seed, h);
+    if (cudaMemcpy(n->net.params, h.data(), sizeof(float) * h.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+        n->net.release();
+        delete n;
+        return fail(c, MSL_E_CUDA, "closure parameter upload failed");
+    }
+    *out = n;
+    return MSL_OK;
+}
+
+int msl_closure_destroy(msl_closure *n) {
+    if (!n) return MSL_E_ARG;
+    int cur = 0;
+    cudaGetDevice(&cur);
+    cudaSetDevice(n->device);
+    n->net.release();
+    cudaSetDevice(cur);
+    delete n;
+    return MSL_OK;
+}
+
+int msl_closure_get_params(msl_ctx *c, const msl_closure *n, float *out) {
+    if (!c || !n || !out) return MSL_E_ARG;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    CUDA_TRY(c, cudaMemcpy(out, n->net.params, sizeof(float) * msl::closure_param_count(), cudaMemcpyDefault));
+    return MSL_OK;
+}
+
+int msl_closure_set_params(msl_ctx *c, msl_closure *n, const float *in) {
+    if (!c || !n || !in) return MSL_E_ARG;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    const size_t b = sizeof(float) * msl::closure_param_count();
+    CUDA_TRY(c, cudaMemcpy(n->net.params, in, b, cudaMemcpyDefault));
+    CUDA_TRY(c, cudaMemset(n->net.adam_m, 0, b));
+    CUDA_TRY(c, cudaMemset(n->net.adam_v, 0, b));
+    n->net.step = 0;
+    return MSL_OK;
+}
+
+int msl_closure_apply(msl_ctx *c, msl_closure *n, float *psi, int batch, int h, int w) {
+    int rc = closure_check(c, n, batch, h, w);
+    if (rc) return rc;
+    if (!psi) return fail(c, MSL_E_ARG, "psi is null");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    if ((rc = err_reset(c))) return rc;
+    const size_t bytes = sizeof(float2) * (size_t)batch * h * w;
+    const float2 *pd;
+    if ((rc = stage_in(c, (const float2 *)psi, bytes, c->in_stage, &pd))) return rc;
+    float2 *io = (float2 *)pd;
+    LAUNCH_TRY(c, timed(c, MSL_PROF_OTHER, [&] {
+                   return n->net.forward(io, batch, h, w, io, nullptr, false, c->dflag, c->stream, c->nsm,
+                                         &c->launches);
+               }));
+    if ((const void *)io != (const void *)psi)
+        CUDA_TRY(c, cudaMemcpyAsync(psi, io, bytes, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    collect_profile(c);
+    return err_check(c);
+}
+
+// Shared by msl_closure_gradients and msl_closure_train_step.
+static int closure_fwd_bwd(msl_ctx *c, msl_closure *n, const float *coarse, const float *fine, int batch, int h,
+                           int w, double *loss) {
+    int rc = closure_check(c, n, batch, h, w);
+    if (rc) return rc;
+    if (!coarse || !fine) return fail(c, MSL_E_ARG, "coarse and fine waves are required");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    if ((rc = err_reset(c))) return rc;
+    const size_t npix = (size_t)batch * h * w, bytes = sizeof(float2) * npix;
+    const float2 *cd, *fd;
+    if ((rc = stage_in(c, (const float2 *)coarse, bytes, c->in_stage, &cd))) return rc;
+    if ((rc = stage_in(c, (const float2 *)fine, bytes, c->trans_stage, &fd))) return rc;
+    LAUNCH_TRY(c, timed(c, MSL_PROF_OTHER, [&] {
+                   return n->net.forward(cd, batch, h, w, nullptr, fd, true, c->dflag, c->stream, c->nsm,
+                                         &c->launches);
+               }));
+    LAUNCH_TRY(c, timed(c, MSL_PROF_OTHER, [&] {
+                   return n->net.backward(batch, h, w, c->dflag, c->stream, c->nsm, &c->launches);
+               }));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    if ((rc = closure_loss(c, n, npix, loss))) return rc;
+    return MSL_OK;
+}
+
+int msl_closure_gradients(msl_ctx *c, msl_closure *n, const float *coarse, const float *fine, int batch, int h,
+                          int w, float *grad, double *loss) {
+    int rc = closure_fwd_bwd(c, n, coarse, fine, batch, h, w, loss);
+    if (rc) return rc;
+    if (grad)
+        CUDA_TRY(c, cudaMemcpy(grad, n->net.grads, sizeof(float) * msl::closure_param_count(), cudaMemcpyDefault));
+    collect_profile(c);
+    return err_check(c);
+}
+
+int msl_closure_train_step(msl_ctx *c, msl_closure *n, const float *coarse, const float *fine, int batch, int h,
+                           int w, float lr, double *loss) {
+    if (!(lr > 0) || !is_fin(lr)) return fail(c, MSL_E_ARG, "learning rate must be positive");
+    int rc = closure_fwd_bwd(c, n, coarse, fine, batch, h, w, loss);
+    if (rc) return rc;
+    LAUNCH_TRY(c, n->net.adam(lr, c->stream, c->nsm, &c->launches));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    collect_profile(c);
+    return err_check(c);
+}
+
 int msl_stem_scan_phonon(msl_ctx *c, const msl_atoms *at, const double *fparams, const msl_grid *g,
                          int nslice, double radius, const msl_optics *o, const msl_probe *pr,
                          const double *probe_xy, int nprobe, const msl_detectors *det,

@@ -1,14 +1,48 @@
 // Internal host-side interface between the C ABI (msl_api.cu) and the kernels.
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
 #include <vector>
 
 #include "../../include/msl.h"
 
 namespace msl {
+
+// Launch set-up of one kernel, kept per device: cudaFuncSetAttribute acts on
+// the current device only, so the dynamic shared-memory limit is raised and
+// the occupancy computed once for every device that launches the kernel, and
+// a mutex makes first launches from several host threads safe.
+constexpr int kMaxDevices = 64;
+struct KernelSetup {
+    std::mutex mu;
+    int per_sm[kMaxDevices] = {};
+    // *out = resident CTAs per SM (at least 1; need_one: fail instead when none fit)
+    template <class K> cudaError_t get(K kern, int threads, size_t smem, bool need_one, int *out) {
+        int dev = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e != cudaSuccess) return e;
+        if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+        std::lock_guard<std::mutex> lock(mu);
+        if (!per_sm[dev]) {
+            e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return e;
+            int b = 0;
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, threads, smem);
+            if (e != cudaSuccess) return e;
+            if (b < 1) {
+                if (need_one) return cudaErrorInvalidConfiguration;
+                b = 1;
+            }
+            per_sm[dev] = b;
+        }
+        *out = per_sm[dev];
+        return cudaSuccess;
+    }
+};
 
 // Every grid side the line transforms are built for.
 #define MSL_FOR_EACH_SIDE(X) X(64) X(128) X(256) X(384) X(512) X(768) X(1024) X(2048)
@@ -153,6 +187,43 @@ cudaError_t launch_transmission_phase(const float *v, double scale, size_t n, fl
 cudaError_t launch_detector_accumulate(int nconf, int np, int ntile, int ndet, const double *partial,
                                        double scale, double *out, int out_stride, cudaStream_t s,
                                        int64_t *launches);
+// D[M][N] (FP32) = A[M][K] * B[N][K]^T, bf16 operands, on the tensor cores
+// (tcgen05, accumulator in tensor memory); M % 128 == 0, K % 64 == 0,
+// 16 <= N <= 256, N % 16 == 0.  *err is raised if an MMA completion wait gives up.
+cudaError_t launch_tc_gemm(const void *A, const void *B, float *D, int M, int N, int K, int *err,
+                           cudaStream_t s, int64_t *launches);
+// ------------------------------------------------- learned closure (msl_closure.cu)
+// The network's parameters, Adam state and work buffers on one device.
+struct ClosureNet {
+    float *params = nullptr, *grads = nullptr, *adam_m = nullptr, *adam_v = nullptr;
+    __nv_bfloat16 *wt = nullptr;      // expanded bf16 weights of the tensor-core layers
+    float *dwreal = nullptr;          // one layer's real weight gradient + bias gradient
+    void *acts = nullptr;             // activations
+    float *partial = nullptr;         // weight-gradient partial sums
+    double *loss_part = nullptr;      // per-block loss sums
+    float *scale = nullptr;           // per-image s and 1/s
+    size_t cap_pix = 0;
+    int cap_img = 0;
+    bool cap_train = false;
+    int step = 0;
+    int loss_blocks = 0;
+    __nv_bfloat16 *hbuf[6] = {}, *dh[2] = {}, *xbuf = nullptr;
+    float *g6 = nullptr;
+    cudaError_t alloc_params();
+    void release();
+    cudaError_t ensure(size_t npix, int nimg, bool train);
+    cudaError_t expand(cudaStream_t s, int nsm, int64_t *launches);
+    cudaError_t conv_tc(const __nv_bfloat16 *in, const __nv_bfloat16 *w, const float *bias,
+                        const __nv_bfloat16 *mask, __nv_bfloat16 *out, int B, int H, int W, int epi, int *err,
+                        cudaStream_t s, int nsm, int64_t *launches);
+    cudaError_t forward(const float2 *psi, int B, int H, int W, float2 *out, const float2 *target, bool train,
+                        int *err, cudaStream_t s, int nsm, int64_t *launches);
+    cudaError_t backward(int B, int H, int W, int *err, cudaStream_t s, int nsm, int64_t *launches);
+    cudaError_t adam(float lr, cudaStream_t s, int nsm, int64_t *launches);
+};
+int closure_param_count();
+void closure_init_params(uint64_t seed, std::vector<float> &h);
+
 cudaError_t launch_detector_finalize(int nb, int ntile, int ndet, const double *partial,
                                      double scale, double *out, int out_stride, cudaStream_t s,
                                      int64_t *launches);

@@ -14,7 +14,6 @@
 #include <math.h>
 #include <stdint.h>
 
-#include <mutex>
 #include <vector>
 
 #include "msl_fft.cuh"
@@ -25,37 +24,6 @@ namespace msl {
 
 constexpr int kMaxDet = 8;
 
-// Launch set-up of one kernel, kept per device: cudaFuncSetAttribute acts on
-// the current device only, so the dynamic shared-memory limit is raised and
-// the occupancy computed once for every device that launches the kernel, and
-// a mutex makes first launches from several host threads safe.
-constexpr int kMaxDevices = 64;
-struct KernelSetup {
-    std::mutex mu;
-    int per_sm[kMaxDevices] = {};
-    // *out = resident CTAs per SM (at least 1; need_one: fail instead when none fit)
-    template <class K> cudaError_t get(K kern, int threads, size_t smem, bool need_one, int *out) {
-        int dev = 0;
-        cudaError_t e = cudaGetDevice(&dev);
-        if (e != cudaSuccess) return e;
-        if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
-        std::lock_guard<std::mutex> lock(mu);
-        if (!per_sm[dev]) {
-            e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e != cudaSuccess) return e;
-            int b = 0;
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, threads, smem);
-            if (e != cudaSuccess) return e;
-            if (b < 1) {
-                if (need_one) return cudaErrorInvalidConfiguration;
-                b = 1;
-            }
-            per_sm[dev] = b;
-        }
-        *out = per_sm[dev];
-        return cudaSuccess;
-    }
-};
 
 template <int N> struct RowCfg {
     using P = Plan<N>;

@@ -1,0 +1,102 @@
+// Fifth-generation tensor core (tcgen05) helpers for sm_103a, inline PTX.
+//
+// The MMA operands live in shared memory in the K-major, 128-byte-swizzled
+// canonical layout: a tile row holds 64 bf16 of K (128 bytes), eight rows form
+// a 1024-byte swizzle atom in which the 16-byte chunk c of row r sits at chunk
+// position c ^ (r & 7), atoms follow each other every 1024 bytes along M (or
+// N), and the tile base is 1024-byte aligned.  One tcgen05.mma of kind::f16
+// consumes K = 16 (32 bytes of a row); the next K step starts 32 bytes further.
+// The FP32 accumulator lives in tensor memory (TMEM): for M = 128 and
+// cta_group::1, row i of D is TMEM lane i and column j is TMEM column j; warp w
+// of the CTA reads lanes 32 (w % 4) .. 32 (w % 4) + 31.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "msl_tma.cuh"
+
+namespace msl {
+namespace tc {
+
+// Byte offset of element (row, k) (bf16, k < 64) inside a 128B-swizzled K-major tile.
+__host__ __device__ __forceinline__ uint32_t sw128_offset(uint32_t row, uint32_t k) {
+    const uint32_t chunk = (k >> 3) ^ (row & 7);
+    return (row >> 3) * 1024u + (row & 7) * 128u + chunk * 16u + (k & 7) * 2u;
+}
+
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, atoms of 8 rows
+// every 1024 bytes (stride byte offset), tcgen05 descriptor version 1.
+__device__ __forceinline__ uint64_t desc_sw128(uint32_t smem_addr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((smem_addr & 0x3FFFFu) >> 4);   // start address
+    d |= (uint64_t)(16u >> 4) << 16;                 // leading byte offset (unused for this layout)
+    d |= (uint64_t)(1024u >> 4) << 32;               // stride byte offset: next 8-row atom
+    d |= (uint64_t)1 << 46;                          // descriptor version
+    d |= (uint64_t)2 << 61;                          // 128-byte swizzle
+    return d;
+}
+
+// Instruction descriptor of kind::f16: bf16 A and B (both K-major), FP32 D, M x N.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+    return (1u << 4)                       // D format: F32
+           | (1u << 7)                     // A format: BF16
+           | (1u << 10)                    // B format: BF16
+           | ((uint32_t)(N >> 3) << 17)    // N / 8
+           | ((uint32_t)(M >> 4) << 24);   // M / 16
+}
+
+// TMEM allocation by one full warp; the base address is written to *dst (shared).
+__device__ __forceinline__ void tmem_alloc(uint32_t *dst, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst)),
+                 "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_free(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+// D[tmem] (+)= A[smem] * B[smem]^T, issued by one thread.
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+                                         uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+// The mbarrier receives one arrival when every MMA this thread issued so far has completed.
+__device__ __forceinline__ void mma_commit(uint64_t *bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                     smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void fence_before_sync() {
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void fence_after_sync() {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// 16 consecutive FP32 columns of this thread's TMEM lane (32x32b shape).
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+        "%14, %15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr)
+        : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+}  // namespace tc
+}  // namespace msl
