@@ -320,6 +320,24 @@ int msl_closure_gradients(msl_ctx *ctx, msl_closure *net, const float *coarse, c
 int msl_closure_train_step(msl_ctx *ctx, msl_closure *net, const float *coarse, const float *fine, int batch,
                            int h, int w, float lr, double *loss);
 
+/* Exit waves of a STEM scan: each probe of probe_xy (msl_stem_scan's probe)
+ * through the slice loop of msl_multislice; psi_out: complex64
+ * [nprobe][nx][ny] in real space (host or device).  The probe-and-slice part
+ * of MSProjectReuse.cs:254-347 without detection. */
+int msl_stem_exit_waves(msl_ctx *ctx, const msl_grid *grid, const msl_optics *optics, const float *trans,
+                        int ntrans, const double *dz, const int *layer_seq, int nslice, const msl_probe *probe,
+                        const double *probe_xy, int nprobe, float *psi_out);
+
+/* STEM scan through coarse slices corrected by the closure: every probe runs
+ * the slice loop over (typically 4x thicker) layers, its real-space exit wave
+ * is corrected by msl_closure_apply, and the corrected wave's spectrum inside
+ * the band limit is summed over each annulus (msl_stem_scan's detector, in its
+ * scale).  det_out: double [nprobe][ndet].  ny must be a multiple of 128. */
+int msl_stem_scan_closure(msl_ctx *ctx, msl_closure *net, const msl_grid *grid, const msl_optics *optics,
+                          const float *trans, int ntrans, const double *dz, const int *layer_seq, int nslice,
+                          const msl_probe *probe, const double *probe_xy, int nprobe, const msl_detectors *det,
+                          double *det_out);
+
 /* ------------------------------------------------------- uneven batches */
 
 #define MSL_PLANE_WAVE 0

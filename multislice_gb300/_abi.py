@@ -26,7 +26,8 @@ EXPORTS = (
     "msl_run_jobs", "msl_ctem_partial_coherence", "msl_check_wait_timeout", "msl_set_memory_limit",
     "msl_memory_in_use", "msl_stem_scan_phonon", "msl_tc_gemm_bf16", "msl_closure_create",
     "msl_closure_destroy", "msl_closure_param_count", "msl_closure_get_params", "msl_closure_set_params",
-    "msl_closure_apply", "msl_closure_gradients", "msl_closure_train_step",
+    "msl_closure_apply", "msl_closure_gradients", "msl_closure_train_step", "msl_stem_exit_waves",
+    "msl_stem_scan_closure",
 )
 PLANE_WAVE, PROBE = 0, 1
 # Muslib-shaped exports (reference names, no msl_ prefix)
@@ -136,6 +137,10 @@ def load(path=LIB_PATH):
                                       ctypes.c_uint64, P, P]),
         "msl_tc_gemm_bf16": (c_int, [P, P, P, P, c_int, c_int, c_int]),
         "msl_closure_create": (c_int, [P, ctypes.c_uint64, P]),
+        "msl_stem_exit_waves": (c_int, [P, POINTER(Grid), POINTER(Optics), P, c_int, P, P, c_int,
+                                        POINTER(Probe), P, c_int, P]),
+        "msl_stem_scan_closure": (c_int, [P, P, POINTER(Grid), POINTER(Optics), P, c_int, P, P, c_int,
+                                          POINTER(Probe), P, c_int, POINTER(Detectors), P]),
         "msl_closure_destroy": (c_int, [P]),
         "msl_closure_param_count": (c_int, []),
         "msl_closure_get_params": (c_int, [P, P, P]),

@@ -373,6 +373,51 @@ class Context:
         return out
 
 
+    def stem_exit_waves(self, trans, dz, layer_seq, ax, by, kev, k_ap, probe_xy, df=0.0, cs=0.0, k_ap_in=0.0,
+                        bandlimit=2.0 / 3.0, out=None):
+        """Real-space exit waves of the scan's probes, complex64 [nprobe, nx, ny]
+        (or into `out`, e.g. a torch device tensor [nprobe, nx, ny, 2])."""
+        trans = _as(trans, np.complex64)
+        nt, nx, ny = _cshape(trans)
+        dz = np.ascontiguousarray(np.broadcast_to(np.asarray(dz, np.float64), (nt,)))
+        seq = np.ascontiguousarray(layer_seq, np.int32)
+        xy = np.ascontiguousarray(probe_xy, np.float64).reshape(-1, 2)
+        pr = Probe(float(k_ap_in), float(k_ap), float(df), float(cs))
+        g = Grid(nx, ny, float(ax), float(by))
+        o = self._optics(kev, bandlimit)
+        if out is None:
+            out = np.empty((len(xy), nx, ny), np.complex64)
+        self._check(self._lib.msl_stem_exit_waves(self._h, ctypes.byref(g), ctypes.byref(o),
+                                                  _ptr(trans, np.complex64), nt, _ptr(dz, np.float64),
+                                                  _ptr(seq, np.int32), len(seq), ctypes.byref(pr),
+                                                  _ptr(xy, np.float64), len(xy), _ptr(out, np.complex64)))
+        return out
+
+    def stem_scan_closure(self, net, trans, dz, layer_seq, ax, by, kev, k_ap, probe_xy, det_k, df=0.0, cs=0.0,
+                          k_ap_in=0.0, bandlimit=2.0 / 3.0, out=None):
+        """Detector sums [nprobe, ndet] of coarse-slice exit waves corrected by the closure."""
+        trans = _as(trans, np.complex64)
+        nt, nx, ny = _cshape(trans)
+        dz = np.ascontiguousarray(np.broadcast_to(np.asarray(dz, np.float64), (nt,)))
+        seq = np.ascontiguousarray(layer_seq, np.int32)
+        xy = np.ascontiguousarray(probe_xy, np.float64).reshape(-1, 2)
+        det = np.asarray(det_k, np.float64).reshape(-1, 2)
+        kin = np.ascontiguousarray(det[:, 0])
+        kout = np.ascontiguousarray(det[:, 1])
+        dets = Detectors(len(det), kin.ctypes.data, kout.ctypes.data)
+        pr = Probe(float(k_ap_in), float(k_ap), float(df), float(cs))
+        g = Grid(nx, ny, float(ax), float(by))
+        o = self._optics(kev, bandlimit)
+        if out is None:
+            out = np.empty((len(xy), len(det)), np.float64)
+        self._check(self._lib.msl_stem_scan_closure(self._h, net._h, ctypes.byref(g), ctypes.byref(o),
+                                                    _ptr(trans, np.complex64), nt, _ptr(dz, np.float64),
+                                                    _ptr(seq, np.int32), len(seq), ctypes.byref(pr),
+                                                    _ptr(xy, np.float64), len(xy), ctypes.byref(dets),
+                                                    _ptr(out, np.float64)))
+        return out
+
+
 def phonon_displacements(seed, config, natom, sigma):
     """Frozen-phonon displacements [natom, 3] of configuration `config` (msl_phonon_displacements)."""
     d = np.empty((natom, 3), np.float64)

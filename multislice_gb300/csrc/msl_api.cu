@@ -1683,6 +1683,224 @@ int msl_closure_train_step(msl_ctx *c, msl_closure *n, const float *coarse, cons
     return err_check(c);
 }
 
+}  // extern "C"
+
+namespace {
+
+// Shared set-up of the exit-wave scans (msl_stem_exit_waves, msl_stem_scan_closure):
+// slice tables of ntrans layers plus an identity layer (index ntrans: band limit
+// and the 1/(nx ny) scale only), twiddles, the probe table and, when det is given,
+// the detector mask; work buffers for B probes.
+struct ExitScan {
+    SliceTables st;
+    float2 *twr = nullptr, *twc = nullptr;
+    const float2 *td = nullptr;
+    float2 *apchi = nullptr, *ex = nullptr, *ey = nullptr, *w = nullptr;
+    uint8_t *mask = nullptr;
+    double *fxy = nullptr, *partial = nullptr;
+    int B = 0, ntile = 0, ntrans = 0;
+};
+
+int exit_scan_setup(msl_ctx *c, const msl_grid *g, const msl_optics *o, const float *trans, int ntrans,
+                    const double *dz, const msl_probe *pr, const msl_detectors *det, int nprobe, size_t max_b,
+                    ExitScan &X) {
+    const int nx = g->nx, ny = g->ny, ndet = det ? det->ndet : 0;
+    const size_t n2 = (size_t)nx * ny;
+    int rc;
+    if ((rc = stage_in(c, (const float2 *)trans, sizeof(float2) * n2 * ntrans, c->trans_stage, &X.td))) return rc;
+    std::vector<double> dze(dz, dz + ntrans);
+    dze.push_back(0.0);  // the identity layer
+    if ((rc = build_slice_tables(c, g, o, ntrans + 1, dze.data(), X.st))) return rc;
+    X.ntrans = ntrans;
+    X.twr = twiddles(c, ny);
+    X.twc = twiddles(c, nx);
+    if (!X.twr || !X.twc) return fail(c, MSL_E_NOMEM, "twiddle table allocation failed");
+    std::vector<double> hk(nx + ny + 2 * ndet);
+    for (int i = 0; i < nx; ++i) hk[i] = (double)(i < nx / 2 ? i : i - nx) / g->ax;
+    for (int i = 0; i < ny; ++i) hk[nx + i] = (double)(i < ny / 2 ? i : i - ny) / g->by;
+    for (int d = 0; d < ndet; ++d) {
+        hk[nx + ny + d] = det->k_in[d] * det->k_in[d];
+        hk[nx + ny + ndet + d] = det->k_out[d] * det->k_out[d];
+    }
+    if ((rc = upload(c, c->fxy, hk.data(), sizeof(double) * hk.size()))) return rc;
+    const double *kxd = (const double *)c->fxy.p, *kyd = kxd + nx;
+    CUDA_TRY(c, c->apchi.ensure(sizeof(float2) * n2 + n2));
+    X.apchi = (float2 *)c->apchi.p;
+    X.mask = (uint8_t *)(X.apchi + n2);
+    const double lam = msl_wavelength(o->kev);
+    LAUNCH_TRY(c, timed(c, MSL_PROF_OTHER, [&] {
+                   return msl::launch_probe_table(nx, ny, kxd, kyd, pr->k_in * pr->k_in, pr->k_out * pr->k_out, lam,
+                                                  pr->df, pr->cs, 1.0 / ((double)nx * ny), X.apchi, c->stream,
+                                                  &c->launches);
+               }));
+    if (det)
+        LAUNCH_TRY(c, timed(c, MSL_PROF_OTHER, [&] {
+                       return msl::launch_detector_mask(nx, ny, kxd, kyd, ndet, kyd + ny, kyd + ny + ndet, X.mask,
+                                                        c->stream, &c->launches);
+                   }));
+    int B = c->probe_batch;
+    if (B <= 0) {
+        size_t budget = (size_t)8 << 30;
+        if (c->mem.limit && c->mem.limit / 2 < budget) budget = c->mem.limit / 2;
+        B = (int)std::max<size_t>(1, std::min<size_t>(budget / (sizeof(float2) * n2), 65536));
+    }
+    if ((size_t)B > max_b) B = (int)max_b;
+    if (B > nprobe) B = nprobe;
+    X.B = B;
+    CUDA_TRY(c, c->wave.ensure(sizeof(float2) * n2 * B));
+    CUDA_TRY(c, c->exy.ensure(sizeof(float2) * (size_t)B * (nx + ny) + sizeof(double) * 2 * B));
+    X.w = (float2 *)c->wave.p;
+    X.ex = (float2 *)c->exy.p;
+    X.ey = X.ex + (size_t)B * nx;
+    X.fxy = (double *)(X.ey + (size_t)B * ny);
+    if (det) {
+        ColArgs probe_cfg = col_args(g, X.st, X.twc, 0, X.w, 1, msl::COL_LOAD | msl::COL_STORE, c->dflag);
+        X.ntile = ny / msl::plan_col_c_launch(nx, probe_cfg);
+        CUDA_TRY(c, c->partial.ensure(sizeof(double) * (size_t)B * X.ntile * ndet));
+        X.partial = (double *)c->partial.p;
+    }
+    return MSL_OK;
+}
+
+// Probes p0 .. p0 + nb - 1 through the slice loop: X.w receives their real-space exit waves.
+int exit_scan_batch(msl_ctx *c, const msl_grid *g, ExitScan &X, const int *layer_seq, int nslice,
+                    const double *probe_xy, int p0, int nb) {
+    const int nx = g->nx, ny = g->ny;
+    std::vector<double> hf(2 * (size_t)nb);
+    for (int b = 0; b < nb; ++b) {
+        hf[2 * b] = probe_xy[2 * (p0 + b)] / g->ax;
+        hf[2 * b + 1] = probe_xy[2 * (p0 + b) + 1] / g->by;
+    }
+    CUDA_TRY(c, cudaMemcpyAsync(X.fxy, hf.data(), sizeof(double) * 2 * nb, cudaMemcpyHostToDevice, c->stream));
+    LAUNCH_TRY(c, timed(c, MSL_PROF_OTHER, [&] {
+                   return msl::launch_probe_shifts(nx, ny, nb, X.fxy, X.ex, X.ey, c->stream, &c->launches);
+               }));
+    ColArgs pa = col_args(g, X.st, X.twc, 0, X.w, nb, msl::COL_PROBE | msl::COL_INV | msl::COL_STORE, c->dflag);
+    pa.apchi = X.apchi;
+    pa.ex = X.ex;
+    pa.ey = X.ey;
+    LAUNCH_TRY(c, timed(c, MSL_PROF_COL, [&] { return msl::launch_col_pass(nx, pa, c->stream, c->nsm, &c->launches); }));
+    const size_t n2 = (size_t)nx * ny;
+    for (int s = 0; s < nslice; ++s) {
+        const int l = layer_seq[s];
+        RowArgs r = row_args(g, X.twr, X.td + (size_t)l * n2, X.w, nb,
+                             msl::ROW_LOAD | msl::ROW_INV | msl::ROW_TRANS | msl::ROW_FWD, c->dflag);
+        LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_row_pass(ny, r, c->stream, c->nsm, &c->launches); }));
+        ColArgs ca = col_args(g, X.st, X.twc, l, X.w, nb,
+                              msl::COL_LOAD | msl::COL_FWD | msl::COL_PROP | msl::COL_INV | msl::COL_STORE, c->dflag);
+        LAUNCH_TRY(c, timed(c, MSL_PROF_COL, [&] { return msl::launch_col_pass(nx, ca, c->stream, c->nsm, &c->launches); }));
+    }
+    RowArgs r = row_args(g, X.twr, nullptr, X.w, nb, msl::ROW_LOAD | msl::ROW_INV, c->dflag);
+    LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_row_pass(ny, r, c->stream, c->nsm, &c->launches); }));
+    return MSL_OK;
+}
+
+int exit_scan_check(msl_ctx *c, const msl_grid *g, const msl_optics *o, const float *trans, int ntrans,
+                    const double *dz, const int *layer_seq, int nslice, const msl_probe *pr, const double *probe_xy,
+                    int nprobe) {
+    int rc = check_grid(c, g);
+    if (rc) return rc;
+    if ((rc = check_optics(c, o))) return rc;
+    if ((rc = check_layers(c, ntrans, dz, layer_seq, nslice))) return rc;
+    if (!trans || !pr || !probe_xy) return fail(c, MSL_E_ARG, "null argument");
+    if (nprobe < 1) return fail(c, MSL_E_ARG, "nprobe must be >= 1");
+    if (!(pr->k_in >= 0) || !(pr->k_out > pr->k_in) || !is_fin(pr->k_out) || !is_fin(pr->df) || !is_fin(pr->cs))
+        return fail(c, MSL_E_ARG, "probe aperture must satisfy 0 <= k_in < k_out; df, cs finite");
+    for (int p = 0; p < 2 * nprobe; ++p)
+        if (!is_fin(probe_xy[p])) return fail(c, MSL_E_ARG, "probe positions must be finite");
+    return MSL_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int msl_stem_exit_waves(msl_ctx *c, const msl_grid *g, const msl_optics *o, const float *trans, int ntrans,
+                        const double *dz, const int *layer_seq, int nslice, const msl_probe *pr,
+                        const double *probe_xy, int nprobe, float *psi_out) {
+    if (!c) return MSL_E_ARG;
+    int rc = exit_scan_check(c, g, o, trans, ntrans, dz, layer_seq, nslice, pr, probe_xy, nprobe);
+    if (rc) return rc;
+    if (!psi_out) return fail(c, MSL_E_ARG, "psi_out is null");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    if ((rc = err_reset(c))) return rc;
+    ExitScan X;
+    if ((rc = exit_scan_setup(c, g, o, trans, ntrans, dz, pr, nullptr, nprobe, (size_t)nprobe, X))) return rc;
+    const size_t n2 = (size_t)g->nx * g->ny;
+    for (int p0 = 0; p0 < nprobe; p0 += X.B) {
+        const int nb = std::min(X.B, nprobe - p0);
+        if ((rc = exit_scan_batch(c, g, X, layer_seq, nslice, probe_xy, p0, nb))) return rc;
+        CUDA_TRY(c, cudaMemcpyAsync(psi_out + 2 * n2 * p0, X.w, sizeof(float2) * n2 * nb, cudaMemcpyDefault,
+                                    c->stream));
+        CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    }
+    collect_profile(c);
+    return err_check(c);
+}
+
+int msl_stem_scan_closure(msl_ctx *c, msl_closure *n, const msl_grid *g, const msl_optics *o, const float *trans,
+                          int ntrans, const double *dz, const int *layer_seq, int nslice, const msl_probe *pr,
+                          const double *probe_xy, int nprobe, const msl_detectors *det, double *det_out) {
+    if (!c || !n) return MSL_E_ARG;
+    int rc = exit_scan_check(c, g, o, trans, ntrans, dz, layer_seq, nslice, pr, probe_xy, nprobe);
+    if (rc) return rc;
+    if (n->device != c->device) return fail(c, MSL_E_ARG, "closure and context are on different devices");
+    if (g->ny % 128) return fail(c, MSL_E_ARG, "the closure needs ny to be a multiple of 128");
+    if (!det || !det_out || det->ndet < 1 || det->ndet > MSL_MAX_DETECTORS || !det->k_in || !det->k_out)
+        return fail(c, MSL_E_ARG, "1..8 detectors with k_in/k_out arrays and det_out are required");
+    for (int d = 0; d < det->ndet; ++d)
+        if (!(det->k_in[d] >= 0) || !(det->k_out[d] >= det->k_in[d]) || !is_fin(det->k_out[d]))
+            return fail(c, MSL_E_ARG, "detector bounds must satisfy 0 <= k_in <= k_out");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    if ((rc = err_reset(c))) return rc;
+    const int nx = g->nx, ny = g->ny, ndet = det->ndet;
+    const size_t n2 = (size_t)nx * ny;
+    // the closure keeps two bf16 activation planes of 64 channels per pixel: its
+    // sub-batch is sized to 4 GiB of them, the wave batch to a whole number of those
+    const int CB = (int)std::max<size_t>(1, ((size_t)4 << 30) / (256 * n2));
+    ExitScan X;
+    if ((rc = exit_scan_setup(c, g, o, trans, ntrans, dz, pr, det, nprobe, (size_t)1 << 30, X))) return rc;
+    const size_t obytes = sizeof(double) * (size_t)nprobe * ndet;
+    const bool odev = on_device(det_out);
+    double *od;
+    if (odev) {
+        od = det_out;
+    } else {
+        CUDA_TRY(c, c->detout.ensure(obytes));
+        od = (double *)c->detout.p;
+    }
+    const double dscale = (double)n2 * (double)n2;
+    for (int p0 = 0; p0 < nprobe; p0 += X.B) {
+        const int nb = std::min(X.B, nprobe - p0);
+        if ((rc = exit_scan_batch(c, g, X, layer_seq, nslice, probe_xy, p0, nb))) return rc;
+        for (int b0 = 0; b0 < nb; b0 += CB) {
+            const int cb = std::min(CB, nb - b0);
+            float2 *wb = X.w + n2 * b0;
+            LAUNCH_TRY(c, timed(c, MSL_PROF_OTHER, [&] {
+                           return n->net.forward(wb, cb, nx, ny, wb, nullptr, false, c->dflag, c->stream, c->nsm,
+                                                 &c->launches);
+                       }));
+        }
+        // forward transform of the corrected exit waves and detection inside the band limit
+        RowArgs r = row_args(g, X.twr, nullptr, X.w, nb, msl::ROW_LOAD | msl::ROW_FWD, c->dflag);
+        LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_row_pass(ny, r, c->stream, c->nsm, &c->launches); }));
+        ColArgs ca = col_args(g, X.st, X.twc, X.ntrans, X.w, nb, msl::COL_LOAD | msl::COL_FWD | msl::COL_PROP | msl::COL_DETECT,
+                              c->dflag);
+        ca.detmask = X.mask;
+        ca.ndet = ndet;
+        ca.partial = X.partial;
+        LAUNCH_TRY(c, timed(c, MSL_PROF_COL, [&] { return msl::launch_col_pass(nx, ca, c->stream, c->nsm, &c->launches); }));
+        LAUNCH_TRY(c, timed(c, MSL_PROF_OTHER, [&] {
+                       return msl::launch_detector_finalize(nb, X.ntile, ndet, X.partial, dscale, od + (size_t)p0 * ndet,
+                                                            ndet, c->stream, &c->launches);
+                   }));
+    }
+    if (!odev) CUDA_TRY(c, cudaMemcpyAsync(det_out, od, obytes, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    collect_profile(c);
+    return err_check(c);
+}
+
 int msl_stem_scan_phonon(msl_ctx *c, const msl_atoms *at, const double *fparams, const msl_grid *g,
                          int nslice, double radius, const msl_optics *o, const msl_probe *pr,
                          const double *probe_xy, int nprobe, const msl_detectors *det,

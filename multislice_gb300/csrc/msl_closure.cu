@@ -186,7 +186,11 @@ __global__ void __launch_bounds__(128) conv_tc_kernel(const __nv_bfloat16 *__res
             __align__(16) __nv_bfloat16 ob[16];
             if (epi == EPI_BIAS_RELU) {
 #pragma unroll
-                for (int j = 0; j < 16; ++j) ob[j] = __float2bfloat16_rn(fmaxf(v[j] + bias[c0 + j], 0.0f));
+                for (int j = 0; j < 16; ++j) {
+                    // real channel n = c0 + j: the complex bias [o][2] holds (re, im) of channel n % 32
+                    const int n = c0 + j;
+                    ob[j] = __float2bfloat16_rn(fmaxf(v[j] + bias[(n & (kC - 1)) * 2 + (n >> 5)], 0.0f));
+                }
             } else {
                 const __nv_bfloat16 *m = mask + pix * 64 + c0;
 #pragma unroll

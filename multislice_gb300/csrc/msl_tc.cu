@@ -103,9 +103,11 @@ cudaError_t launch_tc_gemm(const void *A, const void *B, float *D, int M, int N,
     int ncols = 32;
     while (ncols < N) ncols <<= 1;
     const size_t smem = 1024 + (size_t)kTcM * kTcK * 2 + (size_t)N * kTcK * 2;
+    // the attribute is the largest dynamic size any call uses (N = 256)
+    const size_t smem_max = 1024 + (size_t)kTcM * kTcK * 2 + (size_t)256 * kTcK * 2;
     static KernelSetup ks;
     int per_sm = 0;
-    cudaError_t e = ks.get(tc_gemm_kernel, 128, smem, true, &per_sm);
+    cudaError_t e = ks.get(tc_gemm_kernel, 128, smem_max, true, &per_sm);
     if (e != cudaSuccess) return e;
     ++*launches;
     tc_gemm_kernel<<<M / kTcM, 128, smem, s>>>((const __nv_bfloat16 *)A, (const __nv_bfloat16 *)B, D, M, N, K,

@@ -58,11 +58,13 @@ def test_closure_gradient_matches_oracle(ctx):
 def test_closure_training_reduces_loss(ctx):
     from multislice_gb300.api import Closure
     net = Closure(ctx, seed=3)
-    c, f = _waves(4, 4, 8, 128)
+    c, _ = _waves(4, 4, 8, 128)
+    # a target the network can represent: a local linear map of the coarse wave
+    f = (c + 0.05 * np.roll(c, 1, axis=2) + 0.03j * c).astype(np.complex64)
     first = net.train_step(c, f, 3e-3)
-    for _ in range(60):
+    for _ in range(100):
         last = net.train_step(c, f, 3e-3)
-    assert last < 0.5 * first
+    assert last < 0.2 * first, (first, last)
     # the trained parameters leave the library and come back unchanged
     p = net.get_params()
     net2 = Closure(ctx, seed=99)
@@ -70,3 +72,27 @@ def test_closure_training_reduces_loss(ctx):
     np.testing.assert_array_equal(net2.apply(c.copy()), net.apply(c.copy()))
     net.close()
     net2.close()
+
+
+def test_closure_gain_on_held_out_srtio3_probes(ctx):
+    """Trained on pairs the library makes (SrTiO3, 4x thicker slices), the closure
+    brings held-out coarse-slice exit waves closer to the fine-slice ones than the
+    coarse waves alone -- the gain over the method without it."""
+    import torch
+
+    from multislice_gb300 import closure as CL
+    from multislice_gb300.api import Closure
+    coarse, fine = CL.make_pairs(ctx, 192, seed=5, nconfig=4)
+    tr_c, tr_f = coarse[:128].contiguous(), fine[:128].contiguous()
+    va_c, va_f = coarse[128:].contiguous(), fine[128:].contiguous()
+    net = Closure(ctx, seed=1)
+    e_coarse, e_before = CL.evaluate(net, va_c, va_f)
+    assert e_coarse > 1e-3                       # thicker slices do change the wave
+    hist = CL.train(ctx, net, tr_c, tr_f, steps=300, batch=8, lr=2e-3, lr_final=2e-4, seed=2)
+    assert hist[-1] < hist[0]
+    e_coarse2, e_after = CL.evaluate(net, va_c, va_f)
+    assert e_coarse2 == e_coarse
+    assert e_after < 0.9 * e_coarse, (e_coarse, e_after)
+    net.close()
+    del coarse, fine
+    torch.cuda.empty_cache()

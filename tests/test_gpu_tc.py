@@ -1,8 +1,6 @@
 """The tensor-core GEMM (tcgen05.mma, bf16 operands in 128B-swizzled shared
 memory, FP32 accumulator in tensor memory) against a plain FP32 product of the
 same bf16 values."""
-import ctypes
-
 import numpy as np
 import pytest
 
@@ -35,10 +33,8 @@ def test_tc_gemm_matches_fp32_product(ctx, M, N, K):
 
 
 def test_tc_gemm_rejects_bad_shapes(ctx):
-    from multislice_gb300 import MslError
     A = np.zeros((100, 64), np.uint16)
     B = np.zeros((16, 64), np.uint16)
     D = np.zeros((100, 16), np.float32)
     rc = ctx._lib.msl_tc_gemm_bf16(ctx._h, A.ctypes.data, B.ctypes.data, D.ctypes.data, 100, 16, 64)
     assert rc == _abi.MSL_E_ARG
-    del MslError, ctypes
