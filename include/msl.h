@@ -297,8 +297,9 @@ int msl_tc_gemm_bf16(msl_ctx *ctx, const uint16_t *A, const uint16_t *B, float *
  * in the reference; the reference's fine-slice loop, mulslice.cpp:706-739, is
  * its fallback and the judge of its error).  Six complex 3x3 convolutions with
  * periodic boundaries -- 1 -> 32 -> 32 -> 32 -> 32 -> 32 -> 1 channels, CReLU
- * between them -- act on the wave divided by its RMS s, and the output adds
- * s times the result to the wave.  Parameters are FP32 master copies used as
+ * between them -- act on the wave divided by s = sqrt(sum |psi|^2 / 256^2) (its
+ * RMS on a 256^2 grid, so a probe keeps its per-pixel scale on any grid), and
+ * the output adds s times the result to the wave.  Parameters are FP32 master copies used as
  * bf16; the 32 -> 32 layers run on the tensor cores (forward and input
  * gradient), the rest on the CUDA cores; training uses Adam.  Waves are
  * complex64 [batch][h][w] (w a multiple of 128, h >= 3), host or device. */

@@ -4,7 +4,7 @@
 // loop (mulslice.cpp:706-739) is its fallback and the judge of its error.
 //
 // Network (complex channels, 3x3 taps, periodic boundaries as the wave itself):
-//   x = psi / s                 (s = RMS of psi over the image)
+//   x = psi / s                 (s = norm of psi / 256: its RMS on a 256^2 grid)
 //   h1 = CReLU(conv(x; 1 -> C))
 //   h2..h5 = CReLU(conv(h; C -> C))
 //   d = conv(h5; C -> 1)
@@ -437,7 +437,10 @@ __global__ void bias_contract_kernel(const float *db, int co, float *g) {
 // first layer's weight gradient needs dy = dh1 (bf16 [p][64]) and x = xin ([p][2])
 // -> handled by dw_kernel with kr = 2.
 
-// Per-image scale s = RMS |psi| (and 1/s).
+// Per-image scale s = sqrt(sum |psi|^2 / 256^2) (and 1/s): the wave's norm over
+// a fixed reference area of 256^2 pixels, so a probe keeps its per-pixel scale
+// whatever the grid it is computed on.
+constexpr double kRefPixels = 65536.0;
 __global__ void rms_kernel(const float2 *__restrict__ psi, int HW, float *__restrict__ s, float *__restrict__ inv) {
     __shared__ double red[256];
     const int b = blockIdx.x;
@@ -453,7 +456,7 @@ __global__ void rms_kernel(const float2 *__restrict__ psi, int HW, float *__rest
         __syncthreads();
     }
     if (threadIdx.x == 0) {
-        double r = sqrt(red[0] / HW);
+        double r = sqrt(red[0] / kRefPixels);
         if (!(r > 0)) r = 1.0;
         s[b] = (float)r;
         inv[b] = (float)(1.0 / r);

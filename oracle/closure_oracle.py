@@ -5,7 +5,8 @@ libmsl.so (msl_closure_* in include/msl.h).
 
 A float64 numpy statement of the network msl_closure.cu implements -- six
 complex 3x3 convolutions with periodic boundaries (1 -> 32 -> 32 -> 32 -> 32 ->
-32 -> 1 channels), CReLU between them, applied to the wave divided by its RMS,
+32 -> 1 channels), CReLU between them, applied to the wave divided by its RMS on a
+256^2 reference grid (sqrt(sum |psi|^2 / 256^2)),
 the output added back scaled -- with its loss and its gradient with respect to
 every parameter.  With ``bf16=True`` it rounds to bfloat16 where the GPU stores
 bfloat16 (the scaled input, the weights, every activation and every stored
@@ -96,7 +97,7 @@ def forward(params, coarse, fine=None, bf=True):
     rnd = bf16 if bf else (lambda v: np.asarray(v, np.float64))
     coarse = np.asarray(coarse, np.complex128)
     B, H, W = coarse.shape
-    s = np.sqrt(np.mean(np.abs(coarse) ** 2, axis=(1, 2)))
+    s = np.sqrt(np.sum(np.abs(coarse) ** 2, axis=(1, 2)) / 65536.0)   # norm over a 256^2 reference area
     s = np.where(s > 0, s, 1.0).astype(np.float32).astype(np.float64)
     inv = (1.0 / s).astype(np.float32).astype(np.float64)
     layers = split_params(params)
