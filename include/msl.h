@@ -377,6 +377,27 @@ int msl_run_jobs(msl_ctx *ctx, const msl_job *jobs, int njobs, double bandlimit)
  * otherwise.  Every TMA wait in the pass kernels takes the same path. */
 int msl_check_wait_timeout(msl_ctx *ctx, uint32_t polls);
 
+/* Pass schedules and their autotuner.  Each grid side's row and column passes
+ * can run on one of three kernel families: MSL_FAM_FAST (warp-owned, two-stage
+ * and warp-pair line kernels fed by bulk / TMA copies; the default),
+ * MSL_FAM_TMA (TMA-tiled kernels with block-wide exchanges) or MSL_FAM_REG
+ * (register-only kernels with plain loads).  All compute the same transforms
+ * (not bit for bit: their radix plans differ).  msl_autotune times one slice
+ * step of `batch` synthetic waves of `side` for every pair of families (`reps`
+ * steps each after a warm-up, CUDA events on the context's stream), keeps the
+ * fastest pair as the schedule of that side on the context's device, and
+ * returns it and the times (ms[row_family * 3 + col_family], ms per step; may
+ * be NULL).  With msl_set_autotune(ctx, 1), msl_multislice and msl_stem_scan
+ * tune each side once per device on first use (waves of 256 MiB).  The
+ * reference has no counterpart (cuFFTW plans its own transforms). */
+#define MSL_FAM_FAST 0
+#define MSL_FAM_TMA 1
+#define MSL_FAM_REG 2
+int msl_autotune(msl_ctx *ctx, int side, int batch, int reps, int *row_family, int *col_family, double *ms);
+int msl_set_schedule(msl_ctx *ctx, int side, int row_family, int col_family);
+int msl_get_schedule(msl_ctx *ctx, int side, int *row_family, int *col_family);
+int msl_set_autotune(msl_ctx *ctx, int on);
+
 /* Probe batch size used by msl_stem_scan (0 = automatic).  Work buffers are
  * sized batch * nx * ny * 8 bytes. */
 int msl_set_probe_batch(msl_ctx *ctx, int batch);

@@ -27,7 +27,7 @@ EXPORTS = (
     "msl_memory_in_use", "msl_stem_scan_phonon", "msl_tc_gemm_bf16", "msl_closure_create",
     "msl_closure_destroy", "msl_closure_param_count", "msl_closure_get_params", "msl_closure_set_params",
     "msl_closure_apply", "msl_closure_gradients", "msl_closure_train_step", "msl_stem_exit_waves",
-    "msl_stem_scan_closure",
+    "msl_stem_scan_closure", "msl_autotune", "msl_set_schedule", "msl_get_schedule", "msl_set_autotune",
 )
 PLANE_WAVE, PROBE = 0, 1
 # Muslib-shaped exports (reference names, no msl_ prefix)
@@ -137,6 +137,10 @@ def load(path=LIB_PATH):
                                       ctypes.c_uint64, P, P]),
         "msl_tc_gemm_bf16": (c_int, [P, P, P, P, c_int, c_int, c_int]),
         "msl_closure_create": (c_int, [P, ctypes.c_uint64, P]),
+        "msl_autotune": (c_int, [P, c_int, c_int, c_int, P, P, P]),
+        "msl_set_schedule": (c_int, [P, c_int, c_int, c_int]),
+        "msl_get_schedule": (c_int, [P, c_int, P, P]),
+        "msl_set_autotune": (c_int, [P, c_int]),
         "msl_stem_exit_waves": (c_int, [P, POINTER(Grid), POINTER(Optics), P, c_int, P, P, c_int,
                                         POINTER(Probe), P, c_int, P]),
         "msl_stem_scan_closure": (c_int, [P, P, POINTER(Grid), POINTER(Optics), P, c_int, P, P, c_int,

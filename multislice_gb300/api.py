@@ -117,6 +117,28 @@ class Context:
     def set_probe_batch(self, batch):
         self._check(self._lib.msl_set_probe_batch(self._h, int(batch)))
 
+    FAMILIES = ("fast", "tma", "register")
+
+    def autotune(self, side, batch, reps=3):
+        """Time every pair of pass families at `side` and keep the fastest;
+        returns (row_family, col_family, times [3, 3] ms per slice step)."""
+        rf, cf = ctypes.c_int(), ctypes.c_int()
+        ms = np.zeros(9, np.float64)
+        self._check(self._lib.msl_autotune(self._h, int(side), int(batch), int(reps), ctypes.byref(rf),
+                                           ctypes.byref(cf), ms.ctypes.data))
+        return rf.value, cf.value, ms.reshape(3, 3)
+
+    def set_schedule(self, side, row_family, col_family):
+        self._check(self._lib.msl_set_schedule(self._h, int(side), int(row_family), int(col_family)))
+
+    def get_schedule(self, side):
+        rf, cf = ctypes.c_int(), ctypes.c_int()
+        self._check(self._lib.msl_get_schedule(self._h, int(side), ctypes.byref(rf), ctypes.byref(cf)))
+        return rf.value, cf.value
+
+    def set_autotune(self, on):
+        self._check(self._lib.msl_set_autotune(self._h, 1 if on else 0))
+
     def set_memory_limit(self, nbytes):
         """Cap the device memory of the context's work buffers (0: no cap)."""
         self._check(self._lib.msl_set_memory_limit(self._h, int(nbytes)))

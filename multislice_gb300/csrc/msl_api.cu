@@ -8,6 +8,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <map>
 #include <string>
@@ -130,6 +131,7 @@ struct msl_ctx {
     std::map<int, float2 *> tw;
     // optional per-kernel-kind timing with events on the context's stream
     bool prof = false;
+    bool autotune = false;  // tune each side's pass families on first use (per device)
     std::vector<cudaEvent_t> ev_free;
     struct Pending { int kind; cudaEvent_t a, b; };
     std::vector<Pending> pending;
@@ -511,6 +513,115 @@ uint64_t splitmix64(uint64_t x) {
     x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
     x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
     return x ^ (x >> 31);
+}
+
+}  // namespace
+
+namespace {
+
+// ---------------------------------------------------------------- autotuner
+// Tuned sides per device (bit = side slot), shared by every context of a device.
+std::atomic<uint32_t> g_tuned[64];
+
+int side_bit(int n) {
+    switch (n) {
+        case 64: return 0;
+        case 128: return 1;
+        case 256: return 2;
+        case 384: return 3;
+        case 512: return 4;
+        case 768: return 5;
+        case 1024: return 6;
+        case 2048: return 7;
+        default: return -1;
+    }
+}
+
+// Times one slice step (the slice loop's row pass then its column pass) of
+// `batch` synthetic waves of side n for every pair of pass families, `reps`
+// steps after one warm-up step, with events on the context's stream; keeps the
+// fastest pair as the device's schedule for side n.  ms[rf * 3 + cf] receives
+// the time per step of each pair.
+int tune_side(msl_ctx *c, int n, int batch, int reps, int *best_r, int *best_c, double *ms) {
+    const size_t n2 = (size_t)n * n;
+    if (c->mem.limit) {
+        const size_t cap = c->mem.limit / 4 / (sizeof(float2) * n2);
+        if ((size_t)batch > cap) batch = (int)std::max<size_t>(1, cap);
+    }
+    CUDA_TRY(c, c->wave.ensure(sizeof(float2) * n2 * batch));
+    CUDA_TRY(c, c->trans_stage.ensure(sizeof(float2) * n2));
+    CUDA_TRY(c, cudaMemsetAsync(c->wave.p, 0, sizeof(float2) * n2 * batch, c->stream));
+    CUDA_TRY(c, cudaMemsetAsync(c->trans_stage.p, 0, sizeof(float2) * n2, c->stream));
+    msl_grid g = {n, n, 0.1 * n, 0.1 * n};
+    msl_optics o = {200.0, 2.0 / 3.0, 0.0, 0.0, 0};
+    const double dz = 1.5;
+    SliceTables st;
+    int rc;
+    if ((rc = build_slice_tables(c, &g, &o, 1, &dz, st))) return rc;
+    float2 *tw = twiddles(c, n);
+    if (!tw) return fail(c, MSL_E_NOMEM, "twiddle table allocation failed");
+    float2 *w = (float2 *)c->wave.p;
+    const float2 *t = (const float2 *)c->trans_stage.p;
+    cudaEvent_t e0 = take_event(c), e1 = take_event(c);
+    int prev_r = 0, prev_c = 0;
+    msl::get_schedule(n, &prev_r, &prev_c);
+    double best = 1e300;
+    *best_r = prev_r;
+    *best_c = prev_c;
+    for (int rf = 0; rf < msl::FAM_COUNT; ++rf)
+        for (int cf = 0; cf < msl::FAM_COUNT; ++cf) {
+            msl::set_schedule(n, rf, cf);
+            auto step = [&]() -> cudaError_t {
+                RowArgs r = row_args(&g, tw, t, w, batch, msl::ROW_LOAD | msl::ROW_INV | msl::ROW_TRANS | msl::ROW_FWD,
+                                     c->dflag);
+                cudaError_t e = msl::launch_row_pass(n, r, c->stream, c->nsm, &c->launches);
+                if (e != cudaSuccess) return e;
+                ColArgs ca = col_args(&g, st, tw, 0, w, batch,
+                                      msl::COL_LOAD | msl::COL_FWD | msl::COL_PROP | msl::COL_INV | msl::COL_STORE,
+                                      c->dflag);
+                return msl::launch_col_pass(n, ca, c->stream, c->nsm, &c->launches);
+            };
+            cudaError_t e = step();
+            if (e == cudaSuccess) e = cudaEventRecord(e0, c->stream);
+            for (int i = 0; i < reps && e == cudaSuccess; ++i) e = step();
+            if (e == cudaSuccess) e = cudaEventRecord(e1, c->stream);
+            if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+            float t_ms = 0.f;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&t_ms, e0, e1);
+            if (e != cudaSuccess) {
+                msl::set_schedule(n, prev_r, prev_c);
+                c->ev_free.push_back(e0);
+                c->ev_free.push_back(e1);
+                return fail(c, MSL_E_CUDA, std::string("autotune: ") + cudaGetErrorString(e));
+            }
+            const double per = (double)t_ms / reps;
+            if (ms) ms[rf * msl::FAM_COUNT + cf] = per;
+            if (per < best) {
+                best = per;
+                *best_r = rf;
+                *best_c = cf;
+            }
+        }
+    c->ev_free.push_back(e0);
+    c->ev_free.push_back(e1);
+    msl::set_schedule(n, *best_r, *best_c);
+    if ((rc = err_check(c))) return rc;
+    return MSL_OK;
+}
+
+// First use of side n on this device with autotuning on: tune it once.
+int maybe_tune(msl_ctx *c, int n) {
+    if (!c->autotune) return MSL_OK;
+    const int b = side_bit(n);
+    if (b < 0 || c->device < 0 || c->device >= 64) return MSL_OK;
+    if (g_tuned[c->device].load() & (1u << b)) return MSL_OK;
+    int rf, cf;
+    const int batch = (int)std::max<size_t>(1, ((size_t)256 << 20) / (sizeof(float2) * (size_t)n * n));
+    int rc = err_reset(c);
+    if (rc) return rc;
+    if ((rc = tune_side(c, n, batch, 3, &rf, &cf, nullptr))) return rc;
+    g_tuned[c->device].fetch_or(1u << b);
+    return MSL_OK;
 }
 
 }  // namespace
@@ -1030,6 +1141,43 @@ int msl_memory_in_use(msl_ctx *c, size_t *bytes) {
     return MSL_OK;
 }
 
+int msl_autotune(msl_ctx *c, int side, int batch, int reps, int *row_family, int *col_family, double *ms) {
+    if (!c) return MSL_E_ARG;
+    if (!msl::plan_supported(side)) return fail(c, MSL_E_UNSUPPORTED, "side not supported");
+    if (batch < 1 || reps < 1) return fail(c, MSL_E_ARG, "batch and reps must be >= 1");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    int rc = err_reset(c);
+    if (rc) return rc;
+    int rf = 0, cf = 0;
+    if ((rc = tune_side(c, side, batch, reps, &rf, &cf, ms))) return rc;
+    if (c->device >= 0 && c->device < 64) g_tuned[c->device].fetch_or(1u << side_bit(side));
+    if (row_family) *row_family = rf;
+    if (col_family) *col_family = cf;
+    return MSL_OK;
+}
+
+int msl_set_schedule(msl_ctx *c, int side, int row_family, int col_family) {
+    if (!c) return MSL_E_ARG;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    if (!msl::set_schedule(side, row_family, col_family))
+        return fail(c, MSL_E_ARG, "unknown side or pass family (0 fast, 1 TMA, 2 register)");
+    if (c->device >= 0 && c->device < 64) g_tuned[c->device].fetch_or(1u << side_bit(side));
+    return MSL_OK;
+}
+
+int msl_get_schedule(msl_ctx *c, int side, int *row_family, int *col_family) {
+    if (!c || !row_family || !col_family) return MSL_E_ARG;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    if (!msl::get_schedule(side, row_family, col_family)) return fail(c, MSL_E_ARG, "unknown side");
+    return MSL_OK;
+}
+
+int msl_set_autotune(msl_ctx *c, int on) {
+    if (!c) return MSL_E_ARG;
+    c->autotune = on != 0;
+    return MSL_OK;
+}
+
 int msl_set_probe_batch(msl_ctx *c, int batch) {
     if (!c || batch < 0) return fail(c, MSL_E_ARG, "probe batch must be >= 0");
     c->probe_batch = batch;
@@ -1332,6 +1480,7 @@ int msl_multislice(msl_ctx *c, const msl_grid *g, const msl_optics *o, const flo
     if ((rc = check_layers(c, ntrans, dz, layer_seq, nslice))) return rc;
     if (!trans || !psi || batch < 1) return fail(c, MSL_E_ARG, "trans/psi null or batch < 1");
     CUDA_TRY(c, cudaSetDevice(c->device));
+    if ((rc = maybe_tune(c, g->nx)) || (g->ny != g->nx && (rc = maybe_tune(c, g->ny)))) return rc;
     if ((rc = err_reset(c))) return rc;
     const int nx = g->nx, ny = g->ny;
     const size_t n2 = (size_t)nx * ny;
@@ -1399,6 +1548,7 @@ int msl_stem_scan(msl_ctx *c, const msl_grid *g, const msl_optics *o, const floa
     for (int p = 0; p < 2 * nprobe; ++p)
         if (!is_fin(probe_xy[p])) return fail(c, MSL_E_ARG, "probe positions must be finite");
     CUDA_TRY(c, cudaSetDevice(c->device));
+    if ((rc = maybe_tune(c, g->nx)) || (g->ny != g->nx && (rc = maybe_tune(c, g->ny)))) return rc;
     if ((rc = err_reset(c))) return rc;
     const int nx = g->nx, ny = g->ny, ndet = det->ndet;
     const size_t n2 = (size_t)nx * ny;

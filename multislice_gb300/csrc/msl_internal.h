@@ -124,6 +124,10 @@ struct PotArgs {
 };
 
 bool plan_supported(int n);
+// Kernel families of a side's passes (the autotuner's choices), per device.
+enum PassFamily { FAM_FAST = 0, FAM_TMA = 1, FAM_REG = 2, FAM_COUNT = 3 };
+bool set_schedule(int n, int row_family, int col_family);
+bool get_schedule(int n, int *row_family, int *col_family);
 // Entries the twiddle buffer of side n needs (0: the plan's own tables only) and
 // the tables appended for the two-stage row kernels, written into `tables`
 // (which holds at least that many entries).

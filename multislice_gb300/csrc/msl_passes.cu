@@ -10,6 +10,7 @@
 // probe-slice), and every pointwise step of the reference runs in registers
 // between two line transforms.  Kirkland's 1/(nx ny) ifft scale rides in py.
 #include <cuda_runtime.h>
+#include <atomic>
 #include <type_traits>
 #include <math.h>
 #include <stdint.h>
@@ -1510,6 +1511,65 @@ static bool row_warp_eligible(int ny, const RowArgs &a) {
     return true;
 }
 
+// ------------------------------------------------------------- schedules
+// Which kernel family each side's row and column passes take, per device: the
+// fast family (the warp-owned / two-stage / warp-pair kernels), the TMA-tiled
+// kernels, or the register-only kernels.  Set by the autotuner
+// (msl_autotune) or by hand (msl_set_schedule); all families compute the same
+// transforms (the pass-family tests check each against the oracle).
+namespace {
+std::atomic<int> g_sched_row[kMaxDevices][8];
+std::atomic<int> g_sched_col[kMaxDevices][8];
+
+int side_slot(int n) {
+    switch (n) {
+        case 64: return 0;
+        case 128: return 1;
+        case 256: return 2;
+        case 384: return 3;
+        case 512: return 4;
+        case 768: return 5;
+        case 1024: return 6;
+        case 2048: return 7;
+        default: return -1;
+    }
+}
+
+int current_device() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+        cudaGetLastError();
+        return 0;
+    }
+    return dev;
+}
+
+int sched_row(int n) {
+    const int k = side_slot(n);
+    return k < 0 ? FAM_FAST : g_sched_row[current_device()][k].load(std::memory_order_relaxed);
+}
+int sched_col(int n) {
+    const int k = side_slot(n);
+    return k < 0 ? FAM_FAST : g_sched_col[current_device()][k].load(std::memory_order_relaxed);
+}
+}  // namespace
+
+bool set_schedule(int n, int row_family, int col_family) {
+    const int k = side_slot(n);
+    if (k < 0 || row_family < 0 || row_family >= FAM_COUNT || col_family < 0 || col_family >= FAM_COUNT) return false;
+    const int dev = current_device();
+    g_sched_row[dev][k].store(row_family);
+    g_sched_col[dev][k].store(col_family);
+    return true;
+}
+
+bool get_schedule(int n, int *row_family, int *col_family) {
+    if (side_slot(n) < 0) return false;
+    *row_family = sched_row(n);
+    *col_family = sched_col(n);
+    return true;
+}
+
 bool plan_supported(int n) {
     switch (n) {
 #define X(N) case N:
@@ -1530,12 +1590,13 @@ int plan_col_c(int n) {
 }
 
 int plan_col_c_launch(int n, const ColArgs &a) {
-    if (tma_eligible(a)) {
+    const int fam = sched_col(n);
+    if (fam != FAM_REG && tma_eligible(a)) {
         // the slice loop's column pass (load, forward, inverse) on two-stage
         // columns writes detector partials per 4 columns
         ColArgs f = a;
         f.flags = (f.flags | COL_LOAD | COL_FWD) & ~COL_PROBE;
-        if (col_half_side(n, f)) return 4;
+        if (fam == FAM_FAST && col_half_side(n, f)) return 4;
         switch (n) {
 #define X(N) case N: return ColPlan<N>::col_c;
             MSL_FOR_EACH_SIDE(X)
@@ -1618,7 +1679,8 @@ void append_row_two_twiddles(int n, float2 *tables) {
 
 cudaError_t launch_row_pass(int ny, const RowArgs &a, cudaStream_t s, int nsm, int64_t *launches) {
     ++*launches;
-    if (row_warp_eligible(ny, a)) {
+    const int fam = sched_row(ny);
+    if (fam == FAM_FAST && row_warp_eligible(ny, a)) {
         switch (ny) {
             case 256:
                 if (a.nlines % 2 == 0 && !(((uintptr_t)a.out | (uintptr_t)a.in) & 15u))
@@ -1637,7 +1699,7 @@ cudaError_t launch_row_pass(int ny, const RowArgs &a, cudaStream_t s, int nsm, i
             default: break;
         }
     }
-    if (row_tma_eligible(a)) {
+    if (fam != FAM_REG && row_tma_eligible(a)) {
         switch (ny) {
 #define X(N) case N: return row_tma_launch<N>(a, s, nsm);
             MSL_FOR_EACH_SIDE(X)
@@ -1655,9 +1717,10 @@ cudaError_t launch_row_pass(int ny, const RowArgs &a, cudaStream_t s, int nsm, i
 
 cudaError_t launch_col_pass(int nx, const ColArgs &a, cudaStream_t s, int nsm, int64_t *launches) {
     ++*launches;
-    if (tma_eligible(a)) {
+    const int fam = sched_col(nx);
+    if (fam != FAM_REG && tma_eligible(a)) {
         // the slice loop's passes at 256, 512 and 1024: two-stage columns
-        switch (col_half_side(nx, a)) {
+        switch (fam == FAM_FAST ? col_half_side(nx, a) : 0) {
             case 256: return col_half_launch<ColHalfL256>(a, s, nsm);
             case 512: return col_half_launch<ColHalfL512>(a, s, nsm);
             case 1024: return col_half_launch<ColPairL1024>(a, s, nsm);
