@@ -339,6 +339,20 @@ int msl_stem_scan_closure(msl_ctx *ctx, msl_closure *net, const msl_grid *grid, 
                           const msl_probe *probe, const double *probe_xy, int nprobe, const msl_detectors *det,
                           double *det_out);
 
+/* msl_stem_scan with every probe's wave kept on chip across all slices
+ * (arguments, outputs and conventions as msl_stem_scan): one 8-CTA thread-block
+ * cluster per probe holds the 256 x 256 wave in its shared memory (32 rows per
+ * CTA); row transforms run in place, column transforms gather and scatter
+ * through distributed shared memory, so HBM sees the probe once and the
+ * transmission rows, not the wave every slice.  Built for 256^2 grids (the
+ * 512^2 wave and its exchange space exceed a 16-CTA cluster's shared memory);
+ * other sides return MSL_E_UNSUPPORTED.  The reference's scan is serial over
+ * probes (MSProjectReuse.cs:254-347). */
+int msl_stem_scan_resident(msl_ctx *ctx, const msl_grid *grid, const msl_optics *optics, const float *trans,
+                           int ntrans, const double *dz, const int *layer_seq, int nslice, const msl_probe *probe,
+                           const double *probe_xy, int nprobe, const msl_detectors *det, const int *checkpoints,
+                           int ncheck, double *det_out);
+
 /* ------------------------------------------------------- uneven batches */
 
 #define MSL_PLANE_WAVE 0

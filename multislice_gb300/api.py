@@ -368,8 +368,9 @@ class Context:
     # ------------------------------------------------------------------ STEM
     def stem_scan(self, trans, dz, layer_seq, ax, by, kev, k_ap, probe_xy, det_k,
                   checkpoints=None, df=0.0, cs=0.0, k_ap_in=0.0, bandlimit=2.0 / 3.0,
-                  f32_prop_args=False, out=None):
-        """Annular detector sums, float64 [nprobe, ncheck, ndet] (reference scale)."""
+                  f32_prop_args=False, out=None, resident=False):
+        """Annular detector sums, float64 [nprobe, ncheck, ndet] (reference scale).
+        resident=True runs the on-chip slice loop (msl_stem_scan_resident, 256^2)."""
         trans = _as(trans, np.complex64)
         nt, nx, ny = _cshape(trans)
         dz = np.ascontiguousarray(np.broadcast_to(np.asarray(dz, np.float64), (nt,)))
@@ -387,7 +388,8 @@ class Context:
         o = self._optics(kev, bandlimit, (0.0, 0.0), f32_prop_args)
         if out is None:
             out = np.empty((len(xy), len(cps), len(det)), np.float64)
-        self._check(self._lib.msl_stem_scan(self._h, ctypes.byref(g), ctypes.byref(o),
+        fn = self._lib.msl_stem_scan_resident if resident else self._lib.msl_stem_scan
+        self._check(fn(self._h, ctypes.byref(g), ctypes.byref(o),
                                             _ptr(trans, np.complex64), nt, _ptr(dz, np.float64),
                                             _ptr(seq, np.int32), len(seq), ctypes.byref(pr),
                                             _ptr(xy, np.float64), len(xy), ctypes.byref(dets),

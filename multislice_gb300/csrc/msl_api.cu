@@ -2051,6 +2051,94 @@ int msl_stem_scan_closure(msl_ctx *c, msl_closure *n, const msl_grid *g, const m
     return err_check(c);
 }
 
+int msl_stem_scan_resident(msl_ctx *c, const msl_grid *g, const msl_optics *o, const float *trans, int ntrans,
+                           const double *dz, const int *layer_seq, int nslice, const msl_probe *pr,
+                           const double *probe_xy, int nprobe, const msl_detectors *det, const int *checkpoints,
+                           int ncheck, double *det_out) {
+    if (!c) return MSL_E_ARG;
+    int rc = exit_scan_check(c, g, o, trans, ntrans, dz, layer_seq, nslice, pr, probe_xy, nprobe);
+    if (rc) return rc;
+    const int side = msl::resident_side();
+    if (g->nx != side || g->ny != side)
+        return fail(c, MSL_E_UNSUPPORTED, "the resident slice loop is built for " + std::to_string(side) + "^2 grids");
+    if (!det || !det_out || !checkpoints || det->ndet < 1 || det->ndet > MSL_MAX_DETECTORS || !det->k_in || !det->k_out)
+        return fail(c, MSL_E_ARG, "1..8 detectors with k_in/k_out arrays, checkpoints and det_out are required");
+    for (int d = 0; d < det->ndet; ++d)
+        if (!(det->k_in[d] >= 0) || !(det->k_out[d] >= det->k_in[d]) || !is_fin(det->k_out[d]))
+            return fail(c, MSL_E_ARG, "detector bounds must satisfy 0 <= k_in <= k_out");
+    if (ncheck < 1) return fail(c, MSL_E_ARG, "ncheck must be >= 1");
+    for (int i = 0; i < ncheck; ++i)
+        if (checkpoints[i] < 0 || checkpoints[i] >= nslice || (i > 0 && checkpoints[i] <= checkpoints[i - 1]))
+            return fail(c, MSL_E_ARG, "checkpoints must be ascending slice indices in [0, nslice)");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    if ((rc = err_reset(c))) return rc;
+    const int ndet = det->ndet, ncl = msl::resident_cluster();
+    const size_t n2 = (size_t)side * side;
+    ExitScan X;
+    if ((rc = exit_scan_setup(c, g, o, trans, ntrans, dz, pr, det, nprobe, (size_t)nprobe, X))) return rc;
+    // device copies of the slice sequence and checkpoints
+    std::vector<int> seqc(nslice + ncheck);
+    for (int s2 = 0; s2 < nslice; ++s2) seqc[s2] = layer_seq[s2];
+    for (int i = 0; i < ncheck; ++i) seqc[nslice + i] = checkpoints[i];
+    if ((rc = upload(c, c->jobtab, seqc.data(), sizeof(int) * seqc.size()))) return rc;
+    const int *dseq = (const int *)c->jobtab.p;
+    CUDA_TRY(c, c->partial.ensure(sizeof(double) * (size_t)ncheck * X.B * ncl * ndet));
+    double *partial = (double *)c->partial.p;
+    const size_t obytes = sizeof(double) * (size_t)nprobe * ncheck * ndet;
+    const bool odev = on_device(det_out);
+    double *od;
+    if (odev) {
+        od = det_out;
+    } else {
+        CUDA_TRY(c, c->detout.ensure(obytes));
+        od = (double *)c->detout.p;
+    }
+    const double dscale = (double)n2 * (double)n2;
+    std::vector<double> hf(2 * (size_t)X.B);
+    for (int p0 = 0; p0 < nprobe; p0 += X.B) {
+        const int nb = std::min(X.B, nprobe - p0);
+        for (int b = 0; b < nb; ++b) {
+            hf[2 * b] = probe_xy[2 * (p0 + b)] / g->ax;
+            hf[2 * b + 1] = probe_xy[2 * (p0 + b) + 1] / g->by;
+        }
+        CUDA_TRY(c, cudaMemcpyAsync(X.fxy, hf.data(), sizeof(double) * 2 * nb, cudaMemcpyHostToDevice, c->stream));
+        LAUNCH_TRY(c, timed(c, MSL_PROF_OTHER, [&] {
+                       return msl::launch_probe_shifts(side, side, nb, X.fxy, X.ex, X.ey, c->stream, &c->launches);
+                   }));
+        ColArgs pa = col_args(g, X.st, X.twc, 0, X.w, nb, msl::COL_PROBE | msl::COL_INV | msl::COL_STORE, c->dflag);
+        pa.apchi = X.apchi;
+        pa.ex = X.ex;
+        pa.ey = X.ey;
+        LAUNCH_TRY(c, timed(c, MSL_PROF_COL, [&] { return msl::launch_col_pass(side, pa, c->stream, c->nsm, &c->launches); }));
+        msl::ResidentArgs ra;
+        ra.w0 = X.w;
+        ra.trans = X.td;
+        ra.prop = X.st.d_prop;
+        ra.kx2 = X.st.d_kx2;
+        ra.ky2 = X.st.d_ky2;
+        ra.k2max = X.st.k2max;
+        ra.mask = X.mask;
+        ra.ndet = ndet;
+        ra.layer_seq = dseq;
+        ra.nslice = nslice;
+        ra.checkpoints = dseq + nslice;
+        ra.ncheck = ncheck;
+        ra.partial = partial;
+        ra.nprobe = nb;
+        LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_stem_resident(ra, c->stream, c->nsm, &c->launches); }));
+        for (int ic = 0; ic < ncheck; ++ic)
+            LAUNCH_TRY(c, timed(c, MSL_PROF_OTHER, [&] {
+                           return msl::launch_detector_finalize(nb, ncl, ndet, partial + (size_t)ic * nb * ncl * ndet,
+                                                                dscale, od + ((size_t)p0 * ncheck + ic) * ndet,
+                                                                ncheck * ndet, c->stream, &c->launches);
+                       }));
+    }
+    if (!odev) CUDA_TRY(c, cudaMemcpyAsync(det_out, od, obytes, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    collect_profile(c);
+    return err_check(c);
+}
+
 int msl_stem_scan_phonon(msl_ctx *c, const msl_atoms *at, const double *fparams, const msl_grid *g,
                          int nslice, double radius, const msl_optics *o, const msl_probe *pr,
                          const double *probe_xy, int nprobe, const msl_detectors *det,

@@ -196,6 +196,28 @@ cudaError_t launch_detector_accumulate(int nconf, int np, int ntile, int ndet, c
 // 16 <= N <= 256, N % 16 == 0.  *err is raised if an MMA completion wait gives up.
 cudaError_t launch_tc_gemm(const void *A, const void *B, float *D, int M, int N, int K, int *err,
                            cudaStream_t s, int64_t *launches);
+// ------------------------------------------ on-chip STEM slice loop (msl_resident.cu)
+// One 8-CTA cluster per probe, the 256^2 wave resident in the cluster's shared
+// memory across slices.  All pointers are device pointers.
+struct ResidentArgs {
+    const float2 *w0;          // [nprobe][256][256] entrance waves (after the probe's x inverse)
+    const float2 *trans;       // [ntrans][256][256]
+    const float2 *prop;        // [ntrans][px 256 | py 256]
+    const float *kx2, *ky2;    // float k^2 tables
+    float k2max;
+    const uint8_t *mask;       // [256][256] detector bits
+    int ndet;
+    const int *layer_seq;      // [nslice]
+    int nslice;
+    const int *checkpoints;    // [ncheck] ascending slice indices
+    int ncheck;
+    double *partial;           // [ncheck][nprobe][8][ndet]
+    int nprobe;
+};
+cudaError_t launch_stem_resident(const ResidentArgs &a, cudaStream_t s, int nsm, int64_t *launches);
+int resident_side();
+int resident_cluster();
+
 // ------------------------------------------------- learned closure (msl_closure.cu)
 // The network's parameters, Adam state and work buffers on one device.
 struct ClosureNet {
