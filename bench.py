@@ -348,6 +348,56 @@ def _time(fn, steps):
     return (time.perf_counter() - t0) / steps
 
 
+def resident_compare(ctx, cfg, side_probes, steps, which=("streaming", "resident")):
+    """The on-chip slice loop against the streaming passes on SrTiO3 at 256^2
+    (4 x 4 x 50 cells, the 512^2 scan's 0.061 A pixels), side_probes^2 probes
+    x 100 slices."""
+    import torch
+
+    from multislice_gb300 import specimen as S
+    from oracle import msl_oracle as O
+    dev = torch.device("cuda", torch.cuda.current_device())
+    names = ("HAADF", "ABF")
+    a = 3.905
+    spec2 = S.srtio3(4, 4, 50, a)
+    v = torch.empty((NSLICE, 256, 256), dtype=torch.float32, device=dev)
+    ctx.potential(spec2, 256, 256, NSLICE, cfg["radius"], out=v)
+    t2 = torch.empty((NSLICE, 256, 256, 2), dtype=torch.float32, device=dev)
+    ctx.transmission(v, spec2.ax, spec2.by, 200.0, out=t2)
+    del v
+    xy2 = S.raster(1.5 * a, 2.5 * a, 1.5 * a, 2.5 * a, side_probes, side_probes)
+    outs = {k: torch.empty((len(xy2), 1, 2), dtype=torch.float64, device=dev) for k in which}
+    args2 = (t2, spec2.cz / NSLICE, np.arange(NSLICE), spec2.ax, spec2.by, 200.0, cfg["k_ap"], xy2, cfg["det_k"])
+    units = len(xy2) * NSLICE
+    res = {"workload": f"SrTiO3 [001] 4x4x50 cells, 256x256 (0.061 A pixels), 100 slices, {len(xy2)} probes",
+           "unit": UNIT}
+    for k in which:
+        el = _time(lambda: ctx.stem_scan(*args2, out=outs[k], resident=(k == "resident")), steps)
+        res[k] = units / el
+    if len(which) == 2:
+        rs, rr = outs["streaming"].cpu().numpy(), outs["resident"].cpu().numpy()
+        res["resident_over_streaming"] = res["resident"] / res["streaming"]
+        res["hbm_bytes_per_probe_slice"] = {"streaming": 32 * 256 * 256,
+                                            "resident": "transmission rows only (8 N^2 per slice per cluster, "
+                                                        "shared through L2)"}
+        res["rel_l2_resident_vs_streaming"] = {n: O.rel_l2(rr[:, 0, k], rs[:, 0, k]) for k, n in enumerate(names)}
+    del t2
+    torch.cuda.empty_cache()
+    return res
+
+
+def run_resident(args):
+    """--resident: the 256^2 on-chip vs streaming comparison alone (one JSON line)."""
+    import torch
+
+    from multislice_gb300 import Context
+    torch.cuda.set_device(0)
+    side = max(1, int(round(args.probes ** 0.5)))
+    with Context(0) as ctx:
+        which = ("resident",) if args.resident_only else ("streaming", "resident")
+        print(json.dumps(resident_compare(ctx, workload(), side, max(1, args.steps), which)), flush=True)
+
+
 def run_variants(ctx, cfg, xy, plain, ref64, args):
     """The other forms of the scan, timed after the headline (not part of `value`):
     * closure: 25 slices 4x thicker + the learned closure, as fine-slice-equivalent
@@ -403,30 +453,7 @@ def run_variants(ctx, cfg, xy, plain, ref64, args):
         del tc_
         torch.cuda.empty_cache()
     # ---- on-chip slice loop at 256^2
-    a = 3.905
-    spec2 = S.srtio3(4, 4, 50, a)
-    v = torch.empty((NSLICE, 256, 256), dtype=torch.float32, device=dev)
-    ctx.potential(spec2, 256, 256, NSLICE, cfg["radius"], out=v)
-    t2 = torch.empty((NSLICE, 256, 256, 2), dtype=torch.float32, device=dev)
-    ctx.transmission(v, spec2.ax, spec2.by, 200.0, out=t2)
-    del v
-    xy2 = S.raster(1.5 * a, 2.5 * a, 1.5 * a, 2.5 * a, 64, 64)
-    o_s = torch.empty((len(xy2), 1, 2), dtype=torch.float64, device=dev)
-    o_r = torch.empty_like(o_s)
-    args2 = (t2, spec2.cz / NSLICE, np.arange(NSLICE), spec2.ax, spec2.by, 200.0, cfg["k_ap"], xy2, cfg["det_k"])
-    ts = _time(lambda: ctx.stem_scan(*args2, out=o_s), max(1, args.steps))
-    tr = _time(lambda: ctx.stem_scan(*args2, out=o_r, resident=True), max(1, args.steps))
-    rs, rr = o_s.cpu().numpy(), o_r.cpu().numpy()
-    units = len(xy2) * NSLICE
-    out["resident_256"] = {
-        "workload": "SrTiO3 [001] 4x4x50 cells, 256x256 (0.061 A pixels), 100 slices, 4096 probes",
-        "streaming": units / ts, "resident": units / tr, "unit": UNIT, "resident_over_streaming": ts / tr,
-        "hbm_bytes_per_probe_slice": {"streaming": 32 * 256 * 256,
-                                      "resident": "transmission rows only (8 N^2 per slice per cluster, "
-                                                  "shared through L2)"},
-        "rel_l2_resident_vs_streaming": {n: O.rel_l2(rr[:, 0, k], rs[:, 0, k]) for k, n in enumerate(names)}}
-    del t2, o_s, o_r
-    torch.cuda.empty_cache()
+    out["resident_256"] = resident_compare(ctx, cfg, 64, max(1, args.steps))
     # ---- autotuner at 512
     rf, cf, ms = ctx.autotune(512, 128, reps=2)
     fam = ("fast", "tma", "register")
@@ -547,6 +574,9 @@ def main():
                     help="probes of the 64x64 raster per GPU (smaller cases are for profiling)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 accuracy check of every probe")
+    ap.add_argument("--resident", action="store_true",
+                    help="time the on-chip slice loop against the streaming passes at 256^2 (--probes probes)")
+    ap.add_argument("--resident-only", action="store_true", help="with --resident: the on-chip loop alone")
     ap.add_argument("--no-variants", action="store_true",
                     help="skip the closure, on-chip and autotuner forms reported beside the headline")
     ap.add_argument("--batch", type=int, default=0, help="probes per launch (0: library default)")
@@ -555,7 +585,9 @@ def main():
     ap.add_argument("--frozen-phonon", action="store_true",
                     help="time the Au 2048^2, 32-configuration frozen-phonon image instead of the scan")
     args = ap.parse_args()
-    if args.sides:
+    if args.resident:
+        run_resident(args)
+    elif args.sides:
         run_sides(args)
     elif args.frozen_phonon:
         run_frozen_phonon(args)

@@ -407,6 +407,14 @@ int msl_check_wait_timeout(msl_ctx *ctx, uint32_t polls);
 #define MSL_FAM_FAST 0
 #define MSL_FAM_TMA 1
 #define MSL_FAM_REG 2
+/* The tensor-core form of the slice loop's passes (sides 256 and 512): every
+ * line DFT as two dense contractions (four-step, 16 x N/16) on tcgen05 with
+ * split-bf16 products (hi + lo per operand, three products, FP32 accumulate),
+ * twiddles, transmission, propagator and detector sums as in the FP32 passes.
+ * Set with msl_set_schedule only (the autotuner times the FP32 families); the
+ * other passes of the side (probe formation, the plane-wave first slice, the
+ * closing inverse) keep MSL_FAM_FAST. */
+#define MSL_FAM_TC 3
 int msl_autotune(msl_ctx *ctx, int side, int batch, int reps, int *row_family, int *col_family, double *ms);
 int msl_set_schedule(msl_ctx *ctx, int side, int row_family, int col_family);
 int msl_get_schedule(msl_ctx *ctx, int side, int *row_family, int *col_family);

@@ -117,7 +117,7 @@ class Context:
     def set_probe_batch(self, batch):
         self._check(self._lib.msl_set_probe_batch(self._h, int(batch)))
 
-    FAMILIES = ("fast", "tma", "register")
+    FAMILIES = ("fast", "tma", "register", "tensor-core")
 
     def autotune(self, side, batch, reps=3):
         """Time every pair of pass families at `side` and keep the fastest;

@@ -17,7 +17,7 @@ BUILD = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-Xptxas", "-warn-spills"]
-SOURCES = ["msl_passes.cu", "msl_potential.cu", "msl_api.cu", "msl_noalloc.cu", "msl_muslib.cu", "msl_tc.cu", "msl_closure.cu", "msl_resident.cu"]
+SOURCES = ["msl_passes.cu", "msl_potential.cu", "msl_api.cu", "msl_noalloc.cu", "msl_muslib.cu", "msl_tc.cu", "msl_closure.cu", "msl_resident.cu", "msl_tcfft.cu"]
 
 
 def nvcc():

@@ -125,7 +125,10 @@ struct PotArgs {
 
 bool plan_supported(int n);
 // Kernel families of a side's passes (the autotuner's choices), per device.
-enum PassFamily { FAM_FAST = 0, FAM_TMA = 1, FAM_REG = 2, FAM_COUNT = 3 };
+// FAM_TC: line DFTs as split-bf16 contractions on the tensor cores (msl_tcfft.cu;
+// sides 256 and 512, the slice loop's passes; other passes of the side keep FAM_FAST);
+// chosen by hand, not by the autotuner (it changes the arithmetic, not only the speed).
+enum PassFamily { FAM_FAST = 0, FAM_TMA = 1, FAM_REG = 2, FAM_COUNT = 3, FAM_TC = 3 };
 bool set_schedule(int n, int row_family, int col_family);
 bool get_schedule(int n, int *row_family, int *col_family);
 // Entries the twiddle buffer of side n needs (0: the plan's own tables only) and
@@ -196,6 +199,30 @@ cudaError_t launch_detector_accumulate(int nconf, int np, int ntile, int ndet, c
 // 16 <= N <= 256, N % 16 == 0.  *err is raised if an MMA completion wait gives up.
 cudaError_t launch_tc_gemm(const void *A, const void *B, float *D, int M, int N, int K, int *err,
                            cudaStream_t s, int64_t *launches);
+// ------------------------------------------------ tensor-core line DFTs (msl_tcfft.cu)
+enum TcMode { TC_MODE_NONE = 0, TC_MODE_TRANS = 1, TC_MODE_PROP = 2 };
+struct TcPassArgs {
+    float2 *data;               // waves [images][nx][ny], in place
+    int nlines;                 // rows: images * nx; columns: images * ny (multiple of 8)
+    int nx, ny;
+    int cols;                   // 0: row lines (along iy), 1: column lines (along ix)
+    int dir1, dir2;             // signs of the first and second transform
+    int second;                 // 0: stop after the pointwise step (detection only)
+    int mode;                   // TcMode pointwise step between the transforms
+    const float2 *trans;        // TC_MODE_TRANS: [nx][ny] of the layer
+    const float2 *const *trans_b;  // or per-image pointers
+    const float2 *px, *py;      // TC_MODE_PROP
+    const float *kx2, *ky2;
+    float k2max;
+    const uint8_t *detmask;     // column passes: detector bits [nx][ny] (null: none)
+    int ndet;
+    double *partial;            // [images][ny / 8][ndet]
+    int *err;
+};
+bool tc_side(int n);
+int tc_col_tile();
+cudaError_t launch_tc_pass(const TcPassArgs &a, cudaStream_t s, int nsm, int64_t *launches);
+
 // ------------------------------------------ on-chip STEM slice loop (msl_resident.cu)
 // One 8-CTA cluster per probe, the 256^2 wave resident in the cluster's shared
 // memory across slices.  All pointers are device pointers.

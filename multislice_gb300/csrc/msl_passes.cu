@@ -1556,7 +1556,8 @@ int sched_col(int n) {
 
 bool set_schedule(int n, int row_family, int col_family) {
     const int k = side_slot(n);
-    if (k < 0 || row_family < 0 || row_family >= FAM_COUNT || col_family < 0 || col_family >= FAM_COUNT) return false;
+    if (k < 0 || row_family < 0 || row_family > FAM_TC || col_family < 0 || col_family > FAM_TC) return false;
+    if ((row_family == FAM_TC || col_family == FAM_TC) && !tc_side(n)) return false;
     const int dev = current_device();
     g_sched_row[dev][k].store(row_family);
     g_sched_col[dev][k].store(col_family);
@@ -1589,8 +1590,18 @@ int plan_col_c(int n) {
     }
 }
 
+static bool col_tc_eligible(int nx, const ColArgs &a);
+
 int plan_col_c_launch(int n, const ColArgs &a) {
-    const int fam = sched_col(n);
+    const int fam0 = sched_col(n);
+    if (fam0 == FAM_TC) {
+        // the slice loop's column passes (loaded, forward) run on the tensor cores in tiles of 8 columns
+        ColArgs f = a;
+        f.flags = COL_LOAD | COL_FWD | COL_PROP;
+        f.in = f.out;
+        if (col_tc_eligible(n, f)) return tc_col_tile();
+    }
+    const int fam = fam0 == FAM_TC ? FAM_FAST : fam0;
     if (fam != FAM_REG && tma_eligible(a)) {
         // the slice loop's column pass (load, forward, inverse) on two-stage
         // columns writes detector partials per 4 columns
@@ -1677,9 +1688,66 @@ void append_row_two_twiddles(int n, float2 *tables) {
         }
 }
 
+// The slice loop's row pass (load, inverse, * t, forward, store) on the tensor cores.
+static bool row_tc_eligible(int ny, const RowArgs &a) {
+    const int need = ROW_LOAD | ROW_INV | ROW_TRANS | ROW_FWD;
+    return tc_side(ny) && (a.flags & ~need) == 0 && a.flags == need && a.in == a.out && a.scale == 1.0f &&
+           a.nlines % tc_col_tile() == 0 && a.nx % tc_col_tile() == 0;
+}
+// The slice loop's column pass (load, forward, propagator, [detect], [inverse, store]).
+static bool col_tc_eligible(int nx, const ColArgs &a) {
+    const int base = COL_LOAD | COL_FWD | COL_PROP;
+    const int rest = a.flags & ~(base | COL_DETECT);
+    if (!tc_side(nx) || (a.flags & base) != base || a.in != a.out || a.prop_b || a.k2_b) return false;
+    if (rest != 0 && rest != (COL_INV | COL_STORE)) return false;
+    return a.ny % tc_col_tile() == 0;
+}
+static TcPassArgs tc_row_args(int ny, const RowArgs &a) {
+    TcPassArgs t = {};
+    t.data = a.out;
+    t.nlines = a.nlines;
+    t.nx = a.nx;
+    t.ny = ny;
+    t.cols = 0;
+    t.dir1 = -1;
+    t.dir2 = +1;
+    t.second = 1;
+    t.mode = TC_MODE_TRANS;
+    t.trans = a.trans;
+    t.trans_b = a.trans_b;
+    t.err = a.err;
+    return t;
+}
+static TcPassArgs tc_col_args(int nx, const ColArgs &a) {
+    TcPassArgs t = {};
+    t.data = a.out;
+    t.nlines = a.batch * a.ny;
+    t.nx = nx;
+    t.ny = a.ny;
+    t.cols = 1;
+    t.dir1 = +1;
+    t.dir2 = -1;
+    t.second = (a.flags & COL_INV) ? 1 : 0;
+    t.mode = TC_MODE_PROP;
+    t.px = a.px;
+    t.py = a.py;
+    t.kx2 = a.kx2;
+    t.ky2 = a.ky2;
+    t.k2max = a.k2max;
+    if (a.flags & COL_DETECT) {
+        t.detmask = a.detmask;
+        t.ndet = a.ndet;
+        t.partial = a.partial;
+    }
+    t.err = a.err;
+    return t;
+}
+
 cudaError_t launch_row_pass(int ny, const RowArgs &a, cudaStream_t s, int nsm, int64_t *launches) {
+    const int fam0 = sched_row(ny);
+    if (fam0 == FAM_TC && row_tc_eligible(ny, a)) return launch_tc_pass(tc_row_args(ny, a), s, nsm, launches);
     ++*launches;
-    const int fam = sched_row(ny);
+    const int fam = fam0 == FAM_TC ? FAM_FAST : fam0;
     if (fam == FAM_FAST && row_warp_eligible(ny, a)) {
         switch (ny) {
             case 256:
@@ -1716,8 +1784,10 @@ cudaError_t launch_row_pass(int ny, const RowArgs &a, cudaStream_t s, int nsm, i
 }
 
 cudaError_t launch_col_pass(int nx, const ColArgs &a, cudaStream_t s, int nsm, int64_t *launches) {
+    const int fam0 = sched_col(nx);
+    if (fam0 == FAM_TC && col_tc_eligible(nx, a)) return launch_tc_pass(tc_col_args(nx, a), s, nsm, launches);
     ++*launches;
-    const int fam = sched_col(nx);
+    const int fam = fam0 == FAM_TC ? FAM_FAST : fam0;
     if (fam != FAM_REG && tma_eligible(a)) {
         // the slice loop's passes at 256, 512 and 1024: two-stage columns
         switch (fam == FAM_FAST ? col_half_side(nx, a) : 0) {
