@@ -255,7 +255,7 @@ def run_ours(args):
             if acc:
                 line["accuracy"] = acc
             if not args.no_variants:
-                line["variants"] = run_variants(ctx, cfg, xy, full, ref64, args)
+                line["variants"] = run_variants(ctx, cfg, xy, full, ref64, args, t_dev)
         line["clocks"] = clk.summary()
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -398,8 +398,10 @@ def run_resident(args):
         print(json.dumps(resident_compare(ctx, workload(), side, max(1, args.steps), which)), flush=True)
 
 
-def run_variants(ctx, cfg, xy, plain, ref64, args):
+def run_variants(ctx, cfg, xy, plain, ref64, args, t_dev):
     """The other forms of the scan, timed after the headline (not part of `value`):
+    * tensor_core: the same scan with the passes' line DFTs as split-bf16
+      contractions on the tensor cores, with its error against the FP64 oracle;
     * closure: 25 slices 4x thicker + the learned closure, as fine-slice-equivalent
       probe-slices/s, with its HAADF / ABF error against the FP64 oracle; it is
       used only when that error is within the bar -- else the fine-slice scan is
@@ -417,6 +419,22 @@ def run_variants(ctx, cfg, xy, plain, ref64, args):
     dev = torch.device("cuda", torch.cuda.current_device())
     names = ("HAADF", "ABF")
     out = {}
+    # ---- the tensor-core form of the passes (split-bf16 line DFTs on tcgen05)
+    o_tc = torch.empty((len(xy), 1, 2), dtype=torch.float64, device=dev)
+    ctx.set_schedule(512, 3, 3)
+    try:
+        el = _time(lambda: ctx.stem_scan(t_dev, spec.cz / NSLICE, np.arange(NSLICE), spec.ax, spec.by, 200.0,
+                                         cfg["k_ap"], xy, cfg["det_k"], out=o_tc), max(1, args.steps))
+    finally:
+        ctx.set_schedule(512, 0, 0)
+    d = o_tc.cpu().numpy()
+    ent = {"value": len(xy) * NSLICE / el, "unit": UNIT, "schedule": "tensor-core row and column passes",
+           "rel_l2_vs_plain": {n: O.rel_l2(d[:, 0, k], plain[:, 0, k]) for k, n in enumerate(names)}}
+    if ref64 is not None:
+        ent["rel_l2_vs_fp64"] = {n: O.rel_l2(d[:, 0, k], ref64[:, 0, k]) for k, n in enumerate(names)}
+        ent["within_bar"] = bool(max(ent["rel_l2_vs_fp64"].values()) <= 1e-3)
+    out["tensor_core"] = ent
+    del o_tc
     # ---- closure
     wfile = os.path.join(ROOT, "multislice_gb300", "data", "closure_srtio3.npy")
     if os.path.exists(wfile):
