@@ -139,6 +139,8 @@ def run_ours(args):
     ctx = Context(local)
     if args.batch:
         ctx.set_probe_batch(args.batch)
+    if args.tc:
+        ctx.set_schedule(nx, 3, 3)  # profiling aid: the tensor-core passes for the timed scan
     # device-resident inputs for `value`
     v_dev = torch.empty((NSLICE, nx, ny), dtype=torch.float32, device=dev)
     ctx.potential(spec, nx, ny, NSLICE, cfg["radius"], out=v_dev)
@@ -592,6 +594,8 @@ def main():
                     help="probes of the 64x64 raster per GPU (smaller cases are for profiling)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 accuracy check of every probe")
+    ap.add_argument("--tc", action="store_true",
+                    help="run the timed scan on the tensor-core passes (profiling; the headline uses the FP32 passes)")
     ap.add_argument("--resident", action="store_true",
                     help="time the on-chip slice loop against the streaming passes at 256^2 (--probes probes)")
     ap.add_argument("--resident-only", action="store_true", help="with --resident: the on-chip loop alone")
