@@ -2125,6 +2125,7 @@ int msl_stem_scan_resident(msl_ctx *c, const msl_grid *g, const msl_optics *o, c
         ra.ncheck = ncheck;
         ra.partial = partial;
         ra.nprobe = nb;
+        ra.err = c->dflag;
         LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_stem_resident(ra, c->stream, c->nsm, &c->launches); }));
         for (int ic = 0; ic < ncheck; ++ic)
             LAUNCH_TRY(c, timed(c, MSL_PROF_OTHER, [&] {

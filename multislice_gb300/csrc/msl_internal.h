@@ -240,6 +240,7 @@ struct ResidentArgs {
     int ncheck;
     double *partial;           // [ncheck][nprobe][8][ndet]
     int nprobe;
+    int *err;                  // raised when a bounded wait for a peer's copies gives up
 };
 cudaError_t launch_stem_resident(const ResidentArgs &a, cudaStream_t s, int nsm, int64_t *launches);
 int resident_side();
