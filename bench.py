@@ -512,6 +512,87 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_jobs_bench(args):
+    """--jobs: the uneven batch of 256 seeded jobs (grid sides 256-1024, 20-300
+    slices of 1-2 A, amorphous C/Si/Cu/Au at 0.05 atoms/A^3, 80/200/300 kV,
+    plane waves and probes mixed) through msl_run_jobs, once on the FP32 passes
+    and once with the tensor-core passes where they are built (sides 256 and
+    512); every job's exit wave against the FP64 oracle (its own FP64 potential,
+    transmission and slice loop).  One JSON line."""
+    import torch
+
+    from multislice_gb300 import Context, fparams_table, specimen as S
+    from oracle import fp64_gpu
+    from oracle import msl_oracle as O
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    t0 = time.perf_counter()
+    descs = S.uneven_jobs(args.jobs_seed, args.njobs)
+    gen_s = time.perf_counter() - t0
+    fp = fparams_table()
+    line = {"workload": f"{args.njobs} uneven jobs (seed {args.jobs_seed}): sides 256-1024, 20-300 slices of 1-2 A, "
+                        "amorphous C/Si/Cu/Au 0.05 atoms/A^3, 80/200/300 kV, plane waves and probes",
+            "unit": UNIT, "specimen_seconds": gen_s,
+            "atoms": int(sum(d["spec"].natom for d in descs)),
+            "probe_slices": int(sum(d["nslice"] for d in descs)),
+            "sides": {str(n): sum(1 for d in descs if d["n"] == n) for n in (256, 384, 512, 768, 1024)}}
+    with Context(0) as ctx:
+        jobs = []
+        for d in descs:
+            s, n = d["spec"], d["n"]
+            v = torch.empty((d["nslice"], n, n), dtype=torch.float32, device=dev)
+            ctx.potential(s, n, n, d["nslice"], 3.0, out=v)
+            t = torch.empty((d["nslice"], n, n, 2), dtype=torch.float32, device=dev)
+            ctx.transmission(v, s.ax, s.by, d["kev"], out=t)
+            del v
+            job = dict(trans=t, ax=s.ax, by=s.by, kev=d["kev"], dz=d["dz"], layer_seq=np.arange(d["nslice"]),
+                       out=torch.empty((n, n, 2), dtype=torch.float32, device=dev))
+            if d["probe"] is not None:
+                job["probe"] = d["probe"]
+            jobs.append(job)
+        units = line["probe_slices"]
+        arms = {}
+        for arm in ("fp32", "tensor_core"):
+            if arm == "tensor_core":
+                ctx.set_schedule(256, 3, 3)
+                ctx.set_schedule(512, 3, 3)
+            el = _time(lambda: ctx.run_jobs(jobs), max(1, args.steps))
+            waves = [j["out"].cpu().numpy() for j in jobs]
+            arms[arm] = {"value": units / el, "seconds": el,
+                         "waves": [w[..., 0] + 1j * w[..., 1] for w in waves]}
+            ctx.set_schedule(256, 0, 0)
+            ctx.set_schedule(512, 0, 0)
+        del jobs
+        torch.cuda.empty_cache()
+        errs = {"fp32": [], "tensor_core": []}
+        t1 = time.perf_counter()
+        for i, d in enumerate(descs):
+            s, n = d["spec"], d["n"]
+            V = fp64_gpu.potential(s.x, s.y, s.z, s.Z, fp, s.ax, s.by, s.cz, n, n, d["nslice"], 3.0, dev)
+            T = fp64_gpu.transmission(V, d["kev"], s.ax, s.by)
+            del V
+            P = fp64_gpu.propagator(n, n, s.ax, s.by, d["kev"], d["dz"], dev)
+            if d["probe"] is None:
+                w0 = torch.ones((n, n), dtype=torch.complex128, device=dev)
+            else:
+                k_ap, x, y = d["probe"]
+                w0 = fp64_gpu.probes(n, n, s.ax, s.by, d["kev"], 0.0, k_ap, 0.0, 0.0, [[x, y]], dev)[0]
+            ref = fp64_gpu.multislice(w0, T, P, range(d["nslice"])).cpu().numpy()
+            del T
+            for arm in errs:
+                errs[arm].append(O.rel_l2(arms[arm]["waves"][i], ref))
+        torch.cuda.empty_cache()
+        line["fp64_seconds"] = time.perf_counter() - t1
+    for arm in arms:
+        e = np.array(errs[arm])
+        arms[arm].pop("waves")
+        arms[arm]["rel_l2_vs_fp64"] = {"worst": float(e.max()), "median": float(np.median(e)),
+                                       "worst_job": int(e.argmax())}
+    arms["tensor_core"]["note"] = "tensor-core passes at sides 256 and 512, FP32 passes at 384, 768, 1024"
+    line["arms"] = arms
+    print(json.dumps(line), flush=True)
+
+
 def run_sides(args):
     """Per-pass device time of the slice loop at every supported side from 256 up
     (batched plane waves, 20 slices over 4 random phase layers, waves larger than
@@ -594,6 +675,10 @@ def main():
                     help="probes of the 64x64 raster per GPU (smaller cases are for profiling)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 accuracy check of every probe")
+    ap.add_argument("--jobs", action="store_true",
+                    help="the 256-job uneven batch, FP32 and tensor-core arms, each against FP64")
+    ap.add_argument("--njobs", type=int, default=256)
+    ap.add_argument("--jobs-seed", type=int, default=2026)
     ap.add_argument("--tc", action="store_true",
                     help="run the timed scan on the tensor-core passes (profiling; the headline uses the FP32 passes)")
     ap.add_argument("--resident", action="store_true",
@@ -607,7 +692,9 @@ def main():
     ap.add_argument("--frozen-phonon", action="store_true",
                     help="time the Au 2048^2, 32-configuration frozen-phonon image instead of the scan")
     args = ap.parse_args()
-    if args.resident:
+    if args.jobs:
+        run_jobs_bench(args)
+    elif args.resident:
         run_resident(args)
     elif args.sides:
         run_sides(args)

@@ -248,6 +248,19 @@ int msl_ctem_partial_coherence(msl_ctx *ctx, const msl_grid *grid, const msl_opt
  * d_out: double [natom][3]. */
 int msl_phonon_displacements(uint64_t seed, int config, int natom, double sigma, double *d_out);
 
+/* Amorphous specimen of the uneven-batch workload (host code): atoms uniform in
+ * a bx x by x thickness box at `density` atoms / A^3 with no two closer than
+ * dmin (periodic in x and y), thrown one by one from the library's splitmix64
+ * stream of `seed` onto a grid of cells of side >= dmin and kept when no
+ * accepted atom of the 27 neighbouring cells is too close; Z drawn from zs[nz]
+ * with the given weights.  xyz[3 * count] (Angstrom) and Z[count] receive
+ * round(density * volume) atoms (fewer only if 100 throws per atom cannot
+ * place them); when capacity is too small the call returns MSL_E_ARG with the
+ * needed count in *count.  No counterpart in the reference (its specimens come
+ * from .coo files). */
+int msl_amorphous(uint64_t seed, double bx, double by, double thickness, double density, double dmin, int nz,
+                  const int *zs, const double *weights, int capacity, double *xyz, int *Z, int *count);
+
 /* Frozen-phonon CTEM: for each of nconfig configurations displace the atoms
  * (msl_phonon_displacements), build the potential and transmission functions
  * of nslice equal slices, run a plane wave through them and image it; image and

@@ -28,7 +28,7 @@ EXPORTS = (
     "msl_closure_destroy", "msl_closure_param_count", "msl_closure_get_params", "msl_closure_set_params",
     "msl_closure_apply", "msl_closure_gradients", "msl_closure_train_step", "msl_stem_exit_waves",
     "msl_stem_scan_closure", "msl_autotune", "msl_set_schedule", "msl_get_schedule", "msl_set_autotune",
-    "msl_stem_scan_resident",
+    "msl_stem_scan_resident", "msl_amorphous",
 )
 PLANE_WAVE, PROBE = 0, 1
 # Muslib-shaped exports (reference names, no msl_ prefix)
@@ -139,6 +139,8 @@ def load(path=LIB_PATH):
         "msl_tc_gemm_bf16": (c_int, [P, P, P, P, c_int, c_int, c_int]),
         "msl_closure_create": (c_int, [P, ctypes.c_uint64, P]),
         "msl_autotune": (c_int, [P, c_int, c_int, c_int, P, P, P]),
+        "msl_amorphous": (c_int, [ctypes.c_uint64, c_double, c_double, c_double, c_double, c_double, c_int, P, P,
+                                  c_int, P, P, P]),
         "msl_stem_scan_resident": (c_int, [P, POINTER(Grid), POINTER(Optics), P, c_int, P, P, c_int,
                                            POINTER(Probe), P, c_int, POINTER(Detectors), P, c_int, P]),
         "msl_set_schedule": (c_int, [P, c_int, c_int, c_int]),

@@ -699,6 +699,70 @@ int msl_profile_read(const msl_ctx *c, int kind, int64_t *launches, double *ms) 
 }
 
 
+int msl_amorphous(uint64_t seed, double bx, double by, double thickness, double density, double dmin, int nz,
+                  const int *zs, const double *weights, int capacity, double *xyz, int *zout, int *count) {
+    if (!(bx > 0) || !(by > 0) || !(thickness > 0) || !(density > 0) || !(dmin >= 0) || nz < 1 || !zs || !weights ||
+        !count || capacity < 0 || !is_fin(bx + by + thickness + density + dmin))
+        return MSL_E_ARG;
+    const long target = std::lround(density * bx * by * thickness);
+    if (target > capacity || (target > 0 && (!xyz || !zout))) {
+        *count = (int)target;  // the capacity a call needs
+        return MSL_E_ARG;
+    }
+    double wsum = 0.0;
+    for (int i = 0; i < nz; ++i) {
+        if (!(weights[i] >= 0)) return MSL_E_ARG;
+        wsum += weights[i];
+    }
+    if (!(wsum > 0)) return MSL_E_ARG;
+    // cells of side >= dmin: a conflict can only come from the 27 neighbouring cells
+    const double cell = dmin > 0 ? dmin : 1.0;
+    const int ncx = std::max(1, (int)(bx / cell)), ncy = std::max(1, (int)(by / cell)),
+              ncz = std::max(1, (int)(thickness / cell));
+    const double sx = bx / ncx, sy = by / ncy, sz = thickness / ncz;
+    std::vector<std::vector<int>> grid((size_t)ncx * ncy * ncz);
+    uint64_t ctr = 0;
+    auto uni = [&]() { return (double)(splitmix64(seed ^ splitmix64(ctr++)) >> 11) * (1.0 / 9007199254740992.0); };
+    long n = 0;
+    const long max_tries = 100 * std::max<long>(target, 1);
+    const double d2min = dmin * dmin;
+    for (long tries = 0; n < target && tries < max_tries; ++tries) {
+        const double x = uni() * bx, y = uni() * by, z = uni() * thickness;
+        const int cx = std::min(ncx - 1, (int)(x / sx)), cy = std::min(ncy - 1, (int)(y / sy)),
+                  cz = std::min(ncz - 1, (int)(z / sz));
+        bool ok = true;
+        for (int ox = -1; ox <= 1 && ok; ++ox)
+            for (int oy = -1; oy <= 1 && ok; ++oy)
+                for (int oz = -1; oz <= 1 && ok; ++oz) {
+                    const int qz = cz + oz;
+                    if (qz < 0 || qz >= ncz) continue;
+                    const int qx = (cx + ox + ncx) % ncx, qy = (cy + oy + ncy) % ncy;
+                    for (int a : grid[((size_t)qx * ncy + qy) * ncz + qz]) {
+                        double dx = x - xyz[3 * a], dy = y - xyz[3 * a + 1];
+                        const double dz = z - xyz[3 * a + 2];
+                        dx -= bx * std::round(dx / bx);
+                        dy -= by * std::round(dy / by);
+                        if (dx * dx + dy * dy + dz * dz < d2min) {
+                            ok = false;
+                            break;
+                        }
+                    }
+                }
+        if (!ok) continue;
+        xyz[3 * n] = x;
+        xyz[3 * n + 1] = y;
+        xyz[3 * n + 2] = z;
+        double u = uni() * wsum;
+        int k = 0;
+        while (k < nz - 1 && u >= weights[k]) u -= weights[k++];
+        zout[n] = zs[k];
+        grid[((size_t)cx * ncy + cy) * ncz + cz].push_back((int)n);
+        ++n;
+    }
+    *count = (int)n;
+    return MSL_OK;
+}
+
 int msl_phonon_displacements(uint64_t seed, int config, int natom, double sigma, double *d) {
     if (natom < 0 || config < 0 || !(sigma >= 0) || (natom > 0 && !d)) return MSL_E_ARG;
     const double two_pi = 6.283185307179586477;

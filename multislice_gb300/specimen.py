@@ -83,43 +83,29 @@ def jitter(spec: Specimen, sigma, rng):
                     spec.ax, spec.by, spec.cz)
 
 
-def amorphous(box, thickness, density, dmin, Zs, weights, rng, max_tries=60):
-    """Atoms uniform in a box with a minimum separation (dart throwing on a cell grid)."""
-    vol = box[0] * box[1] * thickness
-    n_target = int(round(density * vol))
-    cell = dmin
-    nc = np.maximum((np.array([box[0], box[1], thickness]) / cell).astype(int), 1)
-    grid = {}
-    pts = []
-    tries = 0
-    while len(pts) < n_target and tries < max_tries * n_target:
-        tries += 1
-        p = rng.random(3) * np.array([box[0], box[1], thickness])
-        c = tuple((p / cell).astype(int) % nc)
-        ok = True
-        for dx in (-1, 0, 1):
-            for dy in (-1, 0, 1):
-                for dz in (-1, 0, 1):
-                    q = ((c[0] + dx) % nc[0], (c[1] + dy) % nc[1], (c[2] + dz) % nc[2])
-                    for o in grid.get(q, ()):
-                        d = p - pts[o]
-                        d[:2] -= np.round(d[:2] / np.array(box)) * np.array(box)
-                        if d @ d < dmin * dmin:
-                            ok = False
-                            break
-                    if not ok:
-                        break
-                if not ok:
-                    break
-            if not ok:
-                break
-        if ok:
-            grid.setdefault(c, []).append(len(pts))
-            pts.append(p)
-    pts = np.array(pts).reshape(-1, 3)
-    Z = rng.choice(np.asarray(Zs), size=len(pts), p=np.asarray(weights) / np.sum(weights))
-    return Specimen(pts[:, 0].copy(), pts[:, 1].copy(), pts[:, 2].copy(), Z.astype(np.int32),
-                    float(box[0]), float(box[1]), float(thickness))
+def amorphous(box, thickness, density, dmin, Zs, weights, rng):
+    """Atoms uniform in a box with a minimum separation (periodic in x and y), Z
+    drawn with the given weights: msl_amorphous (dart throwing on a cell grid in
+    the library's host code), seeded from rng."""
+    import ctypes
+
+    from . import _abi
+    lib = _abi.load()
+    seed = int(rng.integers(0, 2 ** 63))
+    zs = np.ascontiguousarray(Zs, np.int32)
+    w = np.ascontiguousarray(weights, np.float64)
+    cap = int(round(density * box[0] * box[1] * thickness)) + 1
+    xyz = np.empty((cap, 3), np.float64)
+    Z = np.empty(cap, np.int32)
+    n = ctypes.c_int()
+    rc = lib.msl_amorphous(seed, float(box[0]), float(box[1]), float(thickness), float(density), float(dmin),
+                           len(zs), zs.ctypes.data, w.ctypes.data, cap, xyz.ctypes.data, Z.ctypes.data,
+                           ctypes.byref(n))
+    if rc != _abi.MSL_OK:
+        raise _abi.MslError(rc, "msl_amorphous failed")
+    k = n.value
+    return Specimen(xyz[:k, 0].copy(), xyz[:k, 1].copy(), xyz[:k, 2].copy(), Z[:k].copy(), float(box[0]),
+                    float(box[1]), float(thickness))
 
 
 def uneven_jobs(seed, njobs, max_slices=300, max_box=None):
