@@ -137,10 +137,15 @@ __global__ void __launch_bounds__(kThreads, 1) stem_resident_kernel(ResidentArgs
 #pragma unroll
                 for (int e = 0; e < RP::E; ++e) v[e] = R[(e >> 1) * kLines * kLines + bslot(j, t + 16 * (e & 1))];
             }
-            fft_line_tab<RP, -1>(v, t, adX, tw);
+            // the transmission row is requested before the inverse transform, so its
+            // L2 latency hides behind it
             const float2 *trow = a.trans + ((size_t)l * kN + ix_row) * kN;
+            float2 tv[RP::E];
 #pragma unroll
-            for (int e = 0; e < RP::E; ++e) v[e] = c_mul(v[e], __ldg(trow + t + 16 * e));
+            for (int e = 0; e < RP::E; ++e) tv[e] = __ldg(trow + t + 16 * e);
+            fft_line_tab<RP, -1>(v, t, adX, tw);
+#pragma unroll
+            for (int e = 0; e < RP::E; ++e) v[e] = c_mul(v[e], tv[e]);
             fft_line_tab<RP, +1>(v, t, adX, tw);
 #pragma unroll
             for (int e = 0; e < RP::E; ++e) R[(e >> 1) * kLines * kLines + bslot(j, t + 16 * (e & 1))] = v[e];
@@ -157,14 +162,18 @@ __global__ void __launch_bounds__(kThreads, 1) stem_resident_kernel(ResidentArgs
             ps ^= 1u;
 #pragma unroll
             for (int e = 0; e < RP::E; ++e) v[e] = S[(e >> 1) * kLines * kLines + bslot(t + 16 * (e & 1), j)];
-            fft_line_tab<RP, +1>(v, t, adX, tw);
+            // propagator factors requested before the forward transform (their latency hides behind it)
             const float2 *px = a.prop + (size_t)l * 2 * kN, *py = px + kN;
             const float2 pyv = __ldg(py + iy_col);
+            float2 pv[RP::E];
+#pragma unroll
+            for (int e = 0; e < RP::E; ++e) pv[e] = __ldg(px + t + 16 * e);
+            fft_line_tab<RP, +1>(v, t, adX, tw);
 #pragma unroll
             for (int e = 0; e < RP::E; ++e) {
                 const int ix = t + 16 * e;
                 const float k2 = a.kx2[ix] + ky2;
-                v[e] = k2 < a.k2max ? c_mul(c_mul(v[e], pyv), __ldg(px + ix)) : make_float2(0.f, 0.f);
+                v[e] = k2 < a.k2max ? c_mul(c_mul(v[e], pyv), pv[e]) : make_float2(0.f, 0.f);
             }
             const bool detect = ic < a.ncheck && a.checkpoints[ic] == s;
             if (detect) {
