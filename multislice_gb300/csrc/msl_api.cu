@@ -1390,15 +1390,31 @@ int msl_potential_build(msl_ctx *c, const msl_atoms *at, const double *fparams, 
             sp[z * 12 + 7 + 2 * i] = (float)(PIK * PIK / d);
         }
     }
-    // one upload: off | x | y | Z | sp | xf | yf
+    // tabulated radial profiles of the species present (up to kPotMaxSp): cubic
+    // pieces of vzatom evaluated in FP64 over [0.15 A, radius]
+    std::vector<int> zlist, zslot(104, -1);
+    for (int z = 1; z <= 103; ++z)
+        if (used[z]) {
+            zslot[z] = (int)zlist.size();
+            zlist.push_back(z);
+        }
+    const double tab_r0 = 0.15;
+    const int nsp = (zlist.size() <= (size_t)msl::kPotMaxSp && radius > 2 * tab_r0) ? (int)zlist.size() : 0;
+    std::vector<float4> tab((size_t)std::max(nsp, 1) * msl::kPotTabN);
+    if (nsp) msl::potential_tables(fparams, zlist.data(), nsp, tab_r0, radius, tab.data());
+    // one upload: off | x | y | Z | sp | xf | yf | tab | zslot
     std::vector<float> xf(xs.begin(), xs.end()), yf(ys.begin(), ys.end());
     const size_t o_off = 0, o_x = ((sizeof(int) * (nslice + 1) + 15) / 16) * 16;
     const size_t o_y = o_x + sizeof(double) * xs.size(), o_z = o_y + sizeof(double) * ys.size();
     const size_t o_sp = ((o_z + sizeof(int) * zs.size() + 15) / 16) * 16;
     const size_t o_xf = ((o_sp + sizeof(float) * sp.size() + 15) / 16) * 16;
     const size_t o_yf = ((o_xf + sizeof(float) * xf.size() + 15) / 16) * 16;
-    const size_t total = o_yf + sizeof(float) * yf.size();
+    const size_t o_tab = ((o_yf + sizeof(float) * yf.size() + 15) / 16) * 16;
+    const size_t o_zs = o_tab + sizeof(float4) * tab.size();
+    const size_t total = o_zs + sizeof(int) * zslot.size();
     std::vector<unsigned char> h(total, 0);
+    memcpy(h.data() + o_tab, tab.data(), sizeof(float4) * tab.size());
+    memcpy(h.data() + o_zs, zslot.data(), sizeof(int) * zslot.size());
     memcpy(h.data() + o_off, count.data(), sizeof(int) * (nslice + 1));
     memcpy(h.data() + o_x, xs.data(), sizeof(double) * xs.size());
     memcpy(h.data() + o_y, ys.data(), sizeof(double) * ys.size());
@@ -1435,6 +1451,11 @@ int msl_potential_build(msl_ctx *c, const msl_atoms *at, const double *fparams, 
     a.rad2 = (float)(radius * radius);
     a.sp = (const float *)(d + o_sp);
     a.v = vd;
+    a.tab = (const float4 *)(d + o_tab);
+    a.zslot = (const int *)(d + o_zs);
+    a.nsp = nsp;
+    a.tab_r0 = (float)tab_r0;
+    a.tab_inv_h = (float)(msl::kPotTabN / (radius - tab_r0));
     LAUNCH_TRY(c, timed(c, MSL_PROF_POTENTIAL, [&] { return msl::launch_potential(a, c->stream, &c->launches); }));
     if (!vdev) CUDA_TRY(c, cudaMemcpyAsync(v_out, vd, vbytes, cudaMemcpyDeviceToHost, c->stream));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));

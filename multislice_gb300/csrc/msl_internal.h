@@ -121,7 +121,17 @@ struct PotArgs {
     float rad2;               // radius^2 (float compare, r < radius)
     const float *sp;          // [104][12] A1 B1 A2 B2 A3 B3 C1 D1 C2 D2 C3 D3
     float *v;                 // [nslice][nx][ny]
+    // tabulated radial profiles (nsp > 0): cubic pieces over [tab_r0, cutoff] per
+    // species slot zslot[Z]; below tab_r0 the analytic form
+    const float4 *tab;
+    const int *zslot;
+    int nsp;
+    float tab_r0, tab_inv_h;
 };
+constexpr int kPotTabN = 512;   // cubic pieces per species
+constexpr int kPotMaxSp = 8;    // species the tabulated kernel takes (more: analytic kernel)
+// Cubic pieces of vzatom (FP64) for the species zlist[nsp] over [r0, rmax]: [nsp][kPotTabN].
+void potential_tables(const double *fparams, const int *zlist, int nsp, double r0, double rmax, float4 *out);
 
 bool plan_supported(int n);
 // Kernel families of a side's passes (the autotuner's choices), per device.

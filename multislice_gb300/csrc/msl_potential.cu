@@ -58,13 +58,19 @@ __device__ __forceinline__ float bessk0f(float x) {
 }
 }  // namespace
 
+template <bool TAB>
 __global__ void __launch_bounds__(THREADS) potential_kernel(PotArgs a) {
+    extern __shared__ float4 stab[];  // TAB: [nsp][kPotTabN] cubic pieces of the species' radial profiles
     __shared__ int sZ[CHUNK];
+    __shared__ int sS[CHUNK];
     __shared__ double sxa[CHUNK], sya[CHUNK];
     __shared__ float sdx[CHUNK][TX];
     __shared__ float sdy[CHUNK][TY];
     __shared__ int wcount[THREADS / 32];
     const int tid = threadIdx.x;
+    if (TAB) {
+        for (int i = tid; i < a.nsp * kPotTabN; i += THREADS) stab[i] = a.tab[i];
+    }
     const int ty = tid % TY, txg = tid / TY;  // pixels (txg + 8 j, ty), j < PX
     const int lane = tid & 31, warp = tid >> 5;
     const int iy0 = blockIdx.x * TY, ix0 = blockIdx.y * TX, s = blockIdx.z;
@@ -111,6 +117,7 @@ __global__ void __launch_bounds__(THREADS) potential_kernel(PotArgs a) {
         }
         if (keep) {
             sZ[pos] = z;
+            if (TAB) sS[pos] = a.zslot[z];
             sxa[pos] = xa;
             sya[pos] = ya;
         }
@@ -133,12 +140,22 @@ __global__ void __launch_bounds__(THREADS) potential_kernel(PotArgs a) {
         for (int k = 0; k < total; ++k) {
             const float dy = sdy[k][ty];
             const float *p = a.sp + sZ[k] * 12;
+            const float4 *tb = TAB ? stab + sS[k] * kPotTabN : nullptr;
 #pragma unroll
             for (int j = 0; j < PX; ++j) {
                 const float dx = sdx[k][txg + 8 * j];
                 const float r2 = dx * dx + dy * dy;
                 if (r2 < a.rad2) {
                     const float r = fmaxf(sqrtf(r2), 1.0e-10f);
+                    if (TAB && r >= a.tab_r0) {
+                        // cubic piece of the tabulated profile: ((c3 t + c2) t + c1) t + c0
+                        const float u = (r - a.tab_r0) * a.tab_inv_h;
+                        const int i = min((int)u, kPotTabN - 1);
+                        const float t = u - (float)i;
+                        const float4 c = tb[i];
+                        acc[j] += fmaf(fmaf(fmaf(c.w, t, c.z), t, c.y), t, c.x);
+                        continue;
+                    }
                     float v = __ldg(p + 0) * bessk0f(__ldg(p + 1) * r) +
                               __ldg(p + 2) * bessk0f(__ldg(p + 3) * r) +
                               __ldg(p + 4) * bessk0f(__ldg(p + 5) * r);
@@ -161,8 +178,70 @@ __global__ void __launch_bounds__(THREADS) potential_kernel(PotArgs a) {
 cudaError_t launch_potential(const PotArgs &a, cudaStream_t s, int64_t *launches) {
     ++*launches;
     dim3 grid(a.ny / TY, a.nx / TX, a.nslice);
-    potential_kernel<<<grid, THREADS, 0, s>>>(a);
+    if (a.nsp > 0 && a.tab) {
+        const size_t smem = sizeof(float4) * (size_t)a.nsp * kPotTabN;
+        static KernelSetup ks;
+        int per_sm = 0;
+        cudaError_t e = ks.get(potential_kernel<true>, THREADS, sizeof(float4) * kPotMaxSp * kPotTabN, true, &per_sm);
+        if (e != cudaSuccess) return e;
+        potential_kernel<true><<<grid, THREADS, smem, s>>>(a);
+    } else {
+        potential_kernel<false><<<grid, THREADS, 0, s>>>(a);
+    }
     return cudaGetLastError();
+}
+
+// ------------------------------------------------------------ radial tables
+namespace {
+// vzatom in double (slicelib.cpp:2666-2716 with the A&S Bessel polynomials of :168-235)
+double bessi0d(double x) {
+    static const double c[7] = {1.0, 3.5156229, 3.0899424, 1.2067492, 0.2659732, 0.0360768, 0.0045813};
+    const double t = (x / 3.75) * (x / 3.75);
+    double s = c[6];
+    for (int i = 5; i >= 0; --i) s = s * t + c[i];
+    return s;
+}
+double bessk0d(double x) {
+    static const double a[7] = {-0.57721566, 0.42278420, 0.23069756, 0.03488590, 0.00262698, 0.00010750, 0.00000740};
+    static const double b[7] = {1.25331414, -0.07832358, 0.02189568, -0.01062446, 0.00587872, -0.00251540, 0.00053208};
+    if (x <= 2.0) {
+        const double t = 0.25 * x * x;
+        double s = a[6];
+        for (int i = 5; i >= 0; --i) s = s * t + a[i];
+        return -log(0.5 * x) * bessi0d(x) + s;
+    }
+    const double t = 2.0 / x;
+    double s = b[6];
+    for (int i = 5; i >= 0; --i) s = s * t + b[i];
+    return exp(-x) * s / sqrt(x);
+}
+double vz_double(const double *f, double r) {
+    const double AL = 300.8242834, AG = 150.4121417, PIK = 3.141592654;
+    const double x = 2.0 * PIK * r;
+    double suml = 0.0, sumg = 0.0;
+    for (int i = 0; i < 3; ++i) suml += f[2 * i] * bessk0d(x * sqrt(f[2 * i + 1]));
+    const double x2 = (PIK * r) * (PIK * r);
+    for (int i = 0; i < 3; ++i) sumg += f[6 + 2 * i] * exp(-x2 / f[7 + 2 * i]) / f[7 + 2 * i];
+    return AL * suml + AG * sumg;
+}
+}  // namespace
+
+void potential_tables(const double *fparams, const int *zlist, int nsp, double r0, double rmax, float4 *out) {
+    const double h = (rmax - r0) / kPotTabN;
+    for (int sidx = 0; sidx < nsp; ++sidx) {
+        const double *f = fparams + zlist[sidx] * 12;
+        for (int i = 0; i < kPotTabN; ++i) {
+            // the cubic through the profile at t = 0, 1/3, 2/3, 1 of [r0 + i h, r0 + (i + 1) h]
+            const double r = r0 + i * h;
+            const double y0 = vz_double(f, r), y1 = vz_double(f, r + h / 3), y2 = vz_double(f, r + 2 * h / 3),
+                         y3 = vz_double(f, r + h);
+            const double c0 = y0;
+            const double c1 = (-11 * y0 + 18 * y1 - 9 * y2 + 2 * y3) / 2;
+            const double c2 = 9 * (2 * y0 - 5 * y1 + 4 * y2 - y3) / 2;
+            const double c3 = 27 * (-y0 + 3 * y1 - 3 * y2 + y3) / 6;
+            out[(size_t)sidx * kPotTabN + i] = make_float4((float)c0, (float)c1, (float)c2, (float)c3);
+        }
+    }
 }
 
 }  // namespace msl
