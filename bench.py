@@ -519,6 +519,8 @@ def run_jobs_bench(args):
     and once with the tensor-core passes where they are built (sides 256 and
     512); every job's exit wave against the FP64 oracle (its own FP64 potential,
     transmission and slice loop).  One JSON line."""
+    import ctypes
+
     import torch
 
     from multislice_gb300 import Context, fparams_table, specimen as S
@@ -562,6 +564,20 @@ def run_jobs_bench(args):
                          "waves": [w[..., 0] + 1j * w[..., 1] for w in waves]}
             ctx.set_schedule(256, 0, 0)
             ctx.set_schedule(512, 0, 0)
+        # device time per kind of one FP32 run with per-launch events (the grid
+        # groups then run one after another on the context's stream)
+        ctx._lib.msl_profile_enable(ctx._h, 1)
+        t0 = time.perf_counter()
+        ctx.run_jobs(jobs)
+        devt = {"serialised_wall_ms": 1e3 * (time.perf_counter() - t0)}
+        for k, name in enumerate(("row", "col", "potential", "other")):
+            n, ms = ctypes.c_int64(), ctypes.c_double()
+            ctx._lib.msl_profile_read(ctx._h, k, ctypes.byref(n), ctypes.byref(ms))
+            if n.value:
+                devt[name] = {"launches": n.value, "ms": ms.value}
+        ctx._lib.msl_profile_enable(ctx._h, 0)
+        line["fp32_device_time"] = devt
+        line["algorithmic_bytes"] = int(sum(32 * d["n"] * d["n"] * d["nslice"] for d in descs))
         del jobs
         torch.cuda.empty_cache()
         errs = {"fp32": [], "tensor_core": []}
@@ -649,12 +665,15 @@ def run_frozen_phonon(args):
     k_obj = float(S.mrad_to_k(25.0, kev))
     with Context(0) as c:
         c.frozen_phonon(spec, 2048, 2048, 80, 3.0, kev, 1.2e7, -600.0, k_obj, nconfig=2, sigma=0.085, seed=1)
-        c._lib.msl_profile_enable(c._h, 1)
         t0 = time.perf_counter()
         c.frozen_phonon(spec, 2048, 2048, 80, 3.0, kev, 1.2e7, -600.0, k_obj, nconfig=32, sigma=0.085, seed=2026)
         wall = time.perf_counter() - t0
         line = {"workload": "Au fcc 16x16x40, 2048^2, 80 slices, 32 frozen-phonon configurations, 300 kV",
-                "wall_ms": 1e3 * wall}
+                "wall_ms": 1e3 * wall, "device_ms_by_kind": "a second call with per-launch events"}
+        c._lib.msl_profile_enable(c._h, 1)
+        t0 = time.perf_counter()
+        c.frozen_phonon(spec, 2048, 2048, 80, 3.0, kev, 1.2e7, -600.0, k_obj, nconfig=32, sigma=0.085, seed=2026)
+        line["profiled_wall_ms"] = 1e3 * (time.perf_counter() - t0)
         for k, name in enumerate(("row", "col", "potential", "other")):
             n, ms = ctypes.c_int64(), ctypes.c_double()
             c._lib.msl_profile_read(c._h, k, ctypes.byref(n), ctypes.byref(ms))

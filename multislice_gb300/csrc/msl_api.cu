@@ -141,6 +141,7 @@ struct msl_ctx {
     DevBuf wave, in_stage, trans_stage, tabs, apchi, exy, fxy, detmask, partial, detout, pot,
         atoms, tmpw, ctf, acc, jobtab;
     int *dflag = nullptr;  // device flag raised by a kernel whose bounded wait gave up
+    std::vector<cudaStream_t> side_streams;  // one per grid group of an uneven batch
     msl_ctx() {
         DevBuf *bufs[] = {&wave, &in_stage, &trans_stage, &tabs, &apchi, &exy, &fxy, &detmask,
                           &partial, &detout, &pot, &atoms, &tmpw, &ctf, &acc, &jobtab};
@@ -287,7 +288,8 @@ struct SliceTables {
 };
 
 int build_slice_tables(msl_ctx *c, const msl_grid *g, const msl_optics *o, int ntrans,
-                       const double *dz, SliceTables &st) {
+                       const double *dz, SliceTables &st, DevBuf *dst = nullptr) {
+    DevBuf &tb = dst ? *dst : c->tabs;
     const int nx = g->nx, ny = g->ny;
     freqn_f32(nx, g->ax, st.kx, st.kx2);
     freqn_f32(ny, g->by, st.ky, st.ky2);
@@ -310,13 +312,13 @@ int build_slice_tables(msl_ctx *c, const msl_grid *g, const msl_optics *o, int n
             for (int i = 0; i < ny; ++i) hp[(size_t)l * (nx + ny) + nx + i] = make_float2(scale, 0.f);
         }
     }
-    int rc = upload(c, c->tabs, h.data(), h.size());
+    int rc = upload(c, tb, h.data(), h.size());
     if (rc) return rc;
-    st.d_kx2 = (float *)c->tabs.p;
+    st.d_kx2 = (float *)tb.p;
     st.d_ky2 = st.d_kx2 + nx;
     st.d_kx = st.d_ky2 + ny;
     st.d_ky = st.d_kx + nx;
-    st.d_prop = (float2 *)((unsigned char *)c->tabs.p + fbytes);
+    st.d_prop = (float2 *)((unsigned char *)tb.p + fbytes);
     return MSL_OK;
 }
 
@@ -672,6 +674,7 @@ int msl_ctx_destroy(msl_ctx *c) {
                       &c->tmpw, &c->ctf, &c->acc, &c->jobtab};
     for (DevBuf *b : bufs) b->release();
     if (c->dflag) cudaFree(c->dflag);
+    for (cudaStream_t s : c->side_streams) cudaStreamDestroy(s);
     cudaStreamDestroy(c->stream);
     delete c;
     return MSL_OK;
@@ -832,6 +835,284 @@ int msl_ctem_image(msl_ctx *c, const msl_grid *g, const msl_optics *o, const flo
     return MSL_OK;
 }
 
+namespace {
+
+// Host half of a potential build: the atoms validated and binned by slice
+// (stably, so the sum order inside a slice is the input order), the
+// per-species parameters and radial tables, laid out as one upload image
+// off | x | y | Z | sp | xf | yf | tab | zslot.  The radial tables are kept
+// and reused while the species, the cutoff and the FPARAMS table stay the same.
+struct PotImage {
+    std::vector<unsigned char> h;
+    size_t o_off = 0, o_x = 0, o_y = 0, o_z = 0, o_sp = 0, o_xf = 0, o_yf = 0, o_tab = 0, o_zs = 0;
+    int nsp = 0;
+    double tab_r0 = 0.15;
+    std::vector<int> tab_z;
+    double tab_radius = -1.0;
+    const double *tab_fp = nullptr;
+    std::vector<float4> tab;
+};
+
+int potential_prepare(msl_ctx *c, const msl_atoms *at, const double *fparams, const msl_grid *g, int nslice,
+                      double radius, PotImage &im) {
+    if (!at || !fparams) return fail(c, MSL_E_ARG, "null argument");
+    if (nslice < 1) return fail(c, MSL_E_ARG, "nslice must be >= 1");
+    if (!(at->cz > 0) || !is_fin(at->cz)) return fail(c, MSL_E_ARG, "thickness cz must be positive");
+    if (!(radius > 0) || !(2.0 * radius < g->ax) || !(2.0 * radius < g->by))
+        return fail(c, MSL_E_ARG, "cutoff radius must be positive and below half the cell");
+    if (at->natom < 0 || (at->natom > 0 && (!at->x || !at->y || !at->z || !at->Z)))
+        return fail(c, MSL_E_ARG, "atom arrays are required");
+    const double dz = at->cz / nslice;
+    std::vector<int> kz(at->natom), count(nslice + 1, 0);
+    for (int i = 0; i < at->natom; ++i) {
+        if (!is_fin(at->x[i]) || !is_fin(at->y[i]) || !is_fin(at->z[i]))
+            return fail(c, MSL_E_ARG, "atom coordinates must be finite (atom " + std::to_string(i) + ")");
+        int k = (int)std::floor(at->z[i] / dz);
+        if (at->z[i] < 0.0 || k < 0 || k >= nslice) k = -1;
+        if (k >= 0 && (at->Z[i] < 1 || at->Z[i] > 103))
+            return fail(c, MSL_E_ARG, "atomic number out of range 1..103 (atom " + std::to_string(i) + ")");
+        kz[i] = k;
+        if (k >= 0) count[k + 1]++;
+    }
+    for (int k = 0; k < nslice; ++k) count[k + 1] += count[k];
+    const int nkeep = count[nslice];
+    const size_t nk = nkeep > 0 ? (size_t)nkeep : 1;
+    // per-species float parameters: A = AL a, B = 2 pi sqrt(b), C = AG c / d, D = pi^2 / d
+    // (constants of slicelib.cpp:2673-2674)
+    bool used[104] = {false};
+    for (int i = 0; i < at->natom; ++i)
+        if (kz[i] >= 0) used[at->Z[i]] = true;
+    const double AL = 300.8242834, AG = 150.4121417, PIK = 3.141592654;
+    std::vector<float> sp(104 * 12, 0.f);
+    for (int z = 1; z <= 103; ++z) {
+        if (!used[z]) continue;
+        const double *f = fparams + z * 12;
+        for (int i = 0; i < 3; ++i) {
+            const double a = f[2 * i], b = f[2 * i + 1], cc = f[6 + 2 * i], d = f[7 + 2 * i];
+            if (!(b > 0) || !(d > 0) || !is_fin(a) || !is_fin(cc))
+                return fail(c, MSL_E_ARG, "invalid FPARAMS row for Z=" + std::to_string(z));
+            sp[z * 12 + 2 * i] = (float)(AL * a);
+            sp[z * 12 + 2 * i + 1] = (float)(2.0 * PIK * sqrt(b));
+            sp[z * 12 + 6 + 2 * i] = (float)(AG * cc / d);
+            sp[z * 12 + 7 + 2 * i] = (float)(PIK * PIK / d);
+        }
+    }
+    // tabulated radial profiles of the species present (up to kPotMaxSp): cubic
+    // pieces of vzatom evaluated in FP64 over [0.15 A, radius]
+    std::vector<int> zlist, zslot(104, -1);
+    for (int z = 1; z <= 103; ++z)
+        if (used[z]) {
+            zslot[z] = (int)zlist.size();
+            zlist.push_back(z);
+        }
+    im.nsp = (zlist.size() <= (size_t)msl::kPotMaxSp && radius > 2 * im.tab_r0) ? (int)zlist.size() : 0;
+    const size_t ntab = (size_t)std::max(im.nsp, 1) * msl::kPotTabN;
+    if (im.tab_z != zlist || im.tab_radius != radius || im.tab_fp != fparams || im.tab.size() != ntab) {
+        im.tab.assign(ntab, make_float4(0.f, 0.f, 0.f, 0.f));
+        if (im.nsp) msl::potential_tables(fparams, zlist.data(), im.nsp, im.tab_r0, radius, im.tab.data());
+        im.tab_z = zlist;
+        im.tab_radius = radius;
+        im.tab_fp = fparams;
+    }
+    im.o_off = 0;
+    im.o_x = ((sizeof(int) * (nslice + 1) + 15) / 16) * 16;
+    im.o_y = im.o_x + sizeof(double) * nk;
+    im.o_z = im.o_y + sizeof(double) * nk;
+    im.o_sp = ((im.o_z + sizeof(int) * nk + 15) / 16) * 16;
+    im.o_xf = ((im.o_sp + sizeof(float) * sp.size() + 15) / 16) * 16;
+    im.o_yf = ((im.o_xf + sizeof(float) * nk + 15) / 16) * 16;
+    im.o_tab = ((im.o_yf + sizeof(float) * nk + 15) / 16) * 16;
+    im.o_zs = im.o_tab + sizeof(float4) * im.tab.size();
+    im.h.assign(im.o_zs + sizeof(int) * zslot.size(), 0);
+    unsigned char *h = im.h.data();
+    double *xs = (double *)(h + im.o_x), *ys = (double *)(h + im.o_y);
+    int *zs = (int *)(h + im.o_z);
+    float *xf = (float *)(h + im.o_xf), *yf = (float *)(h + im.o_yf);
+    std::vector<int> fill(count.begin(), count.end() - 1);
+    for (int i = 0; i < at->natom; ++i) {
+        if (kz[i] < 0) continue;
+        const int p = fill[kz[i]]++;
+        double xw, yw;
+        xw = at->x[i] - g->ax * std::floor(at->x[i] / g->ax);
+        yw = at->y[i] - g->by * std::floor(at->y[i] / g->by);
+        memcpy(xs + p, &xw, sizeof(double));
+        memcpy(ys + p, &yw, sizeof(double));
+        zs[p] = at->Z[i];
+        xf[p] = (float)xw;
+        yf[p] = (float)yw;
+    }
+    memcpy(h + im.o_off, count.data(), sizeof(int) * (nslice + 1));
+    memcpy(h + im.o_sp, sp.data(), sizeof(float) * sp.size());
+    memcpy(h + im.o_tab, im.tab.data(), sizeof(float4) * im.tab.size());
+    memcpy(h + im.o_zs, zslot.data(), sizeof(int) * zslot.size());
+    return MSL_OK;
+}
+
+// Device half: launch the gather on the upload image at `d` (device memory).
+int potential_launch(msl_ctx *c, const PotImage &im, const unsigned char *d, const msl_grid *g, int nslice,
+                     double radius, float *vd) {
+    msl::PotArgs a;
+    a.x = (const double *)(d + im.o_x);
+    a.y = (const double *)(d + im.o_y);
+    a.xf = (const float *)(d + im.o_xf);
+    a.yf = (const float *)(d + im.o_yf);
+    a.Z = (const int *)(d + im.o_z);
+    a.off = (const int *)(d + im.o_off);
+    a.nslice = nslice;
+    a.nx = g->nx;
+    a.ny = g->ny;
+    a.ax = g->ax;
+    a.by = g->by;
+    a.dxp = g->ax / g->nx;
+    a.dyp = g->by / g->ny;
+    a.rad2 = (float)(radius * radius);
+    a.sp = (const float *)(d + im.o_sp);
+    a.v = vd;
+    a.tab = (const float4 *)(d + im.o_tab);
+    a.zslot = (const int *)(d + im.o_zs);
+    a.nsp = im.nsp;
+    a.tab_r0 = (float)im.tab_r0;
+    a.tab_inv_h = (float)(msl::kPotTabN / (radius - im.tab_r0));
+    LAUNCH_TRY(c, timed(c, MSL_PROF_POTENTIAL, [&] { return msl::launch_potential(a, c->stream, &c->launches); }));
+    return MSL_OK;
+}
+
+}  // namespace
+
+namespace {
+
+// t = exp(i sigma V) elementwise, then the band limit: forward transform, 2/3
+// mask, inverse transform (mulslice.cpp:414-421, :515-522), on the context's
+// stream; st holds the identity propagator tables of the grid.
+int transmission_enqueue(msl_ctx *c, const msl_grid *g, const msl_optics *o, const float *vd, int nlayer,
+                         float2 *td, const SliceTables &st, float2 *twr, float2 *twc) {
+    const size_t n2 = (size_t)g->nx * g->ny;
+    const double phase_scale = msl_sigma(o->kev) / 1000.0;  // rad per V*A
+    LAUNCH_TRY(c, timed(c, MSL_PROF_OTHER, [&] {
+                   return msl::launch_transmission_phase(vd, phase_scale, n2 * nlayer, td, c->nsm, c->stream,
+                                                         &c->launches);
+               }));
+    RowArgs r = row_args(g, twr, nullptr, td, nlayer, msl::ROW_LOAD | msl::ROW_FWD, c->dflag);
+    LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_row_pass(g->ny, r, c->stream, c->nsm, &c->launches); }));
+    ColArgs ca = col_args(g, st, twc, 0, td, nlayer,
+                          msl::COL_LOAD | msl::COL_FWD | msl::COL_PROP | msl::COL_INV | msl::COL_STORE, c->dflag);
+    LAUNCH_TRY(c, timed(c, MSL_PROF_COL, [&] { return msl::launch_col_pass(g->nx, ca, c->stream, c->nsm, &c->launches); }));
+    r = row_args(g, twr, nullptr, td, nlayer, msl::ROW_LOAD | msl::ROW_INV, c->dflag);
+    LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_row_pass(g->ny, r, c->stream, c->nsm, &c->launches); }));
+    return MSL_OK;
+}
+
+}  // namespace
+
+namespace {
+
+// Transmission functions of frozen-phonon configurations, built on the
+// context's stream: each configuration's atoms are displaced
+// (msl_phonon_displacements), binned and uploaded through one of two pinned
+// buffers, its potential gathered and turned into band-limited transmission
+// functions; the host work of the next configuration runs while the GPU builds
+// the current one.  Nothing here synchronizes with the stream or checks the
+// kernel error flag: the caller does both after its slice loop.
+struct PhononBuilder {
+    msl_ctx *c;
+    const msl_atoms *at;
+    const double *fparams;
+    const msl_grid *g;
+    const msl_optics *o;
+    int nslice, nconfig;
+    double radius, sigma;
+    uint64_t seed;
+    SliceTables st;
+    float2 *twr = nullptr, *twc = nullptr;
+    DevBuf tabs, atoms, pot;
+    PotImage im[2];
+    int prepared[2] = {-1, -1};
+    unsigned char *pin[2] = {nullptr, nullptr};
+    size_t pin_cap = 0;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    std::vector<double> x, y, z, d;
+    msl_atoms jat;
+
+    PhononBuilder(msl_ctx *c_, const msl_atoms *at_, const double *fp, const msl_grid *g_, int nslice_,
+                  double radius_, const msl_optics *o_, int nconfig_, double sigma_, uint64_t seed_)
+        : c(c_), at(at_), fparams(fp), g(g_), o(o_), nslice(nslice_), nconfig(nconfig_), radius(radius_),
+          sigma(sigma_), seed(seed_) {
+        tabs.mb = atoms.mb = pot.mb = &c->mem;
+    }
+    ~PhononBuilder() {
+        for (int i = 0; i < 2; ++i) {
+            if (ev[i]) {
+                cudaEventSynchronize(ev[i]);
+                cudaEventDestroy(ev[i]);
+            }
+            if (pin[i]) cudaFreeHost(pin[i]);
+        }
+    }
+    int init() {
+        const int na = at->natom;
+        x.resize(na);
+        y.resize(na);
+        z.resize(na);
+        d.resize(3 * (size_t)na);
+        jat = *at;
+        jat.x = x.data();
+        jat.y = y.data();
+        jat.z = z.data();
+        int rc;
+        if ((rc = build_slice_tables(c, g, o, 1, nullptr, st, &tabs))) return rc;
+        twr = twiddles(c, g->ny);
+        twc = twiddles(c, g->nx);
+        if (!twr || !twc) return fail(c, MSL_E_NOMEM, "twiddle table allocation failed");
+        CUDA_TRY(c, pot.ensure(sizeof(float) * (size_t)nslice * g->nx * g->ny));
+        for (int i = 0; i < 2; ++i) CUDA_TRY(c, cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming));
+        return prepare(0);
+    }
+    int prepare(int cfg) {
+        msl_phonon_displacements(seed, cfg, at->natom, sigma, d.data());
+        for (int i = 0; i < at->natom; ++i) {
+            x[i] = at->x[i] + d[3 * i];
+            y[i] = at->y[i] + d[3 * i + 1];
+            z[i] = at->z[i] + d[3 * i + 2];
+        }
+        const int rc = potential_prepare(c, &jat, fparams, g, nslice, radius, im[cfg & 1]);
+        if (rc) return rc;
+        prepared[cfg & 1] = cfg;
+        return MSL_OK;
+    }
+    // Enqueue configuration cfg's transmission functions into t (device), then
+    // prepare configuration cfg + 1 on the host.
+    int build(int cfg, float2 *t) {
+        int rc;
+        const int sl = cfg & 1;
+        if (prepared[sl] != cfg && (rc = prepare(cfg))) return rc;
+        const PotImage &m = im[sl];
+        const size_t bytes = m.h.size();
+        if (bytes > pin_cap) {  // (re)allocate both pinned buffers with headroom
+            for (int i = 0; i < 2; ++i) {
+                CUDA_TRY(c, cudaEventSynchronize(ev[i]));
+                if (pin[i]) cudaFreeHost(pin[i]);
+                pin[i] = nullptr;
+            }
+            pin_cap = bytes + bytes / 4;
+            for (int i = 0; i < 2; ++i) CUDA_TRY(c, cudaHostAlloc((void **)&pin[i], pin_cap, cudaHostAllocDefault));
+        }
+        if (bytes > atoms.cap) {  // growth frees the old buffer: let the stream drain first
+            CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+            CUDA_TRY(c, atoms.ensure(bytes + bytes / 4));
+        }
+        CUDA_TRY(c, cudaEventSynchronize(ev[sl]));  // the upload two configurations back has read pin[sl]
+        memcpy(pin[sl], m.h.data(), bytes);
+        CUDA_TRY(c, cudaMemcpyAsync(atoms.p, pin[sl], bytes, cudaMemcpyHostToDevice, c->stream));
+        CUDA_TRY(c, cudaEventRecord(ev[sl], c->stream));
+        if ((rc = potential_launch(c, m, (const unsigned char *)atoms.p, g, nslice, radius, (float *)pot.p))) return rc;
+        if ((rc = transmission_enqueue(c, g, o, (const float *)pot.p, nslice, t, st, twr, twc))) return rc;
+        if (cfg + 1 < nconfig && (rc = prepare(cfg + 1))) return rc;
+        return MSL_OK;
+    }
+};
+
+}  // namespace
+
 int msl_frozen_phonon(msl_ctx *c, const msl_atoms *at, const double *fparams, const msl_grid *g,
                       int nslice, double radius, const msl_optics *o, const msl_lens *lens, int nconfig,
                       double sigma, uint64_t seed, double *image, double *exit_intensity) {
@@ -844,7 +1125,7 @@ int msl_frozen_phonon(msl_ctx *c, const msl_atoms *at, const double *fparams, co
         return fail(c, MSL_E_ARG, "atoms required, nconfig >= 1, sigma >= 0, nslice >= 1");
     if (!image && !exit_intensity) return fail(c, MSL_E_ARG, "nothing to compute: image and exit_intensity null");
     CUDA_TRY(c, cudaSetDevice(c->device));
-    const int nx = g->nx, ny = g->ny, na = at->natom;
+    const int nx = g->nx, ny = g->ny;
     const size_t n2 = (size_t)nx * ny;
     // device buffers: potential (one configuration), transmissions of a batch of
     // configurations, their waves, accumulators.  The configurations of a batch
@@ -855,9 +1136,8 @@ int msl_frozen_phonon(msl_ctx *c, const msl_atoms *at, const double *fparams, co
     size_t budget = (size_t)16 << 30;
     if (c->mem.limit && c->mem.limit / 2 < budget) budget = c->mem.limit / 2;
     const int B = (int)std::max<size_t>(1, std::min<size_t>((size_t)nconfig, budget / (slab + sizeof(float2) * n2)));
-    DevBuf vbuf, tbuf, pbuf;
-    vbuf.mb = tbuf.mb = pbuf.mb = &c->mem;
-    CUDA_TRY(c, vbuf.ensure(sizeof(float) * n2 * nslice));
+    DevBuf tbuf, pbuf;
+    tbuf.mb = pbuf.mb = &c->mem;
     CUDA_TRY(c, tbuf.ensure(slab * B));
     CUDA_TRY(c, pbuf.ensure(sizeof(float2 *) * (size_t)nslice * B));
     CUDA_TRY(c, c->acc.ensure(2 * sizeof(double) * n2));
@@ -868,27 +1148,16 @@ int msl_frozen_phonon(msl_ctx *c, const msl_atoms *at, const double *fparams, co
     float2 *tall = (float2 *)tbuf.p;
     const float2 **ptab = (const float2 **)pbuf.p;
     std::vector<const float2 *> hptab((size_t)nslice * B);
-    std::vector<double> x(na), y(na), z(na), d(3 * (size_t)na);
     std::vector<double> dz(nslice, at->cz / nslice);
     std::vector<int> seq(nslice);
     for (int s = 0; s < nslice; ++s) seq[s] = s;
-    msl_atoms jat = *at;
-    jat.x = x.data();
-    jat.y = y.data();
-    jat.z = z.data();
-    int out = MSL_OK;
+    PhononBuilder pb(c, at, fparams, g, nslice, radius, o, nconfig, sigma, seed);
+    int out = pb.init();
+    if (out == MSL_OK) out = err_reset(c);
     for (int cfg0 = 0; cfg0 < nconfig && out == MSL_OK; cfg0 += B) {
         const int nb = std::min(B, nconfig - cfg0);
         for (int b = 0; b < nb && out == MSL_OK; ++b) {
-            msl_phonon_displacements(seed, cfg0 + b, na, sigma, d.data());
-            for (int i = 0; i < na; ++i) {
-                x[i] = at->x[i] + d[3 * i];
-                y[i] = at->y[i] + d[3 * i + 1];
-                z[i] = at->z[i] + d[3 * i + 2];
-            }
-            float *tb = (float *)(tall + n2 * nslice * b);
-            if ((out = msl_potential_build(c, &jat, fparams, g, nslice, radius, (float *)vbuf.p))) break;
-            if ((out = msl_transmission_build(c, g, o, (const float *)vbuf.p, nslice, tb))) break;
+            if ((out = pb.build(cfg0 + b, tall + n2 * nslice * b))) break;
             for (int s = 0; s < nslice; ++s) hptab[(size_t)s * nb + b] = tall + n2 * nslice * b + n2 * s;
         }
         if (out != MSL_OK) break;
@@ -897,7 +1166,6 @@ int msl_frozen_phonon(msl_ctx *c, const msl_atoms *at, const double *fparams, co
             out = fail(c, MSL_E_CUDA, "frozen phonon: transmission table upload failed");
             break;
         }
-        if ((out = err_reset(c))) break;
         if ((out = ctem_core(c, g, o, tall, nslice, dz.data(), seq.data(), nslice, lens, w, nb, true,
                              1.0 / nconfig, img_d, exit_intensity ? exit_d : nullptr, false, ptab)))
             break;
@@ -921,12 +1189,273 @@ int msl_frozen_phonon(msl_ctx *c, const msl_atoms *at, const double *fparams, co
         cudaStreamSynchronize(c->stream);
     }
     cudaStreamSynchronize(c->stream);
-    vbuf.release();
     tbuf.release();
     pbuf.release();
     return out;
 }
 
+
+namespace {
+
+// One grid shape of an uneven batch: its jobs (by decreasing slice count) and
+// where its buffers sit in the call's arenas.
+struct JobGroup {
+    int nx = 0, ny = 0;
+    std::vector<int> ids;
+    size_t wave_off = 0, tab_off = 0, ptab_off = 0, stage_off = 0, apchi_off = 0, exy_off = 0;
+    size_t kbytes = 0, nprop = 0;
+    std::vector<std::vector<size_t>> layer_prop;  // per job, per layer: row of its propagator table
+    float2 *twr = nullptr, *twc = nullptr;
+};
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+cudaStream_t group_stream(msl_ctx *c, size_t i) {
+    while (c->side_streams.size() <= i) {
+        cudaStream_t s = nullptr;
+        if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return nullptr;
+        c->side_streams.push_back(s);
+    }
+    return c->side_streams[i];
+}
+
+// Run the groups of an uneven batch: every host table first (one upload per
+// arena), then each group's probe formation and lockstep slice loop on its
+// own stream (the context stream when profiling), then the exit waves out.
+int run_job_groups(msl_ctx *c, const msl_job *jobs, std::vector<JobGroup> &groups, double bandlimit) {
+    int rc;
+    size_t wave_bytes = 0, tab_bytes = 0, ptab_bytes = 0, stage_bytes = 0, apchi_bytes = 0, exy_bytes = 0;
+    size_t nprobe = 0;
+    for (JobGroup &g : groups) {
+        const size_t n2 = (size_t)g.nx * g.ny, nb = g.ids.size();
+        const int S = jobs[g.ids[0]].nslice;
+        g.twr = twiddles(c, g.ny);
+        g.twc = twiddles(c, g.nx);
+        if (!g.twr || !g.twc) return fail(c, MSL_E_NOMEM, "twiddle table allocation failed");
+        // one propagator table per distinct slice thickness of a job (layers
+        // of equal dz share it; the tables depend on nothing else)
+        g.layer_prop.assign(nb, {});
+        g.nprop = 0;
+        bool probes = false;
+        for (size_t b = 0; b < nb; ++b) {
+            const msl_job &jb = jobs[g.ids[b]];
+            std::map<uint64_t, size_t> seen;  // keyed by the bits of dz
+            g.layer_prop[b].resize(jb.ntrans);
+            for (int l = 0; l < jb.ntrans; ++l) {
+                uint64_t key;
+                memcpy(&key, &jb.dz[l], sizeof(key));
+                auto it = seen.find(key);
+                if (it == seen.end()) it = seen.emplace(key, g.nprop++).first;
+                g.layer_prop[b][l] = it->second;
+            }
+            if (jb.illumination == MSL_PROBE) {
+                probes = true;
+                ++nprobe;
+            }
+        }
+        g.kbytes = sizeof(float) * (g.nx + g.ny) * nb;
+        g.wave_off = wave_bytes;
+        wave_bytes = align256(wave_bytes + sizeof(float2) * n2 * nb);
+        g.tab_off = tab_bytes;
+        tab_bytes = align256(tab_bytes + g.kbytes + sizeof(float2) * (g.nx + g.ny) * g.nprop);
+        g.ptab_off = ptab_bytes;
+        ptab_bytes = align256(ptab_bytes + sizeof(void *) * ((size_t)2 * S * nb + nb) + sizeof(float) * nb);
+        g.stage_off = stage_bytes;
+        for (size_t b = 0; b < nb; ++b)
+            if (!on_device(jobs[g.ids[b]].trans))
+                stage_bytes = align256(stage_bytes + sizeof(float2) * n2 * jobs[g.ids[b]].ntrans);
+        g.apchi_off = apchi_bytes;
+        g.exy_off = exy_bytes;
+        if (probes) {
+            apchi_bytes = align256(apchi_bytes + sizeof(float2) * n2 + n2);
+            exy_bytes = align256(exy_bytes + sizeof(float2) * (g.nx + g.ny));
+        }
+    }
+    size_t fxy_len = 0;
+    for (JobGroup &g : groups)
+        for (int j : g.ids)
+            if (jobs[j].illumination == MSL_PROBE) fxy_len += (size_t)g.nx + g.ny + 2;
+    CUDA_TRY(c, c->wave.ensure(wave_bytes));
+    CUDA_TRY(c, c->tabs.ensure(tab_bytes));
+    CUDA_TRY(c, c->jobtab.ensure(ptab_bytes));
+    CUDA_TRY(c, c->trans_stage.ensure(stage_bytes));
+    CUDA_TRY(c, c->apchi.ensure(apchi_bytes));
+    CUDA_TRY(c, c->exy.ensure(exy_bytes));
+    CUDA_TRY(c, c->fxy.ensure(sizeof(double) * fxy_len));
+    unsigned char *dtab = (unsigned char *)c->tabs.p, *dptab = (unsigned char *)c->jobtab.p;
+    std::vector<unsigned char> htab(tab_bytes), hptab(ptab_bytes);
+    std::vector<double> hk(fxy_len);
+    size_t fo = 0;
+    for (JobGroup &g : groups) {
+        const int nx = g.nx, ny = g.ny, nb = (int)g.ids.size(), S = jobs[g.ids[0]].nslice;
+        const size_t n2 = (size_t)nx * ny;
+        // transmission stacks on the device (staged when on the host)
+        std::vector<const float2 *> tdev(nb);
+        size_t so = g.stage_off;
+        for (int b = 0; b < nb; ++b) {
+            const msl_job &jb = jobs[g.ids[b]];
+            if (on_device(jb.trans)) {
+                tdev[b] = (const float2 *)jb.trans;
+            } else {
+                const size_t bytes = sizeof(float2) * n2 * jb.ntrans;
+                float2 *dst = (float2 *)((unsigned char *)c->trans_stage.p + so);
+                CUDA_TRY(c, cudaMemcpyAsync(dst, jb.trans, bytes, cudaMemcpyHostToDevice, c->stream));
+                tdev[b] = dst;
+                so = align256(so + bytes);
+            }
+        }
+        // tables: [kx2 ky2] floats per job, then [px py] per distinct thickness
+        float *hk2 = (float *)(htab.data() + g.tab_off);
+        float2 *hprop = (float2 *)(htab.data() + g.tab_off + g.kbytes);
+        std::vector<float> k2max(nb);
+        for (int b = 0; b < nb; ++b) {
+            const msl_job &jb = jobs[g.ids[b]];
+            std::vector<float> kx, kx2, ky, ky2;
+            freqn_f32(nx, jb.grid.ax, kx, kx2);
+            freqn_f32(ny, jb.grid.by, ky, ky2);
+            memcpy(hk2 + (size_t)b * (nx + ny), kx2.data(), sizeof(float) * nx);
+            memcpy(hk2 + (size_t)b * (nx + ny) + nx, ky2.data(), sizeof(float) * ny);
+            k2max[b] = k2max_f32(nx, ny, jb.grid.ax, jb.grid.by, bandlimit);
+            msl_optics o = {jb.kev, bandlimit, 0.0, 0.0, 0};
+            std::vector<char> done(g.nprop, 0);
+            for (int l = 0; l < jb.ntrans; ++l) {
+                const size_t row = g.layer_prop[b][l];
+                if (done[row]) continue;
+                done[row] = 1;
+                float2 *pt = hprop + row * (nx + ny);
+                prop_tables(nx, ny, jb.grid.ax, jb.grid.by, &o, jb.dz[l], kx, kx2, ky, ky2, pt, pt + nx);
+            }
+        }
+        // pointer tables: trans[S][nb], prop[S][nb], k2[nb], then k2max[nb]
+        const float *dk = (const float *)(dtab + g.tab_off);
+        const float2 *dp = (const float2 *)(dtab + g.tab_off + g.kbytes);
+        const void **pt = (const void **)(hptab.data() + g.ptab_off);
+        for (int s = 0; s < S; ++s)
+            for (int b = 0; b < nb; ++b) {
+                const msl_job &jb = jobs[g.ids[b]];
+                const int l = s < jb.nslice ? jb.layer_seq[s] : 0;
+                pt[(size_t)s * nb + b] = tdev[b] + (size_t)l * n2;
+                pt[(size_t)(S + s) * nb + b] = dp + g.layer_prop[b][l] * (nx + ny);
+            }
+        for (int b = 0; b < nb; ++b) pt[(size_t)2 * S * nb + b] = dk + (size_t)b * (nx + ny);
+        memcpy(pt + (size_t)2 * S * nb + nb, k2max.data(), sizeof(float) * nb);
+        // probe k-vectors and positions
+        for (int b = 0; b < nb; ++b) {
+            const msl_job &jb = jobs[g.ids[b]];
+            if (jb.illumination != MSL_PROBE) continue;
+            double *h = hk.data() + fo;
+            for (int i = 0; i < nx; ++i) h[i] = (double)(i < nx / 2 ? i : i - nx) / jb.grid.ax;
+            for (int i = 0; i < ny; ++i) h[nx + i] = (double)(i < ny / 2 ? i : i - ny) / jb.grid.by;
+            h[nx + ny] = jb.probe_x / jb.grid.ax;
+            h[nx + ny + 1] = jb.probe_y / jb.grid.by;
+            fo += (size_t)nx + ny + 2;
+        }
+    }
+    if (tab_bytes) CUDA_TRY(c, cudaMemcpyAsync(dtab, htab.data(), tab_bytes, cudaMemcpyHostToDevice, c->stream));
+    if (ptab_bytes) CUDA_TRY(c, cudaMemcpyAsync(dptab, hptab.data(), ptab_bytes, cudaMemcpyHostToDevice, c->stream));
+    if (fxy_len)
+        CUDA_TRY(c, cudaMemcpyAsync(c->fxy.p, hk.data(), sizeof(double) * fxy_len, cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(c, cudaMemsetAsync(c->wave.p, 0, wave_bytes, c->stream));
+    const bool concurrent = !c->prof && groups.size() > 1;
+    cudaEvent_t fork = take_event(c);
+    std::vector<cudaEvent_t> joins;
+    CUDA_TRY(c, cudaEventRecord(fork, c->stream));
+    std::vector<float2> ones(4096, make_float2(1.f, 0.f));
+    fo = 0;
+    for (size_t gi = 0; gi < groups.size(); ++gi) {
+        JobGroup &g = groups[gi];
+        const int nx = g.nx, ny = g.ny, nb = (int)g.ids.size(), S = jobs[g.ids[0]].nslice;
+        const size_t n2 = (size_t)nx * ny;
+        cudaStream_t st = c->stream;
+        if (concurrent) {
+            st = group_stream(c, gi);
+            if (!st) return fail(c, MSL_E_CUDA, "stream creation failed");
+            CUDA_TRY(c, cudaStreamWaitEvent(st, fork, 0));
+        }
+        float2 *w = (float2 *)((unsigned char *)c->wave.p + g.wave_off);
+        const unsigned char *tp = dptab + g.ptab_off;
+        const float2 *const *ttab = (const float2 *const *)tp;
+        const float2 *const *ptabd = ttab + (size_t)S * nb;
+        const float *const *ktab = (const float *const *)(ttab + (size_t)2 * S * nb);
+        const float *dk2max = (const float *)(ktab + nb);
+        // entrance waves in the column-inverse representation every job shares:
+        // a plane wave is 1 in the ky = 0 column, a probe is ifft_x of its spectrum
+        float2 *apchi = (float2 *)((unsigned char *)c->apchi.p + g.apchi_off);
+        float2 *ex = (float2 *)((unsigned char *)c->exy.p + g.exy_off), *ey = ex + nx;
+        for (int b = 0; b < nb; ++b) {
+            const msl_job &jb = jobs[g.ids[b]];
+            float2 *slot = w + (size_t)b * n2;
+            if (jb.illumination == MSL_PLANE_WAVE) {
+                CUDA_TRY(c, cudaMemcpy2DAsync(slot, sizeof(float2) * ny, ones.data(), sizeof(float2),
+                                              sizeof(float2), nx, cudaMemcpyHostToDevice, st));
+                continue;
+            }
+            const double *kxd = (const double *)c->fxy.p + fo, *kyd = kxd + nx;
+            fo += (size_t)nx + ny + 2;
+            LAUNCH_TRY(c, timed(c, MSL_PROF_OTHER, [&] {
+                           return msl::launch_probe_table(nx, ny, kxd, kyd, jb.probe.k_in * jb.probe.k_in,
+                                                          jb.probe.k_out * jb.probe.k_out, msl_wavelength(jb.kev),
+                                                          jb.probe.df, jb.probe.cs, 1.0 / ((double)nx * ny), apchi,
+                                                          st, &c->launches);
+                       }));
+            LAUNCH_TRY(c, timed(c, MSL_PROF_OTHER, [&] {
+                           return msl::launch_probe_shifts(nx, ny, 1, kyd + ny, ex, ey, st, &c->launches);
+                       }));
+            SliceTables none;
+            none.k2max = 0.f;
+            none.d_kx2 = none.d_ky2 = nullptr;
+            none.d_prop = nullptr;
+            ColArgs pa = col_args(&jb.grid, none, g.twc, 0, slot, 1, msl::COL_PROBE | msl::COL_INV | msl::COL_STORE,
+                                  c->dflag);
+            pa.apchi = apchi;
+            pa.ex = ex;
+            pa.ey = ey;
+            LAUNCH_TRY(c, timed(c, MSL_PROF_COL, [&] { return msl::launch_col_pass(nx, pa, st, c->nsm, &c->launches); }));
+        }
+        // lockstep slice loop over the running prefix
+        msl_grid gg = {nx, ny, 1.0, 1.0};
+        SliceTables none;
+        none.k2max = 0.f;
+        none.d_kx2 = none.d_ky2 = nullptr;
+        none.d_prop = nullptr;
+        for (int s = 0; s < S; ++s) {
+            int nact = 0;
+            while (nact < nb && jobs[g.ids[nact]].nslice > s) ++nact;
+            RowArgs r = row_args(&gg, g.twr, nullptr, w, nact,
+                                 msl::ROW_LOAD | msl::ROW_INV | msl::ROW_TRANS | msl::ROW_FWD, c->dflag);
+            r.trans_b = ttab + (size_t)s * nb;
+            LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_row_pass(ny, r, st, c->nsm, &c->launches); }));
+            ColArgs ca = col_args(&gg, none, g.twc, 0, w, nact,
+                                  msl::COL_LOAD | msl::COL_FWD | msl::COL_PROP | msl::COL_INV | msl::COL_STORE, c->dflag);
+            ca.prop_b = ptabd + (size_t)s * nb;
+            ca.k2_b = ktab;
+            ca.k2max_b = dk2max;
+            LAUNCH_TRY(c, timed(c, MSL_PROF_COL, [&] { return msl::launch_col_pass(nx, ca, st, c->nsm, &c->launches); }));
+        }
+        RowArgs r = row_args(&gg, g.twr, nullptr, w, nb, msl::ROW_LOAD | msl::ROW_INV, c->dflag);
+        LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_row_pass(ny, r, st, c->nsm, &c->launches); }));
+        if (concurrent) {
+            cudaEvent_t e = take_event(c);
+            joins.push_back(e);
+            CUDA_TRY(c, cudaEventRecord(e, st));
+        }
+    }
+    for (cudaEvent_t e : joins) CUDA_TRY(c, cudaStreamWaitEvent(c->stream, e, 0));
+    // exit waves out once every group's loop has been issued
+    for (JobGroup &g : groups) {
+        const size_t n2 = (size_t)g.nx * g.ny;
+        const float2 *w = (const float2 *)((unsigned char *)c->wave.p + g.wave_off);
+        for (size_t b = 0; b < g.ids.size(); ++b)
+            CUDA_TRY(c, cudaMemcpyAsync(jobs[g.ids[b]].exit_wave, w + b * n2, sizeof(float2) * n2,
+                                        cudaMemcpyDefault, c->stream));
+    }
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    c->ev_free.push_back(fork);
+    for (cudaEvent_t e : joins) c->ev_free.push_back(e);
+    return MSL_OK;
+}
+
+}  // namespace
 
 int msl_run_jobs(msl_ctx *c, const msl_job *jobs, int njobs, double bandlimit) {
     if (!c) return MSL_E_ARG;
@@ -952,155 +1481,27 @@ int msl_run_jobs(msl_ctx *c, const msl_job *jobs, int njobs, double bandlimit) {
     CUDA_TRY(c, cudaSetDevice(c->device));
     if ((rc = err_reset(c))) return rc;
     // group by grid shape
-    std::map<std::pair<int, int>, std::vector<int>> groups;
-    for (int j = 0; j < njobs; ++j) groups[{jobs[j].grid.nx, jobs[j].grid.ny}].push_back(j);
-    for (auto &kv : groups) {
-        std::vector<int> &ids = kv.second;
-        std::stable_sort(ids.begin(), ids.end(), [&](int x, int y) { return jobs[x].nslice > jobs[y].nslice; });
-        const int nx = kv.first.first, ny = kv.first.second, nb = (int)ids.size();
-        const size_t n2 = (size_t)nx * ny;
-        const int S = jobs[ids[0]].nslice;
-        float2 *twr = twiddles(c, ny), *twc = twiddles(c, nx);
-        if (!twr || !twc) return fail(c, MSL_E_NOMEM, "twiddle table allocation failed");
-        // transmission stacks on the device (staged into one arena when on the host)
-        std::vector<const float2 *> tdev(nb);
-        size_t stage_bytes = 0;
-        for (int b = 0; b < nb; ++b)
-            if (!on_device(jobs[ids[b]].trans)) stage_bytes += sizeof(float2) * n2 * jobs[ids[b]].ntrans;
-        CUDA_TRY(c, c->trans_stage.ensure(stage_bytes));
-        size_t off = 0;
-        for (int b = 0; b < nb; ++b) {
-            const msl_job &jb = jobs[ids[b]];
-            if (on_device(jb.trans)) {
-                tdev[b] = (const float2 *)jb.trans;
-            } else {
-                const size_t bytes = sizeof(float2) * n2 * jb.ntrans;
-                float2 *dst = (float2 *)((unsigned char *)c->trans_stage.p + off);
-                CUDA_TRY(c, cudaMemcpyAsync(dst, jb.trans, bytes, cudaMemcpyHostToDevice, c->stream));
-                tdev[b] = dst;
-                off += bytes;
-            }
+    std::map<std::pair<int, int>, std::vector<int>> gmap;
+    for (int j = 0; j < njobs; ++j) gmap[{jobs[j].grid.nx, jobs[j].grid.ny}].push_back(j);
+    std::vector<JobGroup> groups;
+    for (auto &kv : gmap) {
+        JobGroup g;
+        g.nx = kv.first.first;
+        g.ny = kv.first.second;
+        g.ids = kv.second;
+        std::stable_sort(g.ids.begin(), g.ids.end(), [&](int x, int y) { return jobs[x].nslice > jobs[y].nslice; });
+        groups.push_back(std::move(g));
+    }
+    // Without a memory cap every group's buffers coexist and the groups run
+    // concurrently, one stream each; under a cap they run one after another
+    // in the same buffers.
+    if (c->mem.limit) {
+        for (auto &g : groups) {
+            std::vector<JobGroup> one(1, std::move(g));
+            if ((rc = run_job_groups(c, jobs, one, bandlimit))) return rc;
         }
-        // per-job tables: [kx2 ky2] floats, then per layer [px py]; pointer tables per step
-        size_t nprop = 0;
-        for (int b = 0; b < nb; ++b) nprop += (size_t)jobs[ids[b]].ntrans;
-        const size_t kbytes = sizeof(float) * (nx + ny) * nb;
-        const size_t pbytes = sizeof(float2) * (nx + ny) * nprop;
-        std::vector<unsigned char> htab(kbytes + pbytes);
-        std::vector<float> k2max(nb);
-        std::vector<size_t> prop_off(nb);
-        size_t po = 0;
-        for (int b = 0; b < nb; ++b) {
-            const msl_job &jb = jobs[ids[b]];
-            std::vector<float> kx, kx2, ky, ky2;
-            freqn_f32(nx, jb.grid.ax, kx, kx2);
-            freqn_f32(ny, jb.grid.by, ky, ky2);
-            float *kt = (float *)htab.data() + (size_t)b * (nx + ny);
-            memcpy(kt, kx2.data(), sizeof(float) * nx);
-            memcpy(kt + nx, ky2.data(), sizeof(float) * ny);
-            k2max[b] = k2max_f32(nx, ny, jb.grid.ax, jb.grid.by, bandlimit);
-            msl_optics o = {jb.kev, bandlimit, 0.0, 0.0, 0};
-            prop_off[b] = po;
-            for (int l = 0; l < jb.ntrans; ++l) {
-                float2 *pt = (float2 *)(htab.data() + kbytes) + po;
-                prop_tables(nx, ny, jb.grid.ax, jb.grid.by, &o, jb.dz[l], kx, kx2, ky, ky2, pt, pt + nx);
-                po += (size_t)(nx + ny);
-            }
-        }
-        if ((rc = upload(c, c->tabs, htab.data(), htab.size()))) return rc;
-        const float *dk = (const float *)c->tabs.p;
-        const float2 *dp = (const float2 *)((unsigned char *)c->tabs.p + kbytes);
-        // pointer tables: trans[S][nb], prop[S][nb], k2[nb], k2max[nb]
-        std::vector<const void *> ptab((size_t)2 * S * nb + nb);
-        for (int s = 0; s < S; ++s)
-            for (int b = 0; b < nb; ++b) {
-                const msl_job &jb = jobs[ids[b]];
-                const int l = s < jb.nslice ? jb.layer_seq[s] : 0;
-                ptab[(size_t)s * nb + b] = tdev[b] + (size_t)l * n2;
-                ptab[(size_t)(S + s) * nb + b] = dp + prop_off[b] + (size_t)l * (nx + ny);
-            }
-        for (int b = 0; b < nb; ++b) ptab[(size_t)2 * S * nb + b] = dk + (size_t)b * (nx + ny);
-        const size_t ptbytes = sizeof(void *) * ptab.size();
-        CUDA_TRY(c, c->jobtab.ensure(ptbytes + sizeof(float) * nb));
-        CUDA_TRY(c, cudaMemcpyAsync(c->jobtab.p, ptab.data(), ptbytes, cudaMemcpyHostToDevice, c->stream));
-        float *dk2max = (float *)((unsigned char *)c->jobtab.p + ptbytes);
-        CUDA_TRY(c, cudaMemcpyAsync(dk2max, k2max.data(), sizeof(float) * nb, cudaMemcpyHostToDevice, c->stream));
-        const float2 *const *ttab = (const float2 *const *)c->jobtab.p;
-        const float2 *const *ptabd = ttab + (size_t)S * nb;
-        const float *const *ktab = (const float *const *)(ttab + (size_t)2 * S * nb);
-        // entrance waves in the column-inverse representation every job shares:
-        // a plane wave is 1 in the ky = 0 column, a probe is ifft_x of its spectrum
-        CUDA_TRY(c, c->wave.ensure(sizeof(float2) * n2 * nb));
-        float2 *w = (float2 *)c->wave.p;
-        CUDA_TRY(c, cudaMemsetAsync(w, 0, sizeof(float2) * n2 * nb, c->stream));
-        std::vector<float2> ones(nx, make_float2(1.f, 0.f));
-        for (int b = 0; b < nb; ++b) {
-            const msl_job &jb = jobs[ids[b]];
-            float2 *slot = w + (size_t)b * n2;
-            if (jb.illumination == MSL_PLANE_WAVE) {
-                CUDA_TRY(c, cudaMemcpy2DAsync(slot, sizeof(float2) * ny, ones.data(), sizeof(float2),
-                                              sizeof(float2), nx, cudaMemcpyHostToDevice, c->stream));
-                continue;
-            }
-            std::vector<double> hk(nx + ny + 2);
-            for (int i = 0; i < nx; ++i) hk[i] = (double)(i < nx / 2 ? i : i - nx) / jb.grid.ax;
-            for (int i = 0; i < ny; ++i) hk[nx + i] = (double)(i < ny / 2 ? i : i - ny) / jb.grid.by;
-            hk[nx + ny] = jb.probe_x / jb.grid.ax;
-            hk[nx + ny + 1] = jb.probe_y / jb.grid.by;
-            CUDA_TRY(c, c->fxy.ensure(sizeof(double) * hk.size()));
-            CUDA_TRY(c, cudaStreamSynchronize(c->stream));  // fxy/apchi/exy of the previous probe are free
-            CUDA_TRY(c, cudaMemcpyAsync(c->fxy.p, hk.data(), sizeof(double) * hk.size(), cudaMemcpyHostToDevice,
-                                        c->stream));
-            const double *kxd = (const double *)c->fxy.p, *kyd = kxd + nx;
-            CUDA_TRY(c, c->apchi.ensure(sizeof(float2) * n2 + n2));
-            CUDA_TRY(c, c->exy.ensure(sizeof(float2) * (nx + ny)));
-            float2 *apchi = (float2 *)c->apchi.p, *ex = (float2 *)c->exy.p, *ey = ex + nx;
-            LAUNCH_TRY(c, timed(c, MSL_PROF_OTHER, [&] {
-                           return msl::launch_probe_table(nx, ny, kxd, kyd, jb.probe.k_in * jb.probe.k_in,
-                                                          jb.probe.k_out * jb.probe.k_out, msl_wavelength(jb.kev),
-                                                          jb.probe.df, jb.probe.cs, 1.0 / ((double)nx * ny), apchi,
-                                                          c->stream, &c->launches);
-                       }));
-            LAUNCH_TRY(c, timed(c, MSL_PROF_OTHER, [&] {
-                           return msl::launch_probe_shifts(nx, ny, 1, kyd + ny, ex, ey, c->stream, &c->launches);
-                       }));
-            SliceTables none;
-            none.k2max = 0.f;
-            none.d_kx2 = none.d_ky2 = nullptr;
-            none.d_prop = nullptr;
-            ColArgs pa = col_args(&jb.grid, none, twc, 0, slot, 1, msl::COL_PROBE | msl::COL_INV | msl::COL_STORE,
-                                  c->dflag);
-            pa.apchi = apchi;
-            pa.ex = ex;
-            pa.ey = ey;
-            LAUNCH_TRY(c, timed(c, MSL_PROF_COL, [&] { return msl::launch_col_pass(nx, pa, c->stream, c->nsm, &c->launches); }));
-        }
-        // lockstep slice loop over the running prefix
-        msl_grid gg = {nx, ny, 1.0, 1.0};
-        SliceTables none;
-        none.k2max = 0.f;
-        none.d_kx2 = none.d_ky2 = nullptr;
-        none.d_prop = nullptr;
-        for (int s = 0; s < S; ++s) {
-            int nact = 0;
-            while (nact < nb && jobs[ids[nact]].nslice > s) ++nact;
-            RowArgs r = row_args(&gg, twr, nullptr, w, nact,
-                                 msl::ROW_LOAD | msl::ROW_INV | msl::ROW_TRANS | msl::ROW_FWD, c->dflag);
-            r.trans_b = ttab + (size_t)s * nb;
-            LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_row_pass(ny, r, c->stream, c->nsm, &c->launches); }));
-            ColArgs ca = col_args(&gg, none, twc, 0, w, nact,
-                                  msl::COL_LOAD | msl::COL_FWD | msl::COL_PROP | msl::COL_INV | msl::COL_STORE, c->dflag);
-            ca.prop_b = ptabd + (size_t)s * nb;
-            ca.k2_b = ktab;
-            ca.k2max_b = dk2max;
-            LAUNCH_TRY(c, timed(c, MSL_PROF_COL, [&] { return msl::launch_col_pass(nx, ca, c->stream, c->nsm, &c->launches); }));
-        }
-        RowArgs r = row_args(&gg, twr, nullptr, w, nb, msl::ROW_LOAD | msl::ROW_INV, c->dflag);
-        LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_row_pass(ny, r, c->stream, c->nsm, &c->launches); }));
-        for (int b = 0; b < nb; ++b)
-            CUDA_TRY(c, cudaMemcpyAsync(jobs[ids[b]].exit_wave, w + (size_t)b * n2, sizeof(float2) * n2,
-                                        cudaMemcpyDefault, c->stream));
-        CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    } else if ((rc = run_job_groups(c, jobs, groups, bandlimit))) {
+        return rc;
     }
     collect_profile(c);
     if (c->dflag && (rc = err_check(c))) return rc;
@@ -1338,94 +1739,12 @@ int msl_potential_build(msl_ctx *c, const msl_atoms *at, const double *fparams, 
     if (!c) return MSL_E_ARG;
     int rc = check_grid(c, g);
     if (rc) return rc;
-    if (!at || !fparams || !v_out) return fail(c, MSL_E_ARG, "null argument");
-    if (nslice < 1) return fail(c, MSL_E_ARG, "nslice must be >= 1");
-    if (!(at->cz > 0) || !is_fin(at->cz)) return fail(c, MSL_E_ARG, "thickness cz must be positive");
-    if (!(radius > 0) || !(2.0 * radius < g->ax) || !(2.0 * radius < g->by))
-        return fail(c, MSL_E_ARG, "cutoff radius must be positive and below half the cell");
-    if (at->natom < 0 || (at->natom > 0 && (!at->x || !at->y || !at->z || !at->Z)))
-        return fail(c, MSL_E_ARG, "atom arrays are required");
+    if (!v_out) return fail(c, MSL_E_ARG, "null argument");
+    PotImage im;
+    if ((rc = potential_prepare(c, at, fparams, g, nslice, radius, im))) return rc;
     CUDA_TRY(c, cudaSetDevice(c->device));
-    const int nx = g->nx, ny = g->ny;
-    const double dz = at->cz / nslice;
-    // bin by slice (stable, so the sum order inside a slice is the input order)
-    std::vector<int> kz(at->natom), count(nslice + 1, 0);
-    for (int i = 0; i < at->natom; ++i) {
-        if (!is_fin(at->x[i]) || !is_fin(at->y[i]) || !is_fin(at->z[i]))
-            return fail(c, MSL_E_ARG, "atom coordinates must be finite (atom " + std::to_string(i) + ")");
-        int k = (int)std::floor(at->z[i] / dz);
-        if (at->z[i] < 0.0 || k < 0 || k >= nslice) k = -1;
-        if (k >= 0 && (at->Z[i] < 1 || at->Z[i] > 103))
-            return fail(c, MSL_E_ARG, "atomic number out of range 1..103 (atom " + std::to_string(i) + ")");
-        kz[i] = k;
-        if (k >= 0) count[k + 1]++;
-    }
-    for (int k = 0; k < nslice; ++k) count[k + 1] += count[k];
-    const int nkeep = count[nslice];
-    std::vector<double> xs(nkeep > 0 ? nkeep : 1), ys(nkeep > 0 ? nkeep : 1);
-    std::vector<int> zs(nkeep > 0 ? nkeep : 1), fill(count.begin(), count.end() - 1);
-    bool used[104] = {false};
-    for (int i = 0; i < at->natom; ++i) {
-        if (kz[i] < 0) continue;
-        const int p = fill[kz[i]]++;
-        xs[p] = at->x[i] - g->ax * std::floor(at->x[i] / g->ax);
-        ys[p] = at->y[i] - g->by * std::floor(at->y[i] / g->by);
-        zs[p] = at->Z[i];
-        used[at->Z[i]] = true;
-    }
-    // per-species float parameters: A = AL a, B = 2 pi sqrt(b), C = AG c / d, D = pi^2 / d
-    // (constants of slicelib.cpp:2673-2674)
-    const double AL = 300.8242834, AG = 150.4121417, PIK = 3.141592654;
-    std::vector<float> sp(104 * 12, 0.f);
-    for (int z = 1; z <= 103; ++z) {
-        if (!used[z]) continue;
-        const double *f = fparams + z * 12;
-        for (int i = 0; i < 3; ++i) {
-            const double a = f[2 * i], b = f[2 * i + 1], cc = f[6 + 2 * i], d = f[7 + 2 * i];
-            if (!(b > 0) || !(d > 0) || !is_fin(a) || !is_fin(cc))
-                return fail(c, MSL_E_ARG, "invalid FPARAMS row for Z=" + std::to_string(z));
-            sp[z * 12 + 2 * i] = (float)(AL * a);
-            sp[z * 12 + 2 * i + 1] = (float)(2.0 * PIK * sqrt(b));
-            sp[z * 12 + 6 + 2 * i] = (float)(AG * cc / d);
-            sp[z * 12 + 7 + 2 * i] = (float)(PIK * PIK / d);
-        }
-    }
-    // tabulated radial profiles of the species present (up to kPotMaxSp): cubic
-    // pieces of vzatom evaluated in FP64 over [0.15 A, radius]
-    std::vector<int> zlist, zslot(104, -1);
-    for (int z = 1; z <= 103; ++z)
-        if (used[z]) {
-            zslot[z] = (int)zlist.size();
-            zlist.push_back(z);
-        }
-    const double tab_r0 = 0.15;
-    const int nsp = (zlist.size() <= (size_t)msl::kPotMaxSp && radius > 2 * tab_r0) ? (int)zlist.size() : 0;
-    std::vector<float4> tab((size_t)std::max(nsp, 1) * msl::kPotTabN);
-    if (nsp) msl::potential_tables(fparams, zlist.data(), nsp, tab_r0, radius, tab.data());
-    // one upload: off | x | y | Z | sp | xf | yf | tab | zslot
-    std::vector<float> xf(xs.begin(), xs.end()), yf(ys.begin(), ys.end());
-    const size_t o_off = 0, o_x = ((sizeof(int) * (nslice + 1) + 15) / 16) * 16;
-    const size_t o_y = o_x + sizeof(double) * xs.size(), o_z = o_y + sizeof(double) * ys.size();
-    const size_t o_sp = ((o_z + sizeof(int) * zs.size() + 15) / 16) * 16;
-    const size_t o_xf = ((o_sp + sizeof(float) * sp.size() + 15) / 16) * 16;
-    const size_t o_yf = ((o_xf + sizeof(float) * xf.size() + 15) / 16) * 16;
-    const size_t o_tab = ((o_yf + sizeof(float) * yf.size() + 15) / 16) * 16;
-    const size_t o_zs = o_tab + sizeof(float4) * tab.size();
-    const size_t total = o_zs + sizeof(int) * zslot.size();
-    std::vector<unsigned char> h(total, 0);
-    memcpy(h.data() + o_tab, tab.data(), sizeof(float4) * tab.size());
-    memcpy(h.data() + o_zs, zslot.data(), sizeof(int) * zslot.size());
-    memcpy(h.data() + o_off, count.data(), sizeof(int) * (nslice + 1));
-    memcpy(h.data() + o_x, xs.data(), sizeof(double) * xs.size());
-    memcpy(h.data() + o_y, ys.data(), sizeof(double) * ys.size());
-    memcpy(h.data() + o_z, zs.data(), sizeof(int) * zs.size());
-    memcpy(h.data() + o_sp, sp.data(), sizeof(float) * sp.size());
-    memcpy(h.data() + o_xf, xf.data(), sizeof(float) * xf.size());
-    memcpy(h.data() + o_yf, yf.data(), sizeof(float) * yf.size());
-    rc = upload(c, c->atoms, h.data(), total);
-    if (rc) return rc;
-    unsigned char *d = (unsigned char *)c->atoms.p;
-    const size_t vbytes = sizeof(float) * (size_t)nslice * nx * ny;
+    if ((rc = upload(c, c->atoms, im.h.data(), im.h.size()))) return rc;
+    const size_t vbytes = sizeof(float) * (size_t)nslice * g->nx * g->ny;
     float *vd;
     const bool vdev = on_device(v_out);
     if (vdev) {
@@ -1434,29 +1753,7 @@ int msl_potential_build(msl_ctx *c, const msl_atoms *at, const double *fparams, 
         CUDA_TRY(c, c->pot.ensure(vbytes));
         vd = (float *)c->pot.p;
     }
-    msl::PotArgs a;
-    a.x = (const double *)(d + o_x);
-    a.y = (const double *)(d + o_y);
-    a.xf = (const float *)(d + o_xf);
-    a.yf = (const float *)(d + o_yf);
-    a.Z = (const int *)(d + o_z);
-    a.off = (const int *)(d + o_off);
-    a.nslice = nslice;
-    a.nx = nx;
-    a.ny = ny;
-    a.ax = g->ax;
-    a.by = g->by;
-    a.dxp = g->ax / nx;
-    a.dyp = g->by / ny;
-    a.rad2 = (float)(radius * radius);
-    a.sp = (const float *)(d + o_sp);
-    a.v = vd;
-    a.tab = (const float4 *)(d + o_tab);
-    a.zslot = (const int *)(d + o_zs);
-    a.nsp = nsp;
-    a.tab_r0 = (float)tab_r0;
-    a.tab_inv_h = (float)(msl::kPotTabN / (radius - tab_r0));
-    LAUNCH_TRY(c, timed(c, MSL_PROF_POTENTIAL, [&] { return msl::launch_potential(a, c->stream, &c->launches); }));
+    if ((rc = potential_launch(c, im, (const unsigned char *)c->atoms.p, g, nslice, radius, vd))) return rc;
     if (!vdev) CUDA_TRY(c, cudaMemcpyAsync(v_out, vd, vbytes, cudaMemcpyDeviceToHost, c->stream));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     collect_profile(c);
@@ -1488,19 +1785,7 @@ int msl_transmission_build(msl_ctx *c, const msl_grid *g, const msl_optics *o, c
     if ((rc = build_slice_tables(c, g, o, 1, nullptr, st))) return rc;
     float2 *twr = twiddles(c, ny), *twc = twiddles(c, nx);
     if (!twr || !twc) return fail(c, MSL_E_NOMEM, "twiddle table allocation failed");
-    // t = exp(i sigma V) elementwise, then the band limit: forward transform,
-    // 2/3 mask, inverse transform (mulslice.cpp:414-421, :515-522)
-    const double phase_scale = msl_sigma(o->kev) / 1000.0;  // rad per V*A
-    LAUNCH_TRY(c, timed(c, MSL_PROF_OTHER, [&] {
-                   return msl::launch_transmission_phase(vd, phase_scale, n2 * nlayer, td, c->nsm, c->stream,
-                                                         &c->launches);
-               }));
-    RowArgs r = row_args(g, twr, nullptr, td, nlayer, msl::ROW_LOAD | msl::ROW_FWD, c->dflag);
-    LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_row_pass(ny, r, c->stream, c->nsm, &c->launches); }));
-    ColArgs ca = col_args(g, st, twc, 0, td, nlayer, msl::COL_LOAD | msl::COL_FWD | msl::COL_PROP | msl::COL_INV | msl::COL_STORE, c->dflag);
-    LAUNCH_TRY(c, timed(c, MSL_PROF_COL, [&] { return msl::launch_col_pass(nx, ca, c->stream, c->nsm, &c->launches); }));
-    r = row_args(g, twr, nullptr, td, nlayer, msl::ROW_LOAD | msl::ROW_INV, c->dflag);
-    LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_row_pass(ny, r, c->stream, c->nsm, &c->launches); }));
+    if ((rc = transmission_enqueue(c, g, o, vd, nlayer, td, st, twr, twc))) return rc;
     if (!tdev)
         CUDA_TRY(c, cudaMemcpyAsync(t_out, td, sizeof(float2) * n2 * nlayer, cudaMemcpyDeviceToHost,
                                     c->stream));
@@ -2254,7 +2539,7 @@ int msl_stem_scan_phonon(msl_ctx *c, const msl_atoms *at, const double *fparams,
     for (int p = 0; p < 2 * nprobe; ++p)
         if (!is_fin(probe_xy[p])) return fail(c, MSL_E_ARG, "probe positions must be finite");
     CUDA_TRY(c, cudaSetDevice(c->device));
-    const int nx = g->nx, ny = g->ny, ndet = det->ndet, na = at->natom;
+    const int nx = g->nx, ny = g->ny, ndet = det->ndet;
     const size_t n2 = (size_t)nx * ny;
 
     // configurations per batch: as many transmission stacks as 16 GiB hold (half
@@ -2269,9 +2554,8 @@ int msl_stem_scan_phonon(msl_ctx *c, const msl_atoms *at, const double *fparams,
                                 : (int)std::max<size_t>(1, wbudget / (sizeof(float2) * n2 * BC));
     if (BP > nprobe) BP = nprobe;
     const int BI = BC * BP;  // images per launch at most
-    DevBuf vbuf, tbuf, pbuf;
-    vbuf.mb = tbuf.mb = pbuf.mb = &c->mem;
-    CUDA_TRY(c, vbuf.ensure(sizeof(float) * n2 * nslice));
+    DevBuf tbuf, pbuf;
+    tbuf.mb = pbuf.mb = &c->mem;
     CUDA_TRY(c, tbuf.ensure(slab * BC));
     CUDA_TRY(c, pbuf.ensure(sizeof(float2 *) * (size_t)nslice * BI));
 
@@ -2297,30 +2581,14 @@ int msl_stem_scan_phonon(msl_ctx *c, const msl_atoms *at, const double *fparams,
     const double dscale = (double)n2 * (double)n2;
     std::vector<const float2 *> hptab((size_t)nslice * BI);
     std::vector<double> hf(2 * (size_t)BI);
-    std::vector<double> x(na), y(na), z(na), dd(3 * (size_t)na);
-    msl_atoms jat = *at;
-    jat.x = x.data();
-    jat.y = y.data();
-    jat.z = z.data();
+    PhononBuilder pb(c, at, fparams, g, nslice, radius, o, nconfig, sigma, seed);
+    if ((rc = pb.init())) return rc;
     if ((rc = err_reset(c))) return rc;
     for (int c0 = 0; c0 < nconfig; c0 += BC) {
         const int nc = std::min(BC, nconfig - c0);
         // this batch's configurations: displaced atoms -> potential -> transmission stack
-        for (int j = 0; j < nc; ++j) {
-            msl_phonon_displacements(seed, c0 + j, na, sigma, dd.data());
-            for (int i = 0; i < na; ++i) {
-                x[i] = at->x[i] + dd[3 * i];
-                y[i] = at->y[i] + dd[3 * i + 1];
-                z[i] = at->z[i] + dd[3 * i + 2];
-            }
-            if ((rc = msl_potential_build(c, &jat, fparams, g, nslice, radius, (float *)vbuf.p))) return rc;
-            if ((rc = msl_transmission_build(c, g, o, (const float *)vbuf.p, nslice,
-                                             (float *)(tall + slab / sizeof(float2) * j))))
-                return rc;
-        }
-        if ((rc = err_reset(c))) return rc;  // the builders above check and clear the flag themselves
-        // the builders above reuse the context's table buffers, so this batch's
-        // slice tables, probe and detector tables are built after them
+        for (int j = 0; j < nc; ++j)
+            if ((rc = pb.build(c0 + j, tall + slab / sizeof(float2) * j))) return rc;
         SliceTables st;
         if ((rc = build_slice_tables(c, g, o, 1, dz.data(), st))) return rc;
         float2 *twr = twiddles(c, ny), *twc = twiddles(c, nx);

@@ -12,15 +12,17 @@
 //
 // GB300 design: one CTA per 32 x 32 pixel tile of one slice, four pixels per
 // thread (independent accumulators for latency hiding).  The slice's atoms
-// stream through in chunks of 128; each chunk is culled against the tile's
-// periodic bounding box (in float, from float copies of the coordinates, with a
-// margin that keeps every atom the FP64 test would: culling only has to be
-// conservative) and compacted in atom order (so the float sum order is
-// fixed), then the per-atom x and y offsets of the tile's 32 columns and 32 rows
-// are formed once in FP64 (so an atom sitting exactly on a pixel gives r = 0,
-// clamped to 1e-10 A as the reference does, never a float rounding residue)
-// and the pair loop runs in FP32 on those offsets.  Every pixel sums its atoms
-// in atom order, whatever the tile shape.
+// stream through in rounds of 512, two per thread; each round is culled
+// against the tile's periodic bounding box (in float, from float copies of the
+// coordinates, with a margin that keeps every atom the FP64 test would:
+// culling only has to be conservative) and compacted in atom order (so the
+// float sum order is fixed) into a list of at most 128 atoms at a time, then
+// the per-atom x and y offsets of the tile's 32 columns and 32 rows are formed
+// once in FP64 (so an atom sitting exactly on a pixel gives r = 0, clamped to
+// 1e-10 A as the reference does, never a float rounding residue) and the pair
+// loop runs in FP32 on those offsets.  A slice of up to 512 atoms is thus one
+// cull, one compaction and one pair loop per tile (four CTA barriers).  Every
+// pixel sums its atoms in atom order, whatever the tile shape.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
@@ -30,9 +32,10 @@
 namespace msl {
 
 namespace {
-// tile and chunk shape picked by timing 16 / 32 / 64-pixel-wide tiles and
-// 32 / 64 / 128-atom chunks on the Au 2048^2 potentials
-constexpr int TX = 32, TY = 32, THREADS = 256, PX = TX * TY / THREADS, CHUNK = 128;
+// tile shape and list capacity picked by timing 16 / 32 / 64-pixel-wide tiles
+// and 32 / 64 / 128-atom lists on the Au 2048^2 potentials
+constexpr int TX = 32, TY = 32, THREADS = 256, PX = TX * TY / THREADS, CAP = 128;
+constexpr int KR = 2, ROUND = KR * THREADS, NW = THREADS / 32;  // atoms culled per thread per round
 
 __device__ __forceinline__ float poly(const float *c, int n, float t) {
     float s = c[n - 1];
@@ -61,12 +64,12 @@ __device__ __forceinline__ float bessk0f(float x) {
 template <bool TAB>
 __global__ void __launch_bounds__(THREADS) potential_kernel(PotArgs a) {
     extern __shared__ float4 stab[];  // TAB: [nsp][kPotTabN] cubic pieces of the species' radial profiles
-    __shared__ int sZ[CHUNK];
-    __shared__ int sS[CHUNK];
-    __shared__ double sxa[CHUNK], sya[CHUNK];
-    __shared__ float sdx[CHUNK][TX];
-    __shared__ float sdy[CHUNK][TY];
-    __shared__ int wcount[THREADS / 32];
+    __shared__ int sZ[CAP];
+    __shared__ int sS[CAP];
+    __shared__ double sxa[CAP], sya[CAP];
+    __shared__ float sdx[CAP][TX];
+    __shared__ float sdy[CAP][TY];
+    __shared__ int wcount[KR * NW];
     const int tid = threadIdx.x;
     if (TAB) {
         for (int i = tid; i < a.nsp * kPotTabN; i += THREADS) stab[i] = a.tab[i];
@@ -87,82 +90,108 @@ __global__ void __launch_bounds__(THREADS) potential_kernel(PotArgs a) {
 #pragma unroll
     for (int j = 0; j < PX; ++j) acc[j] = 0.f;
 
-    for (int c0 = a0; c0 < a1; c0 += CHUNK) {
-        const int ai = c0 + tid;
-        bool keep = false;
-        double xa = 0.0, ya = 0.0;
-        int z = 0;
-        if (tid < CHUNK && ai < a1) {
-            float dx = fabsf(a.xf[ai] - xc);
-            dx = fminf(dx, axf - dx);
-            float dy = fabsf(a.yf[ai] - yc);
-            dy = fminf(dy, byf - dy);
-            keep = (dx - hx < rad) && (dy - hy < rad);
-            if (keep) {
-                xa = a.x[ai];
-                ya = a.y[ai];
-                z = a.Z[ai];
-            }
-        }
-        // order-preserving compaction of the kept atoms
-        const unsigned ball = __ballot_sync(0xffffffffu, keep);
-        __syncthreads();  // the previous chunk's pair loop is done with the lists
-        if (lane == 0) wcount[warp] = __popc(ball);
-        __syncthreads();
-        int pos = __popc(ball & ((1u << lane) - 1u));
-        int total = 0;
-        for (int w = 0; w < THREADS / 32; ++w) {
-            if (w < warp) pos += wcount[w];
-            total += wcount[w];
-        }
-        if (keep) {
-            sZ[pos] = z;
-            if (TAB) sS[pos] = a.zslot[z];
-            sxa[pos] = xa;
-            sya[pos] = ya;
-        }
-        __syncthreads();
-        // per-atom offsets of this tile's columns and rows, formed in FP64 with
-        // the minimum image of ModelPotential.cu:154-203 (|d|, folded past half a cell)
-        for (int idx = tid; idx < total * (TX + TY); idx += THREADS) {
-            const int k = idx / (TX + TY), i = idx % (TX + TY);
-            if (i < TX) {
-                double d = fabs(sxa[k] - (double)(ix0 + i) * a.dxp);
-                if (d >= 0.5 * a.ax) d = a.ax - d;
-                sdx[k][i] = (float)d;
-            } else {
-                double d = fabs(sya[k] - (double)(iy0 + i - TX) * a.dyp);
-                if (d >= 0.5 * a.by) d = a.by - d;
-                sdy[k][i - TX] = (float)d;
-            }
-        }
-        __syncthreads();
-        for (int k = 0; k < total; ++k) {
-            const float dy = sdy[k][ty];
-            const float *p = a.sp + sZ[k] * 12;
-            const float4 *tb = TAB ? stab + sS[k] * kPotTabN : nullptr;
+    for (int c0 = a0; c0 < a1; c0 += ROUND) {
+        // cull: atom c0 + k THREADS + tid; the kept atoms' FP64 coordinates and
+        // species are loaded right away so their latency overlaps the compaction
+        bool keep[KR];
+        unsigned ball[KR];
+        double xa[KR], ya[KR];
+        int za[KR];
 #pragma unroll
-            for (int j = 0; j < PX; ++j) {
-                const float dx = sdx[k][txg + 8 * j];
-                const float r2 = dx * dx + dy * dy;
-                if (r2 < a.rad2) {
-                    const float r = fmaxf(sqrtf(r2), 1.0e-10f);
-                    if (TAB && r >= a.tab_r0) {
-                        // cubic piece of the tabulated profile: ((c3 t + c2) t + c1) t + c0
-                        const float u = (r - a.tab_r0) * a.tab_inv_h;
-                        const int i = min((int)u, kPotTabN - 1);
-                        const float t = u - (float)i;
-                        const float4 c = tb[i];
-                        acc[j] += fmaf(fmaf(fmaf(c.w, t, c.z), t, c.y), t, c.x);
-                        continue;
+        for (int k = 0; k < KR; ++k) {
+            const int ai = c0 + k * THREADS + tid;
+            keep[k] = false;
+            xa[k] = ya[k] = 0.0;
+            za[k] = 0;
+            if (ai < a1) {
+                float dx = fabsf(a.xf[ai] - xc);
+                dx = fminf(dx, axf - dx);
+                float dy = fabsf(a.yf[ai] - yc);
+                dy = fminf(dy, byf - dy);
+                keep[k] = (dx - hx < rad) && (dy - hy < rad);
+                if (keep[k]) {
+                    xa[k] = a.x[ai];
+                    ya[k] = a.y[ai];
+                    za[k] = a.Z[ai];
+                }
+            }
+            ball[k] = __ballot_sync(0xffffffffu, keep[k]);
+        }
+        __syncthreads();  // the previous round's pair loop is done with wcount and the lists
+        if (lane == 0) {
+#pragma unroll
+            for (int k = 0; k < KR; ++k) wcount[k * NW + warp] = __popc(ball[k]);
+        }
+        __syncthreads();
+        // order-preserving positions: atom order is (k, warp, lane)
+        int pos[KR], total = 0;
+#pragma unroll
+        for (int k = 0; k < KR; ++k) {
+            int before = 0, sum = 0;
+            for (int w = 0; w < NW; ++w) {
+                const int n = wcount[k * NW + w];
+                if (w < warp) before += n;
+                sum += n;
+            }
+            pos[k] = total + before + __popc(ball[k] & ((1u << lane) - 1u));
+            total += sum;
+        }
+        for (int piece = 0; piece < total; piece += CAP) {
+            if (piece > 0) __syncthreads();  // the previous piece's pair loop is done with the lists
+#pragma unroll
+            for (int k = 0; k < KR; ++k) {
+                const int p = pos[k] - piece;
+                if (keep[k] && p >= 0 && p < CAP) {
+                    sZ[p] = za[k];
+                    if (TAB) sS[p] = a.zslot[za[k]];
+                    sxa[p] = xa[k];
+                    sya[p] = ya[k];
+                }
+            }
+            __syncthreads();
+            const int n = min(CAP, total - piece);
+            // per-atom offsets of this tile's columns and rows, formed in FP64 with
+            // the minimum image of ModelPotential.cu:154-203 (|d|, folded past half a cell)
+            for (int idx = tid; idx < n * (TX + TY); idx += THREADS) {
+                const int k = idx / (TX + TY), i = idx % (TX + TY);
+                if (i < TX) {
+                    double d = fabs(sxa[k] - (double)(ix0 + i) * a.dxp);
+                    if (d >= 0.5 * a.ax) d = a.ax - d;
+                    sdx[k][i] = (float)d;
+                } else {
+                    double d = fabs(sya[k] - (double)(iy0 + i - TX) * a.dyp);
+                    if (d >= 0.5 * a.by) d = a.by - d;
+                    sdy[k][i - TX] = (float)d;
+                }
+            }
+            __syncthreads();
+            for (int k = 0; k < n; ++k) {
+                const float dy = sdy[k][ty];
+                const float *p = a.sp + sZ[k] * 12;
+                const float4 *tb = TAB ? stab + sS[k] * kPotTabN : nullptr;
+#pragma unroll
+                for (int j = 0; j < PX; ++j) {
+                    const float dx = sdx[k][txg + 8 * j];
+                    const float r2 = dx * dx + dy * dy;
+                    if (r2 < a.rad2) {
+                        const float r = fmaxf(sqrtf(r2), 1.0e-10f);
+                        if (TAB && r >= a.tab_r0) {
+                            // cubic piece of the tabulated profile: ((c3 t + c2) t + c1) t + c0
+                            const float u = (r - a.tab_r0) * a.tab_inv_h;
+                            const int i = min((int)u, kPotTabN - 1);
+                            const float t = u - (float)i;
+                            const float4 c = tb[i];
+                            acc[j] += fmaf(fmaf(fmaf(c.w, t, c.z), t, c.y), t, c.x);
+                            continue;
+                        }
+                        float v = __ldg(p + 0) * bessk0f(__ldg(p + 1) * r) +
+                                  __ldg(p + 2) * bessk0f(__ldg(p + 3) * r) +
+                                  __ldg(p + 4) * bessk0f(__ldg(p + 5) * r);
+                        const float rr = r * r;
+                        v += __ldg(p + 6) * expf(-__ldg(p + 7) * rr) + __ldg(p + 8) * expf(-__ldg(p + 9) * rr) +
+                             __ldg(p + 10) * expf(-__ldg(p + 11) * rr);
+                        acc[j] += v;
                     }
-                    float v = __ldg(p + 0) * bessk0f(__ldg(p + 1) * r) +
-                              __ldg(p + 2) * bessk0f(__ldg(p + 3) * r) +
-                              __ldg(p + 4) * bessk0f(__ldg(p + 5) * r);
-                    const float rr = r * r;
-                    v += __ldg(p + 6) * expf(-__ldg(p + 7) * rr) + __ldg(p + 8) * expf(-__ldg(p + 9) * rr) +
-                         __ldg(p + 10) * expf(-__ldg(p + 11) * rr);
-                    acc[j] += v;
                 }
             }
         }

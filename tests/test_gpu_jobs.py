@@ -97,3 +97,17 @@ def test_uneven_workload_every_side(ctx):
     ref, _ = O.multislice(psi0, job["trans"].astype(np.complex128), props, job["layer_seq"],
                           O.band_mask(nx, ny, job["ax"], job["by"]))
     assert O.rel_l2(outs[j], ref) < 2e-5
+
+
+def test_uneven_batch_same_under_memory_cap():
+    """Groups run concurrently on their own streams without a memory cap and one
+    after another in shared buffers under one; the exit waves are identical."""
+    from multislice_gb300 import Context
+    jobs = _jobs(seed=9, n=12)
+    with Context(0) as c:
+        free = c.run_jobs(jobs)
+        c.set_memory_limit(1 << 30)
+        capped = c.run_jobs(jobs)
+        assert c.memory_in_use() <= 1 << 30
+    for a, b in zip(free, capped):
+        assert np.array_equal(a, b)
