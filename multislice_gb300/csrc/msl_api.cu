@@ -840,11 +840,14 @@ namespace {
 // Host half of a potential build: the atoms validated and binned by slice
 // (stably, so the sum order inside a slice is the input order), the
 // per-species parameters and radial tables, laid out as one upload image
-// off | x | y | Z | sp | xf | yf | tab | zslot.  The radial tables are kept
-// and reused while the species, the cutoff and the FPARAMS table stay the same.
+// off | ic | jc | fx | fy | Z | sp | xf | yf | tab | zslot.  Each atom is
+// given as its nearest pixel (ic, jc) and the residue x - ic dxp, y - jc dyp
+// formed in FP64 and rounded to float.  The radial tables are kept and reused
+// while the species, the cutoff and the FPARAMS table stay the same.
 struct PotImage {
     std::vector<unsigned char> h;
-    size_t o_off = 0, o_x = 0, o_y = 0, o_z = 0, o_sp = 0, o_xf = 0, o_yf = 0, o_tab = 0, o_zs = 0;
+    size_t o_off = 0, o_ic = 0, o_jc = 0, o_fx = 0, o_fy = 0, o_z = 0, o_sp = 0, o_xf = 0, o_yf = 0, o_tab = 0,
+           o_zs = 0;
     int nsp = 0;
     double tab_r0 = 0.15;
     std::vector<int> tab_z;
@@ -914,29 +917,37 @@ int potential_prepare(msl_ctx *c, const msl_atoms *at, const double *fparams, co
         im.tab_radius = radius;
         im.tab_fp = fparams;
     }
+    auto up16 = [](size_t x) { return ((x + 15) / 16) * 16; };
     im.o_off = 0;
-    im.o_x = ((sizeof(int) * (nslice + 1) + 15) / 16) * 16;
-    im.o_y = im.o_x + sizeof(double) * nk;
-    im.o_z = im.o_y + sizeof(double) * nk;
-    im.o_sp = ((im.o_z + sizeof(int) * nk + 15) / 16) * 16;
-    im.o_xf = ((im.o_sp + sizeof(float) * sp.size() + 15) / 16) * 16;
-    im.o_yf = ((im.o_xf + sizeof(float) * nk + 15) / 16) * 16;
-    im.o_tab = ((im.o_yf + sizeof(float) * nk + 15) / 16) * 16;
+    im.o_ic = up16(sizeof(int) * (nslice + 1));
+    im.o_jc = up16(im.o_ic + sizeof(int) * nk);
+    im.o_fx = up16(im.o_jc + sizeof(int) * nk);
+    im.o_fy = up16(im.o_fx + sizeof(float) * nk);
+    im.o_z = up16(im.o_fy + sizeof(float) * nk);
+    im.o_sp = up16(im.o_z + sizeof(int) * nk);
+    im.o_xf = up16(im.o_sp + sizeof(float) * sp.size());
+    im.o_yf = up16(im.o_xf + sizeof(float) * nk);
+    im.o_tab = up16(im.o_yf + sizeof(float) * nk);
     im.o_zs = im.o_tab + sizeof(float4) * im.tab.size();
     im.h.assign(im.o_zs + sizeof(int) * zslot.size(), 0);
     unsigned char *h = im.h.data();
-    double *xs = (double *)(h + im.o_x), *ys = (double *)(h + im.o_y);
-    int *zs = (int *)(h + im.o_z);
+    int *ics = (int *)(h + im.o_ic), *jcs = (int *)(h + im.o_jc), *zs = (int *)(h + im.o_z);
+    float *fxs = (float *)(h + im.o_fx), *fys = (float *)(h + im.o_fy);
     float *xf = (float *)(h + im.o_xf), *yf = (float *)(h + im.o_yf);
+    const double dxp = g->ax / g->nx, dyp = g->by / g->ny;
     std::vector<int> fill(count.begin(), count.end() - 1);
     for (int i = 0; i < at->natom; ++i) {
         if (kz[i] < 0) continue;
         const int p = fill[kz[i]]++;
-        double xw, yw;
-        xw = at->x[i] - g->ax * std::floor(at->x[i] / g->ax);
-        yw = at->y[i] - g->by * std::floor(at->y[i] / g->by);
-        memcpy(xs + p, &xw, sizeof(double));
-        memcpy(ys + p, &yw, sizeof(double));
+        const double xw = at->x[i] - g->ax * std::floor(at->x[i] / g->ax);
+        const double yw = at->y[i] - g->by * std::floor(at->y[i] / g->by);
+        // nearest pixel and the FP64 residue (the same expression as |x - ix dxp|
+        // at that pixel); the pixel index is then wrapped into the grid
+        const double ci = std::floor(xw / dxp + 0.5), cj = std::floor(yw / dyp + 0.5);
+        fxs[p] = (float)(xw - ci * dxp);
+        fys[p] = (float)(yw - cj * dyp);
+        ics[p] = (int)ci % g->nx;
+        jcs[p] = (int)cj % g->ny;
         zs[p] = at->Z[i];
         xf[p] = (float)xw;
         yf[p] = (float)yw;
@@ -952,8 +963,10 @@ int potential_prepare(msl_ctx *c, const msl_atoms *at, const double *fparams, co
 int potential_launch(msl_ctx *c, const PotImage &im, const unsigned char *d, const msl_grid *g, int nslice,
                      double radius, float *vd) {
     msl::PotArgs a;
-    a.x = (const double *)(d + im.o_x);
-    a.y = (const double *)(d + im.o_y);
+    a.ic = (const int *)(d + im.o_ic);
+    a.jc = (const int *)(d + im.o_jc);
+    a.fx = (const float *)(d + im.o_fx);
+    a.fy = (const float *)(d + im.o_fy);
     a.xf = (const float *)(d + im.o_xf);
     a.yf = (const float *)(d + im.o_yf);
     a.Z = (const int *)(d + im.o_z);
@@ -965,6 +978,8 @@ int potential_launch(msl_ctx *c, const PotImage &im, const unsigned char *d, con
     a.by = g->by;
     a.dxp = g->ax / g->nx;
     a.dyp = g->by / g->ny;
+    a.dxpf = (float)a.dxp;
+    a.dypf = (float)a.dyp;
     a.rad2 = (float)(radius * radius);
     a.sp = (const float *)(d + im.o_sp);
     a.v = vd;

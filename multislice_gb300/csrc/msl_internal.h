@@ -112,12 +112,17 @@ struct ColArgs {
 };
 
 struct PotArgs {
-    const double *x, *y;      // wrapped into [0, ax), [0, by)
-    const float *xf, *yf;     // the same, rounded to float (for the conservative tile culling)
+    // atom position as its nearest pixel (ic, jc) plus the residue x - ic dxp,
+    // y - jc dyp formed in FP64 and rounded to float (an atom on a pixel keeps
+    // the FP64 residue there: r is then clamped to 1e-10 A as in vzatom)
+    const int *ic, *jc;
+    const float *fx, *fy;
+    const float *xf, *yf;     // wrapped into [0, ax), [0, by), rounded to float (tile culling)
     const int *Z;
     const int *off;           // [nslice + 1] atom ranges per slice
     int nslice, nx, ny;
     double ax, by, dxp, dyp;
+    float dxpf, dypf;         // pixel sizes rounded to float
     float rad2;               // radius^2 (float compare, r < radius)
     const float *sp;          // [104][12] A1 B1 A2 B2 A3 B3 C1 D1 C2 D2 C3 D3
     float *v;                 // [nslice][nx][ny]

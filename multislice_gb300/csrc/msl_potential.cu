@@ -12,17 +12,19 @@
 //
 // GB300 design: one CTA per 32 x 32 pixel tile of one slice, four pixels per
 // thread (independent accumulators for latency hiding).  The slice's atoms
-// stream through in rounds of 512, two per thread; each round is culled
-// against the tile's periodic bounding box (in float, from float copies of the
-// coordinates, with a margin that keeps every atom the FP64 test would:
+// stream through in rounds of 512, two per thread; each round is culled against
+// the tile's periodic bounding box (in float, from float copies of the
+// coordinates, with a margin that keeps every atom the exact test would:
 // culling only has to be conservative) and compacted in atom order (so the
-// float sum order is fixed) into a list of at most 128 atoms at a time, then
-// the per-atom x and y offsets of the tile's 32 columns and 32 rows are formed
-// once in FP64 (so an atom sitting exactly on a pixel gives r = 0, clamped to
-// 1e-10 A as the reference does, never a float rounding residue) and the pair
-// loop runs in FP32 on those offsets.  A slice of up to 512 atoms is thus one
-// cull, one compaction and one pair loop per tile (four CTA barriers).  Every
-// pixel sums its atoms in atom order, whatever the tile shape.
+// float sum order is fixed) into a list of at most 64 atoms at a time.  Each
+// atom arrives as its nearest pixel (ic, jc) and the residue x - ic dxp,
+// y - jc dyp, formed on the host in FP64 and rounded to float, so the offset of
+// pixel column ix is |residue + m dxp| with m = ic - ix folded to the minimum
+// image in integers: all in FP32, and an atom sitting exactly on a pixel keeps
+// the FP64 residue there (r is then clamped to 1e-10 A as the reference does,
+// never a float rounding residue).  The per-atom offsets of the tile's 32
+// columns and 32 rows are formed once per tile and the pair loop runs in FP32
+// on them.  Every pixel sums its atoms in atom order, whatever the tile shape.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
@@ -34,7 +36,7 @@ namespace msl {
 namespace {
 // tile shape and list capacity picked by timing 16 / 32 / 64-pixel-wide tiles
 // and 32 / 64 / 128-atom lists on the Au 2048^2 potentials
-constexpr int TX = 32, TY = 32, THREADS = 256, PX = TX * TY / THREADS, CAP = 128;
+constexpr int TX = 32, TY = 32, THREADS = 256, PX = TX * TY / THREADS, CAP = 64;
 constexpr int KR = 2, ROUND = KR * THREADS, NW = THREADS / 32;  // atoms culled per thread per round
 
 __device__ __forceinline__ float poly(const float *c, int n, float t) {
@@ -62,11 +64,12 @@ __device__ __forceinline__ float bessk0f(float x) {
 }  // namespace
 
 template <bool TAB>
-__global__ void __launch_bounds__(THREADS) potential_kernel(PotArgs a) {
+__global__ void __launch_bounds__(THREADS, 5) potential_kernel(PotArgs a) {
     extern __shared__ float4 stab[];  // TAB: [nsp][kPotTabN] cubic pieces of the species' radial profiles
     __shared__ int sZ[CAP];
     __shared__ int sS[CAP];
-    __shared__ double sxa[CAP], sya[CAP];
+    __shared__ int sic[CAP], sjc[CAP];
+    __shared__ float sfx[CAP], sfy[CAP];
     __shared__ float sdx[CAP][TX];
     __shared__ float sdy[CAP][TY];
     __shared__ int wcount[KR * NW];
@@ -91,18 +94,18 @@ __global__ void __launch_bounds__(THREADS) potential_kernel(PotArgs a) {
     for (int j = 0; j < PX; ++j) acc[j] = 0.f;
 
     for (int c0 = a0; c0 < a1; c0 += ROUND) {
-        // cull: atom c0 + k THREADS + tid; the kept atoms' FP64 coordinates and
+        // cull: atom c0 + k THREADS + tid; the kept atoms' pixel positions and
         // species are loaded right away so their latency overlaps the compaction
         bool keep[KR];
         unsigned ball[KR];
-        double xa[KR], ya[KR];
-        int za[KR];
+        int ia[KR], ja[KR], za[KR];
+        float fxa[KR], fya[KR];
 #pragma unroll
         for (int k = 0; k < KR; ++k) {
             const int ai = c0 + k * THREADS + tid;
             keep[k] = false;
-            xa[k] = ya[k] = 0.0;
-            za[k] = 0;
+            ia[k] = ja[k] = za[k] = 0;
+            fxa[k] = fya[k] = 0.f;
             if (ai < a1) {
                 float dx = fabsf(a.xf[ai] - xc);
                 dx = fminf(dx, axf - dx);
@@ -110,8 +113,10 @@ __global__ void __launch_bounds__(THREADS) potential_kernel(PotArgs a) {
                 dy = fminf(dy, byf - dy);
                 keep[k] = (dx - hx < rad) && (dy - hy < rad);
                 if (keep[k]) {
-                    xa[k] = a.x[ai];
-                    ya[k] = a.y[ai];
+                    ia[k] = a.ic[ai];
+                    ja[k] = a.jc[ai];
+                    fxa[k] = a.fx[ai];
+                    fya[k] = a.fy[ai];
                     za[k] = a.Z[ai];
                 }
             }
@@ -144,24 +149,28 @@ __global__ void __launch_bounds__(THREADS) potential_kernel(PotArgs a) {
                 if (keep[k] && p >= 0 && p < CAP) {
                     sZ[p] = za[k];
                     if (TAB) sS[p] = a.zslot[za[k]];
-                    sxa[p] = xa[k];
-                    sya[p] = ya[k];
+                    sic[p] = ia[k];
+                    sjc[p] = ja[k];
+                    sfx[p] = fxa[k];
+                    sfy[p] = fya[k];
                 }
             }
             __syncthreads();
             const int n = min(CAP, total - piece);
-            // per-atom offsets of this tile's columns and rows, formed in FP64 with
-            // the minimum image of ModelPotential.cu:154-203 (|d|, folded past half a cell)
+            // per-atom offsets of this tile's columns and rows: |residue + m pixel|,
+            // m the pixel difference folded to the minimum image (ModelPotential.cu:154-203)
             for (int idx = tid; idx < n * (TX + TY); idx += THREADS) {
                 const int k = idx / (TX + TY), i = idx % (TX + TY);
                 if (i < TX) {
-                    double d = fabs(sxa[k] - (double)(ix0 + i) * a.dxp);
-                    if (d >= 0.5 * a.ax) d = a.ax - d;
-                    sdx[k][i] = (float)d;
+                    int m = sic[k] - (ix0 + i);
+                    if (2 * m >= a.nx) m -= a.nx;
+                    else if (2 * m < -a.nx) m += a.nx;
+                    sdx[k][i] = fabsf(fmaf((float)m, a.dxpf, sfx[k]));
                 } else {
-                    double d = fabs(sya[k] - (double)(iy0 + i - TX) * a.dyp);
-                    if (d >= 0.5 * a.by) d = a.by - d;
-                    sdy[k][i - TX] = (float)d;
+                    int m = sjc[k] - (iy0 + i - TX);
+                    if (2 * m >= a.ny) m -= a.ny;
+                    else if (2 * m < -a.ny) m += a.ny;
+                    sdy[k][i - TX] = fabsf(fmaf((float)m, a.dypf, sfy[k]));
                 }
             }
             __syncthreads();

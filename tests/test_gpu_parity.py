@@ -62,6 +62,22 @@ def test_potential_empty_and_outside_atoms(ctx):
     assert np.all(ctx.potential(empty, 64, 64, 2, 3.0) == 0)
 
 
+@pytest.mark.parametrize("natom", [300, 513, 1500])
+def test_potential_dense_slices_vs_oracle(ctx, fparams, natom):
+    """A slice holding fewer and more atoms than the gather keeps in shared memory
+    (512), with tiles that keep more than one list of 64 atoms, and an empty
+    slice after it: equal to the FP64 oracle within FP32 rounding."""
+    rng = np.random.default_rng(natom)
+    a = 16.0
+    x, y = rng.uniform(0, a, natom), rng.uniform(0, a, natom)
+    z = rng.uniform(0, 1.5, natom)                  # all in the first of two 1.5 A slices
+    Z = rng.choice([6, 14, 29, 79], natom).astype(np.int32)
+    spec = S.Specimen(x, y, z, Z, a, a, 3.0)
+    v = ctx.potential(spec, 128, 128, 2, 2.5).astype(np.float64)
+    ref = O.potential(x, y, z, Z, fparams, a, a, 3.0, 128, 128, 2, 2.5)
+    assert O.rel_l2(v, ref) < 2e-6
+
+
 def test_transmission_small_vs_reference(ctx, golden):
     G = golden("si_small.npz")
     t = ctx.transmission(G["v"].astype(np.float32), float(G["ax"]), float(G["by"]), 200.0)
