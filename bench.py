@@ -651,6 +651,40 @@ def run_sides(args):
             torch.cuda.empty_cache()
 
 
+def run_potential(args):
+    """--potential: the projected potential of one Au 2048^2 configuration (fcc Au
+    16x16x40 cells, 80 slices, 3 A cutoff; the frozen-phonon workload's
+    per-configuration build) through msl_potential_build into device memory:
+    device time per launch (CUDA events on the library stream) and the pair
+    evaluations it makes (pixel-atom pairs inside the cutoff)."""
+    import ctypes
+
+    import torch
+
+    from multislice_gb300 import Context, specimen as S
+
+    spec = S.jitter(S.fcc_au(), 0.085, np.random.default_rng(7))
+    n, nslice, radius = 2048, 80, 3.0
+    v = torch.empty((nslice, n, n), dtype=torch.float32, device="cuda:0")
+    with Context(0) as c:
+        c.potential(spec, n, n, nslice, radius, out=v)
+        c._lib.msl_profile_enable(c._h, 1)
+        reps = max(1, args.steps)
+        for _ in range(reps):
+            c.potential(spec, n, n, nslice, radius, out=v)
+        k, ms = ctypes.c_int64(), ctypes.c_double()
+        c._lib.msl_profile_read(c._h, 2, ctypes.byref(k), ctypes.byref(ms))
+        c._lib.msl_profile_enable(c._h, 0)
+    dxp = spec.ax / n
+    pairs_per_pixel = np.pi * radius ** 2 * spec.natom / nslice / (spec.ax * spec.by)
+    pairs = pairs_per_pixel * n * n * nslice
+    line = {"workload": "Au fcc 16x16x40 (40,960 atoms, jittered 0.085 A), 2048^2, 80 slices, 3 A cutoff",
+            "ms_per_launch": ms.value / max(k.value, 1), "launches": k.value,
+            "pixel_size_A": dxp, "pairs_inside_cutoff": pairs,
+            "pairs_per_s": pairs / (ms.value / max(k.value, 1) * 1e-3)}
+    print(json.dumps(line), flush=True)
+
+
 def run_frozen_phonon(args):
     """The Au 2048^2 frozen-phonon image (fcc Au 16x16x40 cells, 80 slices, 32
     configurations, 300 kV, Cs 1.2 mm, defocus -60 nm, 25 mrad objective
@@ -708,6 +742,8 @@ def main():
     ap.add_argument("--batch", type=int, default=0, help="probes per launch (0: library default)")
     ap.add_argument("--sides", action="store_true",
                     help="per-pass bandwidth of the slice loop at every side instead of the scan")
+    ap.add_argument("--potential", action="store_true",
+                    help="time the potential of one Au 2048^2 frozen-phonon configuration")
     ap.add_argument("--frozen-phonon", action="store_true",
                     help="time the Au 2048^2, 32-configuration frozen-phonon image instead of the scan")
     args = ap.parse_args()
@@ -719,6 +755,8 @@ def main():
         run_sides(args)
     elif args.frozen_phonon:
         run_frozen_phonon(args)
+    elif args.potential:
+        run_potential(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -988,6 +988,7 @@ int potential_launch(msl_ctx *c, const PotImage &im, const unsigned char *d, con
     a.nsp = im.nsp;
     a.tab_r0 = (float)im.tab_r0;
     a.tab_inv_h = (float)(msl::kPotTabN / (radius - im.tab_r0));
+    a.tab_off = (float)(-im.tab_r0 * msl::kPotTabN / (radius - im.tab_r0));
     LAUNCH_TRY(c, timed(c, MSL_PROF_POTENTIAL, [&] { return msl::launch_potential(a, c->stream, &c->launches); }));
     return MSL_OK;
 }

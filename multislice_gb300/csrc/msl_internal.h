@@ -131,7 +131,7 @@ struct PotArgs {
     const float4 *tab;
     const int *zslot;
     int nsp;
-    float tab_r0, tab_inv_h;
+    float tab_r0, tab_inv_h, tab_off;  // piece coordinate u = r tab_inv_h + tab_off (= (r - r0) / h)
 };
 constexpr int kPotTabN = 512;   // cubic pieces per species
 constexpr int kPotMaxSp = 8;    // species the tabulated kernel takes (more: analytic kernel)

@@ -175,18 +175,30 @@ __global__ void __launch_bounds__(THREADS, 5) potential_kernel(PotArgs a) {
             }
             __syncthreads();
             for (int k = 0; k < n; ++k) {
-                const float dy = sdy[k][ty];
+                // a warp holds 32 rows x 4 columns of the tile (ty = lane, the
+                // columns txg + 8 j warp-uniform): an atom whose x offset puts all
+                // four columns beyond the cutoff is skipped by the whole warp
+                float dx[PX];
+#pragma unroll
+                for (int j = 0; j < PX; ++j) dx[j] = sdx[k][txg + 8 * j];
+                float dxm = dx[0];
+#pragma unroll
+                for (int j = 1; j < PX; ++j) dxm = fminf(dxm, dx[j]);
+                if (dxm * dxm >= a.rad2) continue;
+                const float dy = sdy[k][ty], dy2 = dy * dy;
+                if (dy2 >= a.rad2) continue;
                 const float *p = a.sp + sZ[k] * 12;
                 const float4 *tb = TAB ? stab + sS[k] * kPotTabN : nullptr;
 #pragma unroll
                 for (int j = 0; j < PX; ++j) {
-                    const float dx = sdx[k][txg + 8 * j];
-                    const float r2 = dx * dx + dy * dy;
+                    const float r2 = fmaf(dx[j], dx[j], dy2);
                     if (r2 < a.rad2) {
-                        const float r = fmaxf(sqrtf(r2), 1.0e-10f);
+                        // r = max(r, 1e-10 A) through the reciprocal square root
+                        const float r2c = fmaxf(r2, 1.0e-20f);
+                        const float r = r2c * rsqrtf(r2c);
                         if (TAB && r >= a.tab_r0) {
                             // cubic piece of the tabulated profile: ((c3 t + c2) t + c1) t + c0
-                            const float u = (r - a.tab_r0) * a.tab_inv_h;
+                            const float u = fmaf(r, a.tab_inv_h, a.tab_off);
                             const int i = min((int)u, kPotTabN - 1);
                             const float t = u - (float)i;
                             const float4 c = tb[i];
