@@ -561,6 +561,7 @@ def run_jobs_bench(args):
             el = _time(lambda: ctx.run_jobs(jobs), max(1, args.steps))
             waves = [j["out"].cpu().numpy() for j in jobs]
             arms[arm] = {"value": units / el, "seconds": el,
+                         "algorithmic_gbs": 1e-9 * sum(40 * d["n"] * d["n"] * d["nslice"] for d in descs) / el,
                          "waves": [w[..., 0] + 1j * w[..., 1] for w in waves]}
             ctx.set_schedule(256, 0, 0)
             ctx.set_schedule(512, 0, 0)
@@ -577,7 +578,9 @@ def run_jobs_bench(args):
                 devt[name] = {"launches": n.value, "ms": ms.value}
         ctx._lib.msl_profile_enable(ctx._h, 0)
         line["fp32_device_time"] = devt
-        line["algorithmic_bytes"] = int(sum(32 * d["n"] * d["n"] * d["nslice"] for d in descs))
+        # per slice: the wave read and written by both passes (32 N^2) and the
+        # job's own transmission layer read once (8 N^2; jobs share no layers)
+        line["algorithmic_bytes"] = int(sum(40 * d["n"] * d["n"] * d["nslice"] for d in descs))
         del jobs
         torch.cuda.empty_cache()
         errs = {"fp32": [], "tensor_core": []}

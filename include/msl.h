@@ -547,7 +547,7 @@ void CreatePots_rs_DT_DW(uint32_t Ntypes, uint32_t Npoints, double dds, int32_t 
  * Work runs on `stream` (a cudaStream_t, NULL for the default stream) and the
  * call waits for that stream before returning.  The first call on each device
  * looks up the array's device address (cudaGetSymbolAddress) with that device
- * current; make that first call before any stream capture.  All calls share
+ * current.  All calls share
  * the array: calls that overlap on the GPU (several host threads, several
  * streams of one device) race on it.  Errors are reported by the return code
  * only (there is no context to hold a message); a pass kernel that gives up a

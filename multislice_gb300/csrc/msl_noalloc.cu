@@ -28,8 +28,7 @@
 //
 // Set-up: the first call on each device looks up the array's device address
 // with cudaGetSymbolAddress while that device is current (a host-side name of
-// a __device__ array is not a device address).  Make that first call before
-// any stream capture begins.
+// a __device__ array is not a device address).
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
