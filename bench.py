@@ -411,7 +411,9 @@ def run_variants(ctx, cfg, xy, plain, ref64, args, t_dev):
     * resident_256: the on-chip slice loop (one 8-CTA cluster per probe) against
       the streaming passes on the same crystal at 256^2 (4 x 4 cells, the same
       0.061 A pixels), 4096 probes x 100 slices;
-    * autotune: the pass-family schedule the autotuner measures at 512."""
+    * autotune: the pass-family schedule the autotuner measures at 512;
+    * uneven_jobs_256 and frozen_phonon_au2048: the uneven-batch and
+      frozen-phonon workloads (jobs_measure, frozen_phonon_measure)."""
     import torch
 
     from multislice_gb300 import specimen as S
@@ -481,6 +483,12 @@ def run_variants(ctx, cfg, xy, plain, ref64, args, t_dev):
                            "ms_per_slice_step_128_waves": {f"{fam[i]}/{fam[j]}": float(ms[i, j])
                                                            for i in range(3) for j in range(3)}}
     ctx.set_schedule(512, 0, 0)
+    torch.cuda.empty_cache()
+    # ---- the other two workloads: the 256-job uneven batch (every 8th job
+    # against FP64 here; --jobs checks all) and the Au 2048^2 frozen-phonon image
+    out["uneven_jobs_256"] = jobs_measure(args, fp64_every=8)
+    torch.cuda.empty_cache()
+    out["frozen_phonon_au2048"] = frozen_phonon_measure()
     return out
 
 
@@ -513,12 +521,17 @@ def run_reference(args):
 
 
 def run_jobs_bench(args):
-    """--jobs: the uneven batch of 256 seeded jobs (grid sides 256-1024, 20-300
-    slices of 1-2 A, amorphous C/Si/Cu/Au at 0.05 atoms/A^3, 80/200/300 kV,
-    plane waves and probes mixed) through msl_run_jobs, once on the FP32 passes
-    and once with the tensor-core passes where they are built (sides 256 and
-    512); every job's exit wave against the FP64 oracle (its own FP64 potential,
-    transmission and slice loop).  One JSON line."""
+    """--jobs: the uneven batch with every job checked against FP64; one JSON line."""
+    print(json.dumps(jobs_measure(args, fp64_every=1)), flush=True)
+
+
+def jobs_measure(args, fp64_every=1):
+    """The uneven batch of 256 seeded jobs (grid sides 256-1024, 20-300 slices of
+    1-2 A, amorphous C/Si/Cu/Au at 0.05 atoms/A^3, 80/200/300 kV, plane waves and
+    probes mixed) through msl_run_jobs, once on the FP32 passes and once with the
+    tensor-core passes where they are built (sides 256 and 512); the exit waves
+    of every `fp64_every`-th job against the FP64 oracle (its own FP64
+    potential, transmission and slice loop)."""
     import ctypes
 
     import torch
@@ -586,6 +599,8 @@ def run_jobs_bench(args):
         errs = {"fp32": [], "tensor_core": []}
         t1 = time.perf_counter()
         for i, d in enumerate(descs):
+            if i % fp64_every:
+                continue
             s, n = d["spec"], d["n"]
             V = fp64_gpu.potential(s.x, s.y, s.z, s.Z, fp, s.ax, s.by, s.cz, n, n, d["nslice"], 3.0, dev)
             T = fp64_gpu.transmission(V, d["kev"], s.ax, s.by)
@@ -602,14 +617,15 @@ def run_jobs_bench(args):
                 errs[arm].append(O.rel_l2(arms[arm]["waves"][i], ref))
         torch.cuda.empty_cache()
         line["fp64_seconds"] = time.perf_counter() - t1
+    checked = [i for i in range(len(descs)) if i % fp64_every == 0]
     for arm in arms:
         e = np.array(errs[arm])
         arms[arm].pop("waves")
         arms[arm]["rel_l2_vs_fp64"] = {"worst": float(e.max()), "median": float(np.median(e)),
-                                       "worst_job": int(e.argmax())}
+                                       "worst_job": checked[int(e.argmax())], "jobs_checked": len(checked)}
     arms["tensor_core"]["note"] = "tensor-core passes at sides 256 and 512, FP32 passes at 384, 768, 1024"
     line["arms"] = arms
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def run_sides(args):
@@ -689,6 +705,11 @@ def run_potential(args):
 
 
 def run_frozen_phonon(args):
+    """--frozen-phonon: the Au 2048^2 frozen-phonon image; one JSON line."""
+    print(json.dumps(frozen_phonon_measure()), flush=True)
+
+
+def frozen_phonon_measure():
     """The Au 2048^2 frozen-phonon image (fcc Au 16x16x40 cells, 80 slices, 32
     configurations, 300 kV, Cs 1.2 mm, defocus -60 nm, 25 mrad objective
     aperture): wall time of one msl_frozen_phonon call after a warm-up call, and
@@ -716,7 +737,7 @@ def run_frozen_phonon(args):
             c._lib.msl_profile_read(c._h, k, ctypes.byref(n), ctypes.byref(ms))
             line[name] = {"launches": n.value, "ms": ms.value}
         c._lib.msl_profile_enable(c._h, 0)
-        print(json.dumps(line), flush=True)
+    return line
 
 
 def main():
