@@ -1291,6 +1291,9 @@ int run_job_groups(msl_ctx *c, const msl_job *jobs, std::vector<JobGroup> &group
     for (JobGroup &g : groups)
         for (int j : g.ids)
             if (jobs[j].illumination == MSL_PROBE) fxy_len += (size_t)g.nx + g.ny + 2;
+    // a column of ones (the plane wave's ky = 0 column) after the tables
+    const size_t ones_off = tab_bytes;
+    tab_bytes = align256(tab_bytes + sizeof(float2) * 2048);
     CUDA_TRY(c, c->wave.ensure(wave_bytes));
     CUDA_TRY(c, c->tabs.ensure(tab_bytes));
     CUDA_TRY(c, c->jobtab.ensure(ptab_bytes));
@@ -1301,6 +1304,7 @@ int run_job_groups(msl_ctx *c, const msl_job *jobs, std::vector<JobGroup> &group
     unsigned char *dtab = (unsigned char *)c->tabs.p, *dptab = (unsigned char *)c->jobtab.p;
     std::vector<unsigned char> htab(tab_bytes), hptab(ptab_bytes);
     std::vector<double> hk(fxy_len);
+    for (int i = 0; i < 2048; ++i) ((float2 *)(htab.data() + ones_off))[i] = make_float2(1.f, 0.f);
     size_t fo = 0;
     for (JobGroup &g : groups) {
         const int nx = g.nx, ny = g.ny, nb = (int)g.ids.size(), S = jobs[g.ids[0]].nslice;
@@ -1376,8 +1380,18 @@ int run_job_groups(msl_ctx *c, const msl_job *jobs, std::vector<JobGroup> &group
     cudaEvent_t fork = take_event(c);
     std::vector<cudaEvent_t> joins;
     CUDA_TRY(c, cudaEventRecord(fork, c->stream));
-    std::vector<float2> ones(4096, make_float2(1.f, 0.f));
+    const float2 *ones = (const float2 *)(dtab + ones_off);
+    // on a failure after launches began, let every group stream drain before
+    // returning (the next call reuses the buffers)
+    auto drain = [&](int rc_) {
+        if (concurrent)
+            for (size_t gi = 0; gi < groups.size() && gi < c->side_streams.size(); ++gi)
+                cudaStreamSynchronize(c->side_streams[gi]);
+        cudaStreamSynchronize(c->stream);
+        return rc_;
+    };
     fo = 0;
+    int lrc = [&]() -> int {
     for (size_t gi = 0; gi < groups.size(); ++gi) {
         JobGroup &g = groups[gi];
         const int nx = g.nx, ny = g.ny, nb = (int)g.ids.size(), S = jobs[g.ids[0]].nslice;
@@ -1402,8 +1416,8 @@ int run_job_groups(msl_ctx *c, const msl_job *jobs, std::vector<JobGroup> &group
             const msl_job &jb = jobs[g.ids[b]];
             float2 *slot = w + (size_t)b * n2;
             if (jb.illumination == MSL_PLANE_WAVE) {
-                CUDA_TRY(c, cudaMemcpy2DAsync(slot, sizeof(float2) * ny, ones.data(), sizeof(float2),
-                                              sizeof(float2), nx, cudaMemcpyHostToDevice, st));
+                CUDA_TRY(c, cudaMemcpy2DAsync(slot, sizeof(float2) * ny, ones, sizeof(float2),
+                                              sizeof(float2), nx, cudaMemcpyDeviceToDevice, st));
                 continue;
             }
             const double *kxd = (const double *)c->fxy.p + fo, *kyd = kxd + nx;
@@ -1456,6 +1470,9 @@ int run_job_groups(msl_ctx *c, const msl_job *jobs, std::vector<JobGroup> &group
             CUDA_TRY(c, cudaEventRecord(e, st));
         }
     }
+    return MSL_OK;
+    }();
+    if (lrc) return drain(lrc);
     for (cudaEvent_t e : joins) CUDA_TRY(c, cudaStreamWaitEvent(c->stream, e, 0));
     // exit waves out once every group's loop has been issued
     for (JobGroup &g : groups) {

@@ -18,6 +18,10 @@
 // split-bf16 products: each operand is hi + lo (hi = bf16(x), lo = bf16(x - hi))
 // and A is packed [hi | lo] along K against B1 = [Bhi | Bhi] and B2 = [Blo | 0],
 // so D = Ahi Bhi + Alo Bhi + Ahi Blo (the lo lo term, 2^-16 relative, dropped).
+// Only the + sign matrices are held: a transform of sign -1 is computed as
+// conj(DFT+(conj(x))), the conjugations being sign flips where the operand is
+// written and the result read, so a CTA fits in half the shared memory and two
+// run per SM.
 // The row pass (ifft_y, * t, fft_y) and the column pass (fft_x, propagator and
 // band limit, [detector sums], ifft_x) of msl_passes.cu take this path when
 // the side's schedule is MSL_FAM_TC; twiddles, pointwise factors and detector
@@ -50,13 +54,17 @@ template <int N> struct TcGeom {
     static constexpr size_t BN2 = (size_t)KR2 * 128;            // one DFT_N2 B tile per K atom
     static constexpr size_t OFF_A1 = 0;
     static constexpr size_t OFF_A2 = OFF_A1 + A1;
-    // B tiles: [dir][B1|B2] for DFT16, [dir][B1|B2][atom] for DFT_N2; dir 0 = +1, 1 = -1
+    // B tiles of the + sign only: [B1|B2] for DFT16, [B1|B2][atom] for DFT_N2 (a
+    // transform of sign -1 runs as conj(DFT+(conj(x))): the conjugations are sign
+    // flips in the epilogues)
     static constexpr size_t OFF_B16 = OFF_A2 + A2;
-    static constexpr size_t OFF_BN2 = OFF_B16 + 4 * B16;
-    static constexpr size_t OFF_TW = OFF_BN2 + 4 * ATOM2 * BN2;       // W_N^m, m < N
-    static constexpr size_t OFF_OUT = OFF_TW + sizeof(float2) * N;     // staging of the tile's lines
-    static constexpr size_t OFF_RED = OFF_OUT + sizeof(float2) * kTcLines * N;
+    static constexpr size_t OFF_BN2 = OFF_B16 + 2 * B16;
+    static constexpr size_t OFF_TW = OFF_BN2 + 2 * ATOM2 * BN2;       // W_N^m, m < N
+    static constexpr size_t OFF_RED = OFF_TW + sizeof(float2) * N;
     static constexpr size_t SMEM = OFF_RED + sizeof(double) * 8 * 8 + 1024;
+    // the staging of the tile's output lines reuses the DFT_N2 operand (free by then)
+    static constexpr size_t OFF_OUT = OFF_A2;
+    static_assert(A2 >= sizeof(float2) * kTcLines * N, "output staging fits the DFT_N2 operand");
 };
 
 __device__ __forceinline__ void split_store(unsigned char *tile, int row, int k, int kr, float x) {
@@ -119,7 +127,7 @@ __device__ __forceinline__ void stage_mma(uint32_t tmem, const unsigned char *a,
 }  // namespace
 
 template <int N>
-__global__ void __launch_bounds__(kTcThreads, 1) tc_pass_kernel(TcPassArgs a) {
+__global__ void __launch_bounds__(kTcThreads, 2) tc_pass_kernel(TcPassArgs a) {
     using G = TcGeom<N>;
     constexpr int N2 = G::N2;
     extern __shared__ __align__(1024) unsigned char smraw[];
@@ -132,14 +140,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_pass_kernel(TcPassArgs a) {
     __shared__ uint32_t tmem_base;
     __shared__ int failed;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int d1 = a.dir1 > 0 ? 0 : 1, d2 = a.dir2 > 0 ? 0 : 1;
-    // constant operands: DFT16 and DFT_N2 of both signs
-    for (int d = 0; d < 2; ++d) {
-        build_b(base + G::OFF_B16 + (size_t)(2 * d) * G::B16, base + G::OFF_B16 + (size_t)(2 * d + 1) * G::B16, 16,
-                d == 0 ? 1 : -1, G::B16);
-        build_b(base + G::OFF_BN2 + (size_t)(2 * d) * G::ATOM2 * G::BN2,
-                base + G::OFF_BN2 + (size_t)(2 * d + 1) * G::ATOM2 * G::BN2, N2, d == 0 ? 1 : -1, G::BN2);
-    }
+    // conjugations that turn the + sign transforms into the - sign ones
+    const float c1 = a.dir1 > 0 ? 1.f : -1.f, c2 = a.dir2 > 0 ? 1.f : -1.f;
+    // constant operands: DFT16 and DFT_N2 of the + sign
+    build_b(base + G::OFF_B16, base + G::OFF_B16 + G::B16, 16, 1, G::B16);
+    build_b(base + G::OFF_BN2, base + G::OFF_BN2 + (size_t)G::ATOM2 * G::BN2, N2, 1, G::BN2);
+    const unsigned char *b16_1 = base + G::OFF_B16, *b16_2 = base + G::OFF_B16 + G::B16;
+    const unsigned char *bn2_1 = base + G::OFF_BN2, *bn2_2 = base + G::OFF_BN2 + (size_t)G::ATOM2 * G::BN2;
     for (int m = tid; m < N; m += kTcThreads) {
         float s, c;
         sincospif((float)(2 * m) / (float)N, &s, &c);
@@ -189,13 +196,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_pass_kernel(TcPassArgs a) {
             const int row = l * N2 + n % N2, k = n / N2;
             unsigned char *t = A1 + (row >> 7) * 128 * 128;
             split_store(t, row & 127, k, 32, x.x);
-            split_store(t, row & 127, 16 + k, 32, x.y);
+            split_store(t, row & 127, 16 + k, 32, c1 * x.y);
         }
-        // ---------------- transform 1 (D1, sign dir1)
-        run(A1, 128 * 128, base + G::OFF_B16 + (size_t)(2 * d1) * G::B16,
-            base + G::OFF_B16 + (size_t)(2 * d1 + 1) * G::B16, G::B16, 1, 32, G::MT1, 128 * 128);
+        // ---------------- transform 1 (D1, sign dir1: the + transform of the input conjugated by c1)
+        run(A1, 128 * 128, b16_1, b16_2, G::B16, 1, 32, G::MT1, 128 * 128);
         if (failed) break;
-        // stage-1 epilogue: row (l, n2) -> twiddle W^(dir1 n2 k1) -> row (l, k1), K n2.
+        // stage-1 epilogue: row (l, n2) -> twiddle W^(n2 k1) -> row (l, k1), K n2.
         // Two 128-row tiles (N = 512): warps 4-7 take the second; one tile (N = 256):
         // warps 0-3 take k1 0..7 and warps 4-7 k1 8..15 of the same rows.
         {
@@ -212,8 +218,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_pass_kernel(TcPassArgs a) {
 #pragma unroll
                 for (int j = 0; j < 8; ++j) {
                     const int k1 = c0 + c + j;
-                    float2 tw = twn[(n2 * k1) % N];
-                    if (a.dir1 < 0) tw.y = -tw.y;
+                    const float2 tw = twn[(n2 * k1) % N];
                     const float xr = re[j] * tw.x - im[j] * tw.y, xi = re[j] * tw.y + im[j] * tw.x;
                     const int row2 = l * 16 + k1;
                     split_store(A2, row2, n2, G::KR2, xr);
@@ -221,8 +226,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_pass_kernel(TcPassArgs a) {
                 }
             }
         }
-        run(A2, 128 * 128, base + G::OFF_BN2 + (size_t)(2 * d1) * G::ATOM2 * G::BN2,
-            base + G::OFF_BN2 + (size_t)(2 * d1 + 1) * G::ATOM2 * G::BN2, G::BN2, G::ATOM2, G::KR2, 1, 0);
+        run(A2, 128 * 128, bn2_1, bn2_2, G::BN2, G::ATOM2, G::KR2, 1, 0);
         if (failed) break;
         // stage-2 epilogue (order L2): row (l, k1) holds X[k1 + 16 k2]; pointwise work, then
         // the same row becomes D2's stage-A operand (K = k2)
@@ -248,7 +252,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_pass_kernel(TcPassArgs a) {
 #pragma unroll
             for (int c = 0; c < H; ++c) {
                 const int k2 = half * H + c, n = k1 + 16 * k2;   // element index along the line
-                float2 x = make_float2(re[c], im[c]);
+                float2 x = make_float2(re[c], c1 * im[c]);
                 if (a.mode == TC_MODE_TRANS) {
                     // row lines: line = ix, n = iy
                     const float2 *tr = a.trans_b ? a.trans_b[img] : a.trans;
@@ -274,7 +278,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_pass_kernel(TcPassArgs a) {
                 }
                 if (second) {
                     split_store(A2, row, k2, G::KR2, x.x);
-                    split_store(A2, row, N2 + k2, G::KR2, x.y);
+                    split_store(A2, row, N2 + k2, G::KR2, c2 * x.y);
                 }
             }
             if (a.detmask) {
@@ -297,11 +301,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_pass_kernel(TcPassArgs a) {
             __syncthreads();
             continue;
         }
-        // ---------------- transform 2 (D2, sign dir2): stage A on A2 as written
-        run(A2, 128 * 128, base + G::OFF_BN2 + (size_t)(2 * d2) * G::ATOM2 * G::BN2,
-            base + G::OFF_BN2 + (size_t)(2 * d2 + 1) * G::ATOM2 * G::BN2, G::BN2, G::ATOM2, G::KR2, 1, 0);
+        // ---------------- transform 2 (D2, sign dir2): stage A on A2 as written (conjugated by c2)
+        run(A2, 128 * 128, bn2_1, bn2_2, G::BN2, G::ATOM2, G::KR2, 1, 0);
         if (failed) break;
-        // stage-A epilogue: row (l, na), columns kb -> twiddle W^(dir2 na kb) -> row (l, kb), K na
+        // stage-A epilogue: row (l, na), columns kb -> twiddle W^(na kb) -> row (l, kb), K na
         {
             const int wq = warp & 3, half = warp >> 2;
             const int row = 32 * wq + lane, l = row / 16, na = row % 16;
@@ -321,8 +324,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_pass_kernel(TcPassArgs a) {
 #pragma unroll
             for (int c = 0; c < H; ++c) {
                 const int kb = half * H + c;
-                float2 tw = twn[(na * kb) % N];
-                if (a.dir2 < 0) tw.y = -tw.y;
+                const float2 tw = twn[(na * kb) % N];
                 const float xr = re[c] * tw.x - im[c] * tw.y, xi = re[c] * tw.y + im[c] * tw.x;
                 const int row1 = l * N2 + kb;
                 unsigned char *t = A1 + (row1 >> 7) * 128 * 128;
@@ -330,8 +332,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_pass_kernel(TcPassArgs a) {
                 split_store(t, row1 & 127, 16 + na, 32, xi);
             }
         }
-        run(A1, 128 * 128, base + G::OFF_B16 + (size_t)(2 * d2) * G::B16,
-            base + G::OFF_B16 + (size_t)(2 * d2 + 1) * G::B16, G::B16, 1, 32, G::MT1, 128 * 128);
+        run(A1, 128 * 128, b16_1, b16_2, G::B16, 1, 32, G::MT1, 128 * 128);
         if (failed) break;
         // stage-B epilogue: row (l, kb) holds X[N2 ka + kb]: stage the tile, then store coalesced
         {
@@ -346,7 +347,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_pass_kernel(TcPassArgs a) {
                 tc::tmem_ld8(tmem + lanes + tcol + (uint32_t)(c0 + c), re);
                 tc::tmem_ld8(tmem + lanes + tcol + (uint32_t)(16 + c0 + c), im);
 #pragma unroll
-                for (int j = 0; j < 8; ++j) stage[l * N + N2 * (c0 + c + j) + kb] = make_float2(re[j], im[j]);
+                for (int j = 0; j < 8; ++j) stage[l * N + N2 * (c0 + c + j) + kb] = make_float2(re[j], c2 * im[j]);
             }
         }
         tc::fence_before_sync();
