@@ -189,14 +189,28 @@ __global__ void __launch_bounds__(kTcThreads, 2) tc_pass_kernel(TcPassArgs a) {
             return cols ? a.data + ((size_t)img * a.nx + n) * a.ny + lin0 + l
                         : a.data + ((size_t)img * a.nx + lin0 + l) * a.ny + n;
         };
-        // ---- load in order L1 into the DFT16 operand: row (l, n2), K n1 (re) / 16 + n1 (im)
-        for (int i = tid; i < kTcLines * N; i += kTcThreads) {
-            const int l = cols ? i % kTcLines : i / N, n = cols ? i / kTcLines : i % N;
-            const float2 x = *gaddr(l, n);
-            const int row = l * N2 + n % N2, k = n / N2;
-            unsigned char *t = A1 + (row >> 7) * 128 * 128;
-            split_store(t, row & 127, k, 32, x.x);
-            split_store(t, row & 127, 16 + k, 32, c1 * x.y);
+        // ---- load in order L1 into the DFT16 operand: row (l, n2), K n1 (re) / 16 + n1 (im);
+        // all of a thread's loads are issued before its shared-memory stores
+        constexpr int PER = kTcLines * N / kTcThreads, CH = 8;  // in chunks of 8 (registers)
+        static_assert(PER % CH == 0, "load chunks");
+#pragma unroll 1
+        for (int j0 = 0; j0 < PER; j0 += CH) {
+            float2 xin[CH];
+#pragma unroll
+            for (int j = 0; j < CH; ++j) {
+                const int i = tid + (j0 + j) * kTcThreads;
+                const int l = cols ? i % kTcLines : i / N, n = cols ? i / kTcLines : i % N;
+                xin[j] = *gaddr(l, n);
+            }
+#pragma unroll
+            for (int j = 0; j < CH; ++j) {
+                const int i = tid + (j0 + j) * kTcThreads;
+                const int l = cols ? i % kTcLines : i / N, n = cols ? i / kTcLines : i % N;
+                const int row = l * N2 + n % N2, k = n / N2;
+                unsigned char *t = A1 + (row >> 7) * 128 * 128;
+                split_store(t, row & 127, k, 32, xin[j].x);
+                split_store(t, row & 127, 16 + k, 32, c1 * xin[j].y);
+            }
         }
         // ---------------- transform 1 (D1, sign dir1: the + transform of the input conjugated by c1)
         run(A1, 128 * 128, b16_1, b16_2, G::B16, 1, 32, G::MT1, 128 * 128);
@@ -370,6 +384,10 @@ template <int N> static cudaError_t tc_pass_launch(const TcPassArgs &a, cudaStre
     int per_sm = 0;
     cudaError_t e = ks.get(tc_pass_kernel<N>, kTcThreads, G::SMEM, true, &per_sm);
     if (e != cudaSuccess) return e;
+    // two CTAs fit an SM by registers (launch bounds) and shared memory (at most
+    // 112 KB each); the occupancy query has answered one for this kernel, so the
+    // grid asks for two per SM (a CTA that does not fit waits for a free slot)
+    if (per_sm < 2 && 2 * (G::SMEM + 2048) <= 233472) per_sm = 2;
     const int ntiles = a.nlines / kTcLines;
     int grid = nsm * per_sm < ntiles ? nsm * per_sm : ntiles;
     if (grid < 1) grid = 1;
