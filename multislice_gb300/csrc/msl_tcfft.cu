@@ -62,6 +62,9 @@ template <int N> struct TcGeom {
     static constexpr size_t OFF_TW = OFF_BN2 + 2 * ATOM2 * BN2;       // W_N^m, m < N
     static constexpr size_t OFF_RED = OFF_TW + sizeof(float2) * N;
     static constexpr size_t SMEM = OFF_RED + sizeof(double) * 8 * 8 + 1024;
+    // CTAs per SM: registers (launch bounds) and shared memory allow four at 256, two at 512
+    static constexpr int MINB = N == 256 ? 4 : 2;
+    static_assert(MINB * (SMEM + 2048) <= 233472, "MINB CTAs fit an SM's shared memory");
     // the staging of the tile's output lines reuses the DFT_N2 operand (free by then)
     static constexpr size_t OFF_OUT = OFF_A2;
     static_assert(A2 >= sizeof(float2) * kTcLines * N, "output staging fits the DFT_N2 operand");
@@ -127,7 +130,7 @@ __device__ __forceinline__ void stage_mma(uint32_t tmem, const unsigned char *a,
 }  // namespace
 
 template <int N>
-__global__ void __launch_bounds__(kTcThreads, 2) tc_pass_kernel(TcPassArgs a) {
+__global__ void __launch_bounds__(kTcThreads, TcGeom<N>::MINB) tc_pass_kernel(TcPassArgs a) {
     using G = TcGeom<N>;
     constexpr int N2 = G::N2;
     extern __shared__ __align__(1024) unsigned char smraw[];
@@ -384,10 +387,10 @@ template <int N> static cudaError_t tc_pass_launch(const TcPassArgs &a, cudaStre
     int per_sm = 0;
     cudaError_t e = ks.get(tc_pass_kernel<N>, kTcThreads, G::SMEM, true, &per_sm);
     if (e != cudaSuccess) return e;
-    // two CTAs fit an SM by registers (launch bounds) and shared memory (at most
-    // 112 KB each); the occupancy query has answered one for this kernel, so the
-    // grid asks for two per SM (a CTA that does not fit waits for a free slot)
-    if (per_sm < 2 && 2 * (G::SMEM + 2048) <= 233472) per_sm = 2;
+    // G::MINB CTAs fit an SM by registers (launch bounds) and shared memory; the
+    // occupancy query has answered fewer for this kernel, so the grid asks for
+    // G::MINB per SM (a CTA that does not fit waits for a free slot)
+    if (per_sm < G::MINB) per_sm = G::MINB;
     const int ntiles = a.nlines / kTcLines;
     int grid = nsm * per_sm < ntiles ? nsm * per_sm : ntiles;
     if (grid < 1) grid = 1;
