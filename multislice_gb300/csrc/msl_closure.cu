@@ -153,10 +153,19 @@ __global__ void __launch_bounds__(128) conv_tc_kernel(const __nv_bfloat16 *__res
             const int yy = (y + tap / 3 - 1 + H) % H, dx = tap % 3 - 1;
             const __nv_bfloat16 *row = in + ((size_t)img * H + yy) * W * 64;
             unsigned char *dst = sa + s * kATile;
-            for (int i = tid; i < kTile * 8; i += 128) {
-                const int r = i >> 3, c = i & 7;
+            // the tap's 16 KB: every load of this thread issued before its stores
+            constexpr int PER = kTile * 8 / 128;
+            uint4 va[PER];
+#pragma unroll
+            for (int j = 0; j < PER; ++j) {
+                const int i = tid + 128 * j, r = i >> 3, c = i & 7;
                 const int xx = (x0 + r + dx + W) % W;
-                *(uint4 *)(dst + tc::sw128_offset(r, c * 8)) = *(const uint4 *)(row + (size_t)xx * 64 + c * 8);
+                va[j] = *(const uint4 *)(row + (size_t)xx * 64 + c * 8);
+            }
+#pragma unroll
+            for (int j = 0; j < PER; ++j) {
+                const int i = tid + 128 * j, r = i >> 3, c = i & 7;
+                *(uint4 *)(dst + tc::sw128_offset(r, c * 8)) = va[j];
             }
             fence_proxy_async();
             __syncthreads();
@@ -564,6 +573,11 @@ cudaError_t ClosureNet::conv_tc(const __nv_bfloat16 *in, const __nv_bfloat16 *w,
     int per_sm = 0;
     cudaError_t e = ks.get(conv_tc_kernel, 128, kConvSmem, true, &per_sm);
     if (e != cudaSuccess) return e;
+    // two CTAs fit an SM by shared memory (105 KB each) and registers; the
+    // occupancy query answers one for this tensor-memory kernel, so the grid
+    // asks for two (a CTA that does not fit waits for a free slot)
+    static_assert(2 * (kConvSmem + 2048) <= 233472, "two conv CTAs fit an SM");
+    if (per_sm < 2) per_sm = 2;
     const int ntiles = B * H * (W / kTile);
     int grid = nsm * per_sm < ntiles ? nsm * per_sm : ntiles;
     ++*launches;
