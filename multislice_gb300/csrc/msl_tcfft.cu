@@ -70,13 +70,17 @@ template <int N> struct TcGeom {
     static_assert(A2 >= sizeof(float2) * kTcLines * N, "output staging fits the DFT_N2 operand");
 };
 
-__device__ __forceinline__ void split_store(unsigned char *tile, int row, int k, int kr, float x) {
-    // hi at K position k, lo at K position kr + k (K runs over [hi | lo] atoms of 64)
-    const __nv_bfloat16 hi = __float2bfloat16_rn(x);
-    const __nv_bfloat16 lo = __float2bfloat16_rn(x - __bfloat162float(hi));
+// A complex value (re, im) as split-bf16 K pairs: (hi re, hi im) at K positions
+// k, k + 1 (k even) and (lo re, lo im) at kr + k, kr + k + 1 -- one 4-byte store
+// each.  K runs over [hi | lo] halves of kr; complex inputs are interleaved
+// (re, im) along K, and the B operands are built with the same order.
+__device__ __forceinline__ void split_store2(unsigned char *tile, int row, int k, int kr, float re, float im) {
+    const __nv_bfloat16 hr = __float2bfloat16_rn(re), hi_ = __float2bfloat16_rn(im);
+    const __nv_bfloat16 lr = __float2bfloat16_rn(re - __bfloat162float(hr));
+    const __nv_bfloat16 li = __float2bfloat16_rn(im - __bfloat162float(hi_));
     const int kh = k, kl = kr + k;
-    *(__nv_bfloat16 *)(tile + (kh >> 6) * 128 * 128 + tc::sw128_offset(row, kh & 63)) = hi;
-    *(__nv_bfloat16 *)(tile + (kl >> 6) * 128 * 128 + tc::sw128_offset(row, kl & 63)) = lo;
+    *(__nv_bfloat162 *)(tile + (kh >> 6) * 128 * 128 + tc::sw128_offset(row, kh & 63)) = __halves2bfloat162(hr, hi_);
+    *(__nv_bfloat162 *)(tile + (kl >> 6) * 128 * 128 + tc::sw128_offset(row, kl & 63)) = __halves2bfloat162(lr, li);
 }
 
 // Real form of the L-point DFT of sign dir: row (k, part), column (n, part),
@@ -91,8 +95,9 @@ __device__ __forceinline__ float dft_real(int L, int dir, int row, int col) {
     return pc == 0 ? s : c;
 }
 
-// B1 = [hi | hi], B2 = [lo | 0] of the real DFT matrix (rows = 2L outputs, K = 2L inputs),
-// K packed [hi part | lo part] over atoms of 64; tile t = atom index.
+// B1 = [hi | hi], B2 = [lo | 0] of the real DFT matrix (rows = 2L outputs, K = 2L inputs
+// in the order (n, part) interleaved, as split_store2 writes A), K packed
+// [hi part | lo part] over atoms of 64; tile t = atom index.
 __device__ void build_b(unsigned char *b1, unsigned char *b2, int L, int dir, size_t atom_bytes) {
     const int R = 2 * L;
     for (int i = threadIdx.x; i < R * R; i += blockDim.x) {
@@ -100,7 +105,7 @@ __device__ void build_b(unsigned char *b1, unsigned char *b2, int L, int dir, si
         const float w = dft_real(L, dir, row, col);
         const __nv_bfloat16 hi = __float2bfloat16_rn(w);
         const __nv_bfloat16 lo = __float2bfloat16_rn(w - __bfloat162float(hi));
-        const int kh = col, kl = R + col;
+        const int kh = 2 * (col % L) + col / L, kl = R + kh;  // K order (n, part) interleaved
         *(__nv_bfloat16 *)(b1 + (kh >> 6) * atom_bytes + tc::sw128_offset(row, kh & 63)) = hi;
         *(__nv_bfloat16 *)(b1 + (kl >> 6) * atom_bytes + tc::sw128_offset(row, kl & 63)) = hi;
         *(__nv_bfloat16 *)(b2 + (kh >> 6) * atom_bytes + tc::sw128_offset(row, kh & 63)) = lo;
@@ -211,8 +216,7 @@ __global__ void __launch_bounds__(kTcThreads, TcGeom<N>::MINB) tc_pass_kernel(Tc
                 const int l = cols ? i % kTcLines : i / N, n = cols ? i / kTcLines : i % N;
                 const int row = l * N2 + n % N2, k = n / N2;
                 unsigned char *t = A1 + (row >> 7) * 128 * 128;
-                split_store(t, row & 127, k, 32, xin[j].x);
-                split_store(t, row & 127, 16 + k, 32, c1 * xin[j].y);
+                split_store2(t, row & 127, 2 * k, 32, xin[j].x, c1 * xin[j].y);
             }
         }
         // ---------------- transform 1 (D1, sign dir1: the + transform of the input conjugated by c1)
@@ -238,8 +242,7 @@ __global__ void __launch_bounds__(kTcThreads, TcGeom<N>::MINB) tc_pass_kernel(Tc
                     const float2 tw = twn[(n2 * k1) % N];
                     const float xr = re[j] * tw.x - im[j] * tw.y, xi = re[j] * tw.y + im[j] * tw.x;
                     const int row2 = l * 16 + k1;
-                    split_store(A2, row2, n2, G::KR2, xr);
-                    split_store(A2, row2, N2 + n2, G::KR2, xi);
+                    split_store2(A2, row2, 2 * n2, G::KR2, xr, xi);
                 }
             }
         }
@@ -294,8 +297,7 @@ __global__ void __launch_bounds__(kTcThreads, TcGeom<N>::MINB) tc_pass_kernel(Tc
                     }
                 }
                 if (second) {
-                    split_store(A2, row, k2, G::KR2, x.x);
-                    split_store(A2, row, N2 + k2, G::KR2, c2 * x.y);
+                    split_store2(A2, row, 2 * k2, G::KR2, x.x, c2 * x.y);
                 }
             }
             if (a.detmask) {
@@ -345,8 +347,7 @@ __global__ void __launch_bounds__(kTcThreads, TcGeom<N>::MINB) tc_pass_kernel(Tc
                 const float xr = re[c] * tw.x - im[c] * tw.y, xi = re[c] * tw.y + im[c] * tw.x;
                 const int row1 = l * N2 + kb;
                 unsigned char *t = A1 + (row1 >> 7) * 128 * 128;
-                split_store(t, row1 & 127, na, 32, xr);
-                split_store(t, row1 & 127, 16 + na, 32, xi);
+                split_store2(t, row1 & 127, 2 * na, 32, xr, xi);
             }
         }
         run(A1, 128 * 128, b16_1, b16_2, G::B16, 1, 32, G::MT1, 128 * 128);
