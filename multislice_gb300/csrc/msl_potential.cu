@@ -36,7 +36,7 @@
 namespace msl {
 
 namespace {
-// tile shape and list capacity picked by timing 16 / 32 / 64-pixel-wide tiles
+// tile shape and list capacity picked by timing 16 / 32 / 64 / 128-pixel-wide tiles
 // and 32 / 64 / 128-atom lists on the Au 2048^2 potentials
 constexpr int TX = 64, TY = 32, THREADS = 256, PX = TX * TY / THREADS, CAP = 64;
 constexpr int KR = 2, ROUND = KR * THREADS, NW = THREADS / 32;  // atoms culled per thread per round
@@ -229,7 +229,7 @@ __global__ void __launch_bounds__(THREADS, 4) potential_kernel(PotArgs a) {
 
 cudaError_t launch_potential(const PotArgs &a, cudaStream_t s, int64_t *launches) {
     ++*launches;
-    dim3 grid(a.ny / TY, a.nx / TX, a.nslice);
+    dim3 grid((a.ny + TY - 1) / TY, (a.nx + TX - 1) / TX, a.nslice);
     if (a.nsp > 0 && a.tab) {
         const size_t smem = sizeof(float4) * (size_t)a.nsp * kPotTabN;
         static KernelSetup ks;
