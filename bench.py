@@ -412,6 +412,7 @@ def run_variants(ctx, cfg, xy, plain, ref64, args, t_dev):
       the streaming passes on the same crystal at 256^2 (4 x 4 cells, the same
       0.061 A pixels), 4096 probes x 100 slices;
     * autotune: the pass-family schedule the autotuner measures at 512;
+    * ctem_si256: the Si 256^2 CTEM case against the compiled reference;
     * uneven_jobs_256 and frozen_phonon_au2048: the uneven-batch and
       frozen-phonon workloads (jobs_measure, frozen_phonon_measure)."""
     import torch
@@ -484,6 +485,8 @@ def run_variants(ctx, cfg, xy, plain, ref64, args, t_dev):
                                                            for i in range(3) for j in range(3)}}
     ctx.set_schedule(512, 0, 0)
     torch.cuda.empty_cache()
+    # ---- the CTEM case against the compiled reference
+    out["ctem_si256"] = ctem_config1_measure(ctx, max(1, args.steps))
     # ---- the other two workloads: the 256-job uneven batch (every 8th job
     # against FP64 here; --jobs checks all) and the Au 2048^2 frozen-phonon image
     out["uneven_jobs_256"] = jobs_measure(args, fp64_every=8)
@@ -704,6 +707,57 @@ def run_potential(args):
     print(json.dumps(line), flush=True)
 
 
+def run_ctem(args):
+    """--ctem: the Si 256^2 CTEM case; one JSON line."""
+    import torch
+
+    from multislice_gb300 import Context
+    torch.cuda.set_device(0)
+    with Context(0) as ctx:
+        print(json.dumps(ctem_config1_measure(ctx, max(1, args.steps))), flush=True)
+
+
+def ctem_config1_measure(ctx, steps):
+    """The CTEM case (Si [001] 5x5x20 cells, 256^2, 80 slices of a/4, 200 kV
+    plane wave): the chain potential -> transmission -> slice loop from host
+    atoms to the host exit wave, the slice loop alone on device buffers, and the
+    exit wave against Kirkland's mulslice compiled from the reference sources
+    (the committed golden wave)."""
+    import torch
+
+    from multislice_gb300 import specimen as S
+    from oracle import msl_oracle as O
+    cfg = S.config_si_ctem()
+    spec, n, ns, kev = cfg["spec"], cfg["nx"], cfg["nslice"], cfg["kev"]
+    gold = np.load(os.path.join(ROOT, "tests", "golden", "si_config1.npz"))["wave"]
+    res = {}
+
+    def chain():
+        v = ctx.potential(spec, n, n, ns, cfg["radius"])
+        t = ctx.transmission(v, spec.ax, spec.by, kev)
+        res["w"] = ctx.multislice(t, spec.cz / ns, np.arange(ns), spec.ax, spec.by, kev)[0]
+
+    e2e = _time(chain, steps)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    v = torch.empty((ns, n, n), dtype=torch.float32, device=dev)
+    ctx.potential(spec, n, n, ns, cfg["radius"], out=v)
+    t = torch.empty((ns, n, n, 2), dtype=torch.float32, device=dev)
+    ctx.transmission(v, spec.ax, spec.by, kev, out=t)
+    psi = torch.empty((1, n, n, 2), dtype=torch.float32, device=dev)
+
+    def loop():
+        psi[..., 0] = 1.0
+        psi[..., 1] = 0.0
+        ctx.multislice(t, spec.cz / ns, np.arange(ns), spec.ax, spec.by, kev, psi=psi)
+
+    dt = _time(loop, steps)
+    return {"workload": "Si [001] 5x5x20 cells, 256^2, 80 slices (a/4), 200 kV plane wave",
+            "e2e_ms": 1e3 * e2e, "chain": "host atoms -> potential -> transmission -> slice loop -> host wave",
+            "slice_loop_ms": 1e3 * dt, "slices_per_s": ns / dt,
+            "rel_l2_vs_compiled_reference": O.rel_l2(res["w"], gold),
+            "reference": "Kirkland's mulslice compiled from the reference sources (tests/golden/si_config1.npz)"}
+
+
 def run_frozen_phonon(args):
     """--frozen-phonon: the Au 2048^2 frozen-phonon image; one JSON line."""
     print(json.dumps(frozen_phonon_measure()), flush=True)
@@ -766,6 +820,8 @@ def main():
     ap.add_argument("--batch", type=int, default=0, help="probes per launch (0: library default)")
     ap.add_argument("--sides", action="store_true",
                     help="per-pass bandwidth of the slice loop at every side instead of the scan")
+    ap.add_argument("--ctem", action="store_true",
+                    help="time the Si 256^2 CTEM case and check it against the compiled reference's wave")
     ap.add_argument("--potential", action="store_true",
                     help="time the potential of one Au 2048^2 frozen-phonon configuration")
     ap.add_argument("--frozen-phonon", action="store_true",
@@ -781,6 +837,8 @@ def main():
         run_frozen_phonon(args)
     elif args.potential:
         run_potential(args)
+    elif args.ctem:
+        run_ctem(args)
     elif args.impl == "reference":
         run_reference(args)
     else:
