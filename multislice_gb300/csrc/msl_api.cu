@@ -142,6 +142,15 @@ struct msl_ctx {
         atoms, tmpw, ctf, acc, jobtab;
     int *dflag = nullptr;  // device flag raised by a kernel whose bounded wait gave up
     std::vector<cudaStream_t> side_streams;  // one per grid group of an uneven batch
+    // msl_multislice's launch sequence for small batches, replayed as one CUDA
+    // graph: the key holds every launch argument of the loop (pointers, flags,
+    // schedules, the layer sequence); a key seen twice in a row is captured,
+    // then replayed while it repeats
+    struct LoopGraph {
+        std::vector<unsigned char> seen, key;
+        cudaGraphExec_t exec = nullptr;
+        int64_t nlaunch = 0;
+    } loop_graph;
     msl_ctx() {
         DevBuf *bufs[] = {&wave, &in_stage, &trans_stage, &tabs, &apchi, &exy, &fxy, &detmask,
                           &partial, &detout, &pot, &atoms, &tmpw, &ctf, &acc, &jobtab};
@@ -381,6 +390,61 @@ int err_check(msl_ctx *c) {
     if (h) return fail(c, MSL_E_CUDA, "a pass's bounded wait for its bulk / TMA copy timed out");
     return MSL_OK;
 }
+
+// Runs a launch sequence on the context's stream directly, or through the
+// context's cached CUDA graph: replayed when `key` equals the cached key,
+// captured (then replayed) when the same key came twice in a row, else run
+// directly.  A failed capture leaves the stream out of capture and the cache
+// empty.
+struct LoopGraphRun {
+    msl_ctx *c;
+    explicit LoopGraphRun(msl_ctx *c_) : c(c_) {}
+    template <class F> int run(const std::vector<unsigned char> &key, F &&launches) {
+        msl_ctx::LoopGraph &G = c->loop_graph;
+        if (G.exec && G.key == key) {
+            CUDA_TRY(c, cudaGraphLaunch(G.exec, c->stream));
+            c->launches += G.nlaunch;
+            return MSL_OK;
+        }
+        if (G.seen != key) {  // first sight: run directly, remember it
+            G.seen = key;
+            return launches();
+        }
+        if (G.exec) {
+            cudaGraphExecDestroy(G.exec);
+            G.exec = nullptr;
+            G.key.clear();
+        }
+        CUDA_TRY(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        const int64_t l0 = c->launches;
+        const int rc = launches();
+        cudaGraph_t graph = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
+        if (rc || e != cudaSuccess || !graph) {
+            if (graph) cudaGraphDestroy(graph);
+            cudaGetLastError();
+            G.seen.clear();
+            c->launches = l0;
+            if (rc) return rc;
+            return fail(c, MSL_E_CUDA, std::string("slice-loop graph capture: ") + cudaGetErrorString(e));
+        }
+        cudaGraphExec_t exec = nullptr;
+        const cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ei != cudaSuccess) {
+            cudaGetLastError();
+            G.seen.clear();
+            c->launches = l0;
+            return fail(c, MSL_E_CUDA, std::string("slice-loop graph instantiation: ") + cudaGetErrorString(ei));
+        }
+        G.exec = exec;
+        G.key = key;
+        G.nlaunch = c->launches - l0;
+        CUDA_TRY(c, cudaGraphLaunch(G.exec, c->stream));
+        return MSL_OK;
+    }
+};
+
 
 int check_layers(msl_ctx *c, int ntrans, const double *dz, const int *layer_seq, int nslice) {
     if (ntrans < 1) return fail(c, MSL_E_ARG, "ntrans must be >= 1");
@@ -674,6 +738,7 @@ int msl_ctx_destroy(msl_ctx *c) {
                       &c->tmpw, &c->ctf, &c->acc, &c->jobtab};
     for (DevBuf *b : bufs) b->release();
     if (c->dflag) cudaFree(c->dflag);
+    if (c->loop_graph.exec) cudaGraphExecDestroy(c->loop_graph.exec);
     for (cudaStream_t s : c->side_streams) cudaStreamDestroy(s);
     cudaStreamDestroy(c->stream);
     delete c;
@@ -1905,18 +1970,47 @@ int msl_multislice(msl_ctx *c, const msl_grid *g, const msl_optics *o, const flo
     float2 *twr = twiddles(c, ny), *twc = twiddles(c, nx);
     if (!twr || !twc) return fail(c, MSL_E_NOMEM, "twiddle table allocation failed");
     const int colf = msl::COL_LOAD | msl::COL_FWD | msl::COL_PROP | msl::COL_INV | msl::COL_STORE;
-    for (int s = 0; s < nslice; ++s) {
-        const int l = layer_seq[s];
-        int rf = msl::ROW_TRANS | msl::ROW_FWD;
-        if (s > 0) rf |= msl::ROW_LOAD | msl::ROW_INV;
-        else if (!plane_wave) rf |= msl::ROW_LOAD;
-        RowArgs r = row_args(g, twr, td + (size_t)l * n2, w, batch, rf, c->dflag);
+    auto loop = [&]() -> int {
+        for (int s = 0; s < nslice; ++s) {
+            const int l = layer_seq[s];
+            int rf = msl::ROW_TRANS | msl::ROW_FWD;
+            if (s > 0) rf |= msl::ROW_LOAD | msl::ROW_INV;
+            else if (!plane_wave) rf |= msl::ROW_LOAD;
+            RowArgs r = row_args(g, twr, td + (size_t)l * n2, w, batch, rf, c->dflag);
+            LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_row_pass(ny, r, c->stream, c->nsm, &c->launches); }));
+            ColArgs ca = col_args(g, st, twc, l, w, batch, colf, c->dflag);
+            LAUNCH_TRY(c, timed(c, MSL_PROF_COL, [&] { return msl::launch_col_pass(nx, ca, c->stream, c->nsm, &c->launches); }));
+        }
+        RowArgs r = row_args(g, twr, nullptr, w, batch, msl::ROW_LOAD | msl::ROW_INV, c->dflag);
         LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_row_pass(ny, r, c->stream, c->nsm, &c->launches); }));
-        ColArgs ca = col_args(g, st, twc, l, w, batch, colf, c->dflag);
-        LAUNCH_TRY(c, timed(c, MSL_PROF_COL, [&] { return msl::launch_col_pass(nx, ca, c->stream, c->nsm, &c->launches); }));
+        return MSL_OK;
+    };
+    // Small batches are launch-bound (a 256^2 wave's pass is a few microseconds):
+    // their loop runs as one CUDA graph once the same call has been seen twice.
+    // The tables the kernels read are uploaded above on every call; the graph
+    // holds only launches.
+    const bool graphable = !c->prof && wbytes <= ((size_t)32 << 20) && nslice >= 4;
+    if (!graphable) {
+        if ((rc = loop())) return rc;
+    } else {
+        std::vector<unsigned char> key;
+        auto put = [&](const void *p, size_t n) {
+            key.insert(key.end(), (const unsigned char *)p, (const unsigned char *)p + n);
+        };
+        int sch[4] = {0, 0, 0, 0};
+        msl::get_schedule(nx, &sch[0], &sch[1]);
+        msl::get_schedule(ny, &sch[2], &sch[3]);
+        const void *ptrs[8] = {td, w, twr, twc, st.d_prop, st.d_kx2, st.d_ky2, c->dflag};
+        const int ints[6] = {nx, ny, batch, nslice, plane_wave, ntrans};
+        put(sch, sizeof(sch));
+        put(ptrs, sizeof(ptrs));
+        put(ints, sizeof(ints));
+        put(&st.k2max, sizeof(st.k2max));
+        put(&c->device, sizeof(c->device));
+        put(layer_seq, sizeof(int) * (size_t)nslice);
+        LoopGraphRun lg(c);
+        if ((rc = lg.run(key, loop))) return rc;
     }
-    RowArgs r = row_args(g, twr, nullptr, w, batch, msl::ROW_LOAD | msl::ROW_INV, c->dflag);
-    LAUNCH_TRY(c, timed(c, MSL_PROF_ROW, [&] { return msl::launch_row_pass(ny, r, c->stream, c->nsm, &c->launches); }));
     if (!dev) CUDA_TRY(c, cudaMemcpyAsync(psi, w, wbytes, cudaMemcpyDeviceToHost, c->stream));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     collect_profile(c);
