@@ -227,10 +227,11 @@ __global__ void __launch_bounds__(ColCfg<N>::THREADS) col_pass_kernel(ColArgs a)
 
 
 // ------------------------------------------------- TMA-fed column pass
-// Persistent kernel, one CTA per SM.  Column tiles of C columns x N rows
-// (C * 8 bytes wide: 128 B for N <= 512) arrive by cp.async.bulk.tensor into a
-// ring of three shared-memory buffers: while tile k is transformed in buffer
-// k % 3, tile k+1 is already resident and tile k+2 is in flight.  The same
+// Persistent kernel, as many CTAs per SM as the plan's MINB and its shared
+// memory allow.  Column tiles of C columns x N rows (C * 8 bytes wide) arrive by
+// cp.async.bulk.tensor into a ring of NBUF shared-memory buffers (three: while
+// tile k is transformed in buffer k % 3, tile k+1 is already resident and tile
+// k+2 is in flight; two: tile k+1 loads while tile k is transformed).  The same
 // buffer then serves as the transform's exchange space and as the source of
 // the TMA store of the result, so a tile never touches registers-to-global
 // stores.  Every mbarrier wait is bounded; on a timeout the CTA raises *err,
@@ -588,7 +589,7 @@ __global__ void __launch_bounds__(ColHalfCfg<L>::THREADS, 1)
 }
 
 // ---------------------------------------------------- TMA-fed row pass
-// Persistent kernel, one CTA per SM, 512 threads = L lines x T threads.  Tiles
+// Persistent kernel, MINB CTAs per SM, TH threads = L lines x T threads.  Tiles
 // of L consecutive lines (L * N * 8 bytes, contiguous) arrive by TMA into a ring
 // of three buffers; the buffer is then the line transforms' exchange space and
 // the source of the TMA store.  The tile is viewed as [L][N/BX][BX] so every box
