@@ -415,7 +415,11 @@ struct LoopGraphRun {
             G.exec = nullptr;
             G.key.clear();
         }
-        CUDA_TRY(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            cudaGetLastError();  // no capture on this stream now: launch directly
+            G.seen.clear();
+            return launches();
+        }
         const int64_t l0 = c->launches;
         const int rc = launches();
         cudaGraph_t graph = nullptr;
