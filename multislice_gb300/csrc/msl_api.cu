@@ -1308,9 +1308,7 @@ cudaStream_t group_stream(msl_ctx *c, size_t i) {
 // arena), then each group's probe formation and lockstep slice loop on its
 // own stream (the context stream when profiling), then the exit waves out.
 int run_job_groups(msl_ctx *c, const msl_job *jobs, std::vector<JobGroup> &groups, double bandlimit) {
-    int rc;
     size_t wave_bytes = 0, tab_bytes = 0, ptab_bytes = 0, stage_bytes = 0, apchi_bytes = 0, exy_bytes = 0;
-    size_t nprobe = 0;
     for (JobGroup &g : groups) {
         const size_t n2 = (size_t)g.nx * g.ny, nb = g.ids.size();
         const int S = jobs[g.ids[0]].nslice;
@@ -1333,10 +1331,7 @@ int run_job_groups(msl_ctx *c, const msl_job *jobs, std::vector<JobGroup> &group
                 if (it == seen.end()) it = seen.emplace(key, g.nprop++).first;
                 g.layer_prop[b][l] = it->second;
             }
-            if (jb.illumination == MSL_PROBE) {
-                probes = true;
-                ++nprobe;
-            }
+            if (jb.illumination == MSL_PROBE) probes = true;
         }
         g.kbytes = sizeof(float) * (g.nx + g.ny) * nb;
         g.wave_off = wave_bytes;
